@@ -1,0 +1,288 @@
+// Stackless LBVH traversal.
+//
+// Public interface as in the reference (include/neighbor/LBVHTraverser.h:60-355): setup() with an
+// optional TransformOp (compress once, replay later), reset(), the nine traverse() overloads
+// (LaunchParameters | stream | neither) x (with/without images) x (with/without transform),
+// getData() returning the int4 nodes in the reference's 10-bit layout, std::runtime_error for more
+// than 32 images or an invalid tunable.
+//
+// Routing.  An ExactSphereQueryOp with CountNeighborsOp or NeighborListOp on a tree built from
+// points runs the fast kernel over the LBVH's 16-bit pre-order nodes (no compression step; the
+// transform is applied to the reported ids).  Any other combination of ops -- including the
+// stock SphereQueryOp, whose superset result depends on the node format -- runs the
+// reference-layout rope kernel, so it returns exactly what the reference returns.
+#ifndef NEIGHBOR_LBVH_TRAVERSER_H_
+#define NEIGHBOR_LBVH_TRAVERSER_H_
+
+#include <stdexcept>
+#include <type_traits>
+
+#include <cuda_runtime.h>
+
+#include "LBVH.h"
+#include "LBVHTraverserData.h"
+#include "Memory.h"
+#include "OutputOps.h"
+#include "QueryOps.h"
+#include "TransformOps.h"
+#include "TranslateOps.h"
+#include "Tunable.h"
+#include "kernels/traverse.cuh"
+
+namespace neighbor
+{
+
+class LBVHTraverser : public Tunable<unsigned int>
+    {
+    public:
+        LBVHTraverser()
+            : Tunable<unsigned int>(32, 1024, 32), m_root(0), m_lbvh_lo(1), m_lbvh_hi(1), m_bins(1),
+              m_replay(false), m_fast_enabled(true)
+            {}
+
+        template<class TransformOpT>
+        void setup(const LaunchParameters& params, const LBVH& lbvh, const TransformOpT& transform)
+            {
+            reset();
+            if (lbvh.getN() != 0)
+                {
+                compress(params, lbvh, transform);
+                m_replay = true;
+                }
+            }
+        void setup(const LaunchParameters& params, const LBVH& lbvh) { setup(params, lbvh, NullTransformOp()); }
+        template<class TransformOpT>
+        void setup(cudaStream_t stream, const LBVH& lbvh, const TransformOpT& transform)
+            {
+            setup(LaunchParameters(32, stream), lbvh, transform);
+            }
+        void setup(cudaStream_t stream, const LBVH& lbvh) { setup(stream, lbvh, NullTransformOp()); }
+        template<class TransformOpT>
+        void setup(const LBVH& lbvh, const TransformOpT& transform) { setup(cudaStream_t(0), lbvh, transform); }
+        void setup(const LBVH& lbvh) { setup(cudaStream_t(0), lbvh, NullTransformOp()); }
+
+        void reset() { m_replay = false; }
+
+        template<class QueryOpT, class OutputOpT, class TranslateOpT, class TransformOpT>
+        void traverse(const LaunchParameters& params, const LBVH& lbvh, const QueryOpT& query,
+                      const OutputOpT& out, const TranslateOpT& images, const TransformOpT& transform);
+
+        template<class QueryOpT, class OutputOpT, class TranslateOpT>
+        void traverse(const LaunchParameters& params, const LBVH& lbvh, const QueryOpT& query,
+                      const OutputOpT& out, const TranslateOpT& images)
+            {
+            traverse(params, lbvh, query, out, images, NullTransformOp());
+            }
+
+        template<class QueryOpT, class OutputOpT>
+        void traverse(const LaunchParameters& params, const LBVH& lbvh, const QueryOpT& query, const OutputOpT& out)
+            {
+            traverse(params, lbvh, query, out, SelfOp(), NullTransformOp());
+            }
+
+        template<class QueryOpT, class OutputOpT, class TranslateOpT, class TransformOpT>
+        void traverse(cudaStream_t stream, const LBVH& lbvh, const QueryOpT& query, const OutputOpT& out,
+                      const TranslateOpT& images, const TransformOpT& transform)
+            {
+            traverse(LaunchParameters(32, stream), lbvh, query, out, images, transform);
+            }
+
+        template<class QueryOpT, class OutputOpT, class TranslateOpT>
+        void traverse(cudaStream_t stream, const LBVH& lbvh, const QueryOpT& query, const OutputOpT& out,
+                      const TranslateOpT& images)
+            {
+            traverse(stream, lbvh, query, out, images, NullTransformOp());
+            }
+
+        template<class QueryOpT, class OutputOpT>
+        void traverse(cudaStream_t stream, const LBVH& lbvh, const QueryOpT& query, const OutputOpT& out)
+            {
+            traverse(stream, lbvh, query, out, SelfOp(), NullTransformOp());
+            }
+
+        template<class QueryOpT, class OutputOpT, class TranslateOpT, class TransformOpT>
+        void traverse(const LBVH& lbvh, const QueryOpT& query, const OutputOpT& out, const TranslateOpT& images,
+                      const TransformOpT& transform)
+            {
+            traverse(cudaStream_t(0), lbvh, query, out, images, transform);
+            }
+
+        template<class QueryOpT, class OutputOpT, class TranslateOpT>
+        void traverse(const LBVH& lbvh, const QueryOpT& query, const OutputOpT& out, const TranslateOpT& images)
+            {
+            traverse(cudaStream_t(0), lbvh, query, out, images, NullTransformOp());
+            }
+
+        template<class QueryOpT, class OutputOpT>
+        void traverse(const LBVH& lbvh, const QueryOpT& query, const OutputOpT& out)
+            {
+            traverse(cudaStream_t(0), lbvh, query, out, SelfOp(), NullTransformOp());
+            }
+
+        // Reference-layout nodes written by the last compression (setup(), or a traversal that
+        // took the reference-layout path without a setup()).
+        const shared_array<int4>& getData() const { return m_data; }
+
+        // ---- additions of this library ----
+
+        // Compression frame of getData(): root lower/upper bounds and bin width (managed float[3]).
+        const float* getFrameLo() const { return reinterpret_cast<const float*>(m_lbvh_lo.get()); }
+        const float* getFrameHi() const { return reinterpret_cast<const float*>(m_lbvh_hi.get()); }
+        const float* getFrameBins() const { return reinterpret_cast<const float*>(m_bins.get()); }
+
+        // Route eligible traversals to the fast kernel (default) or always use the
+        // reference-layout kernel.
+        void setFastPath(bool enabled) { m_fast_enabled = enabled; }
+        bool getFastPath() const { return m_fast_enabled; }
+
+        // Self queries on the fast path: every primitive of the tree queries the tree with cutoff
+        // rc.  Queries run in the tree's sorted order; rows_sorted selects whether row s of the
+        // output belongs to sorted slot s (the reference benchmark's layout) or to the original
+        // primitive index.  OutputOpT is CountNeighborsOp or NeighborListOp.
+        template<class OutputOpT, class TranslateOpT, class TransformOpT>
+        void traverseSelf(const LaunchParameters& params, const LBVH& lbvh, float rc, float3 box,
+                          float pad, const OutputOpT& out, const TranslateOpT& images,
+                          const TransformOpT& transform, bool rows_sorted);
+
+    private:
+        int m_root;
+        shared_array<int4> m_data;
+        shared_array<float3> m_lbvh_lo;
+        shared_array<float3> m_lbvh_hi;
+        shared_array<float3> m_bins;
+        bool m_replay;
+        bool m_fast_enabled;
+
+        template<class TransformOpT>
+        void compress(const LaunchParameters& params, const LBVH& lbvh, const TransformOpT& transform)
+            {
+            checkParameter(params);
+            const unsigned int n = lbvh.getNNodes();
+            if (n > m_data.size())
+                {
+                shared_array<int4> tmp(n);
+                m_data.swap(tmp);
+                }
+            m_root = lbvh.getRoot();
+            const unsigned int bs = params.tunable;
+            gpu::k_compress_ref10<TransformOpT><<<detail::ceil_div(n, bs), bs, 0, params.stream>>>(
+                data(), transform, lbvh.data(), lbvh.getNInternal(), n, lbvh.getStatusPointer());
+            detail::check_cuda(cudaGetLastError(), "compress launch");
+            }
+
+        LBVHCompressedData data()
+            {
+            LBVHCompressedData c;
+            c.root = m_root;
+            c.data = m_data.get();
+            c.lo = m_lbvh_lo.get();
+            c.hi = m_lbvh_hi.get();
+            c.bins = m_bins.get();
+            return c;
+            }
+
+        template<class OutputOpT, class TransformOpT>
+        void launch_fast(const LaunchParameters& params, const LBVH& lbvh, gpu::FastQueryArgs a,
+                         const OutputOpT& out, const TransformOpT& transform, unsigned int Q);
+    };
+
+namespace detail
+{
+template<class T> struct is_float3_images : std::false_type {};
+template<> struct is_float3_images<ImageListOp<float3>> : std::true_type {};
+template<> struct is_float3_images<SelfOp> : std::true_type {};
+
+inline const float3* image_pointer(const SelfOp&) { return nullptr; }
+inline const float3* image_pointer(const ImageListOp<float3>& op) { return op.images; }
+template<class T> inline const float3* image_pointer(const T&) { return nullptr; }
+
+inline void set_output(gpu::FastQueryArgs& a, const CountNeighborsOp& out)
+    {
+    a.nneigh = out.nneigh;
+    a.list = nullptr;
+    a.max_neigh = 0;
+    }
+inline void set_output(gpu::FastQueryArgs& a, const NeighborListOp& out)
+    {
+    a.nneigh = out.nneigh;
+    a.list = out.neigh_list;
+    a.max_neigh = out.max_neigh;
+    }
+} // namespace detail
+
+template<class OutputOpT, class TransformOpT>
+void LBVHTraverser::launch_fast(const LaunchParameters& params, const LBVH& lbvh, gpu::FastQueryArgs a,
+                                const OutputOpT& out, const TransformOpT& transform, unsigned int Q)
+    {
+    detail::set_output(a, out);
+    const unsigned int bs = params.tunable;
+    constexpr int kind = output_kind<OutputOpT>::value;
+    gpu::k_traverse_fast<kind, TransformOpT><<<detail::ceil_div(Q, bs), bs, 0, params.stream>>>(
+        lbvh.fastData(), a, transform);
+    detail::check_cuda(cudaGetLastError(), "fast traversal launch");
+    }
+
+template<class QueryOpT, class OutputOpT, class TranslateOpT, class TransformOpT>
+void LBVHTraverser::traverse(const LaunchParameters& params, const LBVH& lbvh, const QueryOpT& query,
+                             const OutputOpT& out, const TranslateOpT& images, const TransformOpT& transform)
+    {
+    if (lbvh.getN() == 0) return;
+    if (query.size() == 0 || images.size() == 0) return;
+    if (images.size() > 32)
+        throw std::runtime_error("A maximum of 32 image vectors are supported by LBVH traversers.");
+    checkParameter(params);
+
+    if constexpr (std::is_same<QueryOpT, ExactSphereQueryOp>::value && output_kind<OutputOpT>::value != 0
+                  && detail::is_float3_images<TranslateOpT>::value)
+        {
+        if (m_fast_enabled && lbvh.hasFastData())
+            {
+            gpu::FastQueryArgs a;
+            a.spheres = query.spheres;
+            a.Q = query.size();
+            a.self_rc = 0.f;
+            a.self_rows_sorted = 1;
+            a.images = detail::image_pointer(images);
+            a.n_images = images.size();
+            a.box = query.box;
+            a.pad = query.pad;
+            launch_fast(params, lbvh, a, out, transform, query.size());
+            return;
+            }
+        }
+
+    if (!m_replay) compress(params, lbvh, transform);
+    const unsigned int bs = params.tunable;
+    gpu::k_traverse_ref10<OutputOpT, QueryOpT, TranslateOpT>
+        <<<detail::ceil_div(query.size(), bs), bs, 0, params.stream>>>(out, data(), query, images,
+                                                                        lbvh.getStatusPointer());
+    detail::check_cuda(cudaGetLastError(), "traversal launch");
+    }
+
+template<class OutputOpT, class TranslateOpT, class TransformOpT>
+void LBVHTraverser::traverseSelf(const LaunchParameters& params, const LBVH& lbvh, float rc, float3 box,
+                                 float pad, const OutputOpT& out, const TranslateOpT& images,
+                                 const TransformOpT& transform, bool rows_sorted)
+    {
+    static_assert(output_kind<OutputOpT>::value != 0, "traverseSelf needs CountNeighborsOp or NeighborListOp");
+    static_assert(detail::is_float3_images<TranslateOpT>::value, "traverseSelf needs SelfOp or ImageListOp<float3>");
+    if (lbvh.getN() == 0 || images.size() == 0) return;
+    if (images.size() > 32)
+        throw std::runtime_error("A maximum of 32 image vectors are supported by LBVH traversers.");
+    if (!lbvh.hasFastData()) throw std::runtime_error("traverseSelf needs a tree built from points.");
+    checkParameter(params);
+    gpu::FastQueryArgs a;
+    a.spheres = nullptr;
+    a.Q = lbvh.getN();
+    a.self_rc = rc;
+    a.self_rows_sorted = rows_sorted ? 1 : 0;
+    a.images = detail::image_pointer(images);
+    a.n_images = images.size();
+    a.box = box;
+    a.pad = pad;
+    launch_fast(params, lbvh, a, out, transform, lbvh.getN());
+    }
+
+} // namespace neighbor
+
+#endif // NEIGHBOR_LBVH_TRAVERSER_H_

@@ -1,0 +1,175 @@
+// Reference-counted CUDA arrays.
+//
+// shared_array<T> and buffered_array<T> keep the reference's interface
+// (include/neighbor/Memory.h:29-296): shared ownership through copies, get(), size(), host-side
+// operator[] (the storage is CUDA managed memory, so results can be read on the host after a
+// synchronize), a std::runtime_error when allocation fails, and a double buffer whose flip()
+// swaps which half is current.
+//
+// device_array<T> is new: plain device memory for internal buffers that the host never indexes
+// (sort ping-pong buffers, scan state, compressed nodes).  It grows and never shrinks.
+#ifndef NEIGHBOR_MEMORY_H_
+#define NEIGHBOR_MEMORY_H_
+
+#include <cstddef>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <utility>
+
+#include <cuda_runtime.h>
+
+namespace neighbor
+{
+
+template<typename T>
+class shared_array
+    {
+    public:
+        shared_array() : size_(0) {}
+
+        explicit shared_array(size_t count) : size_(0) { allocate(count); }
+
+        shared_array(const shared_array& other) = default;
+        shared_array& operator=(const shared_array& other) = default;
+
+        shared_array(shared_array&& other) noexcept
+            : data_(std::move(other.data_)), size_(other.size_)
+            {
+            other.size_ = 0;
+            }
+
+        shared_array& operator=(shared_array&& other) noexcept
+            {
+            if (this != &other)
+                {
+                data_ = std::move(other.data_);
+                size_ = other.size_;
+                other.size_ = 0;
+                }
+            return *this;
+            }
+
+        void swap(shared_array& other)
+            {
+            std::swap(data_, other.data_);
+            std::swap(size_, other.size_);
+            }
+
+        T& operator[](size_t idx) { return data_.get()[idx]; }
+        const T& operator[](size_t idx) const { return data_.get()[idx]; }
+
+        T* get() { return data_.get(); }
+        const T* get() const { return data_.get(); }
+
+        size_t size() const { return size_; }
+
+    private:
+        std::shared_ptr<T> data_;
+        size_t size_;
+
+        struct deleter
+            {
+            void operator()(T* ptr) const
+                {
+                if (ptr) cudaFree(ptr);
+                }
+            };
+
+        void allocate(size_t count)
+            {
+            if (count == 0)
+                {
+                data_.reset();
+                size_ = 0;
+                return;
+                }
+            T* ptr = nullptr;
+            const cudaError_t code = cudaMallocManaged(reinterpret_cast<void**>(&ptr), count * sizeof(T));
+            if (code != cudaSuccess)
+                {
+                (void)cudaGetLastError();
+                data_.reset();
+                size_ = 0;
+                throw std::runtime_error(std::string("Error allocating managed memory: ")
+                                         + cudaGetErrorString(code));
+                }
+            data_ = std::shared_ptr<T>(ptr, deleter());
+            size_ = count;
+            }
+    };
+
+template<typename T>
+class buffered_array
+    {
+    public:
+        buffered_array() : selector_(0) {}
+        explicit buffered_array(size_t count) : x_(count), y_(count), selector_(0) {}
+
+        void swap(buffered_array& other)
+            {
+            x_.swap(other.x_);
+            y_.swap(other.y_);
+            std::swap(selector_, other.selector_);
+            }
+
+        shared_array<T>& current() { return selector_ == 0 ? x_ : y_; }
+        const shared_array<T>& current() const { return selector_ == 0 ? x_ : y_; }
+        shared_array<T>& alternate() { return selector_ == 0 ? y_ : x_; }
+        const shared_array<T>& alternate() const { return selector_ == 0 ? y_ : x_; }
+
+        void flip() { selector_ ^= 1; }
+
+        size_t size() const { return x_.size(); }
+
+    private:
+        shared_array<T> x_;
+        shared_array<T> y_;
+        int selector_;
+    };
+
+// Device-only growable buffer.
+template<typename T>
+class device_array
+    {
+    public:
+        device_array() : ptr_(nullptr), size_(0) {}
+        ~device_array() { release(); }
+        device_array(const device_array&) = delete;
+        device_array& operator=(const device_array&) = delete;
+
+        // Ensure room for count elements; contents are not preserved when it grows.
+        void reserve(size_t count)
+            {
+            if (count <= size_) return;
+            release();
+            T* p = nullptr;
+            const cudaError_t code = cudaMalloc(reinterpret_cast<void**>(&p), count * sizeof(T));
+            if (code != cudaSuccess)
+                {
+                (void)cudaGetLastError();
+                throw std::runtime_error(std::string("Error allocating device memory: ")
+                                         + cudaGetErrorString(code));
+                }
+            ptr_ = p;
+            size_ = count;
+            }
+
+        T* get() { return ptr_; }
+        const T* get() const { return ptr_; }
+        size_t size() const { return size_; }
+
+    private:
+        T* ptr_;
+        size_t size_;
+        void release()
+            {
+            if (ptr_) cudaFree(ptr_);
+            ptr_ = nullptr;
+            size_ = 0;
+            }
+    };
+
+} // namespace neighbor
+
+#endif // NEIGHBOR_MEMORY_H_

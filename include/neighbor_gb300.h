@@ -1,0 +1,149 @@
+/*
+ * neighbor_gb300.h -- C ABI of the GB300 LBVH neighbor-search library.
+ *
+ * The reference (mphowardlab/neighbor) is a header-only C++ template library with no C ABI of
+ * its own; its callers instantiate LBVH::build / LBVHTraverser::traverse with concrete ops.  This
+ * header exports those instantiations as plain functions over device pointers, so a host program
+ * in any language can bind them (ctypes, cgo, JNI, ...).  Each declaration names the reference
+ * interface it stands for.  The C++ template API in include/neighbor/ stays available for custom
+ * ops.
+ *
+ * Conventions
+ *   - All array arguments are device (or managed) pointers; float3 arrays are float[3*n], float4
+ *     arrays float[4*n].  `stream` is a cudaStream_t (NULL = legacy default stream).
+ *   - Work is enqueued asynchronously on `stream`; results are valid after the stream completes.
+ *   - Every function returns NBR_OK (0) or an error code; nbr_last_error() gives the message of
+ *     the last failure on the calling thread.  No C++ exception crosses this boundary.
+ *   - block_size is the reference's tunable launch parameter (32..1024, step 32).
+ */
+#ifndef NEIGHBOR_GB300_H_
+#define NEIGHBOR_GB300_H_
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NBR_OK 0
+#define NBR_ERR_INVALID 1     /* bad handle/argument, > 32 images, invalid tunable */
+#define NBR_ERR_CUDA 2        /* CUDA runtime error */
+#define NBR_ERR_ALLOC 3       /* allocation failed (reference: Memory.h:182-186 throws) */
+#define NBR_ERR_DEVICE_WAIT 4 /* a bounded device wait gave up (see nbr_lbvh_check_status) */
+#define NBR_ERR_UNSUPPORTED 5
+
+#define NBR_QUERY_SPHERE 0 /* SphereQueryOp, include/neighbor/QueryOps.h:32-120 (superset) */
+#define NBR_QUERY_EXACT 1  /* ExactSphereQueryOp: FP32 minimum-image predicate (exact set) */
+
+typedef struct nbr_lbvh_s* nbr_lbvh;
+typedef struct nbr_traverser_s* nbr_traverser;
+
+/* Message of the last failed call on this thread ("" if none). */
+const char* nbr_last_error(void);
+
+/* Library version (major, minor). */
+int nbr_version(int* major, int* minor);
+
+/* ---- LBVH (reference: class LBVH, include/neighbor/LBVH.h:47-219) ---- */
+
+/* LBVH::LBVH() (LBVH.h:224-227) / destructor. */
+int nbr_lbvh_create(nbr_lbvh* out);
+int nbr_lbvh_destroy(nbr_lbvh h);
+
+/* Additions: leaf bucket size of the traversal tree (1..64) and sort digit width (8 or 10). */
+int nbr_lbvh_set_leaf_size(nbr_lbvh h, unsigned int leaf_size);
+int nbr_lbvh_set_radix_bits(nbr_lbvh h, unsigned int bits);
+
+/* LBVH::build(LaunchParameters, PointInsertOp, lo, hi) (LBVH.h:242-318, InsertOps.h:18-54).
+ * points: float3[N]; lo/hi: scene bounds for Morton binning (host float[3]). */
+int nbr_lbvh_build_points(nbr_lbvh h, const float* points, unsigned int N, const float lo[3],
+                          const float hi[3], unsigned int block_size, void* stream);
+
+/* LBVH::build(LaunchParameters, SphereInsertOp, lo, hi) (InsertOps.h:57-96). */
+int nbr_lbvh_build_spheres(nbr_lbvh h, const float* points, float radius, unsigned int N,
+                           const float lo[3], const float hi[3], unsigned int block_size,
+                           void* stream);
+
+/* getRoot/getN/getNInternal/getNNodes (LBVH.h:111-133). */
+int nbr_lbvh_get_sizes(nbr_lbvh h, int* root, unsigned int* N, unsigned int* n_internal,
+                       unsigned int* n_nodes);
+
+/* getParents/getLeftChildren/getRightChildren/getPrimitives/getLowerBounds/getUpperBounds
+ * (LBVH.h:135-169): managed pointers, host-readable after the build's stream completes.
+ * Any output pointer may be NULL. */
+int nbr_lbvh_get_arrays(nbr_lbvh h, const int** parent, const int** left, const int** right,
+                        const unsigned int** primitive, const float** lo, const float** hi);
+
+/* Addition: sorted Morton codes of the last build (managed pointer). */
+int nbr_lbvh_get_codes(nbr_lbvh h, const unsigned int** codes);
+
+/* Addition: the 16-bit pre-order traversal tree (device pointers): nodes uint32[4*n],
+ * points float4[N] (x, y, z, primitive id bits), frame float[9] (root lo, root hi, scale). */
+int nbr_lbvh_get_fast(nbr_lbvh h, const unsigned int** nodes, const float** points,
+                      const float** frame, unsigned int* count_bits, unsigned int* leaf_size);
+
+/* Addition: number of live traversal nodes (synchronises `stream`). */
+int nbr_lbvh_num_fast_nodes(nbr_lbvh h, unsigned int* n, void* stream);
+
+/* Addition: synchronise `stream` and report NBR_ERR_DEVICE_WAIT if a bounded wait of the last
+ * build gave up. */
+int nbr_lbvh_check_status(nbr_lbvh h, void* stream);
+
+/* ---- LBVHTraverser (reference: include/neighbor/LBVHTraverser.h:60-355) ---- */
+
+int nbr_traverser_create(nbr_traverser* out);
+int nbr_traverser_destroy(nbr_traverser t);
+
+/* LBVHTraverser::setup(params, lbvh[, MapTransformOp]) (LBVHTraverser.h:378-390).
+ * map: uint32[N] device array or NULL (NullTransformOp). */
+int nbr_traverser_setup(nbr_traverser t, nbr_lbvh h, const unsigned int* map,
+                        unsigned int block_size, void* stream);
+
+/* LBVHTraverser::reset() (LBVHTraverser.h:135-138). */
+int nbr_traverser_reset(nbr_traverser t);
+
+/* Addition: 0 = always use the reference-layout kernel, 1 = route eligible traversals to the
+ * fast kernel (default). */
+int nbr_traverser_set_fast_path(nbr_traverser t, int enabled);
+
+/* getData() (LBVHTraverser.h:326-329): int4 nodes in the reference's 10-bit layout (managed),
+ * plus the compression frame (lo, hi, bins: managed float[3] each). */
+int nbr_traverser_get_data(nbr_traverser t, const int** data, const float** lo, const float** hi,
+                           const float** bins);
+
+/* LBVHTraverser::traverse(params, lbvh, query, out, images, transform) (LBVHTraverser.h:414-450)
+ * with query = SphereQueryOp or ExactSphereQueryOp (query_kind), out = CountNeighborsOp when
+ * list == NULL else NeighborListOp(list, nneigh, max_neigh) (OutputOps.h:28-176),
+ * images = SelfOp when images == NULL else ImageListOp<float3> (TranslateOps.h:19-91),
+ * transform = NullTransformOp when map == NULL else MapTransformOp (TransformOps.h:25-64).
+ *   spheres: float4[Q] (x, y, z, radius or cutoff)
+ *   points, box, pad: used by the exact query only (positions indexed by the reported id,
+ *   periodic box lengths with 0 = open, radius padding -- see nbr_exact_pad). */
+int nbr_traverse(nbr_traverser t, nbr_lbvh h, int query_kind, const float* spheres, unsigned int Q,
+                 const float* points, const float box[3], float pad, const float* images,
+                 unsigned int n_images, const unsigned int* map, unsigned int* nneigh,
+                 unsigned int* list, unsigned int max_neigh, unsigned int block_size, void* stream);
+
+/* Addition: every primitive of a point tree queries the tree with cutoff rc (exact predicate).
+ * Queries run in the tree's sorted order; rows_sorted = 1 writes row s for sorted slot s (the
+ * layout the reference benchmark uses, benchmark/lbvh_benchmark.cc:177-184), 0 writes row
+ * primitive[s].  list == NULL => counts only. */
+int nbr_traverse_self(nbr_traverser t, nbr_lbvh h, float rc, const float box[3], float pad,
+                      const float* images, unsigned int n_images, const unsigned int* map,
+                      unsigned int* nneigh, unsigned int* list, unsigned int max_neigh,
+                      int rows_sorted, unsigned int block_size, void* stream);
+
+/* Test hook for failure detection (no counterpart in the reference): runs the chained scan
+ * used by the build with its first tile never published, so the look-back of the next tile must
+ * give up after its bounded wait (about a second) instead of hanging.  Writes the resulting
+ * device status word (expected: 2, scan look-back gave up) and returns NBR_OK when the wait
+ * ended, the kernels finished and the context is still usable. */
+int nbr_debug_wait_timeout(unsigned int* status_out, void* stream);
+
+/* Radius padding for the exact query: 16 ulps of twice the largest coordinate magnitude
+ * (centres, points and image translations) plus 1e-6 * rc. */
+float nbr_exact_pad(float rc, float coord_max);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NEIGHBOR_GB300_H_ */

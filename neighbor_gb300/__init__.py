@@ -1,0 +1,406 @@
+"""neighbor_gb300: LBVH neighbor search on NVIDIA GB300 (sm_103a).
+
+Python mirror of the library's C ABI (include/neighbor_gb300.h), which exports the C++ template
+API in include/neighbor/ (LBVH, LBVHTraverser and the insert / query / output / translate /
+transform ops of mphowardlab/neighbor).  Arrays are torch CUDA tensors; every call is enqueued on
+the current torch stream unless a stream is passed.
+
+There is no CPU fallback: if the CUDA library has not been built, or no GPU is present, the
+calls raise.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+from typing import Optional, Sequence
+
+from . import _build
+
+__all__ = ["LBVH", "LBVHTraverser", "NeighborError", "load", "build", "exact_pad", "images27",
+           "QUERY_SPHERE", "QUERY_EXACT", "SENTINEL"]
+
+QUERY_SPHERE = 0
+QUERY_EXACT = 1
+SENTINEL = 0x7FFFFFFF
+
+NBR_OK = 0
+_ERRORS = {1: "invalid argument", 2: "CUDA error", 3: "allocation failed",
+           4: "bounded device wait gave up", 5: "unsupported"}
+
+
+class NeighborError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{_ERRORS.get(code, 'error')} ({code}): {msg}")
+        self.code = code
+
+
+_lib = None
+_lock = threading.Lock()
+
+
+def build(force: bool = False, verbose: bool = False) -> str:
+    """Compile the CUDA library in-tree (nvcc, sm_103a)."""
+    return _build.build(force=force, verbose=verbose)
+
+
+def library_path() -> str:
+    return _build.LIB_PATH
+
+
+def load() -> ctypes.CDLL:
+    """Load libneighbor_gb300.so; raises if it is missing (no fallback path exists)."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(_build.LIB_PATH):
+                raise RuntimeError("neighbor_gb300 CUDA library is not built "
+                                   f"({_build.LIB_PATH}); run neighbor_gb300.build()")
+            L = ctypes.CDLL(_build.LIB_PATH)
+            _declare(L)
+            _lib = L
+    return _lib
+
+
+_P = ctypes.c_void_p
+_U = ctypes.c_uint
+_I = ctypes.c_int
+_F = ctypes.c_float
+_PP = ctypes.POINTER(ctypes.c_void_p)
+
+
+def _declare(L):
+    def sig(name, args, res=ctypes.c_int):
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = res
+    sig("nbr_last_error", [], ctypes.c_char_p)
+    sig("nbr_version", [ctypes.POINTER(_I), ctypes.POINTER(_I)])
+    sig("nbr_lbvh_create", [_PP])
+    sig("nbr_lbvh_destroy", [_P])
+    sig("nbr_lbvh_set_leaf_size", [_P, _U])
+    sig("nbr_lbvh_set_radix_bits", [_P, _U])
+    sig("nbr_lbvh_build_points", [_P, _P, _U, _P, _P, _U, _P])
+    sig("nbr_lbvh_build_spheres", [_P, _P, _F, _U, _P, _P, _U, _P])
+    sig("nbr_lbvh_get_sizes", [_P, ctypes.POINTER(_I), ctypes.POINTER(_U), ctypes.POINTER(_U),
+                               ctypes.POINTER(_U)])
+    sig("nbr_lbvh_get_arrays", [_P, _PP, _PP, _PP, _PP, _PP, _PP])
+    sig("nbr_lbvh_get_codes", [_P, _PP])
+    sig("nbr_lbvh_get_fast", [_P, _PP, _PP, _PP, ctypes.POINTER(_U), ctypes.POINTER(_U)])
+    sig("nbr_lbvh_num_fast_nodes", [_P, ctypes.POINTER(_U), _P])
+    sig("nbr_lbvh_check_status", [_P, _P])
+    sig("nbr_traverser_create", [_PP])
+    sig("nbr_traverser_destroy", [_P])
+    sig("nbr_traverser_setup", [_P, _P, _P, _U, _P])
+    sig("nbr_traverser_reset", [_P])
+    sig("nbr_traverser_set_fast_path", [_P, _I])
+    sig("nbr_traverser_get_data", [_P, _PP, _PP, _PP, _PP])
+    sig("nbr_traverse", [_P, _P, _I, _P, _U, _P, _P, _F, _P, _U, _P, _P, _P, _U, _U, _P])
+    sig("nbr_traverse_self", [_P, _P, _F, _P, _F, _P, _U, _P, _P, _P, _U, _I, _U, _P])
+    sig("nbr_exact_pad", [_F, _F], _F)
+    sig("nbr_debug_wait_timeout", [ctypes.POINTER(_U), _P])
+
+
+# C-ABI symbols declared in include/neighbor_gb300.h (checked by the CPU tests).
+EXPORTED = ["nbr_last_error", "nbr_version", "nbr_lbvh_create", "nbr_lbvh_destroy",
+            "nbr_lbvh_set_leaf_size", "nbr_lbvh_set_radix_bits", "nbr_lbvh_build_points",
+            "nbr_lbvh_build_spheres", "nbr_lbvh_get_sizes", "nbr_lbvh_get_arrays",
+            "nbr_lbvh_get_codes", "nbr_lbvh_get_fast", "nbr_lbvh_num_fast_nodes",
+            "nbr_lbvh_check_status", "nbr_traverser_create", "nbr_traverser_destroy",
+            "nbr_traverser_setup", "nbr_traverser_reset", "nbr_traverser_set_fast_path",
+            "nbr_traverser_get_data", "nbr_traverse", "nbr_traverse_self", "nbr_exact_pad",
+            "nbr_debug_wait_timeout"]
+
+
+def _check(rc: int):
+    if rc != NBR_OK:
+        msg = load().nbr_last_error()
+        raise NeighborError(rc, msg.decode() if msg else "")
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _stream_ptr(stream) -> Optional[int]:
+    torch = _torch()
+    if stream is None:
+        stream = torch.cuda.current_stream()
+    if isinstance(stream, int):
+        return stream or None
+    return stream.cuda_stream or None
+
+
+def _dev(t, dtype, shape_last=None):
+    """Validate a CUDA tensor argument and return it contiguous."""
+    torch = _torch()
+    if not isinstance(t, torch.Tensor) or not t.is_cuda:
+        raise TypeError("expected a CUDA tensor")
+    if t.dtype != dtype:
+        raise TypeError(f"expected dtype {dtype}, got {t.dtype}")
+    if shape_last is not None and (t.dim() != 2 or t.shape[1] != shape_last):
+        raise ValueError(f"expected shape [n, {shape_last}], got {tuple(t.shape)}")
+    return t.contiguous()
+
+
+def _ptr(t) -> Optional[int]:
+    return None if t is None else t.data_ptr()
+
+
+def _f3(v) -> ctypes.Array:
+    a = (ctypes.c_float * 3)(*[float(x) for x in v])
+    return a
+
+
+class _DeviceView:
+    """Non-owning __cuda_array_interface__ over a device or managed pointer."""
+
+    def __init__(self, ptr: int, shape, typestr: str):
+        self.__cuda_array_interface__ = {"shape": tuple(shape), "typestr": typestr,
+                                         "data": (int(ptr), False), "version": 3, "strides": None}
+
+
+def _view(ptr, shape, typestr, dtype):
+    torch = _torch()
+    n = 1
+    for s in shape:
+        n *= s
+    if n == 0 or not ptr:
+        return torch.empty(shape, dtype=dtype, device="cuda")
+    return torch.as_tensor(_DeviceView(ptr, shape, typestr), device="cuda")
+
+
+def exact_pad(rc: float, coord_max: float) -> float:
+    """Radius padding of the exact query (16 ulps of 2*coord_max plus 1e-6*rc)."""
+    return float(load().nbr_exact_pad(float(rc), float(coord_max)))
+
+
+def debug_wait_timeout(stream=None) -> int:
+    """Run the scan with a tile that is never published; returns the device status word."""
+    st = ctypes.c_uint()
+    _check(load().nbr_debug_wait_timeout(ctypes.byref(st), _stream_ptr(stream)))
+    return st.value
+
+
+def images27(L: Sequence[float], device="cuda"):
+    """27 periodic image vectors, ix/iy/iz in -1..1 with iz fastest."""
+    torch = _torch()
+    out = []
+    for ix in (-1, 0, 1):
+        for iy in (-1, 0, 1):
+            for iz in (-1, 0, 1):
+                out.append([float(L[0]) * ix, float(L[1]) * iy, float(L[2]) * iz])
+    return torch.tensor(out, dtype=torch.float32, device=device)
+
+
+class LBVH:
+    """neighbor::LBVH (include/neighbor/LBVH.h) through the C ABI."""
+
+    def __init__(self, leaf_size: Optional[int] = None, radix_bits: Optional[int] = None):
+        L = load()
+        h = ctypes.c_void_p()
+        _check(L.nbr_lbvh_create(ctypes.byref(h)))
+        self._h = h
+        self._L = L
+        if leaf_size is not None:
+            self.set_leaf_size(leaf_size)
+        if radix_bits is not None:
+            self.set_radix_bits(radix_bits)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                self._L.nbr_lbvh_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_leaf_size(self, n: int):
+        _check(self._L.nbr_lbvh_set_leaf_size(self._h, int(n)))
+
+    def set_radix_bits(self, bits: int):
+        _check(self._L.nbr_lbvh_set_radix_bits(self._h, int(bits)))
+
+    def build(self, points, lo, hi, radius: Optional[float] = None, block_size: int = 32,
+              stream=None):
+        """LBVH::build with PointInsertOp (radius None) or SphereInsertOp(radius)."""
+        p = _dev(points, _torch().float32, 3)
+        self._points = p  # keep the input alive while the build is in flight
+        n = p.shape[0]
+        s = _stream_ptr(stream)
+        if radius is None:
+            _check(self._L.nbr_lbvh_build_points(self._h, _ptr(p), n, _f3(lo), _f3(hi), block_size, s))
+        else:
+            _check(self._L.nbr_lbvh_build_spheres(self._h, _ptr(p), float(radius), n, _f3(lo),
+                                                  _f3(hi), block_size, s))
+        return self
+
+    def sizes(self):
+        root, N, ni, nn = ctypes.c_int(), ctypes.c_uint(), ctypes.c_uint(), ctypes.c_uint()
+        _check(self._L.nbr_lbvh_get_sizes(self._h, ctypes.byref(root), ctypes.byref(N),
+                                          ctypes.byref(ni), ctypes.byref(nn)))
+        return root.value, N.value, ni.value, nn.value
+
+    def getRoot(self):
+        return self.sizes()[0]
+
+    def getN(self):
+        return self.sizes()[1]
+
+    def getNInternal(self):
+        return self.sizes()[2]
+
+    def getNNodes(self):
+        return self.sizes()[3]
+
+    def _arrays(self):
+        ptrs = [ctypes.c_void_p() for _ in range(6)]
+        _check(self._L.nbr_lbvh_get_arrays(self._h, *[ctypes.byref(p) for p in ptrs]))
+        return [p.value for p in ptrs]
+
+    def arrays(self):
+        """Copies of parent, left, right, primitive, lo, hi (reference layout) as CUDA tensors."""
+        torch = _torch()
+        _, N, ni, nn = self.sizes()
+        par, lft, rgt, prim, lo, hi = self._arrays()
+        return dict(
+            parent=_view(par, (nn,), "<i4", torch.int32).clone(),
+            left=_view(lft, (ni,), "<i4", torch.int32).clone(),
+            right=_view(rgt, (ni,), "<i4", torch.int32).clone(),
+            primitive=_view(prim, (N,), "<u4", torch.int32).clone(),
+            lo=_view(lo, (nn, 3), "<f4", torch.float32).clone(),
+            hi=_view(hi, (nn, 3), "<f4", torch.float32).clone(),
+        )
+
+    def primitives(self):
+        torch = _torch()
+        _, N, _, _ = self.sizes()
+        return _view(self._arrays()[3], (N,), "<u4", torch.int32)
+
+    def codes(self):
+        torch = _torch()
+        _, N, _, _ = self.sizes()
+        p = ctypes.c_void_p()
+        _check(self._L.nbr_lbvh_get_codes(self._h, ctypes.byref(p)))
+        return _view(p.value, (N,), "<u4", torch.int32).clone()
+
+    def num_fast_nodes(self, stream=None) -> int:
+        n = ctypes.c_uint()
+        _check(self._L.nbr_lbvh_num_fast_nodes(self._h, ctypes.byref(n), _stream_ptr(stream)))
+        return n.value
+
+    def fast(self, stream=None):
+        """Copies of the 16-bit pre-order nodes, the sorted payload and the frame."""
+        torch = _torch()
+        n = self.num_fast_nodes(stream)
+        nodes, pts, frame = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
+        cb, ls = ctypes.c_uint(), ctypes.c_uint()
+        _check(self._L.nbr_lbvh_get_fast(self._h, ctypes.byref(nodes), ctypes.byref(pts),
+                                         ctypes.byref(frame), ctypes.byref(cb), ctypes.byref(ls)))
+        _, N, _, _ = self.sizes()
+        return dict(nodes=_view(nodes.value, (n, 4), "<u4", torch.int32).clone(),
+                    points=_view(pts.value, (N, 4), "<f4", torch.float32).clone(),
+                    frame=_view(frame.value, (9,), "<f4", torch.float32).clone(),
+                    count_bits=cb.value, leaf_size=ls.value)
+
+    def check_status(self, stream=None):
+        _check(self._L.nbr_lbvh_check_status(self._h, _stream_ptr(stream)))
+
+
+class LBVHTraverser:
+    """neighbor::LBVHTraverser (include/neighbor/LBVHTraverser.h) through the C ABI."""
+
+    def __init__(self):
+        L = load()
+        h = ctypes.c_void_p()
+        _check(L.nbr_traverser_create(ctypes.byref(h)))
+        self._h = h
+        self._L = L
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                self._L.nbr_traverser_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    def setup(self, lbvh: LBVH, map=None, block_size: int = 32, stream=None):
+        m = None if map is None else _dev(map, _torch().int32)
+        _check(self._L.nbr_traverser_setup(self._h, lbvh.handle, _ptr(m), block_size,
+                                           _stream_ptr(stream)))
+
+    def reset(self):
+        _check(self._L.nbr_traverser_reset(self._h))
+
+    def set_fast_path(self, enabled: bool):
+        _check(self._L.nbr_traverser_set_fast_path(self._h, 1 if enabled else 0))
+
+    def get_data(self, lbvh: LBVH):
+        """Copy of getData() (int4 reference-layout nodes) and the compression frame."""
+        torch = _torch()
+        d, lo, hi, bins = (ctypes.c_void_p() for _ in range(4))
+        _check(self._L.nbr_traverser_get_data(self._h, ctypes.byref(d), ctypes.byref(lo),
+                                              ctypes.byref(hi), ctypes.byref(bins)))
+        nn = lbvh.getNNodes()
+        return dict(data=_view(d.value, (nn, 4), "<i4", torch.int32).clone(),
+                    lo=_view(lo.value, (3,), "<f4", torch.float32).clone(),
+                    hi=_view(hi.value, (3,), "<f4", torch.float32).clone(),
+                    bins=_view(bins.value, (3,), "<f4", torch.float32).clone())
+
+    def traverse(self, lbvh: LBVH, spheres, query: int = QUERY_SPHERE, points=None, box=None,
+                 pad: float = 0.0, images=None, map=None, max_neigh: Optional[int] = None,
+                 nneigh=None, neigh_list=None, block_size: int = 32, stream=None):
+        """LBVHTraverser::traverse with Count (max_neigh None) or NeighborList output.
+
+        Returns nneigh, or (nneigh, list[Q, max_neigh])."""
+        torch = _torch()
+        sph = _dev(spheres, torch.float32, 4)
+        Q = sph.shape[0]
+        pts = None if points is None else _dev(points, torch.float32, 3)
+        img = None if images is None else _dev(images, torch.float32, 3)
+        m = None if map is None else _dev(map, torch.int32)
+        if nneigh is None:
+            nneigh = torch.empty(Q, dtype=torch.int32, device=sph.device)
+        lst = neigh_list
+        if max_neigh is not None and lst is None:
+            lst = torch.full((Q, max(max_neigh, 1)), -1, dtype=torch.int32, device=sph.device)
+        b = _f3(box if box is not None else (0.0, 0.0, 0.0))
+        _check(self._L.nbr_traverse(self._h, lbvh.handle, int(query), _ptr(sph), Q, _ptr(pts), b,
+                                    float(pad), _ptr(img), 0 if img is None else img.shape[0],
+                                    _ptr(m), _ptr(nneigh), _ptr(lst),
+                                    0 if max_neigh is None else int(max_neigh), block_size,
+                                    _stream_ptr(stream)))
+        if max_neigh is None:
+            return nneigh
+        return nneigh, lst
+
+    def traverse_self(self, lbvh: LBVH, rc: float, box, pad: float, images=None, map=None,
+                      max_neigh: Optional[int] = None, rows_sorted: bool = True, nneigh=None,
+                      neigh_list=None, block_size: int = 256, stream=None):
+        """Every primitive of a point tree queries the tree (exact predicate, fast path)."""
+        torch = _torch()
+        _, N, _, _ = lbvh.sizes()
+        img = None if images is None else _dev(images, torch.float32, 3)
+        m = None if map is None else _dev(map, torch.int32)
+        if nneigh is None:
+            nneigh = torch.empty(N, dtype=torch.int32, device="cuda")
+        lst = neigh_list
+        if max_neigh is not None and lst is None:
+            lst = torch.full((N, max(max_neigh, 1)), -1, dtype=torch.int32, device="cuda")
+        _check(self._L.nbr_traverse_self(self._h, lbvh.handle, float(rc), _f3(box), float(pad),
+                                         _ptr(img), 0 if img is None else img.shape[0], _ptr(m),
+                                         _ptr(nneigh), _ptr(lst),
+                                         0 if max_neigh is None else int(max_neigh),
+                                         1 if rows_sorted else 0, block_size,
+                                         _stream_ptr(stream)))
+        if max_neigh is None:
+            return nneigh
+        return nneigh, lst

@@ -1,0 +1,378 @@
+// C ABI over concrete instantiations of the neighbor C++ templates (include/neighbor_gb300.h).
+#include <cstring>
+#include <exception>
+#include <new>
+#include <stdexcept>
+#include <string>
+
+#include <cuda_runtime.h>
+
+#include "neighbor/neighbor.h"
+#include "neighbor_gb300.h"
+
+struct nbr_lbvh_s
+    {
+    neighbor::LBVH lbvh;
+    };
+
+struct nbr_traverser_s
+    {
+    neighbor::LBVHTraverser trav;
+    };
+
+namespace
+{
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg)
+    {
+    g_last_error = msg;
+    return code;
+    }
+
+// Map an exception from the C++ layer to a status code.
+int from_exception(const std::exception& e)
+    {
+    const std::string m = e.what();
+    if (m.find("allocating") != std::string::npos) return fail(NBR_ERR_ALLOC, m);
+    if (m.find("bounded device wait") != std::string::npos) return fail(NBR_ERR_DEVICE_WAIT, m);
+    if (m.find("Invalid tuning") != std::string::npos || m.find("maximum of 32") != std::string::npos
+        || m.find("must be") != std::string::npos)
+        return fail(NBR_ERR_INVALID, m);
+    return fail(NBR_ERR_CUDA, m);
+    }
+
+template<class F>
+int guarded(F&& f)
+    {
+    try
+        {
+        f();
+        g_last_error.clear();
+        return NBR_OK;
+        }
+    catch (const std::bad_alloc&)
+        {
+        return fail(NBR_ERR_ALLOC, "host allocation failed");
+        }
+    catch (const std::exception& e)
+        {
+        return from_exception(e);
+        }
+    catch (...)
+        {
+        return fail(NBR_ERR_CUDA, "unknown error");
+        }
+    }
+
+inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+inline float3 f3(const float v[3]) { return make_float3(v[0], v[1], v[2]); }
+
+bool valid_block(unsigned int bs) { return bs >= 32 && bs <= 1024 && bs % 32 == 0; }
+
+template<class OutputOpT, class TransformOpT>
+void dispatch_images(neighbor::LBVHTraverser& t, const neighbor::LBVH& h,
+                     const neighbor::LBVHTraverser::LaunchParameters& p, int query_kind,
+                     const float* spheres, unsigned int Q, const float* points, float3 box, float pad,
+                     const float* images, unsigned int n_images, const OutputOpT& out,
+                     const TransformOpT& transform)
+    {
+    if (query_kind == NBR_QUERY_SPHERE)
+        {
+        neighbor::SphereQueryOp q(reinterpret_cast<float4*>(const_cast<float*>(spheres)), Q);
+        if (images)
+            t.traverse(p, h, q, out, neighbor::ImageListOp<float3>(reinterpret_cast<const float3*>(images), n_images), transform);
+        else
+            t.traverse(p, h, q, out, neighbor::SelfOp(), transform);
+        }
+    else
+        {
+        neighbor::ExactSphereQueryOp q(reinterpret_cast<const float4*>(spheres), Q,
+                                       reinterpret_cast<const float3*>(points), box, pad);
+        if (images)
+            t.traverse(p, h, q, out, neighbor::ImageListOp<float3>(reinterpret_cast<const float3*>(images), n_images), transform);
+        else
+            t.traverse(p, h, q, out, neighbor::SelfOp(), transform);
+        }
+    }
+
+template<class OutputOpT>
+void dispatch_transform(neighbor::LBVHTraverser& t, const neighbor::LBVH& h,
+                        const neighbor::LBVHTraverser::LaunchParameters& p, int query_kind,
+                        const float* spheres, unsigned int Q, const float* points, float3 box, float pad,
+                        const float* images, unsigned int n_images, const unsigned int* map,
+                        const OutputOpT& out)
+    {
+    if (map)
+        dispatch_images(t, h, p, query_kind, spheres, Q, points, box, pad, images, n_images, out,
+                        neighbor::MapTransformOp(map));
+    else
+        dispatch_images(t, h, p, query_kind, spheres, Q, points, box, pad, images, n_images, out,
+                        neighbor::NullTransformOp());
+    }
+
+template<class OutputOpT>
+void self_transform(neighbor::LBVHTraverser& t, const neighbor::LBVH& h,
+                    const neighbor::LBVHTraverser::LaunchParameters& p, float rc, float3 box, float pad,
+                    const float* images, unsigned int n_images, const unsigned int* map,
+                    const OutputOpT& out, bool rows_sorted)
+    {
+    if (images)
+        {
+        neighbor::ImageListOp<float3> img(reinterpret_cast<const float3*>(images), n_images);
+        if (map)
+            t.traverseSelf(p, h, rc, box, pad, out, img, neighbor::MapTransformOp(map), rows_sorted);
+        else
+            t.traverseSelf(p, h, rc, box, pad, out, img, neighbor::NullTransformOp(), rows_sorted);
+        }
+    else
+        {
+        if (map)
+            t.traverseSelf(p, h, rc, box, pad, out, neighbor::SelfOp(), neighbor::MapTransformOp(map), rows_sorted);
+        else
+            t.traverseSelf(p, h, rc, box, pad, out, neighbor::SelfOp(), neighbor::NullTransformOp(), rows_sorted);
+        }
+    }
+} // namespace
+
+extern "C" {
+
+const char* nbr_last_error(void) { return g_last_error.c_str(); }
+
+int nbr_version(int* major, int* minor)
+    {
+    if (major) *major = 0;
+    if (minor) *minor = 1;
+    return NBR_OK;
+    }
+
+int nbr_lbvh_create(nbr_lbvh* out)
+    {
+    if (!out) return fail(NBR_ERR_INVALID, "null output handle");
+    return guarded([&] { *out = new nbr_lbvh_s(); });
+    }
+
+int nbr_lbvh_destroy(nbr_lbvh h)
+    {
+    return guarded([&] { delete h; });
+    }
+
+int nbr_lbvh_set_leaf_size(nbr_lbvh h, unsigned int leaf_size)
+    {
+    if (!h) return fail(NBR_ERR_INVALID, "null handle");
+    return guarded([&] { h->lbvh.setLeafSize(leaf_size); });
+    }
+
+int nbr_lbvh_set_radix_bits(nbr_lbvh h, unsigned int bits)
+    {
+    if (!h) return fail(NBR_ERR_INVALID, "null handle");
+    return guarded([&] { h->lbvh.setRadixBits(bits); });
+    }
+
+int nbr_lbvh_build_points(nbr_lbvh h, const float* points, unsigned int N, const float lo[3],
+                          const float hi[3], unsigned int block_size, void* stream)
+    {
+    if (!h || !lo || !hi || (N > 0 && !points)) return fail(NBR_ERR_INVALID, "null argument");
+    if (!valid_block(block_size)) return fail(NBR_ERR_INVALID, "Invalid tuning parameter.");
+    return guarded([&] {
+        h->lbvh.build(neighbor::LBVH::LaunchParameters(block_size, as_stream(stream)),
+                      neighbor::PointInsertOp(reinterpret_cast<const float3*>(points), N), f3(lo), f3(hi));
+    });
+    }
+
+int nbr_lbvh_build_spheres(nbr_lbvh h, const float* points, float radius, unsigned int N,
+                           const float lo[3], const float hi[3], unsigned int block_size, void* stream)
+    {
+    if (!h || !lo || !hi || (N > 0 && !points)) return fail(NBR_ERR_INVALID, "null argument");
+    if (!valid_block(block_size)) return fail(NBR_ERR_INVALID, "Invalid tuning parameter.");
+    return guarded([&] {
+        h->lbvh.build(neighbor::LBVH::LaunchParameters(block_size, as_stream(stream)),
+                      neighbor::SphereInsertOp(reinterpret_cast<const float3*>(points), radius, N), f3(lo),
+                      f3(hi));
+    });
+    }
+
+int nbr_lbvh_get_sizes(nbr_lbvh h, int* root, unsigned int* N, unsigned int* n_internal,
+                       unsigned int* n_nodes)
+    {
+    if (!h) return fail(NBR_ERR_INVALID, "null handle");
+    if (root) *root = h->lbvh.getRoot();
+    if (N) *N = h->lbvh.getN();
+    if (n_internal) *n_internal = h->lbvh.getNInternal();
+    if (n_nodes) *n_nodes = h->lbvh.getNNodes();
+    return NBR_OK;
+    }
+
+int nbr_lbvh_get_arrays(nbr_lbvh h, const int** parent, const int** left, const int** right,
+                        const unsigned int** primitive, const float** lo, const float** hi)
+    {
+    if (!h) return fail(NBR_ERR_INVALID, "null handle");
+    const neighbor::ConstLBVHData d = h->lbvh.data();
+    if (parent) *parent = d.parent;
+    if (left) *left = d.left;
+    if (right) *right = d.right;
+    if (primitive) *primitive = d.primitive;
+    if (lo) *lo = reinterpret_cast<const float*>(d.lo);
+    if (hi) *hi = reinterpret_cast<const float*>(d.hi);
+    return NBR_OK;
+    }
+
+int nbr_lbvh_get_codes(nbr_lbvh h, const unsigned int** codes)
+    {
+    if (!h || !codes) return fail(NBR_ERR_INVALID, "null argument");
+    *codes = h->lbvh.getCodes().get();
+    return NBR_OK;
+    }
+
+int nbr_lbvh_get_fast(nbr_lbvh h, const unsigned int** nodes, const float** points, const float** frame,
+                      unsigned int* count_bits, unsigned int* leaf_size)
+    {
+    if (!h) return fail(NBR_ERR_INVALID, "null handle");
+    const neighbor::FastLBVHData f = h->lbvh.fastData();
+    if (nodes) *nodes = reinterpret_cast<const unsigned int*>(f.nodes);
+    if (points) *points = reinterpret_cast<const float*>(f.points);
+    if (frame) *frame = reinterpret_cast<const float*>(f.frame);
+    if (count_bits) *count_bits = f.count_bits;
+    if (leaf_size) *leaf_size = f.leaf_size;
+    return NBR_OK;
+    }
+
+int nbr_lbvh_num_fast_nodes(nbr_lbvh h, unsigned int* n, void* stream)
+    {
+    if (!h || !n) return fail(NBR_ERR_INVALID, "null argument");
+    return guarded([&] { *n = h->lbvh.getNumFastNodes(as_stream(stream)); });
+    }
+
+int nbr_lbvh_check_status(nbr_lbvh h, void* stream)
+    {
+    if (!h) return fail(NBR_ERR_INVALID, "null handle");
+    return guarded([&] { h->lbvh.checkStatus(as_stream(stream)); });
+    }
+
+int nbr_traverser_create(nbr_traverser* out)
+    {
+    if (!out) return fail(NBR_ERR_INVALID, "null output handle");
+    return guarded([&] { *out = new nbr_traverser_s(); });
+    }
+
+int nbr_traverser_destroy(nbr_traverser t)
+    {
+    return guarded([&] { delete t; });
+    }
+
+int nbr_traverser_setup(nbr_traverser t, nbr_lbvh h, const unsigned int* map, unsigned int block_size,
+                        void* stream)
+    {
+    if (!t || !h) return fail(NBR_ERR_INVALID, "null handle");
+    if (!valid_block(block_size)) return fail(NBR_ERR_INVALID, "Invalid tuning parameter.");
+    return guarded([&] {
+        const neighbor::LBVHTraverser::LaunchParameters p(block_size, as_stream(stream));
+        if (map)
+            t->trav.setup(p, h->lbvh, neighbor::MapTransformOp(map));
+        else
+            t->trav.setup(p, h->lbvh, neighbor::NullTransformOp());
+    });
+    }
+
+int nbr_traverser_reset(nbr_traverser t)
+    {
+    if (!t) return fail(NBR_ERR_INVALID, "null handle");
+    t->trav.reset();
+    return NBR_OK;
+    }
+
+int nbr_traverser_set_fast_path(nbr_traverser t, int enabled)
+    {
+    if (!t) return fail(NBR_ERR_INVALID, "null handle");
+    t->trav.setFastPath(enabled != 0);
+    return NBR_OK;
+    }
+
+int nbr_traverser_get_data(nbr_traverser t, const int** data, const float** lo, const float** hi,
+                           const float** bins)
+    {
+    if (!t) return fail(NBR_ERR_INVALID, "null handle");
+    if (data) *data = reinterpret_cast<const int*>(t->trav.getData().get());
+    if (lo) *lo = t->trav.getFrameLo();
+    if (hi) *hi = t->trav.getFrameHi();
+    if (bins) *bins = t->trav.getFrameBins();
+    return NBR_OK;
+    }
+
+int nbr_traverse(nbr_traverser t, nbr_lbvh h, int query_kind, const float* spheres, unsigned int Q,
+                 const float* points, const float box[3], float pad, const float* images,
+                 unsigned int n_images, const unsigned int* map, unsigned int* nneigh, unsigned int* list,
+                 unsigned int max_neigh, unsigned int block_size, void* stream)
+    {
+    if (!t || !h) return fail(NBR_ERR_INVALID, "null handle");
+    if (query_kind != NBR_QUERY_SPHERE && query_kind != NBR_QUERY_EXACT)
+        return fail(NBR_ERR_INVALID, "unknown query kind");
+    if (Q > 0 && (!spheres || !nneigh)) return fail(NBR_ERR_INVALID, "null argument");
+    if (query_kind == NBR_QUERY_EXACT && (!points || !box)) return fail(NBR_ERR_INVALID, "exact query needs points and box");
+    if (list && max_neigh == 0) return fail(NBR_ERR_INVALID, "max_neigh must be positive with a list");
+    if (images && n_images > 32) return fail(NBR_ERR_INVALID, "A maximum of 32 image vectors are supported by LBVH traversers.");
+    if (!valid_block(block_size)) return fail(NBR_ERR_INVALID, "Invalid tuning parameter.");
+    const float3 b = box ? f3(box) : make_float3(0.f, 0.f, 0.f);
+    return guarded([&] {
+        const neighbor::LBVHTraverser::LaunchParameters p(block_size, as_stream(stream));
+        if (list)
+            dispatch_transform(t->trav, h->lbvh, p, query_kind, spheres, Q, points, b, pad, images, n_images,
+                               map, neighbor::NeighborListOp(list, nneigh, max_neigh));
+        else
+            dispatch_transform(t->trav, h->lbvh, p, query_kind, spheres, Q, points, b, pad, images, n_images,
+                               map, neighbor::CountNeighborsOp(nneigh));
+    });
+    }
+
+int nbr_traverse_self(nbr_traverser t, nbr_lbvh h, float rc, const float box[3], float pad, const float* images,
+                      unsigned int n_images, const unsigned int* map, unsigned int* nneigh, unsigned int* list,
+                      unsigned int max_neigh, int rows_sorted, unsigned int block_size, void* stream)
+    {
+    if (!t || !h || !box) return fail(NBR_ERR_INVALID, "null argument");
+    if (h->lbvh.getN() > 0 && !nneigh) return fail(NBR_ERR_INVALID, "null output");
+    if (list && max_neigh == 0) return fail(NBR_ERR_INVALID, "max_neigh must be positive with a list");
+    if (images && n_images > 32) return fail(NBR_ERR_INVALID, "A maximum of 32 image vectors are supported by LBVH traversers.");
+    if (!valid_block(block_size)) return fail(NBR_ERR_INVALID, "Invalid tuning parameter.");
+    return guarded([&] {
+        const neighbor::LBVHTraverser::LaunchParameters p(block_size, as_stream(stream));
+        if (list)
+            self_transform(t->trav, h->lbvh, p, rc, f3(box), pad, images, n_images, map,
+                           neighbor::NeighborListOp(list, nneigh, max_neigh), rows_sorted != 0);
+        else
+            self_transform(t->trav, h->lbvh, p, rc, f3(box), pad, images, n_images, map,
+                           neighbor::CountNeighborsOp(nneigh), rows_sorted != 0);
+    });
+    }
+
+float nbr_exact_pad(float rc, float coord_max) { return neighbor::exact_query_pad(rc, coord_max); }
+
+int nbr_debug_wait_timeout(unsigned int* status_out, void* stream)
+    {
+    if (!status_out) return fail(NBR_ERR_INVALID, "null argument");
+    return guarded([&] {
+        using neighbor::detail::check_cuda;
+        cudaStream_t st = as_stream(stream);
+        const unsigned int n = 2 * neighbor::gpu::kScanTile;
+        const unsigned int tiles = neighbor::detail::ceil_div((size_t)n + 1, neighbor::gpu::kScanTile);
+        neighbor::device_array<unsigned int> in, out, words;
+        neighbor::device_array<unsigned long long> status;
+        in.reserve(n);
+        out.reserve((size_t)n + 1);
+        status.reserve(tiles + 1);
+        words.reserve(2);  // [0] tile ticket, [1] status word
+        check_cuda(cudaMemsetAsync(in.get(), 0, n * sizeof(unsigned int), st), "memset");
+        check_cuda(cudaMemsetAsync(status.get(), 0, (tiles + 1) * sizeof(unsigned long long), st), "memset");
+        const unsigned int init[2] = {1u, 0u};  // tickets start at 1: tile 0 is never taken
+        check_cuda(cudaMemcpyAsync(words.get(), init, sizeof(init), cudaMemcpyHostToDevice, st), "copy");
+        neighbor::gpu::k_scan_exclusive<<<tiles, neighbor::gpu::kScanBlock, 0, st>>>(
+            in.get(), out.get(), n, status.get(), 1u, words.get(), nullptr, words.get() + 1);
+        check_cuda(cudaGetLastError(), "launch");
+        unsigned int result[2] = {0u, 0u};
+        check_cuda(cudaMemcpyAsync(result, words.get(), sizeof(result), cudaMemcpyDeviceToHost, st), "copy");
+        check_cuda(cudaStreamSynchronize(st), "sync");
+        *status_out = result[1];
+    });
+    }
+
+} // extern "C"

@@ -691,10 +691,12 @@ uint32_t orc_fast_nodes(uint32_t N, uint32_t leaf_size, uint32_t count_bits,
             link = 0x80000000u | (first[v] << count_bits) | (size - 1);
         else
             link = live_first_count[last[v] + 1];
+        // hi bins are stored complemented (65535 - hi) so that both the union of two boxes
+        // and the overlap test reduce to packed unsigned 16-bit minima.
         uint32_t* o = nodes + 4 * (size_t)pre[v];
         o[0] = qlo[0] | (qlo[1] << 16);
-        o[1] = qlo[2] | (qhi[0] << 16);
-        o[2] = qhi[1] | (qhi[2] << 16);
+        o[1] = qlo[2] | ((65535u - qhi[0]) << 16);
+        o[2] = (65535u - qhi[1]) | ((65535u - qhi[2]) << 16);
         o[3] = link;
     }
     return n_live;

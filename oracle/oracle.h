@@ -125,7 +125,8 @@ double orc_pair_distance_minus_rc_f64(const float* pi, const float* pj, float rc
 
 /* ---- the project's own 16-bit pre-order node format (restated for bit-exact checks of
  *      the CUDA build) ----
- * nodes: uint32[4*n] with words {lo.x|lo.y<<16, lo.z|hi.x<<16, hi.y|hi.z<<16, link};
+ * nodes: uint32[4*n] with words {lo.x|lo.y<<16, lo.z|~hi.x<<16, ~hi.y|~hi.z<<16, link}
+ * where ~h = 65535-h (complemented upper bins);
  * link = skip index for an internal node, or 0x80000000 | first<<cbits | (count-1) for a
  * leaf bucket.  Returns the number of live nodes.  frame: {root_lo[3], scale[3]}. */
 uint32_t orc_fast_nodes(uint32_t N, uint32_t leaf_size, uint32_t count_bits,

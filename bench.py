@@ -45,6 +45,7 @@ def parse():
     ap.add_argument("--leaf", type=int, default=4)
     ap.add_argument("--radix-bits", type=int, default=8)
     ap.add_argument("--block", type=int, default=256)
+    ap.add_argument("--mode", type=int, default=1, help="0 = thread per query, 1 = warp packet")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
@@ -86,6 +87,15 @@ class ClockSampler:
     def _read(self):
         for line in self.proc.stdout:
             self.lines.append(line.strip())
+
+    def wait_first(self, timeout):
+        t0 = time.time()
+        while self.proc is not None and not self.lines and time.time() - t0 < timeout:
+            time.sleep(0.05)
+
+    def mark(self):
+        """Forget samples taken so far: only the timed region's samples are summarised."""
+        self.lines = []
 
     def stop(self):
         if self.proc is None:
@@ -243,10 +253,11 @@ def run_ours(args):
     box = [L, L, L]
     stream = torch.cuda.current_stream()
     frames = make_frames(n, L, args.warmup + args.steps, seed=1000 + rank)
-    imgs = nb.images27(box)
+    imgs = "periodic"
     pad = nb.exact_pad(RC, 2 * L)
     lbvh = nb.LBVH(leaf_size=args.leaf, radix_bits=args.radix_bits)
     trav = nb.LBVHTraverser()
+    trav.set_mode(args.mode)
     counts = torch.empty(n, dtype=torch.int32, device="cuda")
     cap = 64
     lst = torch.empty(n * cap, dtype=torch.int32, device="cuda")
@@ -274,17 +285,21 @@ def run_ours(args):
             record[4].record(stream)
         return mx
 
+    # the sampler starts before the warm-up so that nvidia-smi's start-up falls outside the
+    # timed region
+    sampler = ClockSampler(local)
+    sampler.start()
     for i in range(args.warmup):
         step(frames[i])
+    sampler.wait_first(10.0)
     lbvh.check_status()
     torch.cuda.synchronize()
 
     recs = [[ev() for _ in range(5)] for _ in range(args.steps)]
     pair_counts = []
-    sampler = ClockSampler(local)
     barrier(ws)
     torch.cuda.synchronize()
-    sampler.start()
+    sampler.mark()
     t_start = ev()
     t_end = ev()
     t_start.record(stream)
@@ -373,6 +388,7 @@ def run_ours(args):
         "config": {"workload": f"uniform trajectory N={n} density 0.85 L={L:.2f} rc=1.3 "
                                f"sigma=0.05, 27 images, build+count+fill per frame",
                    "leaf_size": args.leaf, "radix_bits": args.radix_bits, "block": args.block,
+                   "traversal": "warp packet" if args.mode == 1 else "thread per query",
                    "l2": "inputs larger than L2 (201 MB/frame, new frame every step)",
                    "parallelism": f"replicas x{ws}"},
         "stages_ms": {k: round(v, 4) for k, v in stages.items()},

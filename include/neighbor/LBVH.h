@@ -150,12 +150,11 @@ class LBVH : public Tunable<unsigned int>
             {
             FastLBVHData f;
             f.nodes = m_nodes.get();
-            f.n_nodes = m_small.get() + kSmallLiveCount;
+            f.n_boxes = m_small.get() + kSmallLiveCount;
             f.points = m_payload.get();
             f.frame = reinterpret_cast<const QuantFrame*>(m_small.get() + kSmallFrame);
             f.status = m_small.get() + kSmallStatus;
             f.N = m_N;
-            f.count_bits = detail::bits_for_count(m_leaf_size);
             f.leaf_size = m_leaf_size;
             return f;
             }
@@ -177,15 +176,15 @@ class LBVH : public Tunable<unsigned int>
             return s;
             }
 
-        // Number of live traversal nodes of the last build (synchronises the stream).
+        // Number of traversal records (box + point) of the last build (synchronises the stream).
         unsigned int getNumFastNodes(cudaStream_t stream = 0) const
             {
             if (m_N == 0) return 0;
             unsigned int n = 0;
-            detail::check_cuda(cudaMemcpyAsync(&n, fastData().n_nodes, sizeof(unsigned int),
+            detail::check_cuda(cudaMemcpyAsync(&n, fastData().n_boxes, sizeof(unsigned int),
                                                cudaMemcpyDeviceToHost, stream), "node count copy");
             detail::check_cuda(cudaStreamSynchronize(stream), "node count sync");
-            return n;
+            return n + m_N;
             }
 
     private:
@@ -267,17 +266,18 @@ class LBVH : public Tunable<unsigned int>
 namespace gpu
 {
 // Single-primitive tree (the reference's lbvh_one_primitive case): identity order, sentinel
-// parent, one live node.
+// parent, and a traversal tree of one point record (no box records).
 __global__ void k_single_init(unsigned int* primitive, int* parent, unsigned int* live)
     {
     if (threadIdx.x == 0 && blockIdx.x == 0)
         {
         primitive[0] = 0u;
         parent[0] = LBVHSentinel;
-        live[0] = 1u;
+        live[0] = 0u;
         }
     }
-// The root is live: it adds 1 at position 0 before the hierarchy kernel adds its children.
+// The root (N > 1) is a box record: it adds 1 at position 0 before the hierarchy kernel adds
+// its children's.
 __global__ void k_root_live(unsigned int* live)
     {
     if (threadIdx.x == 0 && blockIdx.x == 0) live[0] = 1u;
@@ -462,7 +462,6 @@ void LBVH::build(const LaunchParameters& params, const InsertOpT& insert, const 
     a.bounds = small + kSmallBounds;
     a.frame_out = reinterpret_cast<QuantFrame*>(small + kSmallFrame);
     a.leaf_size = m_leaf_size;
-    a.count_bits = detail::bits_for_count(m_leaf_size);
     a.error = small + kSmallStatus;
     a.node_capacity = (unsigned int)m_nodes.size();
     const unsigned int bs = params.tunable;

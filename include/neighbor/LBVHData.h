@@ -4,12 +4,13 @@
 // (include/neighbor/LBVHData.h:14-43): node 0 is the root, internal nodes 0..N-2 precede leaves
 // N-1..2N-2, leaf N-1+i holds sorted primitive i.
 //
-// FastLBVHData (new) is the traversal form this library builds alongside: live nodes of the tree
-// after collapsing every subtree of at most leaf_size primitives into one leaf bucket, stored in
-// depth-first pre-order as 16-byte records {lo.x|lo.y<<16, lo.z|~hi.x<<16, ~hi.y|~hi.z<<16, link}.
-// Bounds are 16-bit bins of the root box rounded outward (~h = 65535-h).  The left child of an
-// internal node is the next record; link is the skip index past its subtree, or for a bucket
-// 0x80000000 | first<<count_bits | (count-1) over the sorted primitives.
+// FastLBVHData (new) is the traversal form this library builds alongside: the tree after
+// collapsing every subtree of at most leaf_size primitives into a bucket, as 16-byte records in
+// depth-first pre-order.  A box record {lo.x|lo.y<<16, lo.z|~hi.x<<16, ~hi.y|~hi.z<<16, skip}
+// (15-bit bins of the root box in 16-bit fields, rounded outward, ~h = 32767-h) covers an internal node or a
+// bucket; the next record is its first child (or its bucket's first point) and skip is the index
+// just past its subtree.  A point record {x, y, z as float bits, 0x80000000 | primitive id}
+// holds one primitive with exact coordinates.
 #ifndef NEIGHBOR_LBVH_DATA_H_
 #define NEIGHBOR_LBVH_DATA_H_
 
@@ -42,7 +43,7 @@ struct ConstLBVHData
     int root;
     };
 
-// 16-bit quantisation frame of the fast nodes: bins = (x - lo) * scale, scale = 65535 / extent
+// Quantisation frame of the box records: bins = (x - lo) * scale, scale = 32767 / extent
 // rounded down.
 struct QuantFrame
     {
@@ -53,13 +54,12 @@ struct QuantFrame
 
 struct FastLBVHData
     {
-    const uint4* nodes;          // live nodes in pre-order
-    const unsigned int* n_nodes; // device scalar: number of live nodes
+    const uint4* nodes;          // records in pre-order
+    const unsigned int* n_boxes; // device scalar: number of box records (records = boxes + N)
     const float4* points;        // sorted leaf payload: (x, y, z, primitive id as bits)
     const QuantFrame* frame;     // device scalar
     const unsigned int* status;  // build status word; traversals do nothing when it is set
-    unsigned int N;              // primitives
-    unsigned int count_bits;     // bits of (count-1) in a bucket link
+    unsigned int N;              // primitives (= point records)
     unsigned int leaf_size;
     };
 

@@ -37,7 +37,8 @@ class LBVHTraverser : public Tunable<unsigned int>
     public:
         LBVHTraverser()
             : Tunable<unsigned int>(32, 1024, 32), m_root(0), m_lbvh_lo(1), m_lbvh_hi(1), m_bins(1),
-              m_replay(false), m_fast_enabled(true)
+              m_replay(false), m_fast_enabled(true), m_mode(kPacketTraversal),
+              m_stats(nullptr)
             {}
 
         template<class TransformOpT>
@@ -135,6 +136,21 @@ class LBVHTraverser : public Tunable<unsigned int>
         void setFastPath(bool enabled) { m_fast_enabled = enabled; }
         bool getFastPath() const { return m_fast_enabled; }
 
+        // Fast-path kernel: kThreadTraversal (one thread walks the tree per query) or
+        // kPacketTraversal (a warp walks it once for 32 consecutive queries; default).
+        enum Mode { kThreadTraversal = 0, kPacketTraversal = 1 };
+        void setMode(int mode)
+            {
+            if (mode != kThreadTraversal && mode != kPacketTraversal)
+                throw std::runtime_error("Traversal mode must be 0 (thread) or 1 (packet).");
+            m_mode = mode;
+            }
+        int getMode() const { return m_mode; }
+
+        // Optional device counters (3 x uint64: node visits, point tests, packets walked) that
+        // the fast kernels add to; NULL disables them.
+        void setStats(unsigned long long* counters) { m_stats = counters; }
+
         // Self queries on the fast path: every primitive of the tree queries the tree with cutoff
         // rc.  Queries run in the tree's sorted order; rows_sorted selects whether row s of the
         // output belongs to sorted slot s (the reference benchmark's layout) or to the original
@@ -152,6 +168,8 @@ class LBVHTraverser : public Tunable<unsigned int>
         shared_array<float3> m_bins;
         bool m_replay;
         bool m_fast_enabled;
+        int m_mode;
+        unsigned long long* m_stats;
 
         template<class TransformOpT>
         void compress(const LaunchParameters& params, const LBVH& lbvh, const TransformOpT& transform)
@@ -191,9 +209,15 @@ namespace detail
 template<class T> struct is_float3_images : std::false_type {};
 template<> struct is_float3_images<ImageListOp<float3>> : std::true_type {};
 template<> struct is_float3_images<SelfOp> : std::true_type {};
+template<> struct is_float3_images<PeriodicImagesOp> : std::true_type {};
 
 inline const float3* image_pointer(const SelfOp&) { return nullptr; }
 inline const float3* image_pointer(const ImageListOp<float3>& op) { return op.images; }
+inline const float3* image_pointer(const PeriodicImagesOp&) { return nullptr; }
+template<class T> inline int image_lattice(const T&) { return 0; }
+inline int image_lattice(const PeriodicImagesOp&) { return 1; }
+template<class T> inline float3 lattice_box(const T&, float3 box) { return box; }
+inline float3 lattice_box(const PeriodicImagesOp& op, float3) { return op.L; }
 template<class T> inline const float3* image_pointer(const T&) { return nullptr; }
 
 inline void set_output(gpu::FastQueryArgs& a, const CountNeighborsOp& out)
@@ -215,10 +239,18 @@ void LBVHTraverser::launch_fast(const LaunchParameters& params, const LBVH& lbvh
                                 const OutputOpT& out, const TransformOpT& transform, unsigned int Q)
     {
     detail::set_output(a, out);
+    a.stats = m_stats;
     const unsigned int bs = params.tunable;
     constexpr int kind = output_kind<OutputOpT>::value;
-    gpu::k_traverse_fast<kind, TransformOpT><<<detail::ceil_div(Q, bs), bs, 0, params.stream>>>(
-        lbvh.fastData(), a, transform);
+    if (m_mode == kPacketTraversal)
+        gpu::k_traverse_packet<kind, TransformOpT><<<detail::ceil_div(Q, bs), bs, 0, params.stream>>>(
+            lbvh.fastData(), a, transform);
+    else if (m_stats)
+        gpu::k_traverse_fast<kind, true, TransformOpT><<<detail::ceil_div(Q, bs), bs, 0, params.stream>>>(
+            lbvh.fastData(), a, transform);
+    else
+        gpu::k_traverse_fast<kind, false, TransformOpT><<<detail::ceil_div(Q, bs), bs, 0, params.stream>>>(
+            lbvh.fastData(), a, transform);
     detail::check_cuda(cudaGetLastError(), "fast traversal launch");
     }
 
@@ -244,6 +276,8 @@ void LBVHTraverser::traverse(const LaunchParameters& params, const LBVH& lbvh, c
             a.self_rows_sorted = 1;
             a.images = detail::image_pointer(images);
             a.n_images = images.size();
+            a.lattice = detail::image_lattice(images);
+            a.lattice_L = detail::lattice_box(images, query.box);
             a.box = query.box;
             a.pad = query.pad;
             launch_fast(params, lbvh, a, out, transform, query.size());
@@ -265,7 +299,8 @@ void LBVHTraverser::traverseSelf(const LaunchParameters& params, const LBVH& lbv
                                  const TransformOpT& transform, bool rows_sorted)
     {
     static_assert(output_kind<OutputOpT>::value != 0, "traverseSelf needs CountNeighborsOp or NeighborListOp");
-    static_assert(detail::is_float3_images<TranslateOpT>::value, "traverseSelf needs SelfOp or ImageListOp<float3>");
+    static_assert(detail::is_float3_images<TranslateOpT>::value,
+                  "traverseSelf needs SelfOp, ImageListOp<float3> or PeriodicImagesOp");
     if (lbvh.getN() == 0 || images.size() == 0) return;
     if (images.size() > 32)
         throw std::runtime_error("A maximum of 32 image vectors are supported by LBVH traversers.");
@@ -278,6 +313,8 @@ void LBVHTraverser::traverseSelf(const LaunchParameters& params, const LBVH& lbv
     a.self_rows_sorted = rows_sorted ? 1 : 0;
     a.images = detail::image_pointer(images);
     a.n_images = images.size();
+    a.lattice = detail::image_lattice(images);
+    a.lattice_L = detail::lattice_box(images, box);
     a.box = box;
     a.pad = pad;
     launch_fast(params, lbvh, a, out, transform, lbvh.getN());

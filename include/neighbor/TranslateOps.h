@@ -34,6 +34,25 @@ struct ImageListOp
     const unsigned int N;
     };
 
+// The 27 periodic images of an orthorhombic box: translations (ix*L.x, iy*L.y, iz*L.z) for
+// ix, iy, iz in {-1, 0, 1}, image i = 9*(ix+1) + 3*(iy+1) + (iz+1) -- the list the reference's
+// tests build by hand (test/lbvh_test.cu:427-440).  The fast traversal recognises it and decides
+// which images a query needs with three per-axis tests instead of 27 box tests.
+struct PeriodicImagesOp
+    {
+    typedef float3 type;
+    __host__ __device__ explicit PeriodicImagesOp(float3 L_) : L(L_) {}
+    __host__ __device__ __forceinline__ float3 get(const unsigned int idx) const
+        {
+        const float ix = (float)((int)(idx / 9u) - 1);
+        const float iy = (float)((int)((idx / 3u) % 3u) - 1);
+        const float iz = (float)((int)(idx % 3u) - 1);
+        return make_float3(L.x * ix, L.y * iy, L.z * iz);
+        }
+    __host__ __device__ __forceinline__ unsigned int size() const { return 27; }
+    float3 L;
+    };
+
 } // namespace neighbor
 
 #endif // NEIGHBOR_TRANSLATE_OPS_H_

@@ -392,10 +392,13 @@ __global__ void k_gen_hierarchy(const unsigned int* __restrict__ codes,
     parent[rc] = (int)i;
     if (i == 0) parent[0] = LBVHSentinel;
     ranges[i] = make_uint2((unsigned int)first, (unsigned int)last);
+    // Box records of the traversal tree: every node of more than leaf_size primitives, and every
+    // bucket (2..leaf_size primitives) whose parent is larger than leaf_size.  Each adds 1 at its
+    // first primitive; this node adds its children's.
     if ((unsigned long long)(last - first + 1) > leaf_size)
         {
-        atomicAdd(live + first, 1u);
-        atomicAdd(live + split + 1, 1u);
+        if (split > first) atomicAdd(live + first, 1u);
+        if (last > split + 1) atomicAdd(live + split + 1, 1u);
         }
     }
 
@@ -491,7 +494,7 @@ __global__ void __launch_bounds__(kScanBlock) k_scan_exclusive(const unsigned in
     }
 
 // ---------------------------------------------------------------------------------------------
-// Root-box frame of the 16-bit format from the bounds words.
+// Root-box frame of the record bins from the bounds words.
 // ---------------------------------------------------------------------------------------------
 __device__ __forceinline__ QuantFrame frame_from_bounds(const unsigned int* bounds)
     {
@@ -504,7 +507,8 @@ __device__ __forceinline__ QuantFrame frame_from_bounds(const unsigned int* boun
     if (!(ex > 0.f)) ex = 1.0f;
     if (!(ey > 0.f)) ey = 1.0f;
     if (!(ez > 0.f)) ez = 1.0f;
-    f.scale = make_float3(approx::fdiv_rd(65535.f, ex), approx::fdiv_rd(65535.f, ey), approx::fdiv_rd(65535.f, ez));
+    f.scale = make_float3(approx::fdiv_rd((float)kBinMax, ex), approx::fdiv_rd((float)kBinMax, ey),
+                          approx::fdiv_rd((float)kBinMax, ez));
     return f;
     }
 
@@ -527,7 +531,6 @@ struct BubbleArgs
     const unsigned int* bounds;
     QuantFrame* frame_out;
     unsigned int leaf_size;
-    unsigned int count_bits;
     const unsigned int* error;
     unsigned int node_capacity;
     };
@@ -538,17 +541,27 @@ __device__ __forceinline__ float3 ld_cg_float3(const float3* p)
     return make_float3(__ldcg(f), __ldcg(f + 1), __ldcg(f + 2));
     }
 
-// Write the pre-order record of live node v with primitive range [first,last].  db = number of
-// live nodes below v on its left spine (they share `first` and follow v in pre-order).
-__device__ __forceinline__ void emit_fast_node(const BubbleArgs& a, const QuantFrame& f,
-                                               unsigned int first, unsigned int last,
-                                               unsigned int db, bool bucket, float3 lo, float3 hi)
+// Pre-order slot of a box record with primitive range [first, last]: the box records that start
+// before `first` (pre[first]), the point records before it (first), and the box records above it
+// that start at `first` too.  db = number of box records below it on its left spine.
+__device__ __forceinline__ void emit_box_record(const BubbleArgs& a, const QuantFrame& f,
+                                                unsigned int first, unsigned int last,
+                                                unsigned int db, float3 lo, float3 hi)
     {
     const uint3 w = pack_node_box(f, lo, hi);
-    const unsigned int link = bucket ? (kLeafFlag | (first << a.count_bits) | (last - first))
-                                     : a.pre[last + 1];
-    const unsigned int slot = a.pre[first + 1] - 1u - db;
-    if (slot < a.node_capacity) a.nodes[slot] = make_uint4(w.x, w.y, w.z, link);
+    const unsigned int skip = a.pre[last + 1] + last + 1u;
+    const unsigned int slot = a.pre[first + 1] - 1u - db + first;
+    if (slot < a.node_capacity) a.nodes[slot] = make_uint4(w.x, w.y, w.z, skip);
+    }
+
+// Point record of sorted primitive s: exact coordinates and the primitive id.
+__device__ __forceinline__ void emit_point_record(const BubbleArgs& a, unsigned int s, float3 p,
+                                                  unsigned int prim)
+    {
+    const unsigned int slot = a.pre[s + 1] + s;
+    if (slot < a.node_capacity)
+        a.nodes[slot] = make_uint4(__float_as_uint(p.x), __float_as_uint(p.y), __float_as_uint(p.z),
+                                   kLeafFlag | prim);
     }
 
 template<class InsertOpT>
@@ -577,15 +590,7 @@ __global__ void k_bubble(const InsertOpT insert, const BubbleArgs a)
     a.payload[s] = make_float4(b.lo.x, b.lo.y, b.lo.z, __uint_as_float(prim));
 
     int cur = (N == 1) ? LBVHSentinel : a.parent[leaf];
-    {
-    bool live = (cur == LBVHSentinel);
-    if (!live)
-        {
-        const uint2 pr = a.ranges[cur];
-        live = (pr.y - pr.x + 1u) > a.leaf_size;
-        }
-    if (live) emit_fast_node(a, f, s, s, 0u, true, b.lo, b.hi);
-    }
+    emit_point_record(a, s, b.lo, prim);
     __threadfence();
 
     int last = leaf;
@@ -607,18 +612,20 @@ __global__ void k_bubble(const InsertOpT insert, const BubbleArgs a)
         a.hi[cur] = bhi;
         const uint2 rg = a.ranges[cur];
         const unsigned int size = rg.y - rg.x + 1u;
+        // box records below on the left spine: the left child's own count plus itself, unless the
+        // left child is a single point (point records are not counted) or this node is a bucket
         unsigned int db = 0;
-        if (size > a.leaf_size)
-            db = 1u + ((unsigned int)l >= N - 1 ? 0u : (unsigned int)__ldcg(a.depth_below + l));
+        if (size > a.leaf_size && (unsigned int)l < N - 1)
+            db = 1u + (unsigned int)__ldcg(a.depth_below + l);
         a.depth_below[cur] = (unsigned char)db;
         const int par = a.parent[cur];
-        bool live = (par == LBVHSentinel);
+        bool live = size > a.leaf_size || par == LBVHSentinel;
         if (!live)
             {
             const uint2 pr = a.ranges[par];
             live = (pr.y - pr.x + 1u) > a.leaf_size;
             }
-        if (live) emit_fast_node(a, f, rg.x, rg.y, db, size <= a.leaf_size, blo, bhi);
+        if (live) emit_box_record(a, f, rg.x, rg.y, db, blo, bhi);
         __threadfence();
         last = cur;
         cur = par;

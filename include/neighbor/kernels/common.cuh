@@ -142,20 +142,26 @@ __device__ __forceinline__ unsigned int morton_code(const BoundingBox& b, const 
     }
 
 // ---------------------------------------------------------------------------------------------
-// 16-bit node boxes.  Bins are measured from the root's lower corner with scale = 65535/extent
-// rounded down; lower bounds round down, upper bounds round up, both clamped to [0, 65535].
-// Upper bins are stored complemented (65535-h): the union of two boxes is then a packed u16x2
-// minimum of each word, and "node overlaps query" is "node word <= query word" in every half.
+// Record boxes: 15-bit bins (0..32767) of the root box held in 16-bit fields.  Bins are measured
+// from the root's lower corner with scale = 32767/extent rounded down; lower bounds round down,
+// upper bounds round up, both clamped to [0, 32767].  Upper bins are stored complemented
+// (32767-h), so "box overlaps query" is "every field of the box <= the matching field of the
+// query".  The query's fields carry the guard bit 0x8000: (query|guard) - box is then computed
+// in each 16-bit half without borrowing from its neighbour, and the guard bit survives exactly
+// when box <= query.
 // ---------------------------------------------------------------------------------------------
+constexpr unsigned int kBinMax = 32767u;
+constexpr unsigned int kGuard = 0x80008000u;
+
 __device__ __forceinline__ unsigned int bin_down(float x, float o, float s)
     {
     const int v = __float2int_rd(approx::fmul_rd(approx::fsub_rd(x, o), s));
-    return (unsigned int)min(max(v, 0), 65535);
+    return (unsigned int)min(max(v, 0), (int)kBinMax);
     }
 __device__ __forceinline__ unsigned int bin_up(float x, float o, float s)
     {
     const int v = __float2int_ru(approx::fmul_ru(approx::fsub_ru(x, o), s));
-    return (unsigned int)min(max(v, 0), 65535);
+    return (unsigned int)min(max(v, 0), (int)kBinMax);
     }
 
 __device__ __forceinline__ uint3 pack_node_box(const QuantFrame& f, const float3& lo, const float3& hi)
@@ -166,11 +172,11 @@ __device__ __forceinline__ uint3 pack_node_box(const QuantFrame& f, const float3
     const unsigned int hx = bin_up(hi.x, f.lo.x, f.scale.x);
     const unsigned int hy = bin_up(hi.y, f.lo.y, f.scale.y);
     const unsigned int hz = bin_up(hi.z, f.lo.z, f.scale.z);
-    return make_uint3(lx | (ly << 16), lz | ((65535u - hx) << 16),
-                      (65535u - hy) | ((65535u - hz) << 16));
+    return make_uint3(lx | (ly << 16), lz | ((kBinMax - hx) << 16),
+                      (kBinMax - hy) | ((kBinMax - hz) << 16));
     }
 
-// Query box packed as {hi.x|hi.y<<16, hi.z|~lo.x<<16, ~lo.y|~lo.z<<16}.
+// Query box packed as {hi.x|hi.y<<16, hi.z|~lo.x<<16, ~lo.y|~lo.z<<16} with the guard bits set.
 __device__ __forceinline__ uint3 pack_query_box(const QuantFrame& f, const float3& lo, const float3& hi)
     {
     const unsigned int lx = bin_down(lo.x, f.lo.x, f.scale.x);
@@ -179,15 +185,13 @@ __device__ __forceinline__ uint3 pack_query_box(const QuantFrame& f, const float
     const unsigned int hx = bin_up(hi.x, f.lo.x, f.scale.x);
     const unsigned int hy = bin_up(hi.y, f.lo.y, f.scale.y);
     const unsigned int hz = bin_up(hi.z, f.lo.z, f.scale.z);
-    return make_uint3(hx | (hy << 16), hz | ((65535u - lx) << 16),
-                      (65535u - ly) | ((65535u - lz) << 16));
+    return make_uint3((hx | (hy << 16)) | kGuard, (hz | ((kBinMax - lx) << 16)) | kGuard,
+                      ((kBinMax - ly) | ((kBinMax - lz) << 16)) | kGuard);
     }
 
 __device__ __forceinline__ bool node_overlaps(const uint4& n, const uint3& q)
     {
-    const unsigned int t = (__vminu2(n.x, q.x) ^ n.x) | (__vminu2(n.y, q.y) ^ n.y)
-                           | (__vminu2(n.z, q.z) ^ n.z);
-    return t == 0u;
+    return ((q.x - n.x) & (q.y - n.y) & (q.z - n.z) & kGuard) == kGuard;
     }
 
 constexpr unsigned int kLeafFlag = 0x80000000u;

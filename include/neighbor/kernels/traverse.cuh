@@ -154,7 +154,7 @@ __global__ void k_traverse_ref10(const OutputOpT out, const LBVHCompressedData l
     out.finalize(result);
     }
 
-// Output modes of the fast kernel.
+// Output modes of the fast kernels.
 enum FastOutput : int
     {
     kFastCount = 1,
@@ -167,112 +167,334 @@ struct FastQueryArgs
     unsigned int Q;           // number of queries
     float self_rc;            // cutoff of self queries
     int self_rows_sorted;     // self queries: 1 => row s for sorted slot s, 0 => row primitive[s]
-    const float3* images;     // NULL => self image only
+    const float3* images;     // image list; NULL => self image only, or the lattice below
     unsigned int n_images;
+    int lattice;              // 1 => the 27 periodic images of lattice_L (images ignored)
+    float3 lattice_L;
     float3 box;               // periodic lengths for the minimum image (0 = open)
     float pad;                // radius padding of the traversal volume
     unsigned int* nneigh;
     unsigned int* list;
     unsigned int max_neigh;
+    unsigned long long* stats;  // optional counters: records visited, point tests, walks
     };
 
-template<int OUT, class TransformOpT>
-__global__ void k_traverse_fast(const FastLBVHData tree, const FastQueryArgs a,
-                                                       const TransformOpT transform)
+// Add a thread's (or a packet's) traversal counts to the optional statistics counters.
+__device__ __forceinline__ void add_stats(unsigned long long* stats, unsigned long long visits,
+                                          unsigned long long tests, unsigned long long walks)
     {
-    __shared__ QuantFrame s_frame;
-    __shared__ unsigned int s_nodes;
-    if (threadIdx.x == 0)
+    if (stats)
         {
-        s_frame = *tree.frame;
-        // a failed build leaves no tree to walk
-        s_nodes = ld_status(tree.status) != 0u ? 0u : *tree.n_nodes;
+        atomicAdd(stats + 0, visits);
+        atomicAdd(stats + 1, tests);
+        atomicAdd(stats + 2, walks);
         }
-    __syncthreads();
-    const unsigned int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= a.Q) return;
-    const QuantFrame f = s_frame;
-    const unsigned int n_nodes = s_nodes;
+    }
 
+// Query of a fast traversal: centre, cutoff, output row.
+struct FastQuery
+    {
     float3 p;
     float rc;
     unsigned int row;
+    };
+
+__device__ __forceinline__ FastQuery load_fast_query(const FastLBVHData& tree, const FastQueryArgs& a,
+                                                     unsigned int q)
+    {
+    FastQuery r;
     if (a.spheres)
         {
         const float4 s = a.spheres[q];
-        p = make_float3(s.x, s.y, s.z);
-        rc = s.w;
-        row = q;
+        r.p = make_float3(s.x, s.y, s.z);
+        r.rc = s.w;
+        r.row = q;
         }
     else
         {
         const float4 s = tree.points[q];
-        p = make_float3(s.x, s.y, s.z);
-        rc = a.self_rc;
-        row = a.self_rows_sorted ? q : __float_as_uint(s.w);
+        r.p = make_float3(s.x, s.y, s.z);
+        r.rc = a.self_rc;
+        r.row = a.self_rows_sorted ? q : __float_as_uint(s.w);
         }
-    const float rs = approx::fadd_ru(rc, a.pad);
-    const unsigned int nimg = a.images ? min(a.n_images, 32u) : 1u;
+    return r;
+    }
 
-    // images whose padded query box meets the root box
+__device__ __forceinline__ float3 image_vector(const FastQueryArgs& a, int i)
+    {
+    if (a.lattice) return PeriodicImagesOp(a.lattice_L).get((unsigned int)i);
+    return a.images ? a.images[i] : make_float3(0.f, 0.f, 0.f);
+    }
+
+// Which of the translations {-L, 0, +L} along one axis bring the padded query interval onto the
+// root interval [lo, hi]: bit 0 for -L, bit 1 for 0, bit 2 for +L.  Same rounding as the
+// general image test, so the result is the same conservative answer.
+__device__ __forceinline__ unsigned int axis_images(float p, float rs, float L, float lo, float hi)
+    {
+    unsigned int m = 0;
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+        {
+        const float c = __fadd_rn(p, L * (float)(k - 1));
+        if (approx::fsub_rd(c, rs) <= hi && approx::fadd_ru(c, rs) >= lo) m |= 1u << k;
+        }
+    return m;
+    }
+
+// Images whose padded query box meets the root box.
+__device__ __forceinline__ unsigned int image_flags(const FastQueryArgs& a, const QuantFrame& f,
+                                                    const float3& p, float rs)
+    {
+    if (a.lattice)
+        {
+        // image i = 9*(ix+1) + 3*(iy+1) + (iz+1): replicate the per-axis masks into 27 bits
+        const unsigned int mx = axis_images(p.x, rs, a.lattice_L.x, f.lo.x, f.hi.x);
+        const unsigned int my = axis_images(p.y, rs, a.lattice_L.y, f.lo.y, f.hi.y);
+        const unsigned int mz = axis_images(p.z, rs, a.lattice_L.z, f.lo.z, f.hi.z);
+        const unsigned int X = ((mx & 1u) ? 0x1ffu : 0u) | ((mx & 2u) ? 0x3fe00u : 0u) | ((mx & 4u) ? 0x7fc0000u : 0u);
+        const unsigned int Y = (((my & 1u) ? 0x7u : 0u) | ((my & 2u) ? 0x38u : 0u) | ((my & 4u) ? 0x1c0u : 0u)) * 0x40201u;
+        const unsigned int Z = mz * 0x1249249u;
+        return X & Y & Z;
+        }
+    const unsigned int nimg = a.images ? min(a.n_images, 32u) : 1u;
     unsigned int flags = 0;
     for (unsigned int i = 0; i < nimg; ++i)
         {
-        const float3 t = a.images ? a.images[i] : make_float3(0.f, 0.f, 0.f);
+        const float3 t = image_vector(a, i);
         const float3 c = make_float3(__fadd_rn(p.x, t.x), __fadd_rn(p.y, t.y), __fadd_rn(p.z, t.z));
         const bool hit = approx::fsub_rd(c.x, rs) <= f.hi.x && approx::fadd_ru(c.x, rs) >= f.lo.x
                          && approx::fsub_rd(c.y, rs) <= f.hi.y && approx::fadd_ru(c.y, rs) >= f.lo.y
                          && approx::fsub_rd(c.z, rs) <= f.hi.z && approx::fadd_ru(c.z, rs) >= f.lo.z;
         if (hit) flags |= 1u << i;
         }
+    return flags;
+    }
 
-    const unsigned long long row_first = (unsigned long long)row * a.max_neigh;
-    const unsigned int cmask = (1u << tree.count_bits) - 1u;
+__device__ __forceinline__ bool point_in_box(const float3& x, const float3& lo, const float3& hi)
+    {
+    return x.x >= lo.x && x.x <= hi.x && x.y >= lo.y && x.y <= hi.y && x.z >= lo.z && x.z <= hi.z;
+    }
+
+// One thread per query, stackless: a box record is tested against the query's box (hit: the next
+// record, miss: the skip link); a point record inside the query's padded box goes to the exact
+// predicate.  Images are walked one after the other in the same loop.  When a query visits more
+// than one image, a point is found only through the image whose padded box contains it, so each
+// pair is reported once.
+template<int OUT, bool STATS, class TransformOpT>
+__global__ void k_traverse_fast(const FastLBVHData tree, const FastQueryArgs a,
+                                const TransformOpT transform)
+    {
+    __shared__ QuantFrame s_frame;
+    __shared__ unsigned int s_records;
+    if (threadIdx.x == 0)
+        {
+        s_frame = *tree.frame;
+        // a failed build leaves no tree to walk
+        s_records = ld_status(tree.status) != 0u ? 0u : *tree.n_boxes + tree.N;
+        }
+    __syncthreads();
+    const unsigned int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= a.Q) return;
+    const QuantFrame f = s_frame;
+    const unsigned int n_rec = s_records;
+
+    const FastQuery Q = load_fast_query(tree, a, q);
+    const float rs = approx::fadd_ru(Q.rc, a.pad);
+    unsigned int flags = n_rec ? image_flags(a, f, Q.p, rs) : 0u;
+    const unsigned long long row_first = (unsigned long long)Q.row * a.max_neigh;
+
     unsigned int count = 0;
+    unsigned int visits = 0, tests = 0, walks = 0;
     while (flags)
         {
         const int bit = __ffs(flags) - 1;
         flags &= flags - 1u;
-        const float3 t = a.images ? a.images[bit] : make_float3(0.f, 0.f, 0.f);
-        const float3 c = make_float3(__fadd_rn(p.x, t.x), __fadd_rn(p.y, t.y), __fadd_rn(p.z, t.z));
+        const float3 t = image_vector(a, bit);
+        const float3 c = make_float3(__fadd_rn(Q.p.x, t.x), __fadd_rn(Q.p.y, t.y), __fadd_rn(Q.p.z, t.z));
         const float3 qlo = make_float3(approx::fsub_rd(c.x, rs), approx::fsub_rd(c.y, rs), approx::fsub_rd(c.z, rs));
         const float3 qhi = make_float3(approx::fadd_ru(c.x, rs), approx::fadd_ru(c.y, rs), approx::fadd_ru(c.z, rs));
         const uint3 qb = pack_query_box(f, qlo, qhi);
+        if (STATS) ++walks;
         unsigned int i = 0;
-        while (i < n_nodes)
+        while (i < n_rec)
             {
             const uint4 n = __ldg(tree.nodes + i);
-            const bool hit = node_overlaps(n, qb);
-            if (n.w & kLeafFlag)
+            if (STATS) ++visits;
+            if ((int)n.w < 0)
                 {
-                if (hit)
+                const float3 x = make_float3(__uint_as_float(n.x), __uint_as_float(n.y), __uint_as_float(n.z));
+                if (point_in_box(x, qlo, qhi))
                     {
-                    const unsigned int first = (n.w & ~kLeafFlag) >> tree.count_bits;
-                    const unsigned int end = min(first + (n.w & cmask) + 1u, tree.N);
-                    for (unsigned int k = first; k < end; ++k)
+                    if (STATS) ++tests;
+                    if (exact_pair(Q.p, x, Q.rc, a.box))
                         {
-                        const float4 pt = __ldg(tree.points + k);
-                        const bool inside = pt.x >= qlo.x && pt.x <= qhi.x && pt.y >= qlo.y
-                                            && pt.y <= qhi.y && pt.z >= qlo.z && pt.z <= qhi.z;
-                        if (inside && exact_pair(p, make_float3(pt.x, pt.y, pt.z), rc, a.box))
-                            {
-                            if (OUT == kFastList && count < a.max_neigh)
-                                a.list[row_first + count] = transform(__float_as_uint(pt.w));
-                            ++count;
-                            }
+                        if (OUT == kFastList && count < a.max_neigh)
+                            a.list[row_first + count] = transform(n.w & ~kLeafFlag);
+                        ++count;
                         }
                     }
                 ++i;
                 }
             else
                 {
-                // skip links always point forward in a valid tree; max() keeps even a damaged
-                // one from looping
-                i = hit ? i + 1u : max(n.w, i + 1u);
+                // skip links point forward in a valid tree; max() keeps a damaged one from looping
+                i = node_overlaps(n, qb) ? i + 1u : max(n.w, i + 1u);
                 }
             }
         }
-    a.nneigh[row] = count;
+    a.nneigh[Q.row] = count;
+    if (STATS) add_stats(a.stats, visits, tests, walks);
+    }
+
+// ---------------------------------------------------------------------------------------------
+// Warp-cooperative (packet) traversal.  The 32 queries of a warp are consecutive in the query
+// order (Morton order when the queries are the tree's own points).  The warp walks the tree once
+// with the union of their padded boxes: record loads are one broadcast address and every branch
+// is warp-uniform; at a point record every lane applies the exact predicate to its own query.
+// Where the Morton curve jumps the union box is much larger than its halves' boxes and the packet
+// is split (recursively).  Measured slower than one thread per query on uniform inputs (the
+// union box makes a warp visit several times more records than its lanes need); kept as a mode.
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ float warp_min(float v)
+    {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+    }
+__device__ __forceinline__ float warp_max(float v)
+    {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+    }
+
+struct PacketBox
+    {
+    float3 lo;
+    float3 hi;
+    };
+
+// Union over the lanes in [a, b) with on == true of their boxes (empty box if none).
+__device__ __forceinline__ PacketBox packet_union(const float3& lo, const float3& hi, bool on,
+                                                  int lane, int a, int b)
+    {
+    const bool in = on && lane >= a && lane < b;
+    PacketBox r;
+    r.lo = make_float3(warp_min(in ? lo.x : 3.0e38f), warp_min(in ? lo.y : 3.0e38f), warp_min(in ? lo.z : 3.0e38f));
+    r.hi = make_float3(warp_max(in ? hi.x : -3.0e38f), warp_max(in ? hi.y : -3.0e38f), warp_max(in ? hi.z : -3.0e38f));
+    return r;
+    }
+
+__device__ __forceinline__ float packet_volume(const PacketBox& b)
+    {
+    const float dx = fmaxf(b.hi.x - b.lo.x, 0.f);
+    const float dy = fmaxf(b.hi.y - b.lo.y, 0.f);
+    const float dz = fmaxf(b.hi.z - b.lo.z, 0.f);
+    return dx * dy * dz;
+    }
+
+constexpr float kPacketSplitRatio = 1.5f;
+
+template<int OUT, class TransformOpT>
+__global__ void k_traverse_packet(const FastLBVHData tree, const FastQueryArgs a,
+                                  const TransformOpT transform)
+    {
+    __shared__ QuantFrame s_frame;
+    __shared__ unsigned int s_records;
+    if (threadIdx.x == 0)
+        {
+        s_frame = *tree.frame;
+        s_records = ld_status(tree.status) != 0u ? 0u : *tree.n_boxes + tree.N;
+        }
+    __syncthreads();
+    const QuantFrame f = s_frame;
+    const unsigned int n_rec = s_records;
+    const unsigned int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if ((q & ~31u) >= a.Q) return;  // whole warp idle
+    const bool valid = q < a.Q;
+    const int lane = threadIdx.x & 31;
+
+    FastQuery Q;
+    Q.p = make_float3(0.f, 0.f, 0.f);
+    Q.rc = 0.f;
+    Q.row = 0;
+    if (valid) Q = load_fast_query(tree, a, q);
+    const float rs = approx::fadd_ru(Q.rc, a.pad);
+    const unsigned int flags = valid ? image_flags(a, f, Q.p, rs) : 0u;
+    unsigned int wflags = __reduce_or_sync(0xffffffffu, flags);
+    const bool multi = __popc(wflags) > 1;
+    const unsigned long long row_first = (unsigned long long)Q.row * a.max_neigh;
+
+    unsigned int count = 0;
+    unsigned int visits = 0, tests = 0, walks = 0;  // per packet (warp-uniform)
+    while (wflags)
+        {
+        const int bit = __ffs(wflags) - 1;
+        wflags &= wflags - 1u;
+        const float3 t = image_vector(a, bit);
+        const float3 c = make_float3(__fadd_rn(Q.p.x, t.x), __fadd_rn(Q.p.y, t.y), __fadd_rn(Q.p.z, t.z));
+        const bool lane_on = valid && ((flags >> bit) & 1u);
+        const float3 qlo = make_float3(approx::fsub_rd(c.x, rs), approx::fsub_rd(c.y, rs), approx::fsub_rd(c.z, rs));
+        const float3 qhi = make_float3(approx::fadd_ru(c.x, rs), approx::fadd_ru(c.y, rs), approx::fadd_ru(c.z, rs));
+
+        int stack_lo[8], stack_hi[8];
+        stack_lo[0] = 0;
+        stack_hi[0] = 32;
+        int sp = 1;
+        while (sp > 0)
+            {
+            --sp;
+            const int ra = stack_lo[sp];
+            const int rb = stack_hi[sp];
+            const PacketBox g = packet_union(qlo, qhi, lane_on, lane, ra, rb);
+            if (g.lo.x > g.hi.x) continue;  // no active lane in this range
+            if (rb - ra > 1)
+                {
+                const int m = (ra + rb) >> 1;
+                const PacketBox ga = packet_union(qlo, qhi, lane_on, lane, ra, m);
+                const PacketBox gb = packet_union(qlo, qhi, lane_on, lane, m, rb);
+                if (packet_volume(g) > kPacketSplitRatio * (packet_volume(ga) + packet_volume(gb)))
+                    {
+                    stack_lo[sp] = m;
+                    stack_hi[sp] = rb;
+                    ++sp;
+                    stack_lo[sp] = ra;
+                    stack_hi[sp] = m;
+                    ++sp;
+                    continue;
+                    }
+                }
+            const bool mine = lane_on && lane >= ra && lane < rb;
+            const uint3 qb = pack_query_box(f, g.lo, g.hi);
+            ++walks;
+            unsigned int i = 0;
+            while (i < n_rec)
+                {
+                const uint4 n = __ldg(tree.nodes + i);
+                ++visits;
+                if (n.w & kLeafFlag)
+                    {
+                    ++tests;
+                    const float3 x = make_float3(__uint_as_float(n.x), __uint_as_float(n.y), __uint_as_float(n.z));
+                    bool ok = mine && exact_pair(Q.p, x, Q.rc, a.box);
+                    if (multi) ok = ok && point_in_box(x, qlo, qhi);
+                    if (ok)
+                        {
+                        if (OUT == kFastList && count < a.max_neigh)
+                            a.list[row_first + count] = transform(n.w & ~kLeafFlag);
+                        ++count;
+                        }
+                    ++i;
+                    }
+                else
+                    {
+                    i = node_overlaps(n, qb) ? i + 1u : max(n.w, i + 1u);
+                    }
+                }
+            }
+        }
+    if (valid) a.nneigh[Q.row] = count;
+    if (lane == 0) add_stats(a.stats, visits, tests, walks);
     }
 
 } // namespace gpu

@@ -75,12 +75,14 @@ int nbr_lbvh_get_arrays(nbr_lbvh h, const int** parent, const int** left, const 
 /* Addition: sorted Morton codes of the last build (managed pointer). */
 int nbr_lbvh_get_codes(nbr_lbvh h, const unsigned int** codes);
 
-/* Addition: the 16-bit pre-order traversal tree (device pointers): nodes uint32[4*n],
- * points float4[N] (x, y, z, primitive id bits), frame float[9] (root lo, root hi, scale). */
-int nbr_lbvh_get_fast(nbr_lbvh h, const unsigned int** nodes, const float** points,
-                      const float** frame, unsigned int* count_bits, unsigned int* leaf_size);
+/* Addition: the traversal tree (device pointers): records uint32[4*n] in depth-first pre-order
+ * (box record {16-bit bins, skip} or point record {x, y, z, 0x80000000 | primitive id}),
+ * points float4[N] (sorted x, y, z, primitive id bits), frame float[9] (root lo, root hi,
+ * scale). */
+int nbr_lbvh_get_fast(nbr_lbvh h, const unsigned int** records, const float** points,
+                      const float** frame, unsigned int* leaf_size);
 
-/* Addition: number of live traversal nodes (synchronises `stream`). */
+/* Addition: number of traversal records (synchronises `stream`). */
 int nbr_lbvh_num_fast_nodes(nbr_lbvh h, unsigned int* n, void* stream);
 
 /* Addition: synchronise `stream` and report NBR_ERR_DEVICE_WAIT if a bounded wait of the last
@@ -104,6 +106,14 @@ int nbr_traverser_reset(nbr_traverser t);
  * fast kernel (default). */
 int nbr_traverser_set_fast_path(nbr_traverser t, int enabled);
 
+/* Addition: fast-path kernel, 0 = one thread per query, 1 = one warp per 32 consecutive
+ * queries (default). */
+int nbr_traverser_set_mode(nbr_traverser t, int mode);
+
+/* Addition: optional device counters (3 x uint64: node visits, point tests, packets walked)
+ * that fast-path traversals add to; NULL disables them. */
+int nbr_traverser_set_stats(nbr_traverser t, unsigned long long* counters);
+
 /* getData() (LBVHTraverser.h:326-329): int4 nodes in the reference's 10-bit layout (managed),
  * plus the compression frame (lo, hi, bins: managed float[3] each). */
 int nbr_traverser_get_data(nbr_traverser t, const int** data, const float** lo, const float** hi,
@@ -112,7 +122,9 @@ int nbr_traverser_get_data(nbr_traverser t, const int** data, const float** lo, 
 /* LBVHTraverser::traverse(params, lbvh, query, out, images, transform) (LBVHTraverser.h:414-450)
  * with query = SphereQueryOp or ExactSphereQueryOp (query_kind), out = CountNeighborsOp when
  * list == NULL else NeighborListOp(list, nneigh, max_neigh) (OutputOps.h:28-176),
- * images = SelfOp when images == NULL else ImageListOp<float3> (TranslateOps.h:19-91),
+ * images = ImageListOp<float3> (TranslateOps.h:55-91) when images != NULL, the 27 periodic
+ * images of `box` (PeriodicImagesOp, the list test/lbvh_test.cu:427-440 builds) when images ==
+ * NULL and n_images == 27, else SelfOp (TranslateOps.h:19-46),
  * transform = NullTransformOp when map == NULL else MapTransformOp (TransformOps.h:25-64).
  *   spheres: float4[Q] (x, y, z, radius or cutoff)
  *   points, box, pad: used by the exact query only (positions indexed by the reported id,
@@ -125,7 +137,7 @@ int nbr_traverse(nbr_traverser t, nbr_lbvh h, int query_kind, const float* spher
 /* Addition: every primitive of a point tree queries the tree with cutoff rc (exact predicate).
  * Queries run in the tree's sorted order; rows_sorted = 1 writes row s for sorted slot s (the
  * layout the reference benchmark uses, benchmark/lbvh_benchmark.cc:177-184), 0 writes row
- * primitive[s].  list == NULL => counts only. */
+ * primitive[s].  list == NULL => counts only.  Images as in nbr_traverse. */
 int nbr_traverse_self(nbr_traverser t, nbr_lbvh h, float rc, const float box[3], float pad,
                       const float* images, unsigned int n_images, const unsigned int* map,
                       unsigned int* nneigh, unsigned int* list, unsigned int max_neigh,

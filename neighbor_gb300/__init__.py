@@ -86,7 +86,7 @@ def _declare(L):
                                ctypes.POINTER(_U)])
     sig("nbr_lbvh_get_arrays", [_P, _PP, _PP, _PP, _PP, _PP, _PP])
     sig("nbr_lbvh_get_codes", [_P, _PP])
-    sig("nbr_lbvh_get_fast", [_P, _PP, _PP, _PP, ctypes.POINTER(_U), ctypes.POINTER(_U)])
+    sig("nbr_lbvh_get_fast", [_P, _PP, _PP, _PP, ctypes.POINTER(_U)])
     sig("nbr_lbvh_num_fast_nodes", [_P, ctypes.POINTER(_U), _P])
     sig("nbr_lbvh_check_status", [_P, _P])
     sig("nbr_traverser_create", [_PP])
@@ -94,6 +94,8 @@ def _declare(L):
     sig("nbr_traverser_setup", [_P, _P, _P, _U, _P])
     sig("nbr_traverser_reset", [_P])
     sig("nbr_traverser_set_fast_path", [_P, _I])
+    sig("nbr_traverser_set_mode", [_P, _I])
+    sig("nbr_traverser_set_stats", [_P, _P])
     sig("nbr_traverser_get_data", [_P, _PP, _PP, _PP, _PP])
     sig("nbr_traverse", [_P, _P, _I, _P, _U, _P, _P, _F, _P, _U, _P, _P, _P, _U, _U, _P])
     sig("nbr_traverse_self", [_P, _P, _F, _P, _F, _P, _U, _P, _P, _P, _U, _I, _U, _P])
@@ -108,6 +110,7 @@ EXPORTED = ["nbr_last_error", "nbr_version", "nbr_lbvh_create", "nbr_lbvh_destro
             "nbr_lbvh_get_codes", "nbr_lbvh_get_fast", "nbr_lbvh_num_fast_nodes",
             "nbr_lbvh_check_status", "nbr_traverser_create", "nbr_traverser_destroy",
             "nbr_traverser_setup", "nbr_traverser_reset", "nbr_traverser_set_fast_path",
+            "nbr_traverser_set_mode", "nbr_traverser_set_stats",
             "nbr_traverser_get_data", "nbr_traverse", "nbr_traverse_self", "nbr_exact_pad",
             "nbr_debug_wait_timeout"]
 
@@ -296,18 +299,18 @@ class LBVH:
         return n.value
 
     def fast(self, stream=None):
-        """Copies of the 16-bit pre-order nodes, the sorted payload and the frame."""
+        """Copies of the traversal records, the sorted payload and the frame."""
         torch = _torch()
         n = self.num_fast_nodes(stream)
         nodes, pts, frame = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
-        cb, ls = ctypes.c_uint(), ctypes.c_uint()
+        ls = ctypes.c_uint()
         _check(self._L.nbr_lbvh_get_fast(self._h, ctypes.byref(nodes), ctypes.byref(pts),
-                                         ctypes.byref(frame), ctypes.byref(cb), ctypes.byref(ls)))
+                                         ctypes.byref(frame), ctypes.byref(ls)))
         _, N, _, _ = self.sizes()
         return dict(nodes=_view(nodes.value, (n, 4), "<u4", torch.int32).clone(),
                     points=_view(pts.value, (N, 4), "<f4", torch.float32).clone(),
                     frame=_view(frame.value, (9,), "<f4", torch.float32).clone(),
-                    count_bits=cb.value, leaf_size=ls.value)
+                    leaf_size=ls.value)
 
     def check_status(self, stream=None):
         _check(self._L.nbr_lbvh_check_status(self._h, _stream_ptr(stream)))
@@ -343,6 +346,15 @@ class LBVHTraverser:
     def set_fast_path(self, enabled: bool):
         _check(self._L.nbr_traverser_set_fast_path(self._h, 1 if enabled else 0))
 
+    def set_stats(self, counters):
+        """counters: CUDA int64 tensor of 3 (node visits, point tests, packets) or None."""
+        self._stats = counters
+        _check(self._L.nbr_traverser_set_stats(self._h, None if counters is None else counters.data_ptr()))
+
+    def set_mode(self, mode: int):
+        """0 = one thread per query, 1 = one warp per 32 consecutive queries."""
+        _check(self._L.nbr_traverser_set_mode(self._h, int(mode)))
+
     def get_data(self, lbvh: LBVH):
         """Copy of getData() (int4 reference-layout nodes) and the compression frame."""
         torch = _torch()
@@ -360,12 +372,14 @@ class LBVHTraverser:
                  nneigh=None, neigh_list=None, block_size: int = 32, stream=None):
         """LBVHTraverser::traverse with Count (max_neigh None) or NeighborList output.
 
-        Returns nneigh, or (nneigh, list[Q, max_neigh])."""
+        images: a CUDA float32 [n, 3] tensor, None (self image only) or "periodic" (the 27 images
+        of `box`).  Returns nneigh, or (nneigh, list[Q, max_neigh])."""
         torch = _torch()
         sph = _dev(spheres, torch.float32, 4)
         Q = sph.shape[0]
         pts = None if points is None else _dev(points, torch.float32, 3)
-        img = None if images is None else _dev(images, torch.float32, 3)
+        lattice = isinstance(images, str) and images == "periodic"
+        img = None if images is None or lattice else _dev(images, torch.float32, 3)
         m = None if map is None else _dev(map, torch.int32)
         if nneigh is None:
             nneigh = torch.empty(Q, dtype=torch.int32, device=sph.device)
@@ -374,7 +388,8 @@ class LBVHTraverser:
             lst = torch.full((Q, max(max_neigh, 1)), -1, dtype=torch.int32, device=sph.device)
         b = _f3(box if box is not None else (0.0, 0.0, 0.0))
         _check(self._L.nbr_traverse(self._h, lbvh.handle, int(query), _ptr(sph), Q, _ptr(pts), b,
-                                    float(pad), _ptr(img), 0 if img is None else img.shape[0],
+                                    float(pad), _ptr(img),
+                                    27 if lattice else (0 if img is None else img.shape[0]),
                                     _ptr(m), _ptr(nneigh), _ptr(lst),
                                     0 if max_neigh is None else int(max_neigh), block_size,
                                     _stream_ptr(stream)))
@@ -388,7 +403,8 @@ class LBVHTraverser:
         """Every primitive of a point tree queries the tree (exact predicate, fast path)."""
         torch = _torch()
         _, N, _, _ = lbvh.sizes()
-        img = None if images is None else _dev(images, torch.float32, 3)
+        lattice = isinstance(images, str) and images == "periodic"
+        img = None if images is None or lattice else _dev(images, torch.float32, 3)
         m = None if map is None else _dev(map, torch.int32)
         if nneigh is None:
             nneigh = torch.empty(N, dtype=torch.int32, device="cuda")
@@ -396,7 +412,9 @@ class LBVHTraverser:
         if max_neigh is not None and lst is None:
             lst = torch.full((N, max(max_neigh, 1)), -1, dtype=torch.int32, device="cuda")
         _check(self._L.nbr_traverse_self(self._h, lbvh.handle, float(rc), _f3(box), float(pad),
-                                         _ptr(img), 0 if img is None else img.shape[0], _ptr(m),
+                                         _ptr(img),
+                                         27 if lattice else (0 if img is None else img.shape[0]),
+                                         _ptr(m),
                                          _ptr(nneigh), _ptr(lst),
                                          0 if max_neigh is None else int(max_neigh),
                                          1 if rows_sorted else 0, block_size,

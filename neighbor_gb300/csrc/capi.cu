@@ -83,6 +83,8 @@ void dispatch_images(neighbor::LBVHTraverser& t, const neighbor::LBVH& h,
         neighbor::SphereQueryOp q(reinterpret_cast<float4*>(const_cast<float*>(spheres)), Q);
         if (images)
             t.traverse(p, h, q, out, neighbor::ImageListOp<float3>(reinterpret_cast<const float3*>(images), n_images), transform);
+        else if (n_images == 27)
+            t.traverse(p, h, q, out, neighbor::PeriodicImagesOp(box), transform);
         else
             t.traverse(p, h, q, out, neighbor::SelfOp(), transform);
         }
@@ -92,6 +94,8 @@ void dispatch_images(neighbor::LBVHTraverser& t, const neighbor::LBVH& h,
                                        reinterpret_cast<const float3*>(points), box, pad);
         if (images)
             t.traverse(p, h, q, out, neighbor::ImageListOp<float3>(reinterpret_cast<const float3*>(images), n_images), transform);
+        else if (n_images == 27)
+            t.traverse(p, h, q, out, neighbor::PeriodicImagesOp(box), transform);
         else
             t.traverse(p, h, q, out, neighbor::SelfOp(), transform);
         }
@@ -121,6 +125,14 @@ void self_transform(neighbor::LBVHTraverser& t, const neighbor::LBVH& h,
     if (images)
         {
         neighbor::ImageListOp<float3> img(reinterpret_cast<const float3*>(images), n_images);
+        if (map)
+            t.traverseSelf(p, h, rc, box, pad, out, img, neighbor::MapTransformOp(map), rows_sorted);
+        else
+            t.traverseSelf(p, h, rc, box, pad, out, img, neighbor::NullTransformOp(), rows_sorted);
+        }
+    else if (n_images == 27)
+        {
+        neighbor::PeriodicImagesOp img(box);
         if (map)
             t.traverseSelf(p, h, rc, box, pad, out, img, neighbor::MapTransformOp(map), rows_sorted);
         else
@@ -225,15 +237,14 @@ int nbr_lbvh_get_codes(nbr_lbvh h, const unsigned int** codes)
     return NBR_OK;
     }
 
-int nbr_lbvh_get_fast(nbr_lbvh h, const unsigned int** nodes, const float** points, const float** frame,
-                      unsigned int* count_bits, unsigned int* leaf_size)
+int nbr_lbvh_get_fast(nbr_lbvh h, const unsigned int** records, const float** points,
+                      const float** frame, unsigned int* leaf_size)
     {
     if (!h) return fail(NBR_ERR_INVALID, "null handle");
     const neighbor::FastLBVHData f = h->lbvh.fastData();
-    if (nodes) *nodes = reinterpret_cast<const unsigned int*>(f.nodes);
+    if (records) *records = reinterpret_cast<const unsigned int*>(f.nodes);
     if (points) *points = reinterpret_cast<const float*>(f.points);
     if (frame) *frame = reinterpret_cast<const float*>(f.frame);
-    if (count_bits) *count_bits = f.count_bits;
     if (leaf_size) *leaf_size = f.leaf_size;
     return NBR_OK;
     }
@@ -289,6 +300,19 @@ int nbr_traverser_set_fast_path(nbr_traverser t, int enabled)
     return NBR_OK;
     }
 
+int nbr_traverser_set_mode(nbr_traverser t, int mode)
+    {
+    if (!t) return fail(NBR_ERR_INVALID, "null handle");
+    return guarded([&] { t->trav.setMode(mode); });
+    }
+
+int nbr_traverser_set_stats(nbr_traverser t, unsigned long long* counters)
+    {
+    if (!t) return fail(NBR_ERR_INVALID, "null handle");
+    t->trav.setStats(counters);
+    return NBR_OK;
+    }
+
 int nbr_traverser_get_data(nbr_traverser t, const int** data, const float** lo, const float** hi,
                            const float** bins)
     {
@@ -310,6 +334,7 @@ int nbr_traverse(nbr_traverser t, nbr_lbvh h, int query_kind, const float* spher
         return fail(NBR_ERR_INVALID, "unknown query kind");
     if (Q > 0 && (!spheres || !nneigh)) return fail(NBR_ERR_INVALID, "null argument");
     if (query_kind == NBR_QUERY_EXACT && (!points || !box)) return fail(NBR_ERR_INVALID, "exact query needs points and box");
+    if (!images && n_images == 27 && !box) return fail(NBR_ERR_INVALID, "periodic images need the box");
     if (list && max_neigh == 0) return fail(NBR_ERR_INVALID, "max_neigh must be positive with a list");
     if (images && n_images > 32) return fail(NBR_ERR_INVALID, "A maximum of 32 image vectors are supported by LBVH traversers.");
     if (!valid_block(block_size)) return fail(NBR_ERR_INVALID, "Invalid tuning parameter.");

@@ -93,7 +93,7 @@ def _declare(L):
     L.orc_celllist_csr.restype = ctypes.c_int
     L.orc_pair_distance_minus_rc_f64.argtypes = [_P, _P, _f, _P]
     L.orc_pair_distance_minus_rc_f64.restype = ctypes.c_double
-    L.orc_fast_nodes.argtypes = [_u32, _u32, _u32, _P, _P, _P, _P, _P, _P, _P]
+    L.orc_fast_nodes.argtypes = [_u32, _u32, _P, _P, _P, _P, _P, _P, _P, _P]
     L.orc_fast_nodes.restype = _u32
     L.orc_fast_frame.argtypes = [_P, _P, _P]
     L.orc_fast_quantize.argtypes = [_P, _P, _P, _P, _P]
@@ -230,14 +230,14 @@ def pair_distance_minus_rc_f64(pi, pj, rc, box_L=(0, 0, 0)):
                                                 _ptr(_f32(box_L)))
 
 
-def fast_nodes(tree, leaf_size, count_bits):
-    """The project's 16-bit pre-order nodes restated: (nodes[n_live,4] uint32, frame[6])."""
+def fast_nodes(tree, leaf_size):
+    """The project's traversal records restated: (records[n,4] uint32, frame[6])."""
     N = tree["N"]
-    nodes = np.zeros((max(2 * N - 1, 1), 4), np.uint32)
+    nodes = np.zeros((max(2 * N, 1), 4), np.uint32)
     frame = np.zeros(6, np.float32)
-    n = lib().orc_fast_nodes(N, leaf_size, count_bits, _ptr(tree["parent"]), _ptr(tree["left"]),
-                             _ptr(tree["right"]), _ptr(tree["lo"]), _ptr(tree["hi"]),
-                             _ptr(nodes), _ptr(frame))
+    n = lib().orc_fast_nodes(N, leaf_size, _ptr(tree["parent"]), _ptr(tree["left"]),
+                             _ptr(tree["right"]), _ptr(tree["primitive"]), _ptr(tree["lo"]),
+                             _ptr(tree["hi"]), _ptr(nodes), _ptr(frame))
     return nodes[:n].copy(), frame
 
 

@@ -615,12 +615,14 @@ int orc_celllist_csr(const float* qpos, const float* qr, float rc, uint32_t Q, c
 // The project's 16-bit pre-order node format (no counterpart in the reference; the
 // reference compresses to 10-bit int4 nodes in Karras order).
 // ---------------------------------------------------------------------------------------
+// Bins are 15 bits (0..32767) held in 16-bit fields: the top bit of each field is the guard bit
+// of the packed compare the traversal uses.
 void orc_fast_frame(const float* root_lo, const float* root_hi, float* frame) {
     for (int d = 0; d < 3; ++d) {
         float ext = orc_fsub_ru(root_hi[d], root_lo[d]);
         if (!(ext > 0.f)) ext = 1.0f;
         frame[d] = root_lo[d];
-        frame[3 + d] = orc_fdiv_rd(65535.f, ext);
+        frame[3 + d] = orc_fdiv_rd(32767.f, ext);
     }
 }
 
@@ -629,20 +631,19 @@ void orc_fast_quantize(const float* frame, const float* lo, const float* hi, uin
     for (int d = 0; d < 3; ++d) {
         const float a = orc_fmul_rd(orc_fsub_rd(lo[d], frame[d]), frame[3 + d]);
         const float b = orc_fmul_ru(orc_fsub_ru(hi[d], frame[d]), frame[3 + d]);
-        qlo[d] = clampu(std::floor(a), 0.f, 65535.f);
-        qhi[d] = clampu(std::ceil(b), 0.f, 65535.f);
+        qlo[d] = clampu(std::floor(a), 0.f, 32767.f);
+        qhi[d] = clampu(std::ceil(b), 0.f, 32767.f);
     }
 }
 
-uint32_t orc_fast_nodes(uint32_t N, uint32_t leaf_size, uint32_t count_bits,
-                        const int32_t* parent, const int32_t* left, const int32_t* right,
+uint32_t orc_fast_nodes(uint32_t N, uint32_t leaf_size, const int32_t* parent,
+                        const int32_t* left, const int32_t* right, const uint32_t* primitive,
                         const float* lo, const float* hi, uint32_t* nodes, float* frame) {
     (void)parent;
     if (N == 0) return 0;
     orc_fast_frame(lo, hi, frame);  // root box = node 0
     const uint32_t n_int = N - 1;
     const uint32_t n_nodes = 2 * N - 1;
-    // primitive ranges of every node
     std::vector<uint32_t> first(n_nodes), last(n_nodes);
     for (uint32_t s = 0; s < N; ++s) first[n_int + s] = last[n_int + s] = s;
     if (N > 1) {
@@ -661,45 +662,65 @@ uint32_t orc_fast_nodes(uint32_t N, uint32_t leaf_size, uint32_t count_bits,
             last[v] = last[right[v]];
         }
     }
-    // pre-order over live nodes: the root, and both children of every node of size > B
-    uint32_t n_live = 0;
-    std::vector<uint32_t> pre(n_nodes, 0xffffffffu);
-    std::vector<uint32_t> order;
-    std::vector<uint32_t> stack{0};
-    while (!stack.empty()) {
-        const uint32_t v = stack.back();
-        stack.pop_back();
-        pre[v] = n_live++;
-        order.push_back(v);
-        const uint32_t size = last[v] - first[v] + 1;
-        if (size > leaf_size && v < n_int) {
-            stack.push_back((uint32_t)right[v]);
-            stack.push_back((uint32_t)left[v]);
-        }
-    }
-    // skip = pre-order index just past the subtree = number of live nodes whose first
-    // primitive is <= last(v)
-    std::vector<uint32_t> live_first_count(N + 1, 0);
-    for (uint32_t v : order) live_first_count[first[v] + 1]++;
-    for (uint32_t s = 0; s < N; ++s) live_first_count[s + 1] += live_first_count[s];
-    for (uint32_t v : order) {
-        const uint32_t size = last[v] - first[v] + 1;
+    // Depth-first pre-order records.  A node of more than leaf_size primitives is a box record
+    // followed by its two subtrees; a node of 2..leaf_size primitives (a bucket) is a box record
+    // followed by the point records of its primitives in sorted order; a single primitive is a
+    // point record.  Box: {bins, skip = index just past the subtree}; point: {x, y, z as float
+    // bits, 0x80000000 | primitive id}.
+    uint32_t n_rec = 0;
+    auto emit_box = [&](uint32_t v, uint32_t skip) {
         uint32_t qlo[3], qhi[3];
         orc_fast_quantize(frame, lo + 3 * (size_t)v, hi + 3 * (size_t)v, qlo, qhi);
-        uint32_t link;
-        if (size <= leaf_size || v >= n_int)
-            link = 0x80000000u | (first[v] << count_bits) | (size - 1);
-        else
-            link = live_first_count[last[v] + 1];
-        // hi bins are stored complemented (65535 - hi) so that both the union of two boxes
-        // and the overlap test reduce to packed unsigned 16-bit minima.
-        uint32_t* o = nodes + 4 * (size_t)pre[v];
+        uint32_t* o = nodes + 4 * (size_t)n_rec++;
+        // upper bins complemented (32767 - hi): "box overlaps query" is then "every field of the
+        // box <= the query's field", one guarded packed subtraction per word
         o[0] = qlo[0] | (qlo[1] << 16);
-        o[1] = qlo[2] | ((65535u - qhi[0]) << 16);
-        o[2] = (65535u - qhi[1]) | ((65535u - qhi[2]) << 16);
-        o[3] = link;
+        o[1] = qlo[2] | ((32767u - qhi[0]) << 16);
+        o[2] = (32767u - qhi[1]) | ((32767u - qhi[2]) << 16);
+        o[3] = skip;
+    };
+    auto emit_point = [&](uint32_t s) {
+        const float* p = lo + 3 * (size_t)(n_int + s);
+        uint32_t* o = nodes + 4 * (size_t)n_rec++;
+        std::memcpy(o, p, 3 * sizeof(float));
+        o[3] = 0x80000000u | primitive[s];
+    };
+    // records in a subtree: 1 for a point, 1 + size for a bucket, 1 + both subtrees otherwise
+    std::vector<uint32_t> count(n_nodes, 0);
+    for (uint32_t s = 0; s < N; ++s) count[n_int + s] = 1;
+    if (N > 1) {
+        std::vector<int64_t> order;
+        std::vector<int64_t> st{0};
+        while (!st.empty()) {
+            const int64_t v = st.back();
+            st.pop_back();
+            order.push_back(v);
+            if ((uint32_t)left[v] < n_int) st.push_back(left[v]);
+            if ((uint32_t)right[v] < n_int) st.push_back(right[v]);
+        }
+        for (auto it = order.rbegin(); it != order.rend(); ++it) {
+            const uint32_t v = (uint32_t)*it;
+            const uint32_t size = last[v] - first[v] + 1;
+            count[v] = size <= leaf_size ? 1 + size : 1 + count[left[v]] + count[right[v]];
+        }
     }
-    return n_live;
+    std::vector<uint32_t> st{0};
+    while (!st.empty()) {
+        const uint32_t v = st.back();
+        st.pop_back();
+        const uint32_t size = last[v] - first[v] + 1;
+        if (size == 1) {
+            emit_point(first[v]);
+        } else if (size <= leaf_size) {
+            emit_box(v, n_rec + count[v]);
+            for (uint32_t s = first[v]; s <= last[v]; ++s) emit_point(s);
+        } else {
+            emit_box(v, n_rec + count[v]);
+            st.push_back((uint32_t)right[v]);
+            st.push_back((uint32_t)left[v]);
+        }
+    }
+    return n_rec;
 }
 
 }  // extern "C"

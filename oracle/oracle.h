@@ -123,20 +123,21 @@ int orc_celllist_csr(const float* qpos, const float* qr, float rc, uint32_t Q,
 double orc_pair_distance_minus_rc_f64(const float* pi, const float* pj, float rc,
                                       const float box_L[3]);
 
-/* ---- the project's own 16-bit pre-order node format (restated for bit-exact checks of
- *      the CUDA build) ----
- * nodes: uint32[4*n] with words {lo.x|lo.y<<16, lo.z|~hi.x<<16, ~hi.y|~hi.z<<16, link}
- * where ~h = 65535-h (complemented upper bins);
- * link = skip index for an internal node, or 0x80000000 | first<<cbits | (count-1) for a
- * leaf bucket.  Returns the number of live nodes.  frame: {root_lo[3], scale[3]}. */
-uint32_t orc_fast_nodes(uint32_t N, uint32_t leaf_size, uint32_t count_bits,
-                        const int32_t* parent, const int32_t* left, const int32_t* right,
+/* ---- the project's own traversal records (restated for bit-exact checks of the CUDA build) ----
+ * Depth-first pre-order records of 4 uint32 each.  A box record {lo.x|lo.y<<16,
+ * lo.z|~hi.x<<16, ~hi.y|~hi.z<<16, skip} (~h = 32767-h; 15-bit bins of the root box, outward
+ * rounded, in 16-bit fields) covers a subtree of more than leaf_size primitives (followed by its two subtrees) or a
+ * bucket of 2..leaf_size primitives (followed by their point records); a point record
+ * {x, y, z as float bits, 0x80000000 | primitive id} is one primitive.  Returns the record count;
+ * frame: {root_lo[3], scale[3]}. */
+uint32_t orc_fast_nodes(uint32_t N, uint32_t leaf_size, const int32_t* parent,
+                        const int32_t* left, const int32_t* right, const uint32_t* primitive,
                         const float* lo, const float* hi, uint32_t* nodes, float* frame);
 
-/* Quantization frame of the 16-bit format: root_lo and scale = fdiv_rd(65535, fsub_ru(hi,lo)). */
+/* Quantization frame of the records: root_lo and scale = fdiv_rd(32767, fsub_ru(hi,lo)). */
 void orc_fast_frame(const float* root_lo, const float* root_hi, float* frame);
 
-/* Box -> conservative 16-bit bins in the frame (lo rounded down, hi rounded up). */
+/* Box -> conservative 15-bit bins in the frame (lo rounded down, hi rounded up). */
 void orc_fast_quantize(const float* frame, const float* lo, const float* hi, uint32_t* qlo,
                        uint32_t* qhi);
 

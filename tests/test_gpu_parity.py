@@ -66,7 +66,8 @@ def _check_tree(lbvh, P, lo, hi, insert=O.INSERT_POINT, r=0.0):
     T = O.build_tree(P, lo, hi, insert=insert, r=r)
     a = lbvh.arrays()
     N = len(P)
-    assert np.array_equal(lbvh.codes().cpu().numpy().view(np.uint32), T["codes"])
+    if N > 1:  # a one-primitive build computes no codes (reference: LBVH.h:252-257)
+        assert np.array_equal(lbvh.codes().cpu().numpy().view(np.uint32), T["codes"])
     assert np.array_equal(a["primitive"].cpu().numpy().view(np.uint32), T["primitive"])
     assert np.array_equal(a["parent"].cpu().numpy(), T["parent"])
     if N > 1:
@@ -85,8 +86,7 @@ def test_tree_and_nodes_edge_cases(name, P, lo, hi, leaf):
     lbvh.check_status()
     T = _check_tree(lbvh, P, lo, hi)
     fast = lbvh.fast()
-    cb = fast["count_bits"]
-    want_nodes, want_frame = O.fast_nodes(T, leaf, cb)
+    want_nodes, want_frame = O.fast_nodes(T, leaf)
     assert np.array_equal(fast["frame"].cpu().numpy()[[0, 1, 2, 6, 7, 8]], want_frame)
     assert np.array_equal(fast["nodes"].cpu().numpy().view(np.uint32), want_nodes)
     # reference-layout nodes (getData) after setup
@@ -126,7 +126,7 @@ def test_fast_nodes_clustered(leaf):
     lbvh.check_status()
     T = O.build_tree(P, [0, 0, 0], [L, L, L])
     fast = lbvh.fast()
-    want, _ = O.fast_nodes(T, leaf, fast["count_bits"])
+    want, _ = O.fast_nodes(T, leaf)
     assert np.array_equal(fast["nodes"].cpu().numpy().view(np.uint32), want)
 
 
@@ -134,9 +134,11 @@ def _csr_rows(off, nbrs, i):
     return nbrs[off[i]:off[i + 1]]
 
 
+@pytest.mark.parametrize("images", ["list", "periodic"])
+@pytest.mark.parametrize("mode", [0, 1])
 @pytest.mark.parametrize("leaf", [1, 4, 8])
 @pytest.mark.parametrize("dist", ["uniform", "clustered"])
-def test_exact_self_lists_match_cell_list(leaf, dist):
+def test_exact_self_lists_match_cell_list(leaf, dist, mode, images):
     N = 40000
     P, L = _uniform(N, 7)
     if dist == "clustered":
@@ -146,8 +148,9 @@ def test_exact_self_lists_match_cell_list(leaf, dist):
     lbvh = nb.LBVH(leaf_size=leaf)
     lbvh.build(_t(P), [0, 0, 0], box)
     trav = nb.LBVHTraverser()
+    trav.set_mode(mode)
     pad = nb.exact_pad(rc, 2 * L)
-    imgs = nb.images27(box)
+    imgs = nb.images27(box) if images == "list" else "periodic"
     cnt = trav.traverse_self(lbvh, rc, box, pad, images=imgs, rows_sorted=False)
     off, nbrs = O.celllist_csr(P, P, rc, [0, 0, 0], box)
     want = np.diff(off).astype(np.uint32)
@@ -160,6 +163,24 @@ def test_exact_self_lists_match_cell_list(leaf, dist):
     got_sorted = np.sort(np.where(np.arange(mx)[None, :] < want[:, None], lst, 0xFFFFFFFF), axis=1)
     flat = got_sorted[got_sorted != 0xFFFFFFFF]
     assert np.array_equal(flat, nbrs)
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_exact_unsorted_queries(mode):
+    # queries in random order (packets are not compact) and a small open box
+    rng = np.random.default_rng(30)
+    P = (rng.random((6000, 3)) * 12).astype(np.float32)
+    Qp = (rng.random((3000, 3)) * 14 - 1).astype(np.float32)
+    r = rng.uniform(0.3, 1.6, 3000).astype(np.float32)
+    lbvh = nb.LBVH(leaf_size=4)
+    lbvh.build(_t(P), [0, 0, 0], [12, 12, 12])
+    trav = nb.LBVHTraverser()
+    trav.set_mode(mode)
+    sph = np.concatenate([Qp, r[:, None]], 1)
+    got = trav.traverse(lbvh, _t(sph), query=nb.QUERY_EXACT, points=_t(P), box=(0, 0, 0),
+                        pad=nb.exact_pad(1.6, 16.0)).cpu().numpy().view(np.uint32)
+    want = O.brute_count(Qp, r, P, (0, 0, 0))
+    assert np.array_equal(got, want)
 
 
 def test_exact_query_rows_sorted_and_transform():
@@ -250,3 +271,23 @@ def test_rebuild_shrink_and_grow():
         lbvh.build(_t(P), [0, 0, 0], [L, L, L])
         lbvh.check_status()
         _check_tree(lbvh, P, [0, 0, 0], [L, L, L])
+
+
+def test_periodic_images_op_matches_explicit_list():
+    # PeriodicImagesOp must give exactly the explicit 27-image list's results, on the fast path
+    # (exact query) and on the reference-layout path (stock query).
+    P, L = _uniform(15000, 31)
+    box = [L, L, L]
+    lbvh = nb.LBVH()
+    lbvh.build(_t(P), [0, 0, 0], box)
+    sph = _t(np.concatenate([P, np.full((len(P), 1), 1.3, np.float32)], 1))
+    trav = nb.LBVHTraverser()
+    a = trav.traverse(lbvh, sph, images=nb.images27(box))
+    b = trav.traverse(lbvh, sph, images="periodic", box=box)
+    assert torch.equal(a, b)
+    pad = nb.exact_pad(1.3, 2 * L)
+    c = trav.traverse(lbvh, sph, query=nb.QUERY_EXACT, points=_t(P), box=box, pad=pad, images=nb.images27(box))
+    d = trav.traverse(lbvh, sph, query=nb.QUERY_EXACT, points=_t(P), box=box, pad=pad, images="periodic")
+    assert torch.equal(c, d)
+    want, _ = O.celllist_counts(P, P, 1.3, [0, 0, 0], box)
+    assert np.array_equal(d.cpu().numpy().view(np.uint32), want)

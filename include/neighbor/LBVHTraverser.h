@@ -37,7 +37,7 @@ class LBVHTraverser : public Tunable<unsigned int>
     public:
         LBVHTraverser()
             : Tunable<unsigned int>(32, 1024, 32), m_root(0), m_lbvh_lo(1), m_lbvh_hi(1), m_bins(1),
-              m_replay(false), m_fast_enabled(true), m_mode(kPacketTraversal),
+              m_replay(false), m_fast_enabled(true), m_mode(kThreadTraversal),
               m_stats(nullptr)
             {}
 
@@ -136,8 +136,8 @@ class LBVHTraverser : public Tunable<unsigned int>
         void setFastPath(bool enabled) { m_fast_enabled = enabled; }
         bool getFastPath() const { return m_fast_enabled; }
 
-        // Fast-path kernel: kThreadTraversal (one thread walks the tree per query) or
-        // kPacketTraversal (a warp walks it once for 32 consecutive queries; default).
+        // Fast-path kernel: kThreadTraversal (one thread walks the tree per query; default) or
+        // kPacketTraversal (a warp walks it once for 32 consecutive queries).
         enum Mode { kThreadTraversal = 0, kPacketTraversal = 1 };
         void setMode(int mode)
             {

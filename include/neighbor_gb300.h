@@ -106,8 +106,8 @@ int nbr_traverser_reset(nbr_traverser t);
  * fast kernel (default). */
 int nbr_traverser_set_fast_path(nbr_traverser t, int enabled);
 
-/* Addition: fast-path kernel, 0 = one thread per query, 1 = one warp per 32 consecutive
- * queries (default). */
+/* Addition: fast-path kernel, 0 = one thread per query (default), 1 = one warp per 32
+ * consecutive queries. */
 int nbr_traverser_set_mode(nbr_traverser t, int mode);
 
 /* Addition: optional device counters (3 x uint64: node visits, point tests, packets walked)

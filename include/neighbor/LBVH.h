@@ -267,7 +267,7 @@ namespace gpu
 {
 // Single-primitive tree (the reference's lbvh_one_primitive case): identity order, sentinel
 // parent, and a traversal tree of one point record (no box records).
-__global__ void k_single_init(unsigned int* primitive, int* parent, unsigned int* live)
+static __global__ void k_single_init(unsigned int* primitive, int* parent, unsigned int* live)
     {
     if (threadIdx.x == 0 && blockIdx.x == 0)
         {
@@ -278,7 +278,7 @@ __global__ void k_single_init(unsigned int* primitive, int* parent, unsigned int
     }
 // The root (N > 1) is a box record: it adds 1 at position 0 before the hierarchy kernel adds
 // its children's.
-__global__ void k_root_live(unsigned int* live)
+static __global__ void k_root_live(unsigned int* live)
     {
     if (threadIdx.x == 0 && blockIdx.x == 0) live[0] = 1u;
     }

@@ -350,7 +350,7 @@ __device__ __forceinline__ int karras_delta(const unsigned int* __restrict__ cod
     return __clz(ci ^ cj);
     }
 
-__global__ void k_gen_hierarchy(const unsigned int* __restrict__ codes,
+static __global__ void k_gen_hierarchy(const unsigned int* __restrict__ codes,
                                                        unsigned int N, int* __restrict__ left,
                                                        int* __restrict__ right,
                                                        int* __restrict__ parent,
@@ -410,7 +410,7 @@ constexpr int kScanBlock = 256;
 constexpr int kScanItems = 16;
 constexpr int kScanTile = kScanBlock * kScanItems;
 
-__global__ void __launch_bounds__(kScanBlock) k_scan_exclusive(const unsigned int* __restrict__ in,
+static __global__ void __launch_bounds__(kScanBlock) k_scan_exclusive(const unsigned int* __restrict__ in,
                                                                unsigned int* __restrict__ out,
                                                                unsigned int n,
                                                                unsigned long long* __restrict__ status,

@@ -150,6 +150,21 @@ int nbr_traverse_self(nbr_traverser t, nbr_lbvh h, float rc, const float box[3],
  * ended, the kernels finished and the context is still usable. */
 int nbr_debug_wait_timeout(unsigned int* status_out, void* stream);
 
+/* No counterpart in the reference.  The Morton-code and stable-sort stage of the LBVH build for
+ * callers that cannot allocate device memory (a host framework that owns every allocation, a
+ * latency-critical loop that must not touch the allocator, a fully committed memory budget):
+ * codes_out[i] / order_out[i] receive the i-th smallest 30-bit Morton code of the points (scene
+ * bounds lo/hi, as nbr_lbvh_build_points) and the index of its point, equal stably sorted, the
+ * same arrays nbr_lbvh_get_codes / getPrimitives give after a build.  All working memory is one
+ * fixed device array (about 10 MB, held on each GPU that loads the library until exit); N above
+ * NBR_NOALLOC_MAX_POINTS is rejected with NBR_ERR_INVALID.  The first call on a device looks the
+ * array up and should come before any stream capture.  Calls share the array: calls that may
+ * overlap on the GPU must be serialised by the caller. */
+#define NBR_NOALLOC_MAX_POINTS (1u << 20)
+int nbr_morton_sort_noalloc(const float* points, unsigned int N, const float lo[3],
+                            const float hi[3], unsigned int* codes_out, unsigned int* order_out,
+                            void* stream);
+
 /* Radius padding for the exact query: 16 ulps of twice the largest coordinate magnitude
  * (centres, points and image translations) plus 1e-6 * rc. */
 float nbr_exact_pad(float rc, float coord_max);

@@ -101,6 +101,7 @@ def _declare(L):
     sig("nbr_traverse_self", [_P, _P, _F, _P, _F, _P, _U, _P, _P, _P, _U, _I, _U, _P])
     sig("nbr_exact_pad", [_F, _F], _F)
     sig("nbr_debug_wait_timeout", [ctypes.POINTER(_U), _P])
+    sig("nbr_morton_sort_noalloc", [_P, _U, _P, _P, _P, _P, _P])
 
 
 # C-ABI symbols declared in include/neighbor_gb300.h (checked by the CPU tests).
@@ -112,7 +113,9 @@ EXPORTED = ["nbr_last_error", "nbr_version", "nbr_lbvh_create", "nbr_lbvh_destro
             "nbr_traverser_setup", "nbr_traverser_reset", "nbr_traverser_set_fast_path",
             "nbr_traverser_set_mode", "nbr_traverser_set_stats",
             "nbr_traverser_get_data", "nbr_traverse", "nbr_traverse_self", "nbr_exact_pad",
-            "nbr_debug_wait_timeout"]
+            "nbr_debug_wait_timeout", "nbr_morton_sort_noalloc"]
+
+NOALLOC_MAX_POINTS = 1 << 20
 
 
 def _check(rc: int):
@@ -184,6 +187,21 @@ def debug_wait_timeout(stream=None) -> int:
     st = ctypes.c_uint()
     _check(load().nbr_debug_wait_timeout(ctypes.byref(st), _stream_ptr(stream)))
     return st.value
+
+
+def morton_sort_noalloc(points, lo, hi, codes_out, order_out, stream=None):
+    """Morton codes of the points and their stable order, without any device allocation by the
+    library: all working memory is its fixed device array (at most NOALLOC_MAX_POINTS points).
+    codes_out / order_out: preallocated CUDA int32 tensors of N elements."""
+    torch = _torch()
+    p = _dev(points, torch.float32, 3)
+    n = p.shape[0]
+    for t in (codes_out, order_out):
+        if not (isinstance(t, torch.Tensor) and t.is_cuda and t.is_contiguous() and t.numel() >= n
+                and t.element_size() == 4):
+            raise TypeError("outputs must be contiguous 4-byte CUDA tensors of N elements")
+    _check(load().nbr_morton_sort_noalloc(_ptr(p), n, _f3(lo), _f3(hi), _ptr(codes_out),
+                                          _ptr(order_out), _stream_ptr(stream)))
 
 
 def images27(L: Sequence[float], device="cuda"):

@@ -23,6 +23,16 @@ struct nbr_traverser_s
 namespace
 {
 thread_local std::string g_last_error;
+}
+
+namespace neighbor_capi
+{
+// Used by the other translation units of the library (noalloc.cu).
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+}
+
+namespace
+{
 
 int fail(int code, const std::string& msg)
     {

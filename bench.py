@@ -49,6 +49,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-ref-cuda", action="store_true")
     return ap.parse_args()
 
 
@@ -203,6 +204,25 @@ def cpu_baseline(n, L, seconds, threads=0):
     return {"value": pairs / dt, "unit": "pairs/s", "cores": int(used), "kind": "port",
             "sample": f"OpenMP cell list (grid of all {n} points built in the timed call), "
                       f"{q} of {n} queries, counts only, {dt:.2f} s"}
+
+
+def reference_cuda(n, our_ms):
+    """The reference's own CUDA kernels on the same GPU and workload (oracle/ref_harness): the
+    plain two-pass step (build, setup, count, max, fill) with the best block size of 32..512."""
+    try:
+        from oracle import ref_harness
+        if not (ref_harness.build_if_available() and ref_harness.available()):
+            return {"unavailable": "reference kernels not built here"}
+        r = ref_harness.run_bench(n, steps=5, warmup=2, rc=RC)
+    except Exception as e:  # measurement aid only: never fails the bench
+        return {"unavailable": f"{type(e).__name__}: {e}"[:200]}
+    best = min(r["results"], key=lambda x: x["step_ms"])
+    return {"step_ms": best["step_ms"], "block": best["block"],
+            "stages_ms": {k: best[k] for k in ("build_ms", "setup_ms", "count_ms", "fill_ms")},
+            "value": best["pairs_per_step"] / (best["step_ms"] * 1e-3), "unit": "pairs/s",
+            "our_speedup": best["step_ms"] / our_ms, "all_blocks": r["results"],
+            "note": "reference kernels compiled from its headers, launched in its build/setup/"
+                    "traverse order with CUB SortPairs; exact query op; queries in sorted order"}
 
 
 def run_reference(args):
@@ -416,6 +436,8 @@ def run_ours(args):
     }
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(n, L, args.cpu_seconds, os.cpu_count() or 1)
+    if not args.no_ref_cuda:
+        line["reference_cuda"] = reference_cuda(n, line["ms_per_step"])
     print(json.dumps(line))
     return 0
 

@@ -1,0 +1,98 @@
+"""Reference harness -- TEST AND MEASUREMENT INFRASTRUCTURE ONLY.
+
+Builds and runs the reference's own CUDA kernels (mphowardlab/neighbor v0.3.2) on the GPU:
+``ref_kernels.cu`` instantiates them from the reference headers into
+``oracle/_ref/ref_kernels.cubin`` (only where the reference sources exist, i.e. the development
+container), and ``ref_driver.cu`` -- compiled wherever that cubin exists -- loads it and replays
+the reference's build / setup / traverse sequence.  Used by the parity tests (to pin the oracle
+and the library against the real reference) and by bench.py (to time the reference on the same
+GPU).  The product never touches it.
+"""
+from __future__ import annotations
+
+import json
+import os
+import subprocess
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+OUT = os.path.join(os.path.dirname(HERE), "_ref")
+CUBIN = os.path.join(OUT, "ref_kernels.cubin")
+DRIVER = os.path.join(OUT, "ref_driver")
+REFERENCE_INCLUDE = "/root/reference/include"  # the reference sources (development container only)
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def _nvcc():
+    cand = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "bin", "nvcc")
+    return cand if os.path.exists(cand) else "nvcc"
+
+
+def build_cubin(force=False) -> bool:
+    """Compile the reference's kernels from its headers (needs the reference sources)."""
+    if not os.path.isdir(REFERENCE_INCLUDE):
+        return os.path.exists(CUBIN)
+    src = os.path.join(HERE, "ref_kernels.cu")
+    if not force and os.path.exists(CUBIN) and os.path.getmtime(CUBIN) >= os.path.getmtime(src):
+        return True
+    os.makedirs(OUT, exist_ok=True)
+    subprocess.run([_nvcc(), "-std=c++17", "-cubin", *ARCH, "-I", REFERENCE_INCLUDE, "-I", HERE,
+                    "-o", CUBIN, src], check=True)
+    return True
+
+
+def build_driver(force=False) -> bool:
+    """Compile the host driver (wherever the cubin exists)."""
+    if not os.path.exists(CUBIN):
+        return False
+    src = os.path.join(HERE, "ref_driver.cu")
+    if not force and os.path.exists(DRIVER) and os.path.getmtime(DRIVER) >= os.path.getmtime(src):
+        return True
+    subprocess.run([_nvcc(), "-std=c++17", "-O3", *ARCH, "-o", DRIVER, src, "-lcuda"], check=True)
+    return True
+
+
+def build_if_available() -> bool:
+    return build_cubin() and build_driver()
+
+
+def available() -> bool:
+    return os.path.exists(CUBIN) and os.path.exists(DRIVER)
+
+
+def run_bench(n, steps=5, warmup=2, rc=1.3, timeout=600):
+    """Time the reference's plain two-pass step (build, setup, count, max, fill) on uniform
+    trajectory frames for block sizes 32..512; returns the driver's JSON."""
+    r = subprocess.run([DRIVER, "bench", str(n), str(steps), str(warmup), str(rc)],
+                       capture_output=True, text=True, timeout=timeout)
+    if r.returncode != 0:
+        raise RuntimeError(f"reference driver failed ({r.returncode}): {r.stderr.strip()[-400:]}")
+    return json.loads(r.stdout.strip().splitlines()[-1])
+
+
+def run_dump(points, lo, hi, rc, box, timeout=300):
+    """The reference's tree arrays, compressed nodes and counts (stock and exact query, 27
+    periodic images of `box`, queries = the points in input order) for the given points."""
+    P = np.ascontiguousarray(points, np.float32).reshape(-1, 3)
+    n = len(P)
+    with tempfile.TemporaryDirectory() as d:
+        src = os.path.join(d, "points.f32")
+        P.tofile(src)
+        prefix = os.path.join(d, "ref")
+        args = [DRIVER, "dump", src, str(n), *[repr(float(x)) for x in lo], *[repr(float(x)) for x in hi],
+                repr(float(rc)), *[repr(float(x)) for x in box], prefix]
+        r = subprocess.run(args, capture_output=True, text=True, timeout=timeout)
+        if r.returncode != 0:
+            raise RuntimeError(f"reference driver failed ({r.returncode}): {r.stderr.strip()[-400:]}")
+        out = {}
+        for name, dt, shape in [("codes", np.uint32, (n,)), ("primitive", np.uint32, (n,)),
+                                ("parent", np.int32, (2 * n - 1,)), ("left", np.int32, (n - 1,)),
+                                ("right", np.int32, (n - 1,)), ("lo", np.float32, (2 * n - 1, 3)),
+                                ("hi", np.float32, (2 * n - 1, 3)), ("data", np.int32, (2 * n - 1, 4)),
+                                ("count_stock", np.uint32, (n,)), ("count_exact", np.uint32, (n,))]:
+            path = prefix + "." + name
+            if os.path.exists(path):
+                out[name] = np.fromfile(path, dt).reshape(shape)
+        return out

@@ -7,13 +7,20 @@
 // same Karras hierarchy, same boxes.
 //
 // What differs is how it is built (all hand-written sm_103a kernels, no CUB): a fused Morton /
-// histogram / bounds pass, a onesweep radix sort, the Karras kernel, and bottom-up bubbling that
-// also emits the 16-bit pre-order traversal tree (fastData()) with leaf buckets of up to
-// getLeafSize() primitives.  Every spin-wait in those kernels is bounded; checkStatus() reports a
-// wait that gave up.
+// histogram / bounds pass, a onesweep radix sort, a block-local agglomerative climb that forms
+// the radix tree with packed 15-bit boxes, and one pass that writes the 16-bit pre-order
+// traversal tree (fastData()) with leaf buckets of up to getLeafSize() primitives.  Every
+// spin-wait in those kernels is bounded; checkStatus() reports a wait that gave up.
+//
+// The reference-layout arrays (parents, children, float boxes) are not needed by the traversal
+// tree.  For trees of points they are computed when first asked for after a build (a getter,
+// data(), or a traversal with user ops), on the build's stream, so a build that only feeds the
+// fast traversal does not write them; hold no reference to them across builds without calling
+// the getter again.  For every other insert op they are computed during build().
 #ifndef NEIGHBOR_LBVH_H_
 #define NEIGHBOR_LBVH_H_
 
+#include <algorithm>
 #include <cstdint>
 #include <cstring>
 #include <stdexcept>
@@ -60,7 +67,7 @@ class LBVH : public Tunable<unsigned int>
         LBVH()
             : Tunable<unsigned int>(32, 1024, 32), m_root(LBVHSentinel), m_N(0), m_N_internal(0),
               m_N_nodes(0), m_capacity(0), m_leaf_size(4), m_radix_bits(8), m_fast_points(false),
-              m_epoch(0)
+              m_epoch(0), m_block(256), m_stream(0), m_ref_valid(true)
             {}
 
         template<class InsertOpT>
@@ -102,16 +109,21 @@ class LBVH : public Tunable<unsigned int>
         unsigned int getNInternal() const { return m_N_internal; }
         unsigned int getNNodes() const { return m_N_nodes; }
 
-        const shared_array<int>& getParents() const { return m_parent; }
-        const shared_array<int>& getLeftChildren() const { return m_left; }
-        const shared_array<int>& getRightChildren() const { return m_right; }
-        const shared_array<float3>& getLowerBounds() const { return m_lo; }
-        const shared_array<float3>& getUpperBounds() const { return m_hi; }
+        const shared_array<int>& getParents() const { materialize(m_stream); return m_parent; }
+        const shared_array<int>& getLeftChildren() const { materialize(m_stream); return m_left; }
+        const shared_array<int>& getRightChildren() const { materialize(m_stream); return m_right; }
+        const shared_array<float3>& getLowerBounds() const { materialize(m_stream); return m_lo; }
+        const shared_array<float3>& getUpperBounds() const { materialize(m_stream); return m_hi; }
         const shared_array<unsigned int>& getPrimitives() const { return m_indexes.current(); }
         const shared_array<unsigned int>& getCodes() const { return m_codes.current(); }
 
-        const ConstLBVHData data() const
+        const ConstLBVHData data() const { return data(m_stream); }
+
+        // data() with the reference-layout arrays made current on `stream` (for callers whose
+        // kernels run on a stream other than the build's).
+        const ConstLBVHData data(cudaStream_t stream) const
             {
+            materialize(stream);
             ConstLBVHData t;
             t.parent = m_parent.get();
             t.left = m_left.get();
@@ -152,6 +164,8 @@ class LBVH : public Tunable<unsigned int>
             f.nodes = m_nodes.get();
             f.n_boxes = m_small.get() + kSmallLiveCount;
             f.points = m_payload.get();
+            f.primitive = m_indexes.current().get();
+            f.pre = m_live.get();
             f.frame = reinterpret_cast<const QuantFrame*>(m_small.get() + kSmallFrame);
             f.status = m_small.get() + kSmallStatus;
             f.N = m_N;
@@ -191,13 +205,14 @@ class LBVH : public Tunable<unsigned int>
         // layout of the small scratch buffer (uint32 words)
         static constexpr size_t kSmallHist = 0;            // 4 passes x 1024
         static constexpr size_t kSmallOffsets = 4096;      // 4 passes x 1024
-        static constexpr size_t kSmallCounters = 8192;     // tile tickets (one per pass + scan)
+        static constexpr size_t kSmallCounters = 8192;     // tile tickets (passes, scan at +7), climb items at +6
         static constexpr size_t kSmallBounds = 8200;       // 6 words
         static constexpr size_t kSmallStatus = 8206;       // 1 word
         static constexpr size_t kSmallZeroEnd = 8208;      // words cleared before every build
         static constexpr size_t kSmallLiveCount = 8208;    // 1 word
         static constexpr size_t kSmallFrame = 8212;        // QuantFrame (9 floats), 16-byte aligned
         static constexpr size_t kSmallWords = 8224;
+        static constexpr int kClimbBlock = 512;        // sorted leaves per block of the climb
 
         int m_root;
         unsigned int m_N;
@@ -208,19 +223,24 @@ class LBVH : public Tunable<unsigned int>
         unsigned int m_radix_bits;
         bool m_fast_points;
         unsigned int m_epoch;
+        unsigned int m_block;
+        cudaStream_t m_stream;
+        mutable bool m_ref_valid;  // reference-layout arrays match the last build
 
-        shared_array<int> m_parent;
-        shared_array<int> m_left;
-        shared_array<int> m_right;
-        shared_array<float3> m_lo;
-        shared_array<float3> m_hi;
+        mutable shared_array<int> m_parent;
+        mutable shared_array<int> m_left;
+        mutable shared_array<int> m_right;
+        mutable shared_array<float3> m_lo;
+        mutable shared_array<float3> m_hi;
         buffered_array<unsigned int> m_codes;
         buffered_array<unsigned int> m_indexes;
 
-        device_array<uint2> m_ranges;
-        device_array<unsigned int> m_live;     // live-node counts, then their exclusive scan
-        device_array<unsigned int> m_locks;
-        device_array<unsigned char> m_depth;
+        device_array<uint4> m_nbox;            // per internal node: packed box, first primitive
+        device_array<uint2> m_nmeta;           // per internal node: last primitive, db | live
+        device_array<unsigned int> m_kids;     // child ids met at splits across blocks
+        device_array<uint2> m_items;           // nodes whose climb continues across blocks
+        device_array<unsigned int> m_live;     // box records per first primitive, then their scan
+        mutable device_array<unsigned int> m_locks;
         device_array<uint4> m_nodes;
         device_array<float4> m_payload;
         device_array<unsigned int> m_small;
@@ -229,17 +249,13 @@ class LBVH : public Tunable<unsigned int>
 
         void allocate(unsigned int N);
 
-        LBVHData writable()
+        // Reference-layout arrays of the last build (Karras children/parents, float boxes).
+        template<class LeafBoxT>
+        void reference_layout(const LeafBoxT& leaf_box, cudaStream_t stream) const;
+        void materialize(cudaStream_t stream) const
             {
-            LBVHData t;
-            t.parent = m_parent.get();
-            t.left = m_left.get();
-            t.right = m_right.get();
-            t.primitive = m_indexes.current().get();
-            t.lo = m_lo.get();
-            t.hi = m_hi.get();
-            t.root = m_root;
-            return t;
+            if (m_ref_valid) return;
+            reference_layout(gpu::PayloadLeafBox{m_payload.get()}, stream);
             }
 
         unsigned int next_epoch()
@@ -275,12 +291,6 @@ static __global__ void k_single_init(unsigned int* primitive, int* parent, unsig
         parent[0] = LBVHSentinel;
         live[0] = 0u;
         }
-    }
-// The root (N > 1) is a box record: it adds 1 at position 0 before the hierarchy kernel adds
-// its children's.
-static __global__ void k_root_live(unsigned int* live)
-    {
-    if (threadIdx.x == 0 && blockIdx.x == 0) live[0] = 1u;
     }
 } // namespace gpu
 
@@ -319,14 +329,17 @@ inline void LBVH::allocate(unsigned int N)
         m_codes.swap(codes);
         m_indexes.swap(indexes);
         }
-    m_ranges.reserve(N);
+    m_nbox.reserve(N);
+    m_nmeta.reserve(N);
+    m_kids.reserve(2 * (size_t)N);
+    // at most one pending node per split of a block plus two per block edge
+    m_items.reserve((size_t)N + 2 * (size_t)detail::ceil_div(N, kClimbBlock) + 16);
     m_live.reserve((size_t)N + 1 + gpu::kScanTile);
     if (m_locks.size() < N)
         {
         m_locks.reserve(N);
         detail::check_cuda(cudaMemset(m_locks.get(), 0, m_locks.size() * sizeof(unsigned int)), "memset");
         }
-    m_depth.reserve(N);
     m_nodes.reserve(nodes);
     m_payload.reserve(N);
     // one status word per (tile, digit, pass) at the widest configuration: 4 passes x 256 digits
@@ -402,20 +415,49 @@ void LBVH::sort_codes(const InsertOpT& insert, const float3& lo, const float3& e
         }
     }
 
+template<class LeafBoxT>
+void LBVH::reference_layout(const LeafBoxT& leaf_box, cudaStream_t stream) const
+    {
+    m_ref_valid = true;
+    const unsigned int N = m_N;
+    if (N == 0) return;
+    const unsigned int* status = getStatusPointer();
+    const unsigned int bs = m_block;
+    if (N > 1)
+        gpu::k_gen_hierarchy<<<detail::ceil_div(N - 1, bs), bs, 0, stream>>>(
+            m_codes.current().get(), N, m_left.get(), m_right.get(), m_parent.get(), status);
+    gpu::RefBubbleArgs a;
+    a.N = N;
+    a.parent = m_parent.get();
+    a.left = m_left.get();
+    a.right = m_right.get();
+    a.lo = m_lo.get();
+    a.hi = m_hi.get();
+    a.locks = m_locks.get();
+    a.tag = 2u * m_epoch + 1u;
+    a.error = status;
+    gpu::k_ref_bubble<LeafBoxT><<<detail::ceil_div(N, bs), bs, 0, stream>>>(leaf_box, a);
+    detail::check_cuda(cudaGetLastError(), "LBVH reference layout launch");
+    }
+
 template<class InsertOpT>
 void LBVH::build(const LaunchParameters& params, const InsertOpT& insert, const float3& lo, const float3& hi)
     {
     setup(params, insert);
     m_fast_points = is_point_insert<InsertOpT>::value;
+    m_ref_valid = true;
     if (m_N == 0) return;
     checkParameter(params);
     cudaStream_t stream = params.stream;
+    m_stream = stream;
+    m_block = params.tunable;
     const unsigned int N = m_N;
     const unsigned int epoch = next_epoch();
     unsigned int* small = m_small.get();
 
     detail::check_cuda(cudaMemsetAsync(small, 0, kSmallZeroEnd * sizeof(unsigned int), stream), "memset");
-    detail::check_cuda(cudaMemsetAsync(m_live.get(), 0, ((size_t)N + 1) * sizeof(unsigned int), stream), "memset");
+    // counts past the last position stay zero for the scan
+    detail::check_cuda(cudaMemsetAsync(m_live.get() + N, 0, sizeof(unsigned int), stream), "memset");
 
     const float3 ext = make_float3(hi.x - lo.x, hi.y - lo.y, hi.z - lo.z);
     if (N == 1)
@@ -425,48 +467,54 @@ void LBVH::build(const LaunchParameters& params, const InsertOpT& insert, const 
                                                                     small + kSmallBounds);
         gpu::k_single_init<<<1, 32, 0, stream>>>(m_indexes.current().get(), m_parent.get(), m_live.get());
         }
+    else if (m_radix_bits == 10)
+        sort_codes<InsertOpT, 10>(insert, lo, ext, stream, epoch);
     else
-        {
-        if (m_radix_bits == 10)
-            sort_codes<InsertOpT, 10>(insert, lo, ext, stream, epoch);
-        else
-            sort_codes<InsertOpT, 8>(insert, lo, ext, stream, epoch);
+        sort_codes<InsertOpT, 8>(insert, lo, ext, stream, epoch);
 
-        gpu::k_root_live<<<1, 32, 0, stream>>>(m_live.get());
-        const unsigned int bs = params.tunable;
-        gpu::k_gen_hierarchy<<<detail::ceil_div(N - 1, bs), bs, 0, stream>>>(
-            m_codes.current().get(), N, m_left.get(), m_right.get(), m_parent.get(), m_ranges.get(),
-            m_live.get(), m_leaf_size, small + kSmallStatus);
-        }
+    // radix tree, packed boxes, box-record counts
+    gpu::ClimbArgs c;
+    c.N = N;
+    c.codes = m_codes.current().get();
+    c.primitive = m_indexes.current().get();
+    c.payload = m_payload.get();
+    c.nbox = m_nbox.get();
+    c.nmeta = m_nmeta.get();
+    c.kids = m_kids.get();
+    c.locks = m_locks.get();
+    c.tag = 2u * epoch;
+    c.counts = m_live.get();
+    c.items = m_items.get();
+    c.n_items = small + kSmallCounters + 6;
+    c.item_capacity = (unsigned int)m_items.size();
+    c.bounds = small + kSmallBounds;
+    c.frame_out = reinterpret_cast<QuantFrame*>(small + kSmallFrame);
+    c.leaf_size = m_leaf_size;
+    c.error = small + kSmallStatus;
+    gpu::k_climb<InsertOpT, kClimbBlock><<<detail::ceil_div(N, kClimbBlock), kClimbBlock, 0, stream>>>(insert, c);
+    if (N > (unsigned int)kClimbBlock)
+        gpu::k_climb_global<InsertOpT><<<std::min(detail::ceil_div(N, 2048), 152u * 8u), 256, 0, stream>>>(insert, c);
 
-    // pre-order positions of the live nodes
+    // pre-order positions of the box records
     gpu::k_scan_exclusive<<<detail::ceil_div((size_t)N + 1, gpu::kScanTile), gpu::kScanBlock, 0, stream>>>(
         m_live.get(), m_live.get(), N, m_scan_status.get(), epoch & 0x3fffffffu, small + kSmallCounters + 7,
         small + kSmallLiveCount, small + kSmallStatus);
 
-    gpu::BubbleArgs a;
-    a.N = N;
-    a.primitive = m_indexes.current().get();
-    a.parent = m_parent.get();
-    a.left = m_left.get();
-    a.right = m_right.get();
-    a.ranges = m_ranges.get();
-    a.lo = m_lo.get();
-    a.hi = m_hi.get();
-    a.locks = m_locks.get();
-    a.epoch = epoch;
-    a.depth_below = m_depth.get();
-    a.pre = m_live.get();
-    a.nodes = m_nodes.get();
-    a.payload = m_payload.get();
-    a.bounds = small + kSmallBounds;
-    a.frame_out = reinterpret_cast<QuantFrame*>(small + kSmallFrame);
-    a.leaf_size = m_leaf_size;
-    a.error = small + kSmallStatus;
-    a.node_capacity = (unsigned int)m_nodes.size();
-    const unsigned int bs = params.tunable;
-    gpu::k_bubble<InsertOpT><<<detail::ceil_div(N, bs), bs, 0, stream>>>(insert, a);
+    gpu::EmitArgs e;
+    e.N = N;
+    e.payload = m_payload.get();
+    e.nbox = m_nbox.get();
+    e.nmeta = m_nmeta.get();
+    e.pre = m_live.get();
+    e.nodes = m_nodes.get();
+    e.node_capacity = (unsigned int)m_nodes.size();
+    e.error = small + kSmallStatus;
+    gpu::k_emit<<<detail::ceil_div(N, 256), 256, 0, stream>>>(e);
     detail::check_cuda(cudaGetLastError(), "LBVH build launch");
+
+    m_ref_valid = false;
+    if (!is_point_insert<InsertOpT>::value)
+        reference_layout(gpu::InsertLeafBox<InsertOpT>{insert, m_indexes.current().get()}, stream);
     }
 
 } // namespace neighbor

@@ -57,6 +57,8 @@ struct FastLBVHData
     const uint4* nodes;          // records in pre-order
     const unsigned int* n_boxes; // device scalar: number of box records (records = boxes + N)
     const float4* points;        // sorted leaf payload: (x, y, z, primitive id as bits)
+    const unsigned int* primitive; // primitive id of each sorted position
+    const unsigned int* pre;     // box records whose first primitive is below s (N+1 entries)
     const QuantFrame* frame;     // device scalar
     const unsigned int* status;  // build status word; traversals do nothing when it is set
     unsigned int N;              // primitives (= point records)

@@ -38,7 +38,7 @@ class LBVHTraverser : public Tunable<unsigned int>
         LBVHTraverser()
             : Tunable<unsigned int>(32, 1024, 32), m_root(0), m_lbvh_lo(1), m_lbvh_hi(1), m_bins(1),
               m_replay(false), m_fast_enabled(true), m_mode(kThreadTraversal),
-              m_stats(nullptr)
+              m_stats(nullptr), m_symmetric(true)
             {}
 
         template<class TransformOpT>
@@ -151,6 +151,12 @@ class LBVHTraverser : public Tunable<unsigned int>
         // the fast kernels add to; NULL disables them.
         void setStats(unsigned long long* counters) { m_stats = counters; }
 
+        // Self traversals with the self image or PeriodicImagesOp find each unordered pair once
+        // and write it to both rows (default); off: every query walks the whole tree.  Counts,
+        // neighbor sets and the order of each row are the same either way.
+        void setSymmetric(bool enabled) { m_symmetric = enabled; }
+        bool getSymmetric() const { return m_symmetric; }
+
         // Self queries on the fast path: every primitive of the tree queries the tree with cutoff
         // rc.  Queries run in the tree's sorted order; rows_sorted selects whether row s of the
         // output belongs to sorted slot s (the reference benchmark's layout) or to the original
@@ -170,6 +176,10 @@ class LBVHTraverser : public Tunable<unsigned int>
         bool m_fast_enabled;
         int m_mode;
         unsigned long long* m_stats;
+        bool m_symmetric;
+        device_array<unsigned int> m_own;
+        device_array<unsigned int> m_long_rows;
+        device_array<unsigned int> m_n_long;
 
         template<class TransformOpT>
         void compress(const LaunchParameters& params, const LBVH& lbvh, const TransformOpT& transform)
@@ -184,7 +194,7 @@ class LBVHTraverser : public Tunable<unsigned int>
             m_root = lbvh.getRoot();
             const unsigned int bs = params.tunable;
             gpu::k_compress_ref10<TransformOpT><<<detail::ceil_div(n, bs), bs, 0, params.stream>>>(
-                data(), transform, lbvh.data(), lbvh.getNInternal(), n, lbvh.getStatusPointer());
+                data(), transform, lbvh.data(params.stream), lbvh.getNInternal(), n, lbvh.getStatusPointer());
             detail::check_cuda(cudaGetLastError(), "compress launch");
             }
 
@@ -202,6 +212,10 @@ class LBVHTraverser : public Tunable<unsigned int>
         template<class OutputOpT, class TransformOpT>
         void launch_fast(const LaunchParameters& params, const LBVH& lbvh, gpu::FastQueryArgs a,
                          const OutputOpT& out, const TransformOpT& transform, unsigned int Q);
+
+        template<class OutputOpT, class TransformOpT>
+        void launch_half(const LaunchParameters& params, const LBVH& lbvh, const gpu::FastQueryArgs& a,
+                         const OutputOpT& out, const TransformOpT& transform);
     };
 
 namespace detail
@@ -219,6 +233,9 @@ inline int image_lattice(const PeriodicImagesOp&) { return 1; }
 template<class T> inline float3 lattice_box(const T&, float3 box) { return box; }
 inline float3 lattice_box(const PeriodicImagesOp& op, float3) { return op.L; }
 template<class T> inline const float3* image_pointer(const T&) { return nullptr; }
+template<class T> struct is_symmetric_images : std::false_type {};
+template<> struct is_symmetric_images<SelfOp> : std::true_type {};
+template<> struct is_symmetric_images<PeriodicImagesOp> : std::true_type {};
 
 inline void set_output(gpu::FastQueryArgs& a, const CountNeighborsOp& out)
     {
@@ -317,7 +334,60 @@ void LBVHTraverser::traverseSelf(const LaunchParameters& params, const LBVH& lbv
     a.lattice_L = detail::lattice_box(images, box);
     a.box = box;
     a.pad = pad;
-    launch_fast(params, lbvh, a, out, transform, lbvh.getN());
+    detail::set_output(a, out);
+    if (detail::is_symmetric_images<TranslateOpT>::value && m_symmetric && m_mode == kThreadTraversal
+        && !m_stats && lbvh.getN() < gpu::kHalfMaxN
+        && (output_kind<OutputOpT>::value == gpu::kFastCount || a.max_neigh <= gpu::kHalfRowMax))
+        launch_half(params, lbvh, a, out, transform);
+    else
+        launch_fast(params, lbvh, a, out, transform, lbvh.getN());
+    }
+
+template<class OutputOpT, class TransformOpT>
+void LBVHTraverser::launch_half(const LaunchParameters& params, const LBVH& lbvh, const gpu::FastQueryArgs& a,
+                                const OutputOpT& out, const TransformOpT& transform)
+    {
+    constexpr int kind = output_kind<OutputOpT>::value;
+    const unsigned int N = lbvh.getN();
+    cudaStream_t stream = params.stream;
+    gpu::HalfArgs h;
+    h.Q = N;
+    h.rc = a.self_rc;
+    h.pad = a.pad;
+    h.rows_sorted = a.self_rows_sorted;
+    h.lattice = a.lattice;
+    h.lattice_L = a.lattice_L;
+    h.box = a.box;
+    h.nneigh = a.nneigh;
+    h.list = a.list;
+    h.max_neigh = a.max_neigh;
+    h.own = nullptr;
+    if (kind == gpu::kFastList)
+        {
+        m_own.reserve(N);
+        m_long_rows.reserve(N);
+        m_n_long.reserve(1);
+        h.own = m_own.get();
+        }
+    detail::check_cuda(cudaMemsetAsync(a.nneigh, 0, (size_t)N * sizeof(unsigned int), stream), "memset");
+    gpu::k_traverse_half<kind><<<detail::ceil_div(N, 256), 256, 0, stream>>>(lbvh.fastData(), h);
+    if (kind == gpu::kFastList)
+        {
+        gpu::HalfOrderArgs o;
+        o.Q = N;
+        o.nneigh = a.nneigh;
+        o.list = a.list;
+        o.max_neigh = a.max_neigh;
+        o.own = m_own.get();
+        o.primitive = lbvh.fastData().primitive;
+        o.long_rows = m_long_rows.get();
+        o.n_long = m_n_long.get();
+        o.status = lbvh.getStatusPointer();
+        detail::check_cuda(cudaMemsetAsync(o.n_long, 0, sizeof(unsigned int), stream), "memset");
+        gpu::k_half_order_rows<TransformOpT><<<detail::ceil_div(N, 256), 256, 0, stream>>>(o, transform);
+        gpu::k_half_order_long<TransformOpT><<<152u * 4u, 256, 0, stream>>>(o, transform);
+        }
+    detail::check_cuda(cudaGetLastError(), "half traversal launch");
     }
 
 } // namespace neighbor

@@ -1,19 +1,20 @@
 // LBVH build kernels for sm_103a.
 //
-// Stages (one stream, no host synchronisation):
+// Stages of a build (one stream, no host synchronisation):
 //   k_codes_histogram  Morton codes of every primitive -> digit histograms of all radix passes
 //                      and the scene bounds (root box) in one read of the inputs.
 //   k_digit_offsets    exclusive scan of each pass histogram.
 //   k_onesweep         one stable LSD radix pass with decoupled look-back (Adinets & Merrill,
 //                      "Onesweep", 2022); the first pass computes keys from the insert op.
-//   k_gen_hierarchy    Karras 2012 hierarchy (same construction and tie-break as the reference,
-//                      include/neighbor/kernels/LBVH.cuh:169-243), plus primitive ranges and
-//                      the per-position count of live nodes of the collapsed tree.
-//   k_scan_live        chained exclusive scan of those counts (pre-order positions).
-//   k_bubble           bottom-up boxes with one atomic per internal node (as the reference's
-//                      lbvh_bubble_aabbs, include/neighbor/kernels/LBVH.cuh:270-327), writing the
-//                      reference-layout float boxes, the sorted leaf payload and every live
-//                      16-bit pre-order node as soon as its box is final.
+//   k_climb            agglomerative bottom-up construction of the radix tree (the Karras tree of
+//                      the reference, include/neighbor/kernels/LBVH.cuh:169-243) with packed
+//                      15-bit boxes, block-local in shared memory, global across block edges;
+//                      counts the box records of the traversal tree per first primitive.
+//   k_scan_exclusive   chained exclusive scan of those counts (pre-order positions).
+//   k_emit             writes every box and point record at its pre-order slot.
+// Reference-layout arrays (parents, children, float boxes), on demand or for non-point trees:
+//   k_gen_hierarchy    the Karras kernel, k_ref_bubble the reference's bubbling of float boxes
+//                      (include/neighbor/kernels/LBVH.cuh:270-327).
 #ifndef NEIGHBOR_KERNELS_BUILD_CUH_
 #define NEIGHBOR_KERNELS_BUILD_CUH_
 
@@ -335,11 +336,9 @@ __global__ void __launch_bounds__(BLOCK) k_onesweep(const InsertOpT insert, floa
     }
 
 // ---------------------------------------------------------------------------------------------
-// Karras hierarchy.  One thread per internal node i: direction, range end j by exponential and
-// binary search, split by binary search over the longest common prefix with the index tie-break.
-// Also writes range[i] = (first, last) and, for the collapsed tree (buckets of <= leaf_size
-// primitives), adds 1 to live[first(child)] for both children of every node larger than
-// leaf_size (the root's own +1 is set before this kernel).
+// Karras hierarchy (reference layout).  One thread per internal node i: direction, range end j by
+// exponential and binary search, split by binary search over the longest common prefix with the
+// index tie-break; left/right children (leaves at N-1+s) and parents.
 // ---------------------------------------------------------------------------------------------
 __device__ __forceinline__ int karras_delta(const unsigned int* __restrict__ codes, unsigned int ci,
                                             long long i, long long j, long long N)
@@ -350,14 +349,9 @@ __device__ __forceinline__ int karras_delta(const unsigned int* __restrict__ cod
     return __clz(ci ^ cj);
     }
 
-static __global__ void k_gen_hierarchy(const unsigned int* __restrict__ codes,
-                                                       unsigned int N, int* __restrict__ left,
-                                                       int* __restrict__ right,
-                                                       int* __restrict__ parent,
-                                                       uint2* __restrict__ ranges,
-                                                       unsigned int* __restrict__ live,
-                                                       unsigned int leaf_size,
-                                                       const unsigned int* __restrict__ error)
+static __global__ void k_gen_hierarchy(const unsigned int* __restrict__ codes, unsigned int N,
+                                       int* __restrict__ left, int* __restrict__ right,
+                                       int* __restrict__ parent, const unsigned int* __restrict__ error)
     {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long n = N;
@@ -391,15 +385,6 @@ static __global__ void k_gen_hierarchy(const unsigned int* __restrict__ codes,
     parent[lc] = (int)i;
     parent[rc] = (int)i;
     if (i == 0) parent[0] = LBVHSentinel;
-    ranges[i] = make_uint2((unsigned int)first, (unsigned int)last);
-    // Box records of the traversal tree: every node of more than leaf_size primitives, and every
-    // bucket (2..leaf_size primitives) whose parent is larger than leaf_size.  Each adds 1 at its
-    // first primitive; this node adds its children's.
-    if ((unsigned long long)(last - first + 1) > leaf_size)
-        {
-        if (split > first) atomicAdd(live + first, 1u);
-        if (last > split + 1) atomicAdd(live + split + 1, 1u);
-        }
     }
 
 // ---------------------------------------------------------------------------------------------
@@ -512,27 +497,390 @@ __device__ __forceinline__ QuantFrame frame_from_bounds(const unsigned int* boun
     return f;
     }
 
-struct BubbleArgs
+// ---------------------------------------------------------------------------------------------
+// Agglomerative construction of the traversal tree (Apetrei, "Fast and Simple Agglomerative LBVH
+// Construction", 2014).  The binary radix tree over the sorted (code, index) keys is unique, so
+// this is the Karras tree above: node [l, r] is the left child of split r or the right child of
+// split l-1, whichever boundary has the longer common prefix (the Karras delta with its index
+// tie-break, include/neighbor/kernels/LBVH.cuh:73-94); the two can never be equal.
+//
+// One thread per sorted leaf climbs while it is the second child to arrive at a split.  Splits
+// whose two subtrees lie inside the block's range of leaves meet in shared memory; a node whose
+// parent split lies on the block boundary, and a split that only one child reached inside the
+// block, continue after the block's local phase with one global arrival word per split.  Boxes
+// are the packed 15-bit records' words: every field is a "min" field, so the union of two boxes
+// is three 16x2 minima and equals the packing of the union of the float boxes (packing is
+// monotone).  Each internal node p (split index) gets {box, first} and {last, db | live}; a node
+// becomes a box record (live) when its parent has more than leaf_size primitives, or when it is
+// the root, and is then counted at its first primitive for the pre-order scan.
+// ---------------------------------------------------------------------------------------------
+constexpr unsigned int kNodeLeaf = 0x80000000u;  // node id of sorted leaf s: s | kNodeLeaf
+constexpr unsigned int kMetaLive = 0x80000000u;  // set in nmeta.y when the node is a box record
+
+// Common-prefix length of the (code, index) keys at sorted positions i and i + 1.
+__device__ __forceinline__ int adjacent_delta(unsigned int ci, unsigned int cj, unsigned int i)
+    {
+    return (ci != cj) ? __clz(ci ^ cj) : 32 + __clz(i ^ (i + 1u));
+    }
+
+// Split index of the parent of node [l, r] (not the root).
+template<class DeltaF>
+__device__ __forceinline__ unsigned int parent_split(unsigned int l, unsigned int r, unsigned int N,
+                                                     const DeltaF& delta)
+    {
+    if (l == 0u) return r;
+    if (r == N - 1u) return l - 1u;
+    return delta(r) > delta(l - 1u) ? r : l - 1u;
+    }
+
+struct ClimbArgs
     {
     unsigned int N;
-    const unsigned int* primitive;
-    const int* parent;
-    const int* left;
-    const int* right;
-    const uint2* ranges;
-    float3* lo;
-    float3* hi;
-    unsigned int* locks;
-    unsigned int epoch;
-    unsigned char* depth_below;
-    const unsigned int* pre;  // exclusive scan of live counts, N+1 entries
-    uint4* nodes;
-    float4* payload;
+    const unsigned int* codes;      // sorted Morton codes
+    const unsigned int* primitive;  // sorted primitive ids
+    float4* payload;                // per sorted leaf: lower corner of its box, primitive id bits
+    uint4* nbox;                    // internal node p: {packed box (3 words), first}
+    uint2* nmeta;                   // internal node p: {last, db | kMetaLive}
+    unsigned int* kids;             // 2 words per split: child ids met through the arrival words
+    unsigned int* locks;            // arrival word per split, tagged per build
+    unsigned int tag;
+    unsigned int* counts;           // box records per first primitive (written for every position)
+    uint2* items;                   // nodes whose climb continues across blocks: {id, parent split}
+    unsigned int* n_items;          // zero on entry
+    unsigned int item_capacity;
     const unsigned int* bounds;
     QuantFrame* frame_out;
     unsigned int leaf_size;
     const unsigned int* error;
+    };
+
+struct ClimbNode
+    {
+    uint3 box;          // packed bins
+    unsigned int l, r;  // sorted primitive range
+    unsigned int id;    // internal: split index; leaf: s | kNodeLeaf
+    unsigned int db;    // box records below it on its left spine
+    };
+
+__device__ __forceinline__ uint3 merge_boxes(const uint3& a, const uint3& b)
+    {
+    return make_uint3(__vminu2(a.x, b.x), __vminu2(a.y, b.y), __vminu2(a.z, b.z));
+    }
+
+template<class InsertOpT>
+__device__ __forceinline__ ClimbNode climb_leaf(const InsertOpT& insert, const ClimbArgs& A,
+                                                const QuantFrame& f, unsigned int s, bool store)
+    {
+    const unsigned int prim = A.primitive[s];
+    const BoundingBox b = insert.get(prim);
+    if (store) A.payload[s] = make_float4(b.lo.x, b.lo.y, b.lo.z, __uint_as_float(prim));
+    const uint3 w = pack_node_box(f, b.lo, b.hi);
+    ClimbNode n;
+    n.box = w;
+    n.l = s;
+    n.r = s;
+    n.id = s | kNodeLeaf;
+    n.db = 0u;
+    return n;
+    }
+
+// Form internal node p from its left child L and right child R.  LOCAL: counts go to the block's
+// shared counters (index - base), else to the global ones.
+template<bool LOCAL>
+__device__ __forceinline__ ClimbNode form_parent(const ClimbArgs& A, unsigned int p, const ClimbNode& L,
+                                                 const ClimbNode& R, unsigned int* s_count,
+                                                 unsigned int base)
+    {
+    ClimbNode P;
+    P.box = merge_boxes(L.box, R.box);
+    P.l = L.l;
+    P.r = R.r;
+    P.id = p;
+    const bool big = (P.r - P.l + 1u) > A.leaf_size;
+    const bool root = (P.l == 0u && P.r == A.N - 1u);
+    const bool l_internal = !(L.id & kNodeLeaf);
+    const bool r_internal = !(R.id & kNodeLeaf);
+    P.db = (big && l_internal) ? L.db + 1u : 0u;
+    A.nbox[p] = make_uint4(P.box.x, P.box.y, P.box.z, P.l);
+    A.nmeta[p] = make_uint2(P.r, P.db | (root ? kMetaLive : 0u));
+    unsigned int c0 = root ? 1u : 0u;  // records counted at P.l (root, left child)
+    if (big && l_internal)
+        {
+        A.nmeta[L.id] = make_uint2(L.r, L.db | kMetaLive);
+        ++c0;
+        }
+    if (c0)
+        {
+        if (LOCAL) atomicAdd(s_count + (P.l - base), c0);
+        else atomicAdd(A.counts + P.l, c0);
+        }
+    if (big && r_internal)
+        {
+        A.nmeta[R.id] = make_uint2(R.r, R.db | kMetaLive);
+        if (LOCAL) atomicAdd(s_count + (R.l - base), 1u);
+        else atomicAdd(A.counts + R.l, 1u);
+        }
+    return P;
+    }
+
+// Continue a climb through the global arrival words from node X at split p.
+template<class InsertOpT>
+__device__ void climb_global(const InsertOpT& insert, const ClimbArgs& A, const QuantFrame& f,
+                             ClimbNode X, unsigned int p)
+    {
+    const unsigned int N = A.N;
+    const unsigned int* codes = A.codes;
+    const auto delta = [codes](unsigned int i) { return adjacent_delta(__ldg(codes + i), __ldg(codes + i + 1u), i); };
+    while (true)
+        {
+        const unsigned int side = (p == X.r) ? 0u : 1u;
+        A.kids[2 * (size_t)p + side] = X.id;
+        __threadfence();
+        // the first child to arrive leaves; the second finds the first's node complete
+        if (atomicMax(A.locks + p, A.tag) != A.tag) return;
+        __threadfence();
+        const unsigned int oid = __ldcg(A.kids + 2 * (size_t)p + (side ^ 1u));
+        ClimbNode S;
+        if (oid & kNodeLeaf)
+            {
+            S = climb_leaf(insert, A, f, oid & ~kNodeLeaf, false);
+            }
+        else
+            {
+            const uint4 nb = __ldcg(A.nbox + oid);
+            const uint2 nm = __ldcg(A.nmeta + oid);
+            S.box = make_uint3(nb.x, nb.y, nb.z);
+            S.l = nb.w;
+            S.r = nm.x;
+            S.id = oid;
+            S.db = nm.y & ~kMetaLive;
+            }
+        X = side == 0u ? form_parent<false>(A, p, X, S, nullptr, 0u) : form_parent<false>(A, p, S, X, nullptr, 0u);
+        if (X.l == 0u && X.r == N - 1u) return;
+        p = parent_split(X.l, X.r, N, delta);
+        }
+    }
+
+template<class InsertOpT, int T>
+__global__ void __launch_bounds__(T) k_climb(const InsertOpT insert, const ClimbArgs A)
+    {
+    __shared__ unsigned int s_codes[T + 2];  // codes[base - 1 .. base + T]
+    __shared__ unsigned int s_arrive[T];     // arrivals per split of the block
+    __shared__ unsigned int s_count[T];      // box records per first primitive of the block
+    __shared__ uint4 s_box[2 * T];           // per split and side: child box, far end of its range
+    __shared__ uint2 s_idb[2 * T];           // per split and side: child id, child db
+    __shared__ unsigned char s_side[T];
+    __shared__ QuantFrame s_frame;
+    __shared__ unsigned int s_err;
+
+    const unsigned int N = A.N;
+    const unsigned int base = blockIdx.x * T;
+    const unsigned int end = min(base + (unsigned int)T, N);
+    const unsigned int t = threadIdx.x;
+    if (t == 0)
+        {
+        const QuantFrame fr = frame_from_bounds(A.bounds);
+        s_frame = fr;
+        s_err = ld_status(A.error);
+        if (blockIdx.x == 0) *A.frame_out = fr;
+        }
+    for (unsigned int k = t; k < (unsigned int)T + 2u; k += T)
+        {
+        const long long i = (long long)base - 1 + k;
+        s_codes[k] = (i >= 0 && i < (long long)N) ? A.codes[i] : 0u;
+        }
+    s_arrive[t] = 0u;
+    s_count[t] = 0u;
+    __syncthreads();
+    if (s_err != 0u) return;
+    const QuantFrame f = s_frame;
+    const auto delta = [&](unsigned int i) { return adjacent_delta(s_codes[i - base + 1u], s_codes[i - base + 2u], i); };
+
+    // local phase
+    const unsigned int s = base + t;
+    bool boundary = false;
+    unsigned int gp = 0u;
+    ClimbNode X;
+    if (s < end)
+        {
+        X = climb_leaf(insert, A, f, s, true);
+        while (!(X.l == 0u && X.r == N - 1u))
+            {
+            const unsigned int p = parent_split(X.l, X.r, N, delta);
+            if (p < base || p + 1u >= end)
+                {
+                boundary = true;
+                gp = p;
+                break;
+                }
+            const unsigned int side = (p == X.r) ? 0u : 1u;
+            const unsigned int j = p - base;
+            s_box[2 * j + side] = make_uint4(X.box.x, X.box.y, X.box.z, side == 0u ? X.l : X.r);
+            s_idb[2 * j + side] = make_uint2(X.id, X.db);
+            s_side[j] = (unsigned char)side;
+            __threadfence_block();
+            if (atomicAdd(s_arrive + j, 1u) == 0u) break;
+            __threadfence_block();
+            const uint4 ob = s_box[2 * j + (side ^ 1u)];
+            const uint2 oi = s_idb[2 * j + (side ^ 1u)];
+            ClimbNode S;
+            S.box = make_uint3(ob.x, ob.y, ob.z);
+            S.id = oi.x;
+            S.db = oi.y;
+            if (side == 0u)
+                {
+                S.l = p + 1u;
+                S.r = ob.w;
+                X = form_parent<true>(A, p, X, S, s_count, base);
+                }
+            else
+                {
+                S.l = ob.w;
+                S.r = p;
+                X = form_parent<true>(A, p, S, X, s_count, base);
+                }
+            }
+        }
+    __syncthreads();
+    // every position of the block is written here (k_climb_global adds to them afterwards)
+    if (s < end) A.counts[s] = s_count[t];
+
+    // the climb continues across blocks (k_climb_global) from the splits of this block that only
+    // one child reached and from the nodes whose parent split is on the block's edge
+    if (t + 1u < end - base && s_arrive[t] == 1u)
+        {
+        const unsigned int k = atomicAdd(A.n_items, 1u);
+        if (k < A.item_capacity) A.items[k] = make_uint2(s_idb[2 * t + s_side[t]].x, base + t);
+        }
+    if (boundary)
+        {
+        const unsigned int k = atomicAdd(A.n_items, 1u);
+        if (k < A.item_capacity) A.items[k] = make_uint2(X.id, gp);
+        }
+    }
+
+// Second stage of the climb: one thread per pending node, arrival words in global memory.
+template<class InsertOpT>
+__global__ void __launch_bounds__(256) k_climb_global(const InsertOpT insert, const ClimbArgs A)
+    {
+    __shared__ QuantFrame s_frame;
+    __shared__ unsigned int s_err;
+    __shared__ unsigned int s_n;
+    if (threadIdx.x == 0)
+        {
+        s_frame = frame_from_bounds(A.bounds);
+        s_err = ld_status(A.error);
+        s_n = min(*A.n_items, A.item_capacity);
+        }
+    __syncthreads();
+    if (s_err != 0u) return;
+    const QuantFrame f = s_frame;
+    const unsigned int n = s_n;
+    for (unsigned int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+        {
+        const uint2 it = A.items[k];
+        ClimbNode X;
+        if (it.x & kNodeLeaf)
+            {
+            X = climb_leaf(insert, A, f, it.x & ~kNodeLeaf, false);
+            }
+        else
+            {
+            const uint4 nb = A.nbox[it.x];
+            const uint2 nm = A.nmeta[it.x];
+            X.box = make_uint3(nb.x, nb.y, nb.z);
+            X.l = nb.w;
+            X.r = nm.x;
+            X.id = it.x;
+            X.db = nm.y & ~kMetaLive;
+            }
+        climb_global(insert, A, f, X, it.y);
+        }
+    }
+
+// ---------------------------------------------------------------------------------------------
+// Records in depth-first pre-order.  pre[k] = box records whose first primitive is below k.  Box
+// record of node [first, last] with db box records below it on its left spine: slot
+// pre[first + 1] - 1 - db + first, skip pre[last + 1] + last + 1.  Point record of sorted leaf s:
+// slot pre[s + 1] + s, holding the exact position and kLeafFlag | s.
+// ---------------------------------------------------------------------------------------------
+struct EmitArgs
+    {
+    unsigned int N;
+    const float4* payload;
+    const uint4* nbox;
+    const uint2* nmeta;
+    const unsigned int* pre;
+    uint4* nodes;
     unsigned int node_capacity;
+    const unsigned int* error;
+    };
+
+static __global__ void __launch_bounds__(256) k_emit(const EmitArgs a)
+    {
+    __shared__ unsigned int s_err;
+    if (threadIdx.x == 0) s_err = ld_status(a.error);
+    __syncthreads();
+    const unsigned int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= a.N || s_err != 0u) return;
+    const float4 pl = a.payload[k];
+    const unsigned int ps = a.pre[k + 1] + k;
+    if (ps < a.node_capacity)
+        a.nodes[ps] = make_uint4(__float_as_uint(pl.x), __float_as_uint(pl.y), __float_as_uint(pl.z),
+                                 kLeafFlag | k);
+    if (k + 1u < a.N)
+        {
+        const uint2 m = a.nmeta[k];
+        if (m.y & kMetaLive)
+            {
+            const uint4 b = a.nbox[k];
+            const unsigned int first = b.w;
+            const unsigned int last = m.x;
+            const unsigned int db = m.y & ~kMetaLive;
+            const unsigned int slot = a.pre[first + 1] - 1u - db + first;
+            const unsigned int skip = a.pre[last + 1] + last + 1u;
+            if (slot < a.node_capacity) a.nodes[slot] = make_uint4(b.x, b.y, b.z, skip);
+            }
+        }
+    }
+
+// ---------------------------------------------------------------------------------------------
+// Reference-layout float boxes (the reference's lbvh_bubble_aabbs,
+// include/neighbor/kernels/LBVH.cuh:270-327): leaves at N-1+s, internal nodes by bottom-up
+// bubbling over the Karras parent/child arrays with one arrival word per node.
+// ---------------------------------------------------------------------------------------------
+struct RefBubbleArgs
+    {
+    unsigned int N;
+    const int* parent;
+    const int* left;
+    const int* right;
+    float3* lo;
+    float3* hi;
+    unsigned int* locks;
+    unsigned int tag;
+    const unsigned int* error;
+    };
+
+// Leaf boxes of a point tree: the sorted payload.
+struct PayloadLeafBox
+    {
+    const float4* payload;
+    __device__ __forceinline__ BoundingBox operator()(unsigned int s) const
+        {
+        const float4 p = payload[s];
+        const float3 x = make_float3(p.x, p.y, p.z);
+        return BoundingBox(x, x);
+        }
+    };
+
+// Leaf boxes from the insert op.
+template<class InsertOpT>
+struct InsertLeafBox
+    {
+    InsertOpT insert;
+    const unsigned int* primitive;
+    __device__ __forceinline__ BoundingBox operator()(unsigned int s) const { return insert.get(primitive[s]); }
     };
 
 __device__ __forceinline__ float3 ld_cg_float3(const float3* p)
@@ -541,65 +889,27 @@ __device__ __forceinline__ float3 ld_cg_float3(const float3* p)
     return make_float3(__ldcg(f), __ldcg(f + 1), __ldcg(f + 2));
     }
 
-// Pre-order slot of a box record with primitive range [first, last]: the box records that start
-// before `first` (pre[first]), the point records before it (first), and the box records above it
-// that start at `first` too.  db = number of box records below it on its left spine.
-__device__ __forceinline__ void emit_box_record(const BubbleArgs& a, const QuantFrame& f,
-                                                unsigned int first, unsigned int last,
-                                                unsigned int db, float3 lo, float3 hi)
+template<class LeafBoxT>
+__global__ void k_ref_bubble(const LeafBoxT leaf_box, const RefBubbleArgs a)
     {
-    const uint3 w = pack_node_box(f, lo, hi);
-    const unsigned int skip = a.pre[last + 1] + last + 1u;
-    const unsigned int slot = a.pre[first + 1] - 1u - db + first;
-    if (slot < a.node_capacity) a.nodes[slot] = make_uint4(w.x, w.y, w.z, skip);
-    }
-
-// Point record of sorted primitive s: exact coordinates and the primitive id.
-__device__ __forceinline__ void emit_point_record(const BubbleArgs& a, unsigned int s, float3 p,
-                                                  unsigned int prim)
-    {
-    const unsigned int slot = a.pre[s + 1] + s;
-    if (slot < a.node_capacity)
-        a.nodes[slot] = make_uint4(__float_as_uint(p.x), __float_as_uint(p.y), __float_as_uint(p.z),
-                                   kLeafFlag | prim);
-    }
-
-template<class InsertOpT>
-__global__ void k_bubble(const InsertOpT insert, const BubbleArgs a)
-    {
-    __shared__ QuantFrame s_frame;
     __shared__ unsigned int s_err;
-    if (threadIdx.x == 0)
-        {
-        const QuantFrame f = frame_from_bounds(a.bounds);
-        s_frame = f;
-        s_err = ld_status(a.error);
-        if (blockIdx.x == 0) *a.frame_out = f;
-        }
+    if (threadIdx.x == 0) s_err = ld_status(a.error);
     __syncthreads();
     const unsigned int s = blockIdx.x * blockDim.x + threadIdx.x;
     const unsigned int N = a.N;
     if (s >= N || s_err != 0u) return;
-    const QuantFrame f = s_frame;
-
-    const unsigned int prim = a.primitive[s];
-    const BoundingBox b = insert.get(prim);
+    const BoundingBox b = leaf_box(s);
     const int leaf = (int)(N - 1 + s);
     a.lo[leaf] = b.lo;
     a.hi[leaf] = b.hi;
-    a.payload[s] = make_float4(b.lo.x, b.lo.y, b.lo.z, __uint_as_float(prim));
-
     int cur = (N == 1) ? LBVHSentinel : a.parent[leaf];
-    emit_point_record(a, s, b.lo, prim);
     __threadfence();
-
     int last = leaf;
     float3 blo = b.lo;
     float3 bhi = b.hi;
     while (cur != LBVHSentinel)
         {
-        // The second thread to reach a node finishes it; both children are final by then.
-        if (atomicMax(a.locks + cur, a.epoch) != a.epoch) return;
+        if (atomicMax(a.locks + cur, a.tag) != a.tag) return;
         __threadfence();
         const int l = a.left[cur];
         const int r = a.right[cur];
@@ -610,25 +920,9 @@ __global__ void k_bubble(const InsertOpT insert, const BubbleArgs a)
         bhi = make_float3(fmaxf(bhi.x, shi.x), fmaxf(bhi.y, shi.y), fmaxf(bhi.z, shi.z));
         a.lo[cur] = blo;
         a.hi[cur] = bhi;
-        const uint2 rg = a.ranges[cur];
-        const unsigned int size = rg.y - rg.x + 1u;
-        // box records below on the left spine: the left child's own count plus itself, unless the
-        // left child is a single point (point records are not counted) or this node is a bucket
-        unsigned int db = 0;
-        if (size > a.leaf_size && (unsigned int)l < N - 1)
-            db = 1u + (unsigned int)__ldcg(a.depth_below + l);
-        a.depth_below[cur] = (unsigned char)db;
-        const int par = a.parent[cur];
-        bool live = size > a.leaf_size || par == LBVHSentinel;
-        if (!live)
-            {
-            const uint2 pr = a.ranges[par];
-            live = (pr.y - pr.x + 1u) > a.leaf_size;
-            }
-        if (live) emit_box_record(a, f, rg.x, rg.y, db, blo, bhi);
         __threadfence();
         last = cur;
-        cur = par;
+        cur = a.parent[cur];
         }
     }
 

@@ -15,6 +15,10 @@
 //                      sorted points against the exact FP32 minimum-image predicate.  A point is
 //                      accepted only through the image whose padded query box contains it, so
 //                      no pair is reported twice when buckets straddle images.
+//   k_traverse_half    self queries with a symmetric image set: each query walks only the records
+//                      after its own point record and a pair counts for both rows;
+//                      k_half_order_rows / k_half_order_long give each list row the reference's
+//                      order.
 #ifndef NEIGHBOR_KERNELS_TRAVERSE_CUH_
 #define NEIGHBOR_KERNELS_TRAVERSE_CUH_
 
@@ -329,7 +333,7 @@ __global__ void k_traverse_fast(const FastLBVHData tree, const FastQueryArgs a,
                     if (exact_pair(Q.p, x, Q.rc, a.box))
                         {
                         if (OUT == kFastList && count < a.max_neigh)
-                            a.list[row_first + count] = transform(n.w & ~kLeafFlag);
+                            a.list[row_first + count] = transform(tree.primitive[n.w & ~kLeafFlag]);
                         ++count;
                         }
                     }
@@ -344,6 +348,251 @@ __global__ void k_traverse_fast(const FastLBVHData tree, const FastQueryArgs a,
         }
     a.nneigh[Q.row] = count;
     if (STATS) add_stats(a.stats, visits, tests, walks);
+    }
+
+// ---------------------------------------------------------------------------------------------
+// Symmetric (half) self traversal.  When the queries are the tree's own points with one cutoff
+// and the image set is symmetric (the self image, or the 27-image lattice), the FP32
+// minimum-image predicate is symmetric too (d(j,i) = -d(i,j) exactly, and the wrap keeps |d|), so
+// every unordered pair needs to be found once.  Query s starts its walk at its own point record
+// (slot pre[s+1] + s) instead of the root: records before it are its ancestors (which contain it)
+// and subtrees of smaller sorted positions, so the walk meets exactly the partners j >= s, and
+// every record after it is still either visited or excluded by a box it was tested against.
+// A pair (s, j) then counts for both rows.
+//
+// Count: rows start at zero; the partner's row gets an atomic increment, the query's own total
+// one atomic add at the end.
+// Fill: each entry is first written as a key image << 27 | sorted position.  The query writes
+// the entries it found itself from the end of its row backwards (already in ascending key order)
+// and records how many in own[]; entries found for a row by other queries are appended from the
+// front through an atomic cursor (nneigh, zero on entry).  k_half_order_rows then sorts each row
+// by key and maps keys to transform(primitive) ids, which gives every row the order of the
+// reference's rope traversal (images in ascending order, partners in ascending sorted position
+// within an image), independent of the order of the atomics.  The image through which a partner
+// finds the query is the mirror image (26 - image on the lattice).  A row with more than
+// max_neigh entries keeps max_neigh of them (which ones is unspecified) and its full count.
+// ---------------------------------------------------------------------------------------------
+constexpr unsigned int kHalfKeyBits = 27;
+constexpr unsigned int kHalfKeyMask = (1u << kHalfKeyBits) - 1u;
+constexpr unsigned int kHalfMaxN = 1u << kHalfKeyBits;   // sorted positions must fit the key
+constexpr unsigned int kHalfRowThread = 32;              // rows up to this long: one thread
+constexpr unsigned int kHalfRowMax = 4096;               // longest row ordered (one block)
+
+struct HalfArgs
+    {
+    unsigned int Q;          // number of points (= queries)
+    float rc;
+    float pad;
+    int rows_sorted;         // row of sorted position s: s (1) or primitive[s] (0)
+    int lattice;             // 1: the 27 images of lattice_L; 0: the self image only
+    float3 lattice_L;
+    float3 box;              // periodic lengths of the minimum image (0 = open)
+    unsigned int* nneigh;    // zero on entry
+    unsigned int* list;      // fill only: row-major, max_neigh per row
+    unsigned int max_neigh;
+    unsigned int* own;       // fill only: entries each row found itself
+    };
+
+// Images (bits of the 27-image lattice, or bit 0 for the self image) whose padded query box
+// meets the root box.
+__device__ __forceinline__ unsigned int half_image_flags(const HalfArgs& a, const QuantFrame& f,
+                                                         const float3& p, float rs)
+    {
+    if (a.lattice)
+        {
+        const unsigned int mx = axis_images(p.x, rs, a.lattice_L.x, f.lo.x, f.hi.x);
+        const unsigned int my = axis_images(p.y, rs, a.lattice_L.y, f.lo.y, f.hi.y);
+        const unsigned int mz = axis_images(p.z, rs, a.lattice_L.z, f.lo.z, f.hi.z);
+        const unsigned int X = ((mx & 1u) ? 0x1ffu : 0u) | ((mx & 2u) ? 0x3fe00u : 0u) | ((mx & 4u) ? 0x7fc0000u : 0u);
+        const unsigned int Y = (((my & 1u) ? 0x7u : 0u) | ((my & 2u) ? 0x38u : 0u) | ((my & 4u) ? 0x1c0u : 0u)) * 0x40201u;
+        const unsigned int Z = mz * 0x1249249u;
+        return X & Y & Z;
+        }
+    const bool hit = approx::fsub_rd(p.x, rs) <= f.hi.x && approx::fadd_ru(p.x, rs) >= f.lo.x
+                     && approx::fsub_rd(p.y, rs) <= f.hi.y && approx::fadd_ru(p.y, rs) >= f.lo.y
+                     && approx::fsub_rd(p.z, rs) <= f.hi.z && approx::fadd_ru(p.z, rs) >= f.lo.z;
+    return hit ? 1u : 0u;
+    }
+
+template<int OUT>
+__global__ void __launch_bounds__(256) k_traverse_half(const FastLBVHData tree, const HalfArgs a)
+    {
+    __shared__ QuantFrame s_frame;
+    __shared__ unsigned int s_records;
+    if (threadIdx.x == 0)
+        {
+        s_frame = *tree.frame;
+        s_records = ld_status(tree.status) != 0u ? 0u : *tree.n_boxes + tree.N;
+        }
+    __syncthreads();
+    const unsigned int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= a.Q) return;
+    const QuantFrame f = s_frame;
+    const unsigned int n_rec = s_records;
+    const float4 me = tree.points[q];
+    const float3 P = make_float3(me.x, me.y, me.z);
+    const unsigned int row = a.rows_sorted ? q : __float_as_uint(me.w);
+    const float rs = approx::fadd_ru(a.rc, a.pad);
+    unsigned int flags = n_rec ? half_image_flags(a, f, P, rs) : 0u;
+    const bool multi = __popc(flags) > 1;
+    const unsigned int start = n_rec ? tree.pre[q + 1] + q : 0u;
+    const unsigned long long row_first = (unsigned long long)row * a.max_neigh;
+    unsigned int own = 0;
+    while (flags)
+        {
+        const int bit = __ffs(flags) - 1;
+        flags &= flags - 1u;
+        const float3 t = a.lattice ? PeriodicImagesOp(a.lattice_L).get((unsigned int)bit) : make_float3(0.f, 0.f, 0.f);
+        const unsigned int mirror = a.lattice ? 26u - (unsigned int)bit : 0u;
+        const float3 c = make_float3(__fadd_rn(P.x, t.x), __fadd_rn(P.y, t.y), __fadd_rn(P.z, t.z));
+        const float3 qlo = make_float3(approx::fsub_rd(c.x, rs), approx::fsub_rd(c.y, rs), approx::fsub_rd(c.z, rs));
+        const float3 qhi = make_float3(approx::fadd_ru(c.x, rs), approx::fadd_ru(c.y, rs), approx::fadd_ru(c.z, rs));
+        const uint3 qb = pack_query_box(f, qlo, qhi);
+        unsigned int i = start;
+        while (i < n_rec)
+            {
+            const uint4 n = __ldg(tree.nodes + i);
+            if ((int)n.w < 0)
+                {
+                const float3 x = make_float3(__uint_as_float(n.x), __uint_as_float(n.y), __uint_as_float(n.z));
+                if ((!multi || point_in_box(x, qlo, qhi)) && exact_pair(P, x, a.rc, a.box))
+                    {
+                    const unsigned int j = n.w & ~kLeafFlag;
+                    if (OUT == kFastCount)
+                        {
+                        if (j != q) atomicAdd(a.nneigh + (a.rows_sorted ? j : tree.primitive[j]), 1u);
+                        }
+                    else
+                        {
+                        if (own < a.max_neigh)
+                            a.list[row_first + (a.max_neigh - 1u - own)] = ((unsigned int)bit << kHalfKeyBits) | j;
+                        if (j != q)
+                            {
+                            const unsigned int rj = a.rows_sorted ? j : tree.primitive[j];
+                            const unsigned int slot = atomicAdd(a.nneigh + rj, 1u);
+                            if (slot < a.max_neigh)
+                                a.list[(unsigned long long)rj * a.max_neigh + slot] = (mirror << kHalfKeyBits) | q;
+                            }
+                        }
+                    ++own;
+                    }
+                ++i;
+                }
+            else
+                {
+                i = node_overlaps(n, qb) ? i + 1u : max(n.w, i + 1u);
+                }
+            }
+        }
+    if (OUT == kFastCount)
+        {
+        if (own) atomicAdd(a.nneigh + row, own);
+        }
+    else
+        {
+        a.own[row] = own;
+        }
+    }
+
+struct HalfOrderArgs
+    {
+    unsigned int Q;
+    unsigned int* nneigh;       // in: entries appended by other queries; out: row totals
+    unsigned int* list;
+    unsigned int max_neigh;
+    const unsigned int* own;
+    const unsigned int* primitive;
+    unsigned int* long_rows;    // rows longer than kHalfRowThread, for k_half_order_long
+    unsigned int* n_long;       // zero on entry
+    const unsigned int* status;
+    };
+
+// Key k of a row (0 <= k < m): the appended entries first, then the query's own entries in the
+// order it found them (stored backwards from the end of the row).  Rows that overflowed hold
+// max_neigh keys in no particular order.
+__device__ __forceinline__ unsigned int half_row_key(const unsigned int* row, unsigned int k,
+                                                     unsigned int appended, unsigned int total,
+                                                     unsigned int max_neigh)
+    {
+    if (total > max_neigh || k < appended) return row[k];
+    return row[max_neigh - 1u - (k - appended)];
+    }
+
+template<class TransformOpT>
+__global__ void __launch_bounds__(256) k_half_order_rows(const HalfOrderArgs a, const TransformOpT transform)
+    {
+    const unsigned int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= a.Q || ld_status(a.status) != 0u) return;
+    const unsigned int appended = a.nneigh[r];
+    const unsigned int total = appended + a.own[r];
+    a.nneigh[r] = total;
+    const unsigned int m = min(total, a.max_neigh);
+    if (m == 0u) return;
+    if (m > kHalfRowThread)
+        {
+        a.long_rows[atomicAdd(a.n_long, 1u)] = r;
+        return;
+        }
+    unsigned int* row = a.list + (unsigned long long)r * a.max_neigh;
+    unsigned int key[kHalfRowThread];
+    for (unsigned int k = 0; k < m; ++k)
+        {
+        const unsigned int v = half_row_key(row, k, appended, total, a.max_neigh);
+        unsigned int j = k;
+        while (j > 0u && key[j - 1u] > v)
+            {
+            key[j] = key[j - 1u];
+            --j;
+            }
+        key[j] = v;
+        }
+    for (unsigned int k = 0; k < m; ++k) row[k] = transform(a.primitive[key[k] & kHalfKeyMask]);
+    }
+
+// Rows longer than kHalfRowThread entries: one block per row, bitonic sort in shared memory.
+template<class TransformOpT>
+__global__ void __launch_bounds__(256) k_half_order_long(const HalfOrderArgs a, const TransformOpT transform)
+    {
+    __shared__ unsigned int s_key[kHalfRowMax];
+    const unsigned int n_long = min(*a.n_long, a.Q);
+    for (unsigned int b = blockIdx.x; b < n_long; b += gridDim.x)
+        {
+        const unsigned int r = a.long_rows[b];
+        const unsigned int total = a.nneigh[r];
+        const unsigned int appended = total - a.own[r];
+        const unsigned int m = min(min(total, a.max_neigh), kHalfRowMax);
+        unsigned int* row = a.list + (unsigned long long)r * a.max_neigh;
+        unsigned int n2 = 1u;
+        while (n2 < m) n2 <<= 1;
+        for (unsigned int k = threadIdx.x; k < n2; k += blockDim.x)
+            s_key[k] = k < m ? half_row_key(row, k, appended, total, a.max_neigh) : 0xffffffffu;
+        __syncthreads();
+        for (unsigned int size = 2u; size <= n2; size <<= 1)
+            {
+            for (unsigned int stride = size >> 1; stride > 0u; stride >>= 1)
+                {
+                for (unsigned int k = threadIdx.x; k < n2; k += blockDim.x)
+                    {
+                    const unsigned int o = k ^ stride;
+                    if (o > k)
+                        {
+                        const bool up = (k & size) == 0u;
+                        const unsigned int x = s_key[k];
+                        const unsigned int y = s_key[o];
+                        if ((x > y) == up)
+                            {
+                            s_key[k] = y;
+                            s_key[o] = x;
+                            }
+                        }
+                    }
+                __syncthreads();
+                }
+            }
+        for (unsigned int k = threadIdx.x; k < m; k += blockDim.x)
+            row[k] = transform(a.primitive[s_key[k] & kHalfKeyMask]);
+        __syncthreads();
+        }
     }
 
 // ---------------------------------------------------------------------------------------------
@@ -481,7 +730,7 @@ __global__ void k_traverse_packet(const FastLBVHData tree, const FastQueryArgs a
                     if (ok)
                         {
                         if (OUT == kFastList && count < a.max_neigh)
-                            a.list[row_first + count] = transform(n.w & ~kLeafFlag);
+                            a.list[row_first + count] = transform(tree.primitive[n.w & ~kLeafFlag]);
                         ++count;
                         }
                     ++i;

@@ -114,6 +114,11 @@ int nbr_traverser_set_mode(nbr_traverser t, int mode);
  * that fast-path traversals add to; NULL disables them. */
 int nbr_traverser_set_stats(nbr_traverser t, unsigned long long* counters);
 
+/* Addition: self traversals (nbr_traverse_self) with the self image or the 27-image lattice find
+ * each unordered pair once and write it to both rows (1, default) or walk the whole tree per
+ * query (0).  Counts, neighbor sets and the order of each row are the same either way. */
+int nbr_traverser_set_symmetric(nbr_traverser t, int enabled);
+
 /* getData() (LBVHTraverser.h:326-329): int4 nodes in the reference's 10-bit layout (managed),
  * plus the compression frame (lo, hi, bins: managed float[3] each). */
 int nbr_traverser_get_data(nbr_traverser t, const int** data, const float** lo, const float** hi,

@@ -96,6 +96,7 @@ def _declare(L):
     sig("nbr_traverser_set_fast_path", [_P, _I])
     sig("nbr_traverser_set_mode", [_P, _I])
     sig("nbr_traverser_set_stats", [_P, _P])
+    sig("nbr_traverser_set_symmetric", [_P, _I])
     sig("nbr_traverser_get_data", [_P, _PP, _PP, _PP, _PP])
     sig("nbr_traverse", [_P, _P, _I, _P, _U, _P, _P, _F, _P, _U, _P, _P, _P, _U, _U, _P])
     sig("nbr_traverse_self", [_P, _P, _F, _P, _F, _P, _U, _P, _P, _P, _U, _I, _U, _P])
@@ -111,7 +112,7 @@ EXPORTED = ["nbr_last_error", "nbr_version", "nbr_lbvh_create", "nbr_lbvh_destro
             "nbr_lbvh_get_codes", "nbr_lbvh_get_fast", "nbr_lbvh_num_fast_nodes",
             "nbr_lbvh_check_status", "nbr_traverser_create", "nbr_traverser_destroy",
             "nbr_traverser_setup", "nbr_traverser_reset", "nbr_traverser_set_fast_path",
-            "nbr_traverser_set_mode", "nbr_traverser_set_stats",
+            "nbr_traverser_set_mode", "nbr_traverser_set_stats", "nbr_traverser_set_symmetric",
             "nbr_traverser_get_data", "nbr_traverse", "nbr_traverse_self", "nbr_exact_pad",
             "nbr_debug_wait_timeout", "nbr_morton_sort_noalloc"]
 
@@ -368,6 +369,10 @@ class LBVHTraverser:
         """counters: CUDA int64 tensor of 3 (node visits, point tests, packets) or None."""
         self._stats = counters
         _check(self._L.nbr_traverser_set_stats(self._h, None if counters is None else counters.data_ptr()))
+
+    def set_symmetric(self, enabled: bool):
+        """Self traversals: find each pair once and write both rows (True, default)."""
+        _check(self._L.nbr_traverser_set_symmetric(self._h, 1 if enabled else 0))
 
     def set_mode(self, mode: int):
         """0 = one thread per query, 1 = one warp per 32 consecutive queries."""

@@ -666,7 +666,7 @@ uint32_t orc_fast_nodes(uint32_t N, uint32_t leaf_size, const int32_t* parent,
     // followed by its two subtrees; a node of 2..leaf_size primitives (a bucket) is a box record
     // followed by the point records of its primitives in sorted order; a single primitive is a
     // point record.  Box: {bins, skip = index just past the subtree}; point: {x, y, z as float
-    // bits, 0x80000000 | primitive id}.
+    // bits, 0x80000000 | sorted position}.
     uint32_t n_rec = 0;
     auto emit_box = [&](uint32_t v, uint32_t skip) {
         uint32_t qlo[3], qhi[3];
@@ -683,7 +683,7 @@ uint32_t orc_fast_nodes(uint32_t N, uint32_t leaf_size, const int32_t* parent,
         const float* p = lo + 3 * (size_t)(n_int + s);
         uint32_t* o = nodes + 4 * (size_t)n_rec++;
         std::memcpy(o, p, 3 * sizeof(float));
-        o[3] = 0x80000000u | primitive[s];
+        o[3] = 0x80000000u | (uint32_t)s;
     };
     // records in a subtree: 1 for a point, 1 + size for a bucket, 1 + both subtrees otherwise
     std::vector<uint32_t> count(n_nodes, 0);

@@ -1,0 +1,144 @@
+"""Symmetric (half) self traversal: same counts, same neighbor sets, same row order.
+
+With the self image or the 27-image lattice, a self traversal finds each unordered pair once and
+writes it to both rows; the rows are then ordered by (image, sorted position), the order of a
+whole-tree walk (and of the reference's rope traversal).  So the full outputs -- counts and every
+list row -- must be bit-identical to the whole-tree walk's, and the sets must equal the oracle's
+cell list.  Rows longer than 32 entries take the block-per-row ordering kernel; rows that overflow
+max_neigh keep their full count and a subset of their true neighbors.
+"""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+pytestmark = pytest.mark.gpu
+
+import neighbor_gb300 as nb  # noqa: E402
+import oracle as O  # noqa: E402
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib():
+    nb.build()
+    nb.load()
+
+
+def _t(a, dtype=torch.float32):
+    return torch.tensor(np.asarray(a), dtype=dtype, device="cuda")
+
+
+def _uniform(N, seed, density=0.85):
+    rng = np.random.default_rng(seed)
+    L = float((N / density) ** (1.0 / 3.0))
+    return (rng.random((N, 3)) * L).astype(np.float32), L
+
+
+def _clustered(N, seed, L, per=200):
+    rng = np.random.default_rng(seed)
+    nb_ = max(1, N // per)
+    centers = rng.random((nb_, 3)) * L
+    sig = np.exp(rng.uniform(np.log(0.5), np.log(3.0), nb_))
+    k = rng.integers(0, nb_, N)
+    p = centers[k] + rng.normal(size=(N, 3)) * sig[k, None]
+    n_bg = N * 3 // 10
+    p[:n_bg] = rng.random((n_bg, 3)) * L
+    return np.mod(p, L).astype(np.float32)
+
+
+def _both(lbvh, rc, box, pad, images, rows_sorted, max_neigh=None, map=None):
+    out = []
+    for sym in (True, False):
+        trav = nb.LBVHTraverser()
+        trav.set_symmetric(sym)
+        out.append(trav.traverse_self(lbvh, rc, box, pad, images=images, rows_sorted=rows_sorted,
+                                      max_neigh=max_neigh, map=map))
+    return out
+
+
+def _rows(cnt, lst):
+    cnt = cnt.cpu().numpy().view(np.uint32)
+    lst = lst.cpu().numpy().view(np.uint32)
+    mask = np.arange(lst.shape[1])[None, :] < cnt[:, None]
+    return cnt, np.where(mask, lst, 0xFFFFFFFF)
+
+
+@pytest.mark.parametrize("rows_sorted", [True, False])
+@pytest.mark.parametrize("images", ["periodic", "self"])
+@pytest.mark.parametrize("dist", ["uniform", "clustered"])
+@pytest.mark.parametrize("leaf", [1, 4])
+def test_symmetric_equals_whole_tree_walk(leaf, dist, images, rows_sorted):
+    N = 30000
+    P, L = _uniform(N, 41)
+    if dist == "clustered":
+        P = _clustered(N, 42, L)
+    box = [L, L, L] if images == "periodic" else [0, 0, 0]
+    rc = 1.3
+    lbvh = nb.LBVH(leaf_size=leaf)
+    lbvh.build(_t(P), [0, 0, 0], [L, L, L])
+    pad = nb.exact_pad(rc, 2 * L)
+    imgs = "periodic" if images == "periodic" else None
+    c_sym, c_full = _both(lbvh, rc, box, pad, imgs, rows_sorted)
+    assert torch.equal(c_sym, c_full)
+    mx = int(c_full.max().item())
+    (cs, ls), (cf, lf) = _both(lbvh, rc, box, pad, imgs, rows_sorted, max_neigh=mx)
+    cs, ls = _rows(cs, ls)
+    cf, lf = _rows(cf, lf)
+    assert np.array_equal(cs, cf)
+    assert np.array_equal(ls, lf)  # same entries in the same order
+    if dist == "clustered":
+        assert mx > 32  # the block-per-row ordering kernel ran
+    # the sets are the oracle's (open box: a periodic grid three times wider never wraps a pair)
+    if images == "periodic":
+        off, nbrs = O.celllist_csr(P, P, rc, [0, 0, 0], box)
+    else:
+        off, nbrs = O.celllist_csr(P, P, rc, [-L, -L, -L], [3 * L, 3 * L, 3 * L])
+    prim = lbvh.primitives().cpu().numpy().view(np.uint32)
+    row_of = prim if rows_sorted else np.arange(N, dtype=np.uint32)
+    want = np.diff(off).astype(np.uint32)
+    assert np.array_equal(cs, want[row_of])
+    for r in range(0, N, 211):
+        got = np.sort(ls[r, : cs[r]])
+        assert np.array_equal(got, nbrs[off[row_of[r]]:off[row_of[r] + 1]])
+
+
+def test_symmetric_overflow_keeps_counts_and_a_subset():
+    N = 20000
+    P, L = _uniform(N, 43)
+    box = [L, L, L]
+    rc = 1.3
+    lbvh = nb.LBVH()
+    lbvh.build(_t(P), [0, 0, 0], box)
+    pad = nb.exact_pad(rc, 2 * L)
+    trav = nb.LBVHTraverser()
+    full = trav.traverse_self(lbvh, rc, box, pad, images="periodic", rows_sorted=False)
+    cnt, lst = trav.traverse_self(lbvh, rc, box, pad, images="periodic", rows_sorted=False, max_neigh=5)
+    assert torch.equal(cnt, full)
+    off, nbrs = O.celllist_csr(P, P, rc, [0, 0, 0], box)
+    cnt = cnt.cpu().numpy().view(np.uint32)
+    lst = lst.cpu().numpy().view(np.uint32)
+    for r in range(N):
+        k = min(int(cnt[r]), 5)
+        assert set(lst[r, :k].tolist()) <= set(nbrs[off[r]:off[r + 1]].tolist())
+
+
+def test_symmetric_transform_and_long_rows():
+    # dense clusters: rows of several hundred entries, a map transform on the ids
+    N = 20000
+    L = 30.0
+    P = _clustered(N, 44, L, per=2000)
+    box = [L, L, L]
+    rc = 1.5
+    lbvh = nb.LBVH()
+    lbvh.build(_t(P), [0, 0, 0], box)
+    pad = nb.exact_pad(rc, 2 * L)
+    rng = np.random.default_rng(45)
+    m = rng.permutation(N).astype(np.int32)
+    c_full = nb.LBVHTraverser().traverse_self(lbvh, rc, box, pad, images="periodic", rows_sorted=True)
+    mx = int(c_full.max().item())
+    assert 32 < mx <= 4096
+    (cs, ls), (cf, lf) = _both(lbvh, rc, box, pad, "periodic", True, max_neigh=mx, map=_t(m, torch.int32))
+    cs, ls = _rows(cs, ls)
+    cf, lf = _rows(cf, lf)
+    assert np.array_equal(cs, cf)
+    assert np.array_equal(ls, lf)

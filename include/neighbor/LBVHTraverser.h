@@ -166,6 +166,14 @@ class LBVHTraverser : public Tunable<unsigned int>
                           float pad, const OutputOpT& out, const TranslateOpT& images,
                           const TransformOpT& transform, bool rows_sorted);
 
+        // Self queries of the sorted positions subset[0..count) only, each walking the whole tree
+        // (rows as in traverseSelf); used to re-run rows whose one-pass capacity was too small.
+        template<class OutputOpT, class TranslateOpT, class TransformOpT>
+        void traverseSelfSubset(const LaunchParameters& params, const LBVH& lbvh, float rc, float3 box,
+                                float pad, const OutputOpT& out, const TranslateOpT& images,
+                                const TransformOpT& transform, bool rows_sorted, const unsigned int* subset,
+                                unsigned int count);
+
     private:
         int m_root;
         shared_array<int4> m_data;
@@ -249,6 +257,18 @@ inline void set_output(gpu::FastQueryArgs& a, const NeighborListOp& out)
     a.list = out.neigh_list;
     a.max_neigh = out.max_neigh;
     }
+inline void set_output(gpu::FastQueryArgs& a, const CSRNeighborListOp& out)
+    {
+    a.nneigh = out.nneigh;
+    a.list = out.neigh_list;
+    a.max_neigh = out.max_capacity;  // 0 = unknown
+    a.offsets = out.offsets;
+    a.caps = out.capacity;
+    }
+// Longest row a traversal may write (0 = unknown).
+inline unsigned int max_row(const CountNeighborsOp&) { return 0u; }
+inline unsigned int max_row(const NeighborListOp& out) { return out.max_neigh; }
+inline unsigned int max_row(const CSRNeighborListOp& out) { return out.max_capacity; }
 } // namespace detail
 
 template<class OutputOpT, class TransformOpT>
@@ -259,8 +279,8 @@ void LBVHTraverser::launch_fast(const LaunchParameters& params, const LBVH& lbvh
     a.stats = m_stats;
     const unsigned int bs = params.tunable;
     constexpr int kind = output_kind<OutputOpT>::value;
-    if (m_mode == kPacketTraversal)
-        gpu::k_traverse_packet<kind, TransformOpT><<<detail::ceil_div(Q, bs), bs, 0, params.stream>>>(
+    if (m_mode == kPacketTraversal && kind != gpu::kFastCSR && !a.subset)
+        gpu::k_traverse_packet<kind == gpu::kFastCSR ? gpu::kFastList : kind, TransformOpT><<<detail::ceil_div(Q, bs), bs, 0, params.stream>>>(
             lbvh.fastData(), a, transform);
     else if (m_stats)
         gpu::k_traverse_fast<kind, true, TransformOpT><<<detail::ceil_div(Q, bs), bs, 0, params.stream>>>(
@@ -315,7 +335,8 @@ void LBVHTraverser::traverseSelf(const LaunchParameters& params, const LBVH& lbv
                                  float pad, const OutputOpT& out, const TranslateOpT& images,
                                  const TransformOpT& transform, bool rows_sorted)
     {
-    static_assert(output_kind<OutputOpT>::value != 0, "traverseSelf needs CountNeighborsOp or NeighborListOp");
+    static_assert(output_kind<OutputOpT>::value != 0,
+                  "traverseSelf needs CountNeighborsOp, NeighborListOp or CSRNeighborListOp");
     static_assert(detail::is_float3_images<TranslateOpT>::value,
                   "traverseSelf needs SelfOp, ImageListOp<float3> or PeriodicImagesOp");
     if (lbvh.getN() == 0 || images.size() == 0) return;
@@ -335,12 +356,45 @@ void LBVHTraverser::traverseSelf(const LaunchParameters& params, const LBVH& lbv
     a.box = box;
     a.pad = pad;
     detail::set_output(a, out);
+    const unsigned int longest = detail::max_row(out);
     if (detail::is_symmetric_images<TranslateOpT>::value && m_symmetric && m_mode == kThreadTraversal
         && !m_stats && lbvh.getN() < gpu::kHalfMaxN
-        && (output_kind<OutputOpT>::value == gpu::kFastCount || a.max_neigh <= gpu::kHalfRowMax))
+        && (output_kind<OutputOpT>::value == gpu::kFastCount
+            || (longest > 0u && longest <= gpu::kHalfRowMax)
+            || (output_kind<OutputOpT>::value == gpu::kFastList && longest == 0u)))
         launch_half(params, lbvh, a, out, transform);
     else
         launch_fast(params, lbvh, a, out, transform, lbvh.getN());
+    }
+
+template<class OutputOpT, class TranslateOpT, class TransformOpT>
+void LBVHTraverser::traverseSelfSubset(const LaunchParameters& params, const LBVH& lbvh, float rc, float3 box,
+                                       float pad, const OutputOpT& out, const TranslateOpT& images,
+                                       const TransformOpT& transform, bool rows_sorted,
+                                       const unsigned int* subset, unsigned int count)
+    {
+    static_assert(output_kind<OutputOpT>::value != 0,
+                  "traverseSelfSubset needs CountNeighborsOp, NeighborListOp or CSRNeighborListOp");
+    static_assert(detail::is_float3_images<TranslateOpT>::value,
+                  "traverseSelfSubset needs SelfOp, ImageListOp<float3> or PeriodicImagesOp");
+    if (lbvh.getN() == 0 || images.size() == 0 || count == 0) return;
+    if (images.size() > 32)
+        throw std::runtime_error("A maximum of 32 image vectors are supported by LBVH traversers.");
+    if (!lbvh.hasFastData()) throw std::runtime_error("traverseSelfSubset needs a tree built from points.");
+    checkParameter(params);
+    gpu::FastQueryArgs a;
+    a.spheres = nullptr;
+    a.Q = count;
+    a.self_rc = rc;
+    a.self_rows_sorted = rows_sorted ? 1 : 0;
+    a.images = detail::image_pointer(images);
+    a.n_images = images.size();
+    a.lattice = detail::image_lattice(images);
+    a.lattice_L = detail::lattice_box(images, box);
+    a.box = box;
+    a.pad = pad;
+    a.subset = subset;
+    launch_fast(params, lbvh, a, out, transform, count);
     }
 
 template<class OutputOpT, class TransformOpT>
@@ -361,8 +415,10 @@ void LBVHTraverser::launch_half(const LaunchParameters& params, const LBVH& lbvh
     h.nneigh = a.nneigh;
     h.list = a.list;
     h.max_neigh = a.max_neigh;
+    h.offsets = a.offsets;
+    h.caps = a.caps;
     h.own = nullptr;
-    if (kind == gpu::kFastList)
+    if (kind != gpu::kFastCount)
         {
         m_own.reserve(N);
         m_long_rows.reserve(N);
@@ -371,13 +427,15 @@ void LBVHTraverser::launch_half(const LaunchParameters& params, const LBVH& lbvh
         }
     detail::check_cuda(cudaMemsetAsync(a.nneigh, 0, (size_t)N * sizeof(unsigned int), stream), "memset");
     gpu::k_traverse_half<kind><<<detail::ceil_div(N, 256), 256, 0, stream>>>(lbvh.fastData(), h);
-    if (kind == gpu::kFastList)
+    if (kind != gpu::kFastCount)
         {
         gpu::HalfOrderArgs o;
         o.Q = N;
         o.nneigh = a.nneigh;
         o.list = a.list;
         o.max_neigh = a.max_neigh;
+        o.offsets = kind == gpu::kFastCSR ? a.offsets : nullptr;
+        o.caps = a.caps;
         o.own = m_own.get();
         o.primitive = lbvh.fastData().primitive;
         o.long_rows = m_long_rows.get();

@@ -11,6 +11,7 @@
 #ifndef NEIGHBOR_MEMORY_H_
 #define NEIGHBOR_MEMORY_H_
 
+#include <algorithm>
 #include <cstddef>
 #include <memory>
 #include <stdexcept>
@@ -151,6 +152,29 @@ class device_array
                 throw std::runtime_error(std::string("Error allocating device memory: ")
                                          + cudaGetErrorString(code));
                 }
+            ptr_ = p;
+            size_ = count;
+            }
+
+        // Ensure room for count elements keeping the first `keep` (copied on `stream`).
+        void grow(size_t count, size_t keep, cudaStream_t stream)
+            {
+            if (count <= size_) return;
+            T* p = nullptr;
+            const cudaError_t code = cudaMalloc(reinterpret_cast<void**>(&p), count * sizeof(T));
+            if (code != cudaSuccess)
+                {
+                (void)cudaGetLastError();
+                throw std::runtime_error(std::string("Error allocating device memory: ")
+                                         + cudaGetErrorString(code));
+                }
+            if (ptr_ && keep)
+                {
+                const cudaError_t c2 = cudaMemcpyAsync(p, ptr_, std::min(keep, size_) * sizeof(T),
+                                                       cudaMemcpyDeviceToDevice, stream);
+                if (c2 == cudaSuccess) (void)cudaStreamSynchronize(stream);
+                }
+            release();
             ptr_ = p;
             size_ = count;
             }

@@ -1,0 +1,184 @@
+// One-pass self neighbor list with per-row capacities (an addition of this library).
+//
+// The reference fills a neighbor list in two traversals: count, read the largest count on the
+// host, then fill rows of that fixed stride.  Here the rows get individual capacities before any
+// traversal -- predicted by a CapacityModel, or given by the caller -- and one traversal fills a
+// CSR list (row r at offsets[r], capacity caps[r]).  Every count is exact even when a row
+// overflows, so the rows that overflowed are re-run with exactly their count of slots, appended
+// after the main list, by a whole-tree walk of just those queries.  The result is always the
+// exact list, in the same row order as every other self traversal of this library.
+#ifndef NEIGHBOR_ONE_PASS_LIST_H_
+#define NEIGHBOR_ONE_PASS_LIST_H_
+
+#include <cuda_runtime.h>
+
+#include "LBVH.h"
+#include "LBVHTraverser.h"
+#include "Memory.h"
+#include "OutputOps.h"
+#include "TransformOps.h"
+#include "TranslateOps.h"
+#include "kernels/capacity.cuh"
+
+namespace neighbor
+{
+namespace gpu
+{
+// Sorted positions whose row overflowed, with their exact counts.
+static __global__ void __launch_bounds__(256) k_overflow_rows(unsigned int N, int rows_sorted,
+                                                              const unsigned int* __restrict__ primitive,
+                                                              const unsigned int* __restrict__ nneigh,
+                                                              const unsigned int* __restrict__ caps,
+                                                              unsigned int* __restrict__ ovf_q,
+                                                              unsigned int* __restrict__ ovf_count,
+                                                              unsigned int* __restrict__ n_ovf)
+    {
+    const unsigned int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= N) return;
+    const unsigned int row = rows_sorted ? q : primitive[q];
+    const unsigned int c = nneigh[row];
+    if (c > caps[row])
+        {
+        const unsigned int k = atomicAdd(n_ovf, 1u);
+        ovf_q[k] = q;
+        ovf_count[k] = c;
+        }
+    }
+
+// Re-point the overflowed rows at their exact space after the main list.
+static __global__ void __launch_bounds__(256) k_overflow_assign(unsigned int n, int rows_sorted,
+                                                                const unsigned int* __restrict__ primitive,
+                                                                const unsigned int* __restrict__ ovf_q,
+                                                                const unsigned int* __restrict__ ovf_count,
+                                                                const unsigned long long* __restrict__ ovf_off,
+                                                                unsigned long long base,
+                                                                unsigned long long* __restrict__ offsets,
+                                                                unsigned int* __restrict__ caps)
+    {
+    const unsigned int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const unsigned int q = ovf_q[k];
+    const unsigned int row = rows_sorted ? q : primitive[q];
+    offsets[row] = base + ovf_off[k];
+    caps[row] = ovf_count[k];
+    }
+} // namespace gpu
+
+class OnePassNeighborList
+    {
+    public:
+        struct Stats
+            {
+            unsigned long long slots;           // slots of the main list (sum of capacities)
+            unsigned int overflow_rows;         // rows re-run
+            unsigned long long overflow_slots;  // slots appended for them
+            };
+
+        OnePassNeighborList() : m_N(0), m_total(0) {}
+
+        // Capacity array of N rows for the caller (or a CapacityModel) to fill before build().
+        unsigned int* capacity(unsigned int N)
+            {
+            m_caps.reserve(N);
+            return m_caps.get();
+            }
+
+        // Exclusive scan of n 32-bit values into 64-bit offsets; returns the total (synchronises).
+        unsigned long long scan(const unsigned int* in, unsigned int n, unsigned long long* out, cudaStream_t stream)
+            {
+            const unsigned int tiles = detail::ceil_div(n, gpu::kScan64Tile);
+            m_tiles.reserve((size_t)tiles + 1);
+            gpu::k_scan64_tiles<<<tiles, gpu::kScan64Block, 0, stream>>>(in, n, m_tiles.get());
+            gpu::k_scan64_sums<<<1, 1024, 0, stream>>>(m_tiles.get(), tiles, m_tiles.get() + tiles);
+            gpu::k_scan64_apply<<<tiles, gpu::kScan64Block, 0, stream>>>(in, n, m_tiles.get(), out);
+            detail::check_cuda(cudaGetLastError(), "scan launch");
+            unsigned long long total = 0;
+            detail::check_cuda(cudaMemcpyAsync(&total, m_tiles.get() + tiles, sizeof(total), cudaMemcpyDeviceToHost,
+                                               stream), "copy");
+            detail::check_cuda(cudaStreamSynchronize(stream), "sync");
+            return total;
+            }
+
+        // Fill the list of every point of `lbvh` (self queries, cutoff rc, periodic box or open),
+        // rows sized by capacity(); cap_max bounds every capacity (for the symmetric traversal).
+        template<class TransformOpT = NullTransformOp>
+        Stats build(const LBVHTraverser::LaunchParameters& params, const LBVH& lbvh, LBVHTraverser& trav, float rc, float3 box,
+                    float pad, bool periodic, bool rows_sorted, unsigned int cap_max,
+                    const TransformOpT& transform = TransformOpT())
+            {
+            Stats st = {0, 0, 0};
+            const unsigned int N = lbvh.getN();
+            m_N = N;
+            if (N == 0) return st;
+            cudaStream_t stream = params.stream;
+            m_caps.reserve(N);
+            m_nneigh.reserve(N);
+            m_offsets.reserve(N);
+            st.slots = scan(m_caps.get(), N, m_offsets.get(), stream);
+            m_list.grow(st.slots + 1, 0, stream);
+            const CSRNeighborListOp out(m_list.get(), m_nneigh.get(), m_offsets.get(), m_caps.get(), cap_max);
+            if (periodic)
+                trav.traverseSelf(params, lbvh, rc, box, pad, out, PeriodicImagesOp(box), transform, rows_sorted);
+            else
+                trav.traverseSelf(params, lbvh, rc, make_float3(0.f, 0.f, 0.f), pad, out, SelfOp(), transform,
+                                  rows_sorted);
+
+            // rows that overflowed: exact counts are known, re-run them into appended space
+            m_ovf_q.reserve(N);
+            m_ovf_count.reserve(N);
+            m_ovf_off.reserve(N);
+            m_small.reserve(1);
+            detail::check_cuda(cudaMemsetAsync(m_small.get(), 0, sizeof(unsigned int), stream), "memset");
+            gpu::k_overflow_rows<<<detail::ceil_div(N, 256), 256, 0, stream>>>(
+                N, rows_sorted ? 1 : 0, lbvh.fastData().primitive, m_nneigh.get(), m_caps.get(), m_ovf_q.get(),
+                m_ovf_count.get(), m_small.get());
+            detail::check_cuda(cudaGetLastError(), "overflow launch");
+            unsigned int n_ovf = 0;
+            detail::check_cuda(cudaMemcpyAsync(&n_ovf, m_small.get(), sizeof(n_ovf), cudaMemcpyDeviceToHost, stream),
+                               "copy");
+            detail::check_cuda(cudaStreamSynchronize(stream), "sync");
+            st.overflow_rows = n_ovf;
+            m_total = st.slots;
+            if (n_ovf)
+                {
+                st.overflow_slots = scan(m_ovf_count.get(), n_ovf, m_ovf_off.get(), stream);
+                m_list.grow(st.slots + st.overflow_slots + 1, st.slots, stream);
+                gpu::k_overflow_assign<<<detail::ceil_div(n_ovf, 256), 256, 0, stream>>>(
+                    n_ovf, rows_sorted ? 1 : 0, lbvh.fastData().primitive, m_ovf_q.get(), m_ovf_count.get(),
+                    m_ovf_off.get(), st.slots, m_offsets.get(), m_caps.get());
+                detail::check_cuda(cudaGetLastError(), "overflow assign launch");
+                const CSRNeighborListOp exact(m_list.get(), m_nneigh.get(), m_offsets.get(), m_caps.get(), 0u);
+                if (periodic)
+                    trav.traverseSelfSubset(params, lbvh, rc, box, pad, exact, PeriodicImagesOp(box), transform,
+                                            rows_sorted, m_ovf_q.get(), n_ovf);
+                else
+                    trav.traverseSelfSubset(params, lbvh, rc, make_float3(0.f, 0.f, 0.f), pad, exact, SelfOp(),
+                                            transform, rows_sorted, m_ovf_q.get(), n_ovf);
+                m_total += st.overflow_slots;
+                }
+            return st;
+            }
+
+        const unsigned int* list() const { return m_list.get(); }
+        const unsigned long long* offsets() const { return m_offsets.get(); }
+        const unsigned int* capacities() const { return m_caps.get(); }
+        const unsigned int* nneigh() const { return m_nneigh.get(); }
+        unsigned long long totalSlots() const { return m_total; }
+
+    private:
+        unsigned int m_N;
+        unsigned long long m_total;
+        device_array<unsigned int> m_caps;
+        device_array<unsigned int> m_nneigh;
+        device_array<unsigned long long> m_offsets;
+        device_array<unsigned int> m_list;
+        device_array<unsigned int> m_ovf_q;
+        device_array<unsigned int> m_ovf_count;
+        device_array<unsigned long long> m_ovf_off;
+        device_array<unsigned long long> m_tiles;
+        device_array<unsigned int> m_small;
+    };
+
+} // namespace neighbor
+
+#endif // NEIGHBOR_ONE_PASS_LIST_H_

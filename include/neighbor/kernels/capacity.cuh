@@ -1,0 +1,662 @@
+// Learned per-query neighbor capacity (sm_103a).
+//
+// A query's neighbor count is predicted from the occupancy of the coarse Morton cells around it:
+// the 10-bit Morton bins of the build, shifted right by `shift` bits per axis, give a G^3 grid
+// (G = 1024 >> shift) whose cells are indexed by the coarse Morton code (code >> 3*shift).
+//
+// Features of a query (32, FP32):
+//   0..26  log1p(occupancy) of the 27 cells (dx, dy, dz) in {-1,0,1}^3 around its own cell,
+//          k = 9(dx+1) + 3(dy+1) + (dz+1); neighbors wrap around the grid for periodic boxes and
+//          count 0 outside it otherwise
+//   27..29 position inside its own cell along x, y, z, in [0, 1]
+//   30     log1p(sum of the 27 occupancies)
+//   31     1
+// Network: 32 -> 64 (ReLU) -> 64 (ReLU) -> 1 (softplus), weights in BF16, inputs and hidden
+// activations rounded to BF16, every product accumulated in FP32, biases FP32.  The output
+// approximates log1p(count); capacity = ceil(expm1(y + margin)), clamped to [1, cap_max].
+//
+//   k_cap_occupancy      occupancy grid from the sorted Morton codes (warp-aggregated atomics)
+//   k_cap_features       the 32 features of every sorted point (training data, tests)
+//   k_cap_infer          features + network + capacity fused, one warp per 32 queries; the three
+//                        layers are BF16 mma.sync m16n8k16 tiles with FP32 accumulators, and a
+//                        layer's accumulator fragments are the next layer's A fragments
+//   k_cap_train_step     forward + backward of a mini-batch on CUDA cores (one thread per sample,
+//                        block tiles in shared memory), gradients summed in FP32
+//   k_cap_adam           Adam update of the FP32 master weights and their BF16 copies
+#ifndef NEIGHBOR_KERNELS_CAPACITY_CUH_
+#define NEIGHBOR_KERNELS_CAPACITY_CUH_
+
+#include <cuda_bf16.h>
+
+#include "common.cuh"
+
+namespace neighbor
+{
+namespace gpu
+{
+
+constexpr int kCapIn = 32;
+constexpr int kCapHidden = 64;
+// FP32 parameter vector: W1 [64][32], b1 [64], W2 [64][64], b2 [64], W3 [64], b3
+constexpr int kCapOffW1 = 0;
+constexpr int kCapOffB1 = kCapOffW1 + kCapHidden * kCapIn;
+constexpr int kCapOffW2 = kCapOffB1 + kCapHidden;
+constexpr int kCapOffB2 = kCapOffW2 + kCapHidden * kCapHidden;
+constexpr int kCapOffW3 = kCapOffB2 + kCapHidden;
+constexpr int kCapOffB3 = kCapOffW3 + kCapHidden;
+constexpr int kCapParams = kCapOffB3 + 1;
+// BF16 weight vector: W1, W2, W3 (same order, no biases)
+constexpr int kCapBfW1 = 0;
+constexpr int kCapBfW2 = kCapBfW1 + kCapHidden * kCapIn;
+constexpr int kCapBfW3 = kCapBfW2 + kCapHidden * kCapHidden;
+constexpr int kCapBfWeights = kCapBfW3 + kCapHidden;
+
+struct CapFrame
+    {
+    float3 lo;          // Morton frame of the build (scene lower corner and extent)
+    float3 ext;
+    unsigned int shift; // coarse level: bins >> shift
+    int periodic;       // neighbor cells wrap around the grid
+    };
+
+__device__ __forceinline__ unsigned int compact1by2(unsigned int v)
+    {
+    v &= 0x09249249u;
+    v = (v | (v >> 2)) & 0x030c30c3u;
+    v = (v | (v >> 4)) & 0x0300f00fu;
+    v = (v | (v >> 8)) & 0x030000ffu;
+    v = (v | (v >> 16)) & 0x000003ffu;
+    return v;
+    }
+
+__device__ __forceinline__ float bf16_round(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
+
+// Occupancy of every coarse cell: occ[code >> 3*shift] += 1 (occ zero on entry).
+__global__ void __launch_bounds__(256) k_cap_occupancy(const unsigned int* __restrict__ codes, unsigned int N,
+                                                       unsigned int shift, unsigned int* __restrict__ occ)
+    {
+    const unsigned int s = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = s < N;
+    const unsigned int c = valid ? (codes[s] >> (3u * shift)) : 0xffffffffu;
+    const unsigned int peers = __match_any_sync(0xffffffffu, c);
+    if (valid && (threadIdx.x & 31u) == 31u - __clz(peers)) atomicAdd(occ + c, __popc(peers));
+    }
+
+// Features of sorted point s (see the file comment).
+__device__ __forceinline__ void cap_features(const CapFrame& fr, unsigned int code, const float3& p,
+                                             const unsigned int* __restrict__ occ, float* f)
+    {
+    const unsigned int sh = fr.shift;
+    const int G = 1024 >> sh;
+    const unsigned int c = code >> (3u * sh);
+    const int cx = (int)compact1by2(c >> 2);
+    const int cy = (int)compact1by2(c >> 1);
+    const int cz = (int)compact1by2(c);
+    float sum = 0.f;
+#pragma unroll
+    for (int k = 0; k < 27; ++k)
+        {
+        int nx = cx + k / 9 - 1;
+        int ny = cy + (k / 3) % 3 - 1;
+        int nz = cz + k % 3 - 1;
+        unsigned int o = 0u;
+        bool inside = true;
+        if (fr.periodic)
+            {
+            nx = (nx + G) % G;
+            ny = (ny + G) % G;
+            nz = (nz + G) % G;
+            }
+        else
+            {
+            inside = nx >= 0 && nx < G && ny >= 0 && ny < G && nz >= 0 && nz < G;
+            }
+        if (inside)
+            o = __ldg(occ + ((part1by2((unsigned int)nx) << 2) | (part1by2((unsigned int)ny) << 1)
+                             | part1by2((unsigned int)nz)));
+        sum += (float)o;
+        f[k] = log1pf((float)o);
+        }
+    const float inv = 1.0f / (float)(1u << sh);
+    const float tx = fminf(fmaxf(__fmul_rn(__fdiv_rn(__fsub_rn(p.x, fr.lo.x), fr.ext.x), 1023.f), 0.f), 1023.f);
+    const float ty = fminf(fmaxf(__fmul_rn(__fdiv_rn(__fsub_rn(p.y, fr.lo.y), fr.ext.y), 1023.f), 0.f), 1023.f);
+    const float tz = fminf(fmaxf(__fmul_rn(__fdiv_rn(__fsub_rn(p.z, fr.lo.z), fr.ext.z), 1023.f), 0.f), 1023.f);
+    f[27] = fminf(fmaxf((tx - (float)(cx << sh)) * inv, 0.f), 1.f);
+    f[28] = fminf(fmaxf((ty - (float)(cy << sh)) * inv, 0.f), 1.f);
+    f[29] = fminf(fmaxf((tz - (float)(cz << sh)) * inv, 0.f), 1.f);
+    f[30] = log1pf(sum);
+    f[31] = 1.f;
+    }
+
+__global__ void __launch_bounds__(256) k_cap_features(const CapFrame fr, const unsigned int* __restrict__ codes,
+                                                      const float4* __restrict__ points, unsigned int N,
+                                                      const unsigned int* __restrict__ occ, float* __restrict__ out)
+    {
+    const unsigned int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= N) return;
+    const float4 p = points[s];
+    float f[kCapIn];
+    cap_features(fr, codes[s], make_float3(p.x, p.y, p.z), occ, f);
+    float4* o = reinterpret_cast<float4*>(out + (size_t)s * kCapIn);
+#pragma unroll
+    for (int k = 0; k < kCapIn / 4; ++k) o[k] = make_float4(f[4 * k], f[4 * k + 1], f[4 * k + 2], f[4 * k + 3]);
+    }
+
+// Numerically stable softplus and its derivative.
+__device__ __forceinline__ float cap_softplus(float z) { return fmaxf(z, 0.f) + log1pf(expf(-fabsf(z))); }
+__device__ __forceinline__ float cap_sigmoid(float z) { return 1.f / (1.f + expf(-z)); }
+
+__device__ __forceinline__ unsigned int cap_from_output(float y, float margin, unsigned int cap_max)
+    {
+    const float c = ceilf(expm1f(y + margin));
+    if (!(c >= 1.f)) return 1u;
+    if (c >= (float)cap_max) return cap_max;
+    return (unsigned int)c;
+    }
+
+// ---------------------------------------------------------------------------------------------
+// Inference: features, network and capacity fused.  A warp takes 32 consecutive queries (two
+// m16 tiles): each lane computes one query's features into shared memory (BF16), then the warp
+// runs  H1 = relu(X W1^T + b1), H2 = relu(H1 W2^T + b2), z = H2 W3^T + b3  as mma.sync
+// m16n8k16 BF16 tiles with FP32 accumulators.  The accumulator fragment of N-tiles 2t and 2t+1
+// is exactly the A fragment of K-tile t of the next layer (rows: groupID, groupID + 8; columns:
+// 2*tig + {0,1} (+8)), so activations never leave registers between layers.
+// ---------------------------------------------------------------------------------------------
+struct CapInferArgs
+    {
+    CapFrame frame;
+    const unsigned int* codes;      // sorted Morton codes
+    const float4* points;           // sorted payload
+    unsigned int N;
+    const unsigned int* occ;
+    const __nv_bfloat16* w;         // BF16 weights (kCapBfWeights)
+    const float* p;                 // FP32 parameters (biases read from here)
+    float margin;
+    unsigned int cap_max;
+    int rows_sorted;                // row of sorted position s: s or primitive id
+    float* y_out;                   // optional: network output per row
+    unsigned int* cap_out;          // capacity per row
+    };
+
+__device__ __forceinline__ unsigned int pack_bf16x2(float lo, float hi)
+    {
+    const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<const unsigned int*>(&v);
+    }
+
+__device__ __forceinline__ void mma_bf16_16816(float (&d)[4], const unsigned int (&a)[4], unsigned int b0,
+                                               unsigned int b1)
+    {
+    asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+                 "{%0,%1,%2,%3};"
+                 : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+                 : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+    }
+
+constexpr int kCapInferWarps = 8;
+
+__global__ void __launch_bounds__(kCapInferWarps * 32) k_cap_infer(const CapInferArgs a)
+    {
+    // weights as 32-bit pairs of BF16: W1 [64][16], W2 [64][32], W3 [8][32] (rows 1..7 zero)
+    __shared__ unsigned int s_w1[kCapHidden * kCapIn / 2];
+    __shared__ unsigned int s_w2[kCapHidden * kCapHidden / 2];
+    __shared__ unsigned int s_w3[8 * kCapHidden / 2];
+    __shared__ float s_b1[kCapHidden];
+    __shared__ float s_b2[kCapHidden];
+    __shared__ unsigned int s_x[kCapInferWarps][32 * (kCapIn / 2 + 1)];  // per warp: 32 queries x 16 pairs (+1 pad)
+    const unsigned int* wsrc = reinterpret_cast<const unsigned int*>(a.w);
+    for (int i = threadIdx.x; i < kCapHidden * kCapIn / 2; i += blockDim.x) s_w1[i] = wsrc[kCapBfW1 / 2 + i];
+    for (int i = threadIdx.x; i < kCapHidden * kCapHidden / 2; i += blockDim.x) s_w2[i] = wsrc[kCapBfW2 / 2 + i];
+    for (int i = threadIdx.x; i < 8 * kCapHidden / 2; i += blockDim.x) s_w3[i] = i < kCapHidden / 2 ? wsrc[kCapBfW3 / 2 + i] : 0u;
+    for (int i = threadIdx.x; i < kCapHidden; i += blockDim.x)
+        {
+        s_b1[i] = a.p[kCapOffB1 + i];
+        s_b2[i] = a.p[kCapOffB2 + i];
+        }
+    __syncthreads();
+    const float b3 = a.p[kCapOffB3];
+    const unsigned int lane = threadIdx.x & 31u;
+    const unsigned int warp = threadIdx.x >> 5;
+    const unsigned int g = lane >> 2;   // groupID
+    const unsigned int t = lane & 3u;   // thread in group
+    unsigned int* xs = s_x[warp];
+    constexpr int XS = kCapIn / 2 + 1;  // row stride of xs in 32-bit words
+    const unsigned int n_tiles = (a.N + 31u) / 32u;
+    for (unsigned int tile = blockIdx.x * kCapInferWarps + warp; tile < n_tiles; tile += gridDim.x * kCapInferWarps)
+        {
+        const unsigned int base = tile * 32u;
+        // features of query base + lane
+        {
+        const unsigned int s = base + lane;
+        float f[kCapIn];
+        if (s < a.N)
+            {
+            const float4 p = a.points[s];
+            cap_features(a.frame, a.codes[s], make_float3(p.x, p.y, p.z), a.occ, f);
+            }
+        else
+            {
+#pragma unroll
+            for (int k = 0; k < kCapIn; ++k) f[k] = 0.f;
+            }
+#pragma unroll
+        for (int k = 0; k < kCapIn / 2; ++k) xs[lane * XS + k] = pack_bf16x2(f[2 * k], f[2 * k + 1]);
+        }
+        __syncwarp();
+#pragma unroll
+        for (int mt = 0; mt < 2; ++mt)
+            {
+            const unsigned int r0 = mt * 16u + g;  // rows r0 and r0 + 8 of this lane
+            // layer 1: K = 32 (2 k-tiles), N = 64 (8 n-tiles)
+            float h1[8][4];
+#pragma unroll
+            for (int nt = 0; nt < 8; ++nt)
+                {
+                h1[nt][0] = h1[nt][1] = h1[nt][2] = h1[nt][3] = 0.f;
+#pragma unroll
+                for (int kt = 0; kt < 2; ++kt)
+                    {
+                    unsigned int af[4];
+                    af[0] = xs[r0 * XS + kt * 8 + t];
+                    af[1] = xs[(r0 + 8) * XS + kt * 8 + t];
+                    af[2] = xs[r0 * XS + kt * 8 + 4 + t];
+                    af[3] = xs[(r0 + 8) * XS + kt * 8 + 4 + t];
+                    const unsigned int n = nt * 8 + g;
+                    const unsigned int b0 = s_w1[n * (kCapIn / 2) + kt * 8 + t];
+                    const unsigned int b1 = s_w1[n * (kCapIn / 2) + kt * 8 + 4 + t];
+                    mma_bf16_16816(h1[nt], af, b0, b1);
+                    }
+                const float bl = s_b1[nt * 8 + 2 * t];
+                const float bh = s_b1[nt * 8 + 2 * t + 1];
+                h1[nt][0] = fmaxf(h1[nt][0] + bl, 0.f);
+                h1[nt][1] = fmaxf(h1[nt][1] + bh, 0.f);
+                h1[nt][2] = fmaxf(h1[nt][2] + bl, 0.f);
+                h1[nt][3] = fmaxf(h1[nt][3] + bh, 0.f);
+                }
+            // layer 2: A fragments from h1 (k-tile kt = n-tiles 2kt, 2kt+1)
+            unsigned int a2[4][4];
+#pragma unroll
+            for (int kt = 0; kt < 4; ++kt)
+                {
+                a2[kt][0] = pack_bf16x2(h1[2 * kt][0], h1[2 * kt][1]);
+                a2[kt][1] = pack_bf16x2(h1[2 * kt][2], h1[2 * kt][3]);
+                a2[kt][2] = pack_bf16x2(h1[2 * kt + 1][0], h1[2 * kt + 1][1]);
+                a2[kt][3] = pack_bf16x2(h1[2 * kt + 1][2], h1[2 * kt + 1][3]);
+                }
+            float h2[8][4];
+#pragma unroll
+            for (int nt = 0; nt < 8; ++nt)
+                {
+                h2[nt][0] = h2[nt][1] = h2[nt][2] = h2[nt][3] = 0.f;
+#pragma unroll
+                for (int kt = 0; kt < 4; ++kt)
+                    {
+                    const unsigned int n = nt * 8 + g;
+                    const unsigned int b0 = s_w2[n * (kCapHidden / 2) + kt * 8 + t];
+                    const unsigned int b1 = s_w2[n * (kCapHidden / 2) + kt * 8 + 4 + t];
+                    mma_bf16_16816(h2[nt], a2[kt], b0, b1);
+                    }
+                const float bl = s_b2[nt * 8 + 2 * t];
+                const float bh = s_b2[nt * 8 + 2 * t + 1];
+                h2[nt][0] = fmaxf(h2[nt][0] + bl, 0.f);
+                h2[nt][1] = fmaxf(h2[nt][1] + bh, 0.f);
+                h2[nt][2] = fmaxf(h2[nt][2] + bl, 0.f);
+                h2[nt][3] = fmaxf(h2[nt][3] + bh, 0.f);
+                }
+            // layer 3: one n-tile (column 0 = the output)
+            float z[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+            for (int kt = 0; kt < 4; ++kt)
+                {
+                unsigned int af[4];
+                af[0] = pack_bf16x2(h2[2 * kt][0], h2[2 * kt][1]);
+                af[1] = pack_bf16x2(h2[2 * kt][2], h2[2 * kt][3]);
+                af[2] = pack_bf16x2(h2[2 * kt + 1][0], h2[2 * kt + 1][1]);
+                af[3] = pack_bf16x2(h2[2 * kt + 1][2], h2[2 * kt + 1][3]);
+                const unsigned int b0 = s_w3[g * (kCapHidden / 2) + kt * 8 + t];
+                const unsigned int b1 = s_w3[g * (kCapHidden / 2) + kt * 8 + 4 + t];
+                mma_bf16_16816(z, af, b0, b1);
+                }
+            if (t == 0u)
+                {
+#pragma unroll
+                for (int h = 0; h < 2; ++h)
+                    {
+                    const unsigned int s = base + r0 + 8u * h;
+                    if (s < a.N)
+                        {
+                        const float y = cap_softplus(z[2 * h] + b3);
+                        const unsigned int row = a.rows_sorted ? s : __float_as_uint(a.points[s].w);
+                        if (a.y_out) a.y_out[row] = y;
+                        a.cap_out[row] = cap_from_output(y, a.margin, a.cap_max);
+                        }
+                    }
+                }
+            }
+        __syncwarp();
+        }
+    }
+
+// ---------------------------------------------------------------------------------------------
+// Training.  One mini-batch step: sample b of the batch is row (offset + b * stride) mod N of the
+// feature matrix.  Each block runs tiles of kCapTrainTile samples, one thread per sample, with
+// the same BF16 rounding points as inference; per-sample activations and deltas go to shared
+// memory, and the block adds the tile's weight gradients (FP32) into its shared accumulator,
+// then into the global gradient with atomics.  grad = sum over the batch of dL/dp with
+// L = 0.5 (y - target)^2; loss_out += sum of L.
+// ---------------------------------------------------------------------------------------------
+constexpr int kCapTrainTile = 64;
+
+struct CapTrainArgs
+    {
+    const float* features;   // [N][32]
+    const float* target;     // [N] log1p(count)
+    unsigned int N;
+    unsigned int batch;
+    unsigned int offset;
+    unsigned int stride;
+    const __nv_bfloat16* w;
+    const float* p;
+    float* grad;             // [kCapParams], zero on entry
+    float* loss_out;
+    };
+
+struct CapTrainSmem
+    {
+    float w1[kCapHidden * kCapIn];
+    float w2[kCapHidden * kCapHidden];
+    float w3[kCapHidden];
+    float b1[kCapHidden];
+    float b2[kCapHidden];
+    float x[kCapTrainTile][kCapIn + 1];
+    float h1[kCapTrainTile][kCapHidden + 1];
+    float h2[kCapTrainTile][kCapHidden + 1];
+    float d2[kCapTrainTile][kCapHidden + 1];
+    float d1[kCapTrainTile][kCapHidden + 1];
+    float dz[kCapTrainTile];
+    float g[kCapParams];
+    };
+
+__global__ void __launch_bounds__(kCapTrainTile) k_cap_train_step(const CapTrainArgs a)
+    {
+    extern __shared__ __align__(16) unsigned char smem_cap[];
+    CapTrainSmem& S = *reinterpret_cast<CapTrainSmem*>(smem_cap);
+    const int tid = threadIdx.x;
+    for (int i = tid; i < kCapHidden * kCapIn; i += blockDim.x) S.w1[i] = __bfloat162float(a.w[kCapBfW1 + i]);
+    for (int i = tid; i < kCapHidden * kCapHidden; i += blockDim.x) S.w2[i] = __bfloat162float(a.w[kCapBfW2 + i]);
+    for (int i = tid; i < kCapHidden; i += blockDim.x)
+        {
+        S.w3[i] = __bfloat162float(a.w[kCapBfW3 + i]);
+        S.b1[i] = a.p[kCapOffB1 + i];
+        S.b2[i] = a.p[kCapOffB2 + i];
+        }
+    for (int i = tid; i < kCapParams; i += blockDim.x) S.g[i] = 0.f;
+    const float b3 = a.p[kCapOffB3];
+    __syncthreads();
+    float loss = 0.f;
+    const unsigned int n_tiles = (a.batch + kCapTrainTile - 1) / kCapTrainTile;
+    for (unsigned int tile = blockIdx.x; tile < n_tiles; tile += gridDim.x)
+        {
+        const unsigned int b = tile * kCapTrainTile + tid;
+        const bool on = b < a.batch;
+        float dz = 0.f;
+        if (on)
+            {
+            const unsigned int row = (unsigned int)(((unsigned long long)a.offset + (unsigned long long)b * a.stride) % a.N);
+            const float* xf = a.features + (size_t)row * kCapIn;
+            for (int k = 0; k < kCapIn; ++k) S.x[tid][k] = bf16_round(xf[k]);
+            for (int j = 0; j < kCapHidden; ++j)
+                {
+                float acc = 0.f;
+                for (int k = 0; k < kCapIn; ++k) acc = fmaf(S.w1[j * kCapIn + k], S.x[tid][k], acc);
+                S.h1[tid][j] = bf16_round(fmaxf(acc + S.b1[j], 0.f));
+                }
+            for (int j = 0; j < kCapHidden; ++j)
+                {
+                float acc = 0.f;
+                for (int k = 0; k < kCapHidden; ++k) acc = fmaf(S.w2[j * kCapHidden + k], S.h1[tid][k], acc);
+                S.h2[tid][j] = bf16_round(fmaxf(acc + S.b2[j], 0.f));
+                }
+            float z = 0.f;
+            for (int k = 0; k < kCapHidden; ++k) z = fmaf(S.w3[k], S.h2[tid][k], z);
+            z += b3;
+            const float y = cap_softplus(z);
+            const float dy = y - a.target[row];
+            loss += 0.5f * dy * dy;
+            dz = dy * cap_sigmoid(z);
+            for (int j = 0; j < kCapHidden; ++j) S.d2[tid][j] = S.h2[tid][j] > 0.f ? dz * S.w3[j] : 0.f;
+            for (int k = 0; k < kCapHidden; ++k)
+                {
+                float acc = 0.f;
+                for (int j = 0; j < kCapHidden; ++j) acc = fmaf(S.w2[j * kCapHidden + k], S.d2[tid][j], acc);
+                S.d1[tid][k] = S.h1[tid][k] > 0.f ? acc : 0.f;
+                }
+            }
+        else
+            {
+            for (int k = 0; k < kCapIn; ++k) S.x[tid][k] = 0.f;
+            for (int j = 0; j < kCapHidden; ++j)
+                {
+                S.h1[tid][j] = 0.f;
+                S.h2[tid][j] = 0.f;
+                S.d2[tid][j] = 0.f;
+                S.d1[tid][j] = 0.f;
+                }
+            }
+        S.dz[tid] = dz;
+        __syncthreads();
+        // tile gradients: thread tid owns rows j = tid (and tid + 64 ...) of each weight matrix
+        for (int j = tid; j < kCapHidden; j += blockDim.x)
+            {
+            float gb1 = 0.f, gb2 = 0.f, gw3 = 0.f;
+            for (int s = 0; s < kCapTrainTile; ++s)
+                {
+                gb1 += S.d1[s][j];
+                gb2 += S.d2[s][j];
+                gw3 += S.dz[s] * S.h2[s][j];
+                }
+            S.g[kCapOffB1 + j] += gb1;
+            S.g[kCapOffB2 + j] += gb2;
+            S.g[kCapOffW3 + j] += gw3;
+            for (int k = 0; k < kCapIn; ++k)
+                {
+                float acc = 0.f;
+                for (int s = 0; s < kCapTrainTile; ++s) acc = fmaf(S.d1[s][j], S.x[s][k], acc);
+                S.g[kCapOffW1 + j * kCapIn + k] += acc;
+                }
+            for (int k = 0; k < kCapHidden; ++k)
+                {
+                float acc = 0.f;
+                for (int s = 0; s < kCapTrainTile; ++s) acc = fmaf(S.d2[s][j], S.h1[s][k], acc);
+                S.g[kCapOffW2 + j * kCapHidden + k] += acc;
+                }
+            }
+        if (tid == 0)
+            {
+            float gb3 = 0.f;
+            for (int s = 0; s < kCapTrainTile; ++s) gb3 += S.dz[s];
+            S.g[kCapOffB3] += gb3;
+            }
+        __syncthreads();
+        }
+    for (int i = tid; i < kCapParams; i += blockDim.x)
+        if (S.g[i] != 0.f) atomicAdd(a.grad + i, S.g[i]);
+    if (loss != 0.f) atomicAdd(a.loss_out, loss);
+    }
+
+struct CapAdamArgs
+    {
+    float* p;
+    float* m;
+    float* v;
+    const float* grad;
+    __nv_bfloat16* w;
+    float scale;      // 1 / batch
+    float lr;
+    float beta1, beta2, eps;
+    float bias1, bias2;  // 1 - beta^t
+    };
+
+__global__ void __launch_bounds__(256) k_cap_adam(const CapAdamArgs a)
+    {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= kCapParams) return;
+    const float g = a.grad[i] * a.scale;
+    const float m = a.beta1 * a.m[i] + (1.f - a.beta1) * g;
+    const float v = a.beta2 * a.v[i] + (1.f - a.beta2) * g * g;
+    a.m[i] = m;
+    a.v[i] = v;
+    const float p = a.p[i] - a.lr * (m / a.bias1) / (sqrtf(v / a.bias2) + a.eps);
+    a.p[i] = p;
+    int wi = -1;
+    if (i < kCapOffB1) wi = kCapBfW1 + (i - kCapOffW1);
+    else if (i >= kCapOffW2 && i < kCapOffB2) wi = kCapBfW2 + (i - kCapOffW2);
+    else if (i >= kCapOffW3 && i < kCapOffB3) wi = kCapBfW3 + (i - kCapOffW3);
+    if (wi >= 0) a.w[wi] = __float2bfloat16_rn(p);
+    }
+
+// BF16 copies of the FP32 weights.
+__global__ void __launch_bounds__(256) k_cap_cast(const float* __restrict__ p, __nv_bfloat16* __restrict__ w)
+    {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= kCapBfWeights) return;
+    int pi;
+    if (i < kCapBfW2) pi = kCapOffW1 + i;
+    else if (i < kCapBfW3) pi = kCapOffW2 + (i - kCapBfW2);
+    else pi = kCapOffW3 + (i - kCapBfW3);
+    w[i] = __float2bfloat16_rn(p[pi]);
+    }
+
+// Residual target - output of every row (for the capacity margin) and log1p(count) targets.
+__global__ void __launch_bounds__(256) k_cap_targets(const unsigned int* __restrict__ counts, unsigned int N,
+                                                     float* __restrict__ target)
+    {
+    const unsigned int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < N) target[i] = log1pf((float)counts[i]);
+    }
+
+// ---------------------------------------------------------------------------------------------
+// Exclusive scan of 32-bit counts into 64-bit offsets (three phases, deterministic):
+// tile sums, a scan of the tile sums by one block, then each tile's local scan plus its base.
+// ---------------------------------------------------------------------------------------------
+constexpr int kScan64Block = 256;
+constexpr int kScan64Items = 16;
+constexpr int kScan64Tile = kScan64Block * kScan64Items;
+
+__global__ void __launch_bounds__(kScan64Block) k_scan64_tiles(const unsigned int* __restrict__ in, unsigned int n,
+                                                               unsigned long long* __restrict__ tile_sum)
+    {
+    __shared__ unsigned long long s_red[kScan64Block / 32];
+    const unsigned int base = blockIdx.x * kScan64Tile;
+    unsigned long long sum = 0;
+    for (int k = 0; k < kScan64Items; ++k)
+        {
+        const unsigned int i = base + k * kScan64Block + threadIdx.x;
+        if (i < n) sum += in[i];
+        }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = sum;
+    __syncthreads();
+    if (threadIdx.x == 0)
+        {
+        unsigned long long t = 0;
+        for (int w = 0; w < kScan64Block / 32; ++w) t += s_red[w];
+        tile_sum[blockIdx.x] = t;
+        }
+    }
+
+// One block: exclusive scan of the tile sums in place; total to *total.
+__global__ void __launch_bounds__(1024) k_scan64_sums(unsigned long long* __restrict__ tile_sum, unsigned int n_tiles,
+                                                      unsigned long long* __restrict__ total)
+    {
+    __shared__ unsigned long long s_w[32];
+    __shared__ unsigned long long s_carry;
+    if (threadIdx.x == 0) s_carry = 0;
+    __syncthreads();
+    const unsigned int lane = threadIdx.x & 31u;
+    const unsigned int warp = threadIdx.x >> 5;
+    for (unsigned int c = 0; c < n_tiles; c += blockDim.x)
+        {
+        const unsigned int i = c + threadIdx.x;
+        const unsigned long long v = i < n_tiles ? tile_sum[i] : 0ull;
+        unsigned long long incl = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1)
+            {
+            const unsigned long long x = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= (unsigned int)o) incl += x;
+            }
+        if (lane == 31u) s_w[warp] = incl;
+        __syncthreads();
+        if (warp == 0)
+            {
+            const unsigned long long w = s_w[lane];
+            unsigned long long wi = w;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1)
+                {
+                const unsigned long long x = __shfl_up_sync(0xffffffffu, wi, o);
+                if (lane >= (unsigned int)o) wi += x;
+                }
+            s_w[lane] = wi - w;
+            }
+        __syncthreads();
+        const unsigned long long carry = s_carry;
+        if (i < n_tiles) tile_sum[i] = carry + s_w[warp] + incl - v;
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) s_carry = carry + s_w[warp] + incl;
+        __syncthreads();
+        }
+    if (threadIdx.x == 0) *total = s_carry;
+    }
+
+__global__ void __launch_bounds__(kScan64Block) k_scan64_apply(const unsigned int* __restrict__ in, unsigned int n,
+                                                               const unsigned long long* __restrict__ tile_base,
+                                                               unsigned long long* __restrict__ out)
+    {
+    __shared__ unsigned long long s_w[kScan64Block / 32 + 1];
+    const unsigned int base = blockIdx.x * kScan64Tile + threadIdx.x * kScan64Items;
+    unsigned int v[kScan64Items];
+    unsigned long long sum = 0;
+#pragma unroll
+    for (int k = 0; k < kScan64Items; ++k)
+        {
+        v[k] = (base + k < n) ? in[base + k] : 0u;
+        sum += v[k];
+        }
+    const unsigned int lane = threadIdx.x & 31u;
+    const unsigned int warp = threadIdx.x >> 5;
+    unsigned long long incl = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1)
+        {
+        const unsigned long long x = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= (unsigned int)o) incl += x;
+        }
+    if (lane == 31u) s_w[warp] = incl;
+    __syncthreads();
+    if (threadIdx.x == 0)
+        {
+        unsigned long long r = 0;
+        for (int w = 0; w < kScan64Block / 32; ++w)
+            {
+            const unsigned long long x = s_w[w];
+            s_w[w] = r;
+            r += x;
+            }
+        }
+    __syncthreads();
+    unsigned long long run = tile_base[blockIdx.x] + s_w[warp] + incl - sum;
+#pragma unroll
+    for (int k = 0; k < kScan64Items; ++k)
+        {
+        if (base + k < n) out[base + k] = run;
+        run += v[k];
+        }
+    }
+
+} // namespace gpu
+} // namespace neighbor
+
+#endif // NEIGHBOR_KERNELS_CAPACITY_CUH_

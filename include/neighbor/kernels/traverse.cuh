@@ -162,7 +162,8 @@ __global__ void k_traverse_ref10(const OutputOpT out, const LBVHCompressedData l
 enum FastOutput : int
     {
     kFastCount = 1,
-    kFastList = 2,
+    kFastList = 2,   // fixed stride max_neigh
+    kFastCSR = 3,    // per-row offset and capacity
     };
 
 struct FastQueryArgs
@@ -180,8 +181,29 @@ struct FastQueryArgs
     unsigned int* nneigh;
     unsigned int* list;
     unsigned int max_neigh;
-    unsigned long long* stats;  // optional counters: records visited, point tests, walks
+    const unsigned long long* offsets = nullptr;  // kFastCSR: first slot of each row
+    const unsigned int* caps = nullptr;           // kFastCSR: capacity of each row
+    const unsigned int* subset = nullptr;         // optional: thread t runs query subset[t] (Q threads)
+    unsigned long long* stats = nullptr;  // optional counters: records visited, point tests, walks
     };
+
+// First slot and capacity of an output row.
+template<int OUT>
+__device__ __forceinline__ void row_layout(const unsigned long long* offsets, const unsigned int* caps,
+                                           unsigned int max_neigh, unsigned int row,
+                                           unsigned long long& first, unsigned int& cap)
+    {
+    if (OUT == kFastCSR)
+        {
+        first = offsets[row];
+        cap = caps[row];
+        }
+    else
+        {
+        first = (unsigned long long)row * max_neigh;
+        cap = max_neigh;
+        }
+    }
 
 // Add a thread's (or a packet's) traversal counts to the optional statistics counters.
 __device__ __forceinline__ void add_stats(unsigned long long* stats, unsigned long long visits,
@@ -297,15 +319,18 @@ __global__ void k_traverse_fast(const FastLBVHData tree, const FastQueryArgs a,
         s_records = ld_status(tree.status) != 0u ? 0u : *tree.n_boxes + tree.N;
         }
     __syncthreads();
-    const unsigned int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= a.Q) return;
+    const unsigned int tq = blockIdx.x * blockDim.x + threadIdx.x;
+    if (tq >= a.Q) return;
+    const unsigned int q = a.subset ? a.subset[tq] : tq;
     const QuantFrame f = s_frame;
     const unsigned int n_rec = s_records;
 
     const FastQuery Q = load_fast_query(tree, a, q);
     const float rs = approx::fadd_ru(Q.rc, a.pad);
     unsigned int flags = n_rec ? image_flags(a, f, Q.p, rs) : 0u;
-    const unsigned long long row_first = (unsigned long long)Q.row * a.max_neigh;
+    unsigned long long row_first = 0;
+    unsigned int cap = 0;
+    if (OUT != kFastCount) row_layout<OUT>(a.offsets, a.caps, a.max_neigh, Q.row, row_first, cap);
 
     unsigned int count = 0;
     unsigned int visits = 0, tests = 0, walks = 0;
@@ -332,7 +357,7 @@ __global__ void k_traverse_fast(const FastLBVHData tree, const FastQueryArgs a,
                     if (STATS) ++tests;
                     if (exact_pair(Q.p, x, Q.rc, a.box))
                         {
-                        if (OUT == kFastList && count < a.max_neigh)
+                        if (OUT != kFastCount && count < cap)
                             a.list[row_first + count] = transform(tree.primitive[n.w & ~kLeafFlag]);
                         ++count;
                         }
@@ -369,8 +394,10 @@ __global__ void k_traverse_fast(const FastLBVHData tree, const FastQueryArgs a,
 // by key and maps keys to transform(primitive) ids, which gives every row the order of the
 // reference's rope traversal (images in ascending order, partners in ascending sorted position
 // within an image), independent of the order of the atomics.  The image through which a partner
-// finds the query is the mirror image (26 - image on the lattice).  A row with more than
-// max_neigh entries keeps max_neigh of them (which ones is unspecified) and its full count.
+// finds the query is the mirror image (26 - image on the lattice).  A row with more entries than
+// its capacity (max_neigh, or its own capacity in a CSR list) keeps that many of them (which
+// ones is unspecified) and its full count.  Rows longer than kHalfRowMax must not be ordered
+// here: the caller sizes capacities (or routes to the whole-tree walk) so that they are not.
 // ---------------------------------------------------------------------------------------------
 constexpr unsigned int kHalfKeyBits = 27;
 constexpr unsigned int kHalfKeyMask = (1u << kHalfKeyBits) - 1u;
@@ -388,8 +415,10 @@ struct HalfArgs
     float3 lattice_L;
     float3 box;              // periodic lengths of the minimum image (0 = open)
     unsigned int* nneigh;    // zero on entry
-    unsigned int* list;      // fill only: row-major, max_neigh per row
+    unsigned int* list;      // fill only: rows of max_neigh (kFastList) or offsets/caps (kFastCSR)
     unsigned int max_neigh;
+    const unsigned long long* offsets;
+    const unsigned int* caps;
     unsigned int* own;       // fill only: entries each row found itself
     };
 
@@ -436,7 +465,9 @@ __global__ void __launch_bounds__(256) k_traverse_half(const FastLBVHData tree, 
     unsigned int flags = n_rec ? half_image_flags(a, f, P, rs) : 0u;
     const bool multi = __popc(flags) > 1;
     const unsigned int start = n_rec ? tree.pre[q + 1] + q : 0u;
-    const unsigned long long row_first = (unsigned long long)row * a.max_neigh;
+    unsigned long long row_first = 0;
+    unsigned int cap = 0;
+    if (OUT != kFastCount) row_layout<OUT>(a.offsets, a.caps, a.max_neigh, row, row_first, cap);
     unsigned int own = 0;
     while (flags)
         {
@@ -464,14 +495,16 @@ __global__ void __launch_bounds__(256) k_traverse_half(const FastLBVHData tree, 
                         }
                     else
                         {
-                        if (own < a.max_neigh)
-                            a.list[row_first + (a.max_neigh - 1u - own)] = ((unsigned int)bit << kHalfKeyBits) | j;
+                        if (own < cap)
+                            a.list[row_first + (cap - 1u - own)] = ((unsigned int)bit << kHalfKeyBits) | j;
                         if (j != q)
                             {
                             const unsigned int rj = a.rows_sorted ? j : tree.primitive[j];
                             const unsigned int slot = atomicAdd(a.nneigh + rj, 1u);
-                            if (slot < a.max_neigh)
-                                a.list[(unsigned long long)rj * a.max_neigh + slot] = (mirror << kHalfKeyBits) | q;
+                            unsigned long long jfirst;
+                            unsigned int jcap;
+                            row_layout<OUT>(a.offsets, a.caps, a.max_neigh, rj, jfirst, jcap);
+                            if (slot < jcap) a.list[jfirst + slot] = (mirror << kHalfKeyBits) | q;
                             }
                         }
                     ++own;
@@ -500,6 +533,8 @@ struct HalfOrderArgs
     unsigned int* nneigh;       // in: entries appended by other queries; out: row totals
     unsigned int* list;
     unsigned int max_neigh;
+    const unsigned long long* offsets;  // CSR rows (null: stride max_neigh)
+    const unsigned int* caps;
     const unsigned int* own;
     const unsigned int* primitive;
     unsigned int* long_rows;    // rows longer than kHalfRowThread, for k_half_order_long
@@ -526,18 +561,20 @@ __global__ void __launch_bounds__(256) k_half_order_rows(const HalfOrderArgs a, 
     const unsigned int appended = a.nneigh[r];
     const unsigned int total = appended + a.own[r];
     a.nneigh[r] = total;
-    const unsigned int m = min(total, a.max_neigh);
+    const unsigned long long first = a.offsets ? a.offsets[r] : (unsigned long long)r * a.max_neigh;
+    const unsigned int cap = a.offsets ? a.caps[r] : a.max_neigh;
+    const unsigned int m = min(total, cap);
     if (m == 0u) return;
     if (m > kHalfRowThread)
         {
         a.long_rows[atomicAdd(a.n_long, 1u)] = r;
         return;
         }
-    unsigned int* row = a.list + (unsigned long long)r * a.max_neigh;
+    unsigned int* row = a.list + first;
     unsigned int key[kHalfRowThread];
     for (unsigned int k = 0; k < m; ++k)
         {
-        const unsigned int v = half_row_key(row, k, appended, total, a.max_neigh);
+        const unsigned int v = half_row_key(row, k, appended, total, cap);
         unsigned int j = k;
         while (j > 0u && key[j - 1u] > v)
             {
@@ -560,12 +597,14 @@ __global__ void __launch_bounds__(256) k_half_order_long(const HalfOrderArgs a, 
         const unsigned int r = a.long_rows[b];
         const unsigned int total = a.nneigh[r];
         const unsigned int appended = total - a.own[r];
-        const unsigned int m = min(min(total, a.max_neigh), kHalfRowMax);
-        unsigned int* row = a.list + (unsigned long long)r * a.max_neigh;
+        const unsigned long long first = a.offsets ? a.offsets[r] : (unsigned long long)r * a.max_neigh;
+        const unsigned int cap = a.offsets ? a.caps[r] : a.max_neigh;
+        const unsigned int m = min(min(total, cap), kHalfRowMax);
+        unsigned int* row = a.list + first;
         unsigned int n2 = 1u;
         while (n2 < m) n2 <<= 1;
         for (unsigned int k = threadIdx.x; k < n2; k += blockDim.x)
-            s_key[k] = k < m ? half_row_key(row, k, appended, total, a.max_neigh) : 0xffffffffu;
+            s_key[k] = k < m ? half_row_key(row, k, appended, total, cap) : 0xffffffffu;
         __syncthreads();
         for (unsigned int size = 2u; size <= n2; size <<= 1)
             {

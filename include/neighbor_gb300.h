@@ -174,6 +174,76 @@ int nbr_morton_sort_noalloc(const float* points, unsigned int N, const float lo[
  * (centres, points and image translations) plus 1e-6 * rc. */
 float nbr_exact_pad(float rc, float coord_max);
 
+/* ---- Additions with no counterpart in the reference: CSR lists, learned capacities, one-pass
+ * lists.  They replace the reference's two-pass pattern (CountNeighborsOp, host max, then
+ * NeighborListOp with that stride; benchmark/lbvh_benchmark.cc:177-196). ---- */
+
+typedef struct nbr_capmodel_s* nbr_capmodel;
+typedef struct nbr_onepass_s* nbr_onepass;
+
+/* Self traversal (as nbr_traverse_self) into a CSR list: row r occupies
+ * list[offsets[r] .. offsets[r] + caps[r]) (offsets: uint64[N]); the full count always goes to
+ * nneigh[r], entries past caps[r] are dropped.  max_capacity = an upper bound of caps (0 =
+ * unknown) lets the symmetric traversal run.  Images as in nbr_traverse (list images: whole-tree
+ * walk). */
+int nbr_traverse_self_csr(nbr_traverser t, nbr_lbvh h, float rc, const float box[3], float pad,
+                          const float* images, unsigned int n_images, const unsigned int* map,
+                          unsigned int* nneigh, unsigned int* list, const unsigned long long* offsets,
+                          const unsigned int* caps, unsigned int max_capacity, int rows_sorted,
+                          unsigned int block_size, void* stream);
+
+/* Capacity network (32 -> 64 -> 64 -> 1, BF16 weights, FP32 accumulation): create with a seed for
+ * the initial weights; parameters as FP32[NBR_CAP_PARAMS] on the host (W1[64][32], b1[64],
+ * W2[64][64], b2[64], W3[64], b3). */
+#define NBR_CAP_PARAMS 6337
+#define NBR_CAP_FEATURES 32
+int nbr_capmodel_create(nbr_capmodel* out, unsigned long long seed);
+int nbr_capmodel_destroy(nbr_capmodel m);
+int nbr_capmodel_get_params(nbr_capmodel m, float* host_params);
+int nbr_capmodel_set_params(nbr_capmodel m, const float* host_params);
+/* Capacity = ceil(expm1(output + margin)) clamped to [1, cap_max]. */
+int nbr_capmodel_set_margin(nbr_capmodel m, float margin);
+int nbr_capmodel_get_margin(nbr_capmodel m, float* margin);
+/* Coarse-cell level the features use for cutoff rc in a scene of extent hi - lo. */
+int nbr_capmodel_level(float rc, const float lo[3], const float hi[3], unsigned int* level);
+/* Features (float[N][32]) of every sorted point of a built point tree; lo/hi = the build's scene
+ * box, periodic = neighbor cells wrap. */
+int nbr_capmodel_features(nbr_capmodel m, nbr_lbvh h, const float lo[3], const float hi[3], float rc,
+                          int periodic, float* features, void* stream);
+/* Capacity per row (rows as nbr_traverse_self) and, if y != NULL, the network output per row. */
+int nbr_capmodel_predict(nbr_capmodel m, nbr_lbvh h, const float lo[3], const float hi[3], float rc,
+                         int periodic, int rows_sorted, unsigned int cap_max, unsigned int* caps, float* y,
+                         void* stream);
+/* log1p(count) training targets. */
+int nbr_capmodel_targets(const unsigned int* counts, unsigned int N, float* targets, void* stream);
+/* Summed gradient (float[NBR_CAP_PARAMS], device) and summed loss 0.5 (y - target)^2 (device
+ * float) of rows (offset + b * stride) mod N, b < batch; no update. */
+int nbr_capmodel_gradient(nbr_capmodel m, const float* features, const float* targets, unsigned int N,
+                          unsigned int batch, unsigned int offset, unsigned int stride, float* grad,
+                          float* loss, void* stream);
+/* `steps` Adam steps on random batches; *loss = mean loss of the last batch (synchronises). */
+int nbr_capmodel_train(nbr_capmodel m, const float* features, const float* targets, unsigned int N,
+                       unsigned int steps, unsigned int batch, float lr, unsigned long long seed,
+                       float* loss, void* stream);
+
+/* One-pass self neighbor list: nbr_onepass_capacity gives the device array of N row capacities
+ * to fill (e.g. nbr_capmodel_predict); nbr_onepass_build runs one traversal into a CSR list sized
+ * by them, then re-runs the rows that overflowed with their exact counts (the list is always
+ * exact).  cap_max bounds every capacity.  Synchronises the stream. */
+int nbr_onepass_create(nbr_onepass* out);
+int nbr_onepass_destroy(nbr_onepass op);
+int nbr_onepass_capacity(nbr_onepass op, unsigned int N, unsigned int** caps);
+int nbr_onepass_build(nbr_onepass op, nbr_traverser t, nbr_lbvh h, float rc, const float box[3], float pad,
+                      int periodic, int rows_sorted, unsigned int cap_max, const unsigned int* map,
+                      unsigned int block_size, void* stream, unsigned long long* slots,
+                      unsigned int* overflow_rows, unsigned long long* overflow_slots);
+/* The list of the last build: entries, row offsets (uint64[N]), capacities, counts, total slots. */
+int nbr_onepass_get(nbr_onepass op, const unsigned int** list, const unsigned long long** offsets,
+                    const unsigned int** caps, const unsigned int** nneigh, unsigned long long* total);
+/* Exclusive scan of n counts into uint64 offsets; *total = their sum (synchronises). */
+int nbr_onepass_scan(nbr_onepass op, const unsigned int* counts, unsigned int n,
+                     unsigned long long* offsets, unsigned long long* total, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

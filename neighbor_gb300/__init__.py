@@ -103,6 +103,27 @@ def _declare(L):
     sig("nbr_exact_pad", [_F, _F], _F)
     sig("nbr_debug_wait_timeout", [ctypes.POINTER(_U), _P])
     sig("nbr_morton_sort_noalloc", [_P, _U, _P, _P, _P, _P, _P])
+    _ULL = ctypes.c_ulonglong
+    sig("nbr_traverse_self_csr", [_P, _P, _F, _P, _F, _P, _U, _P, _P, _P, _P, _P, _U, _I, _U, _P])
+    sig("nbr_capmodel_create", [_PP, _ULL])
+    sig("nbr_capmodel_destroy", [_P])
+    sig("nbr_capmodel_get_params", [_P, _P])
+    sig("nbr_capmodel_set_params", [_P, _P])
+    sig("nbr_capmodel_set_margin", [_P, _F])
+    sig("nbr_capmodel_get_margin", [_P, ctypes.POINTER(_F)])
+    sig("nbr_capmodel_level", [_F, _P, _P, ctypes.POINTER(_U)])
+    sig("nbr_capmodel_features", [_P, _P, _P, _P, _F, _I, _P, _P])
+    sig("nbr_capmodel_predict", [_P, _P, _P, _P, _F, _I, _I, _U, _P, _P, _P])
+    sig("nbr_capmodel_targets", [_P, _U, _P, _P])
+    sig("nbr_capmodel_gradient", [_P, _P, _P, _U, _U, _U, _U, _P, _P, _P])
+    sig("nbr_capmodel_train", [_P, _P, _P, _U, _U, _U, _F, _ULL, ctypes.POINTER(_F), _P])
+    sig("nbr_onepass_create", [_PP])
+    sig("nbr_onepass_destroy", [_P])
+    sig("nbr_onepass_capacity", [_P, _U, _PP])
+    sig("nbr_onepass_build", [_P, _P, _P, _F, _P, _F, _I, _I, _U, _P, _U, _P,
+                              ctypes.POINTER(_ULL), ctypes.POINTER(_U), ctypes.POINTER(_ULL)])
+    sig("nbr_onepass_get", [_P, _PP, _PP, _PP, _PP, ctypes.POINTER(_ULL)])
+    sig("nbr_onepass_scan", [_P, _P, _U, _P, ctypes.POINTER(_ULL), _P])
 
 
 # C-ABI symbols declared in include/neighbor_gb300.h (checked by the CPU tests).
@@ -114,7 +135,16 @@ EXPORTED = ["nbr_last_error", "nbr_version", "nbr_lbvh_create", "nbr_lbvh_destro
             "nbr_traverser_setup", "nbr_traverser_reset", "nbr_traverser_set_fast_path",
             "nbr_traverser_set_mode", "nbr_traverser_set_stats", "nbr_traverser_set_symmetric",
             "nbr_traverser_get_data", "nbr_traverse", "nbr_traverse_self", "nbr_exact_pad",
-            "nbr_debug_wait_timeout", "nbr_morton_sort_noalloc"]
+            "nbr_debug_wait_timeout", "nbr_morton_sort_noalloc", "nbr_traverse_self_csr",
+            "nbr_capmodel_create", "nbr_capmodel_destroy", "nbr_capmodel_get_params",
+            "nbr_capmodel_set_params", "nbr_capmodel_set_margin", "nbr_capmodel_get_margin",
+            "nbr_capmodel_level", "nbr_capmodel_features", "nbr_capmodel_predict",
+            "nbr_capmodel_targets", "nbr_capmodel_gradient", "nbr_capmodel_train",
+            "nbr_onepass_create", "nbr_onepass_destroy", "nbr_onepass_capacity",
+            "nbr_onepass_build", "nbr_onepass_get", "nbr_onepass_scan"]
+
+CAP_PARAMS = 6337
+CAP_FEATURES = 32
 
 NOALLOC_MAX_POINTS = 1 << 20
 
@@ -445,3 +475,176 @@ class LBVHTraverser:
         if max_neigh is None:
             return nneigh
         return nneigh, lst
+
+    def traverse_self_csr(self, lbvh: LBVH, rc: float, box, pad: float, offsets, caps, list_out,
+                          max_capacity: int = 0, images=None, map=None, rows_sorted: bool = True,
+                          nneigh=None, block_size: int = 256, stream=None):
+        """Self traversal into a CSR list: row r at list_out[offsets[r]:offsets[r]+caps[r]].
+        offsets: CUDA int64 tensor, caps: int32, list_out: int32.  Returns the counts."""
+        torch = _torch()
+        _, N, _, _ = lbvh.sizes()
+        lattice = isinstance(images, str) and images == "periodic"
+        img = None if images is None or lattice else _dev(images, torch.float32, 3)
+        m = None if map is None else _dev(map, torch.int32)
+        if nneigh is None:
+            nneigh = torch.empty(N, dtype=torch.int32, device="cuda")
+        _check(self._L.nbr_traverse_self_csr(self._h, lbvh.handle, float(rc), _f3(box), float(pad),
+                                             _ptr(img),
+                                             27 if lattice else (0 if img is None else img.shape[0]),
+                                             _ptr(m), _ptr(nneigh), _ptr(list_out), _ptr(offsets),
+                                             _ptr(caps), int(max_capacity), 1 if rows_sorted else 0,
+                                             block_size, _stream_ptr(stream)))
+        return nneigh
+
+
+class CapacityModel:
+    """Capacity network (32 -> 64 -> 64 -> 1, BF16 weights, FP32 accumulation) on the GPU."""
+
+    def __init__(self, seed: int = 1):
+        self._L = load()
+        h = ctypes.c_void_p()
+        _check(self._L.nbr_capmodel_create(ctypes.byref(h), int(seed)))
+        self._h = h
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            self._L.nbr_capmodel_destroy(self._h)
+            self._h = None
+
+    @property
+    def handle(self):
+        return self._h
+
+    def params(self):
+        import numpy as np
+        out = np.zeros(CAP_PARAMS, np.float32)
+        _check(self._L.nbr_capmodel_get_params(self._h, out.ctypes.data_as(ctypes.c_void_p)))
+        return out
+
+    def set_params(self, params):
+        import numpy as np
+        p = np.ascontiguousarray(params, np.float32)
+        if p.size != CAP_PARAMS:
+            raise ValueError("expected %d parameters" % CAP_PARAMS)
+        _check(self._L.nbr_capmodel_set_params(self._h, p.ctypes.data_as(ctypes.c_void_p)))
+
+    @property
+    def margin(self) -> float:
+        v = ctypes.c_float()
+        _check(self._L.nbr_capmodel_get_margin(self._h, ctypes.byref(v)))
+        return v.value
+
+    @margin.setter
+    def margin(self, value: float):
+        _check(self._L.nbr_capmodel_set_margin(self._h, float(value)))
+
+    @staticmethod
+    def level(rc, lo, hi) -> int:
+        v = ctypes.c_uint()
+        _check(load().nbr_capmodel_level(float(rc), _f3(lo), _f3(hi), ctypes.byref(v)))
+        return v.value
+
+    def features(self, lbvh: "LBVH", lo, hi, rc: float, periodic: bool = True, stream=None):
+        torch = _torch()
+        _, N, _, _ = lbvh.sizes()
+        out = torch.empty((N, CAP_FEATURES), dtype=torch.float32, device="cuda")
+        _check(self._L.nbr_capmodel_features(self._h, lbvh.handle, _f3(lo), _f3(hi), float(rc),
+                                             1 if periodic else 0, _ptr(out), _stream_ptr(stream)))
+        return out
+
+    def predict(self, lbvh: "LBVH", lo, hi, rc: float, periodic: bool = True, rows_sorted: bool = True,
+                cap_max: int = 4096, caps=None, want_y: bool = False, stream=None):
+        torch = _torch()
+        _, N, _, _ = lbvh.sizes()
+        if caps is None:
+            caps = torch.empty(N, dtype=torch.int32, device="cuda")
+        y = torch.empty(N, dtype=torch.float32, device="cuda") if want_y else None
+        _check(self._L.nbr_capmodel_predict(self._h, lbvh.handle, _f3(lo), _f3(hi), float(rc),
+                                            1 if periodic else 0, 1 if rows_sorted else 0, int(cap_max),
+                                            _ptr(caps), _ptr(y), _stream_ptr(stream)))
+        return (caps, y) if want_y else caps
+
+    @staticmethod
+    def targets(counts, stream=None):
+        torch = _torch()
+        c = _dev(counts, torch.int32)
+        out = torch.empty(c.shape[0], dtype=torch.float32, device="cuda")
+        _check(load().nbr_capmodel_targets(_ptr(c), c.shape[0], _ptr(out), _stream_ptr(stream)))
+        return out
+
+    def gradient(self, features, targets, batch: int, offset: int, stride: int, stream=None):
+        torch = _torch()
+        F = _dev(features, torch.float32, CAP_FEATURES)
+        T = _dev(targets, torch.float32)
+        grad = torch.empty(CAP_PARAMS, dtype=torch.float32, device="cuda")
+        loss = torch.empty(1, dtype=torch.float32, device="cuda")
+        _check(self._L.nbr_capmodel_gradient(self._h, _ptr(F), _ptr(T), T.shape[0], int(batch),
+                                             int(offset), int(stride), _ptr(grad), _ptr(loss),
+                                             _stream_ptr(stream)))
+        return grad, loss
+
+    def train(self, features, targets, steps: int, batch: int = 8192, lr: float = 3e-3, seed: int = 1,
+              stream=None) -> float:
+        torch = _torch()
+        F = _dev(features, torch.float32, CAP_FEATURES)
+        T = _dev(targets, torch.float32)
+        loss = ctypes.c_float()
+        _check(self._L.nbr_capmodel_train(self._h, _ptr(F), _ptr(T), T.shape[0], int(steps), int(batch),
+                                          float(lr), int(seed), ctypes.byref(loss), _stream_ptr(stream)))
+        return loss.value
+
+
+class OnePassList:
+    """One-pass self neighbor list in CSR form with per-row capacities."""
+
+    def __init__(self):
+        self._L = load()
+        h = ctypes.c_void_p()
+        _check(self._L.nbr_onepass_create(ctypes.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            self._L.nbr_onepass_destroy(self._h)
+            self._h = None
+
+    def capacity(self, N: int):
+        """The device capacity array of N rows (an int32 CUDA view) to fill before build()."""
+        torch = _torch()
+        p = ctypes.c_void_p()
+        _check(self._L.nbr_onepass_capacity(self._h, int(N), ctypes.byref(p)))
+        return _view(p.value, (N,), "<u4", torch.int32)
+
+    def build(self, trav: "LBVHTraverser", lbvh: "LBVH", rc: float, box, pad: float, periodic: bool = True,
+              rows_sorted: bool = True, cap_max: int = 4096, map=None, block_size: int = 256, stream=None):
+        torch = _torch()
+        m = None if map is None else _dev(map, torch.int32)
+        slots, ovf, ovf_slots = ctypes.c_ulonglong(), ctypes.c_uint(), ctypes.c_ulonglong()
+        _check(self._L.nbr_onepass_build(self._h, trav._h, lbvh.handle, float(rc), _f3(box), float(pad),
+                                         1 if periodic else 0, 1 if rows_sorted else 0, int(cap_max), _ptr(m),
+                                         block_size, _stream_ptr(stream), ctypes.byref(slots),
+                                         ctypes.byref(ovf), ctypes.byref(ovf_slots)))
+        return dict(slots=slots.value, overflow_rows=ovf.value, overflow_slots=ovf_slots.value)
+
+    def result(self, N: int):
+        """Views of (list, offsets, capacities, counts) of the last build."""
+        torch = _torch()
+        lst, off, caps, nn = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
+        total = ctypes.c_ulonglong()
+        _check(self._L.nbr_onepass_get(self._h, ctypes.byref(lst), ctypes.byref(off), ctypes.byref(caps),
+                                       ctypes.byref(nn), ctypes.byref(total)))
+        return dict(list=_view(lst.value, (max(total.value, 1),), "<u4", torch.int32),
+                    offsets=_view(off.value, (N,), "<i8", torch.int64),
+                    caps=_view(caps.value, (N,), "<u4", torch.int32),
+                    nneigh=_view(nn.value, (N,), "<u4", torch.int32),
+                    total=total.value)
+
+    def scan(self, counts, stream=None):
+        """Exclusive scan of int32 counts into int64 offsets; returns (offsets, total)."""
+        torch = _torch()
+        c = _dev(counts, torch.int32)
+        out = torch.empty(c.shape[0], dtype=torch.int64, device="cuda")
+        total = ctypes.c_ulonglong()
+        _check(self._L.nbr_onepass_scan(self._h, _ptr(c), c.shape[0], _ptr(out), ctypes.byref(total),
+                                        _stream_ptr(stream)))
+        return out, total.value

@@ -7,18 +7,7 @@
 
 #include <cuda_runtime.h>
 
-#include "neighbor/neighbor.h"
-#include "neighbor_gb300.h"
-
-struct nbr_lbvh_s
-    {
-    neighbor::LBVH lbvh;
-    };
-
-struct nbr_traverser_s
-    {
-    neighbor::LBVHTraverser trav;
-    };
+#include "capi_internal.h"
 
 namespace
 {
@@ -27,59 +16,16 @@ thread_local std::string g_last_error;
 
 namespace neighbor_capi
 {
-// Used by the other translation units of the library (noalloc.cu).
 void set_last_error(const std::string& msg) { g_last_error = msg; }
 }
 
 namespace
 {
-
-int fail(int code, const std::string& msg)
-    {
-    g_last_error = msg;
-    return code;
-    }
-
-// Map an exception from the C++ layer to a status code.
-int from_exception(const std::exception& e)
-    {
-    const std::string m = e.what();
-    if (m.find("allocating") != std::string::npos) return fail(NBR_ERR_ALLOC, m);
-    if (m.find("bounded device wait") != std::string::npos) return fail(NBR_ERR_DEVICE_WAIT, m);
-    if (m.find("Invalid tuning") != std::string::npos || m.find("maximum of 32") != std::string::npos
-        || m.find("must be") != std::string::npos)
-        return fail(NBR_ERR_INVALID, m);
-    return fail(NBR_ERR_CUDA, m);
-    }
-
-template<class F>
-int guarded(F&& f)
-    {
-    try
-        {
-        f();
-        g_last_error.clear();
-        return NBR_OK;
-        }
-    catch (const std::bad_alloc&)
-        {
-        return fail(NBR_ERR_ALLOC, "host allocation failed");
-        }
-    catch (const std::exception& e)
-        {
-        return from_exception(e);
-        }
-    catch (...)
-        {
-        return fail(NBR_ERR_CUDA, "unknown error");
-        }
-    }
-
-inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
-
-inline float3 f3(const float v[3]) { return make_float3(v[0], v[1], v[2]); }
-
-bool valid_block(unsigned int bs) { return bs >= 32 && bs <= 1024 && bs % 32 == 0; }
+using neighbor_capi::as_stream;
+using neighbor_capi::f3;
+using neighbor_capi::fail;
+using neighbor_capi::guarded;
+using neighbor_capi::valid_block;
 
 template<class OutputOpT, class TransformOpT>
 void dispatch_images(neighbor::LBVHTraverser& t, const neighbor::LBVH& h,

@@ -98,6 +98,9 @@ def _declare(L):
     L.orc_fast_frame.argtypes = [_P, _P, _P]
     L.orc_fast_quantize.argtypes = [_P, _P, _P, _P, _P]
     L.orc_gen_validate_points.argtypes = [_u32, _P, _u32, _P]
+    L.orc_cap_occupancy.argtypes = [_P, _u32, _u32, _P]
+    L.orc_cap_features.argtypes = [_P, _P, _u32, _P, _P, _u32, ctypes.c_int, _P, _P]
+    L.orc_cap_forward_backward.argtypes = [_P, _P, _P, _u32, _u32, _u32, _u32, ctypes.c_int, _P, _P, _P]
 
 
 def _ptr(a):
@@ -257,3 +260,41 @@ def images27(L):
             for iz in (-1, 0, 1):
                 out.append([L[0] * np.float32(ix), L[1] * np.float32(iy), L[2] * np.float32(iz)])
     return np.asarray(out, np.float32)
+
+
+CAP_PARAMS = 6337
+CAP_FEATURES = 32
+
+
+def cap_occupancy(codes, shift):
+    """Points per coarse Morton cell (G^3, G = 1024 >> shift) of the sorted codes."""
+    c = np.ascontiguousarray(codes, np.uint32)
+    G = 1024 >> shift
+    occ = np.zeros(G ** 3, np.uint32)
+    lib().orc_cap_occupancy(_ptr(c), len(c), shift, _ptr(occ))
+    return occ
+
+
+def cap_features(codes, points4, lo, ext, shift, periodic):
+    """The 32 capacity features of every sorted point (points4: float4 payload)."""
+    c = np.ascontiguousarray(codes, np.uint32)
+    p = _f32(points4, (-1, 4))
+    occ = cap_occupancy(c, shift)
+    out = np.zeros((len(c), CAP_FEATURES), np.float32)
+    lib().orc_cap_features(_ptr(c), _ptr(p), len(c), _ptr(_f32(lo)), _ptr(_f32(ext)), shift,
+                           1 if periodic else 0, _ptr(occ), _ptr(out))
+    return out
+
+
+def cap_forward_backward(params, features, targets, batch, offset, stride, mode=1):
+    """Summed gradient, summed loss and outputs of a batch; mode 1 = BF16 rounding as the GPU,
+    0 = FP32 without rounding, -1 = float64 without rounding."""
+    P = _f32(params)
+    F = _f32(features, (-1, CAP_FEATURES))
+    T = _f32(targets)
+    grad = np.zeros(CAP_PARAMS, np.float64)
+    loss = np.zeros(1, np.float64)
+    y = np.zeros(batch, np.float32)
+    lib().orc_cap_forward_backward(_ptr(P), _ptr(F), _ptr(T), len(T), batch, offset, stride, mode,
+                                   _ptr(grad), _ptr(loss), _ptr(y))
+    return grad, float(loss[0]), y

@@ -746,3 +746,164 @@ void orc_gen_validate_points(uint32_t N, const float L[3], uint32_t seed, float*
 
 }  // extern "C"
 
+
+// ---------------------------------------------------------------------------------------------
+// Learned capacity network: features and forward/backward, restating
+// include/neighbor/kernels/capacity.cuh (cap_features, k_cap_train_step) on the CPU.
+// ---------------------------------------------------------------------------------------------
+namespace {
+uint32_t cap_part1by2(uint32_t v) {
+    v &= 0x3ffu;
+    v = (v | (v << 16)) & 0x030000ffu;
+    v = (v | (v << 8)) & 0x0300f00fu;
+    v = (v | (v << 4)) & 0x030c30c3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+}
+uint32_t cap_compact1by2(uint32_t v) {
+    v &= 0x09249249u;
+    v = (v | (v >> 2)) & 0x030c30c3u;
+    v = (v | (v >> 4)) & 0x0300f00fu;
+    v = (v | (v >> 8)) & 0x030000ffu;
+    v = (v | (v >> 16)) & 0x000003ffu;
+    return v;
+}
+// FP32 -> BF16 -> FP32, round to nearest even (finite inputs).
+float bf16_rne(float x) {
+    uint32_t u;
+    std::memcpy(&u, &x, 4);
+    u += 0x7fffu + ((u >> 16) & 1u);
+    u &= 0xffff0000u;
+    float r;
+    std::memcpy(&r, &u, 4);
+    return r;
+}
+constexpr int kIn = 32, kH = 64;
+constexpr int oW1 = 0, oB1 = oW1 + kH * kIn, oW2 = oB1 + kH, oB2 = oW2 + kH * kH, oW3 = oB2 + kH,
+              oB3 = oW3 + kH, kP = oB3 + 1;
+} // namespace
+
+void orc_cap_occupancy(const uint32_t* codes, uint32_t N, uint32_t shift, uint32_t* occ) {
+    const size_t G = 1024u >> shift;
+    std::fill(occ, occ + G * G * G, 0u);
+    for (uint32_t s = 0; s < N; ++s) occ[codes[s] >> (3 * shift)]++;
+}
+
+void orc_cap_features(const uint32_t* codes, const float* points4, uint32_t N, const float lo[3],
+                      const float ext[3], uint32_t shift, int periodic, const uint32_t* occ,
+                      float* out) {
+    const int G = 1024 >> shift;
+    for (uint32_t s = 0; s < N; ++s) {
+        float* f = out + (size_t)s * kIn;
+        const uint32_t c = codes[s] >> (3 * shift);
+        const int cx = (int)cap_compact1by2(c >> 2), cy = (int)cap_compact1by2(c >> 1),
+                  cz = (int)cap_compact1by2(c);
+        float sum = 0.f;
+        for (int k = 0; k < 27; ++k) {
+            int nx = cx + k / 9 - 1, ny = cy + (k / 3) % 3 - 1, nz = cz + k % 3 - 1;
+            uint32_t o = 0;
+            bool inside = true;
+            if (periodic) {
+                nx = (nx + G) % G;
+                ny = (ny + G) % G;
+                nz = (nz + G) % G;
+            } else {
+                inside = nx >= 0 && nx < G && ny >= 0 && ny < G && nz >= 0 && nz < G;
+            }
+            if (inside)
+                o = occ[(cap_part1by2((uint32_t)nx) << 2) | (cap_part1by2((uint32_t)ny) << 1) |
+                        cap_part1by2((uint32_t)nz)];
+            sum += (float)o;
+            f[k] = std::log1p((float)o);
+        }
+        const float inv = 1.0f / (float)(1u << shift);
+        const float* p = points4 + 4 * (size_t)s;
+        const int cc[3] = {cx, cy, cz};
+        for (int d = 0; d < 3; ++d) {
+            const float t = std::fmin(std::fmax(rn_mul(rn_div(rn_sub(p[d], lo[d]), ext[d]), 1023.f), 0.f), 1023.f);
+            f[27 + d] = std::fmin(std::fmax((t - (float)(cc[d] << shift)) * inv, 0.f), 1.f);
+        }
+        f[30] = std::log1p(sum);
+        f[31] = 1.f;
+    }
+}
+
+namespace {
+template<class T>
+T softplus_t(T z) { return std::max(z, (T)0) + std::log1p(std::exp(-std::fabs(z))); }
+template<class T>
+T sigmoid_t(T z) { return (T)1 / ((T)1 + std::exp(-z)); }
+
+// One sample, template over arithmetic; R rounds to BF16 (or not).
+template<class T, class R>
+void cap_sample(const float* P, const float* xf, float target, R round, T* g, T& loss, float& yout) {
+    T x[kIn], h1[kH], h2[kH], d2[kH], d1[kH];
+    T w1[kH * kIn], w2[kH * kH], w3[kH];
+    for (int i = 0; i < kH * kIn; ++i) w1[i] = round(P[oW1 + i]);
+    for (int i = 0; i < kH * kH; ++i) w2[i] = round(P[oW2 + i]);
+    for (int i = 0; i < kH; ++i) w3[i] = round(P[oW3 + i]);
+    for (int k = 0; k < kIn; ++k) x[k] = round(xf[k]);
+    for (int j = 0; j < kH; ++j) {
+        T acc = 0;
+        for (int k = 0; k < kIn; ++k) acc = std::fma(w1[j * kIn + k], x[k], acc);
+        h1[j] = round(std::max(acc + (T)P[oB1 + j], (T)0));
+    }
+    for (int j = 0; j < kH; ++j) {
+        T acc = 0;
+        for (int k = 0; k < kH; ++k) acc = std::fma(w2[j * kH + k], h1[k], acc);
+        h2[j] = round(std::max(acc + (T)P[oB2 + j], (T)0));
+    }
+    T z = 0;
+    for (int k = 0; k < kH; ++k) z = std::fma(w3[k], h2[k], z);
+    z += (T)P[oB3];
+    const T y = softplus_t(z);
+    yout = (float)y;
+    const T dy = y - (T)target;
+    loss += (T)0.5 * dy * dy;
+    const T dz = dy * sigmoid_t(z);
+    for (int j = 0; j < kH; ++j) d2[j] = h2[j] > 0 ? dz * w3[j] : (T)0;
+    for (int k = 0; k < kH; ++k) {
+        T acc = 0;
+        for (int j = 0; j < kH; ++j) acc = std::fma(w2[j * kH + k], d2[j], acc);
+        d1[k] = h1[k] > 0 ? acc : (T)0;
+    }
+    for (int j = 0; j < kH; ++j) {
+        g[oB1 + j] += d1[j];
+        g[oB2 + j] += d2[j];
+        g[oW3 + j] += dz * h2[j];
+        for (int k = 0; k < kIn; ++k) g[oW1 + j * kIn + k] += d1[j] * x[k];
+        for (int k = 0; k < kH; ++k) g[oW2 + j * kH + k] += d2[j] * h1[k];
+    }
+    g[oB3] += dz;
+}
+} // namespace
+
+void orc_cap_forward_backward(const float* params, const float* features, const float* targets,
+                              uint32_t N, uint32_t batch, uint32_t offset, uint32_t stride, int bf16,
+                              double* grad, double* loss, float* y) {
+    std::vector<double> gd(kP, 0.0);
+    double ld = 0.0;
+    std::vector<float> gf(kP, 0.f);
+    float lf = 0.f;
+    for (uint32_t b = 0; b < batch; ++b) {
+        const uint32_t row = (uint32_t)(((uint64_t)offset + (uint64_t)b * stride) % N);
+        float yo = 0.f;
+        if (bf16 < 0) {
+            double l = 0.0;
+            cap_sample<double>(params, features + (size_t)row * kIn, targets[row],
+                               [](double v) { return v; }, gd.data(), l, yo);
+            ld += l;
+        } else if (bf16 > 0) {
+            cap_sample<float>(params, features + (size_t)row * kIn, targets[row],
+                              [](float v) { return bf16_rne(v); }, gf.data(), lf, yo);
+        } else {
+            cap_sample<float>(params, features + (size_t)row * kIn, targets[row],
+                              [](float v) { return v; }, gf.data(), lf, yo);
+        }
+        if (y) y[b] = yo;
+    }
+    for (int i = 0; i < kP; ++i) {
+        if (grad) grad[i] = bf16 < 0 ? gd[i] : (double)gf[i];
+    }
+    if (loss) *loss = bf16 < 0 ? ld : (double)lf;
+}

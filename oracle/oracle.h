@@ -128,7 +128,7 @@ double orc_pair_distance_minus_rc_f64(const float* pi, const float* pj, float rc
  * lo.z|~hi.x<<16, ~hi.y|~hi.z<<16, skip} (~h = 32767-h; 15-bit bins of the root box, outward
  * rounded, in 16-bit fields) covers a subtree of more than leaf_size primitives (followed by its two subtrees) or a
  * bucket of 2..leaf_size primitives (followed by their point records); a point record
- * {x, y, z as float bits, 0x80000000 | primitive id} is one primitive.  Returns the record count;
+ * {x, y, z as float bits, 0x80000000 | sorted position} is one primitive.  Returns the record count;
  * frame: {root_lo[3], scale[3]}. */
 uint32_t orc_fast_nodes(uint32_t N, uint32_t leaf_size, const int32_t* parent,
                         const int32_t* left, const int32_t* right, const uint32_t* primitive,
@@ -143,6 +143,28 @@ void orc_fast_quantize(const float* frame, const float* lo, const float* hi, uin
 
 /* Points of the reference's randomized validation test (test/lbvh_test.cu:401-409). */
 void orc_gen_validate_points(uint32_t N, const float L[3], uint32_t seed, float* out);
+
+/* ---- learned capacity network (this project's addition; test infrastructure only) ----
+ * Coarse Morton cells: bins >> shift per axis, G = 1024 >> shift, cell index = code >> 3*shift.
+ * occ[G^3] = points per cell of the sorted codes. */
+void orc_cap_occupancy(const uint32_t* codes, uint32_t N, uint32_t shift, uint32_t* occ);
+
+/* The 32 features of each sorted point: log1p of the 27 cell occupancies around its own cell
+ * (k = 9(dx+1)+3(dy+1)+(dz+1); wrapped when periodic, 0 outside otherwise), its position in its
+ * cell along x, y, z, log1p of the sum of the 27, and 1.  points: float4 payload (x,y,z,id). */
+void orc_cap_features(const uint32_t* codes, const float* points4, uint32_t N, const float lo[3],
+                      const float ext[3], uint32_t shift, int periodic, const uint32_t* occ,
+                      float* out);
+
+/* Forward and backward of the network for rows (offset + b*stride) mod N, b < batch:
+ * 32 -> 64 ReLU -> 64 ReLU -> 1 softplus; when bf16 != 0 weights, inputs and hidden activations
+ * are rounded to BF16 (round to nearest even) as on the GPU, products accumulated with fmaf in
+ * ascending index order.  grad[6337] = summed dL/dparams, *loss = summed 0.5 (y - t)^2,
+ * y[batch] = outputs (either may be NULL).  Double precision when bf16 < 0 (for finite-difference
+ * checks of the restated backward). */
+void orc_cap_forward_backward(const float* params, const float* features, const float* targets,
+                              uint32_t N, uint32_t batch, uint32_t offset, uint32_t stride, int bf16,
+                              double* grad, double* loss, float* y);
 
 #ifdef __cplusplus
 }

@@ -50,6 +50,10 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-ref-cuda", action="store_true")
+    ap.add_argument("--no-learned", action="store_true")
+    ap.add_argument("--no-clustered", action="store_true")
+    ap.add_argument("--train-steps", type=int, default=400)
+    ap.add_argument("--climb", type=int, default=512)
     return ap.parse_args()
 
 
@@ -206,6 +210,158 @@ def cpu_baseline(n, L, seconds, threads=0):
                       f"{q} of {n} queries, counts only, {dt:.2f} s"}
 
 
+# Row capacities of the one-pass lists: at most 32 on uniform input (rows that need more overflow
+# and are re-run; the symmetric fill orders rows of up to 32), unbounded in practice on clustered
+# input (the fill then takes the whole-tree walk).
+UNIFORM_CAP_MAX = 32
+CLUSTERED_CAP_MAX = 1 << 16
+
+
+def train_capacity_model(nb, lbvh, trav, frames, L, rc, steps, periodic=True, quantile=0.999):
+    """Train the capacity network on exact counts of the given frames (plain method) and set its
+    margin to the quantile of the training residuals.  Returns (model, seconds, final loss)."""
+    import torch
+    t0 = time.perf_counter()
+    model = nb.CapacityModel(seed=7)
+    box = [L, L, L]
+    pad = nb.exact_pad(rc, 2 * L)
+    feats, targs = [], []
+    for p in frames:
+        lbvh.build(p, [0, 0, 0], box)
+        cnt = trav.traverse_self(lbvh, rc, box if periodic else [0, 0, 0], pad,
+                                 images="periodic" if periodic else None, rows_sorted=True)
+        feats.append(model.features(lbvh, [0, 0, 0], box, rc, periodic=periodic))
+        targs.append(nb.CapacityModel.targets(cnt))
+    F = torch.cat(feats)
+    T = torch.cat(targs)
+    loss = model.train(F, T, steps=steps, batch=16384, lr=3e-3, seed=3)
+    resid = []
+    for p, t in zip(frames, targs):
+        lbvh.build(p, [0, 0, 0], box)
+        _, y = model.predict(lbvh, [0, 0, 0], box, rc, periodic=periodic, want_y=True)
+        resid.append(t - y)
+    r, _ = torch.sort(torch.cat(resid))
+    model.margin = float(r[min(len(r) - 1, int(quantile * len(r)))].item())
+    torch.cuda.synchronize()
+    return model, time.perf_counter() - t0, loss
+
+
+def time_steps(fn, frames, warmup, stream):
+    """CUDA-event time per step of fn over frames[warmup:], after fn on frames[:warmup]."""
+    import torch
+    for p in frames[:warmup]:
+        fn(p)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    outs = [fn(p) for p in frames[warmup:]]
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / max(1, len(frames) - warmup), outs
+
+
+def learned_uniform(nb, n, L, frames, warmup, plain_ms, pairs_step, args, stream):
+    """The learned one-pass form of the same trajectory step: build, capacity prediction,
+    one traversal into a CSR list, exact re-run of the rows that overflowed."""
+    import torch
+    box = [L, L, L]
+    pad = nb.exact_pad(RC, 2 * L)
+    lbvh = nb.LBVH(leaf_size=args.leaf, radix_bits=args.radix_bits, climb_block=args.climb)
+    trav = nb.LBVHTraverser()
+    train = make_frames(n, L, 1, seed=4242)
+    model, train_s, loss = train_capacity_model(nb, lbvh, trav, train, L, RC, args.train_steps)
+    del train
+    op = nb.OnePassList()
+    caps = op.capacity(n)
+
+    def step(p):
+        lbvh.build(p, [0, 0, 0], box, block_size=args.block)
+        model.predict(lbvh, [0, 0, 0], box, RC, caps=caps, cap_max=UNIFORM_CAP_MAX)
+        return op.build(trav, lbvh, RC, box, pad, cap_max=UNIFORM_CAP_MAX, block_size=args.block)
+
+    ms, stats = time_steps(step, frames, warmup, stream)
+    # exactness of the last frame: counts equal to the plain count pass
+    res = op.result(n)
+    cnt = trav.traverse_self(lbvh, RC, box, pad, images="periodic", rows_sorted=True)
+    exact = bool(torch.equal(res["nneigh"].view(torch.int32), cnt))
+    ovf = [s["overflow_rows"] for s in stats]
+    return {"ms_per_step": ms, "value": pairs_step / (ms * 1e-3), "unit": "pairs/s",
+            "vs_plain": plain_ms / ms, "slots_per_point": stats[-1]["slots"] / n,
+            "overflow_rows_mean": sum(ovf) / len(ovf), "counts_equal_plain": exact,
+            "margin": model.margin, "cap_max": UNIFORM_CAP_MAX, "train_s": round(train_s, 2),
+            "train_loss": loss, "train_frames": "1 frame, seed distinct from the timed frames"}
+
+
+def clustered_c3(nb, args, stream, n=4_000_000, rc=1.0, steps=5, warmup=2):
+    """Clustered input: 70% of the points in 2,000 Gaussian blobs (sigma log-uniform in [0.5, 3]),
+    30% uniform, mean density 0.85, cutoff 1.0.  Plain count + scan + exact CSR fill against the
+    learned one-pass CSR fill (model trained on frames of other seeds)."""
+    import numpy as np
+    import torch
+    L = (n / DENSITY) ** (1.0 / 3.0)
+    box = [L, L, L]
+    pad = nb.exact_pad(rc, 2 * L)
+
+    def frame(seed):
+        rng = np.random.default_rng(seed)
+        centers = rng.random((2000, 3)) * L
+        sig = np.exp(rng.uniform(np.log(0.5), np.log(3.0), 2000))
+        nb_ = n * 7 // 10
+        k = rng.integers(0, 2000, nb_)
+        p = np.empty((n, 3))
+        p[:nb_] = centers[k] + rng.normal(size=(nb_, 3)) * sig[k, None]
+        p[nb_:] = rng.random((n - nb_, 3)) * L
+        return torch.tensor(np.mod(p, L).astype(np.float32), device="cuda")
+
+    lbvh = nb.LBVH(leaf_size=args.leaf, radix_bits=args.radix_bits, climb_block=args.climb)
+    trav = nb.LBVHTraverser()
+    model, train_s, loss = train_capacity_model(nb, lbvh, trav, [frame(500), frame(501)], L, rc,
+                                                args.train_steps)
+    frames = [frame(600 + k) for k in range(warmup + steps)]
+    op_plain = nb.OnePassList()
+    counts = torch.empty(n, dtype=torch.int32, device="cuda")
+    rows = torch.empty(n, dtype=torch.int32, device="cuda")
+    store = {}
+
+    def plain(p):
+        lbvh.build(p, [0, 0, 0], box, block_size=args.block)
+        trav.traverse_self(lbvh, rc, box, pad, images="periodic", nneigh=counts, rows_sorted=True,
+                           block_size=args.block)
+        mx = int(counts.max().item())
+        offsets, total = op_plain.scan(counts)
+        if store.get("cap", 0) < total:
+            store["list"] = torch.empty(total + 1, dtype=torch.int32, device="cuda")
+            store["cap"] = total
+        trav.traverse_self_csr(lbvh, rc, box, pad, offsets, counts, store["list"], max_capacity=mx,
+                               images="periodic", nneigh=rows, block_size=args.block)
+        return total
+
+    op = nb.OnePassList()
+    caps = op.capacity(n)
+
+    def learned(p):
+        lbvh.build(p, [0, 0, 0], box, block_size=args.block)
+        model.predict(lbvh, [0, 0, 0], box, rc, caps=caps, cap_max=CLUSTERED_CAP_MAX)
+        return op.build(trav, lbvh, rc, box, pad, cap_max=CLUSTERED_CAP_MAX, block_size=args.block)
+
+    ms_plain, totals = time_steps(plain, frames, warmup, stream)
+    ms_learned, stats = time_steps(learned, frames, warmup, stream)
+    cnt = counts.clone()
+    exact = bool(torch.equal(op.result(n)["nneigh"].view(torch.int32), cnt))
+    pairs = float(sum(totals)) / len(totals)
+    return {"workload": f"clustered N={n} (70% in 2000 blobs, sigma log-U[0.5,3]) density 0.85 "
+                        f"L={L:.2f} rc={rc}, 27 images",
+            "plain_ms_per_step": ms_plain, "learned_ms_per_step": ms_learned,
+            "plain_value": pairs / (ms_plain * 1e-3), "learned_value": pairs / (ms_learned * 1e-3),
+            "unit": "pairs/s", "learned_vs_plain": ms_plain / ms_learned,
+            "pairs_per_step": pairs, "max_count": int(cnt.max().item()),
+            "learned_slots_per_point": stats[-1]["slots"] / n,
+            "overflow_rows_mean": sum(s["overflow_rows"] for s in stats) / len(stats),
+            "counts_equal_plain": exact, "margin": model.margin, "train_s": round(train_s, 2),
+            "train_loss": loss, "plain": "count + exclusive scan + exact CSR fill",
+            "learned": "capacity network + one CSR fill + exact re-run of overflowed rows"}
+
+
 def reference_cuda(n, our_ms):
     """The reference's own CUDA kernels on the same GPU and workload (oracle/ref_harness): the
     plain two-pass step (build, setup, count, max, fill) with the best block size of 32..512."""
@@ -275,7 +431,7 @@ def run_ours(args):
     frames = make_frames(n, L, args.warmup + args.steps, seed=1000 + rank)
     imgs = "periodic"
     pad = nb.exact_pad(RC, 2 * L)
-    lbvh = nb.LBVH(leaf_size=args.leaf, radix_bits=args.radix_bits)
+    lbvh = nb.LBVH(leaf_size=args.leaf, radix_bits=args.radix_bits, climb_block=args.climb)
     trav = nb.LBVHTraverser()
     trav.set_mode(args.mode)
     counts = torch.empty(n, dtype=torch.int32, device="cuda")
@@ -434,6 +590,11 @@ def run_ours(args):
         "e2e": e2e,
         "check_vs_oracle": check,
     }
+    if not args.no_learned:
+        line["learned"] = learned_uniform(nb, n, L, frames, args.warmup, line["ms_per_step"], pairs_step,
+                                          args, stream)
+    if not args.no_clustered:
+        line["clustered_4m"] = clustered_c3(nb, args, stream)
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(n, L, args.cpu_seconds, os.cpu_count() or 1)
     if not args.no_ref_cuda:

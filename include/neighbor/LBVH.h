@@ -67,7 +67,7 @@ class LBVH : public Tunable<unsigned int>
         LBVH()
             : Tunable<unsigned int>(32, 1024, 32), m_root(LBVHSentinel), m_N(0), m_N_internal(0),
               m_N_nodes(0), m_capacity(0), m_leaf_size(4), m_radix_bits(8), m_fast_points(false),
-              m_epoch(0), m_block(256), m_stream(0), m_ref_valid(true)
+              m_epoch(0), m_block(256), m_climb_block(512), m_stream(0), m_ref_valid(true)
             {}
 
         template<class InsertOpT>
@@ -155,6 +155,15 @@ class LBVH : public Tunable<unsigned int>
             }
         unsigned int getRadixBits() const { return m_radix_bits; }
 
+        // Sorted leaves per block of the agglomerative climb: 128, 256 or 512.
+        void setClimbBlock(unsigned int leaves)
+            {
+            if (leaves != 128 && leaves != 256 && leaves != 512)
+                throw std::runtime_error("Climb block must be 128, 256 or 512.");
+            m_climb_block = leaves;
+            }
+        unsigned int getClimbBlock() const { return m_climb_block; }
+
         // True when the last build used a point insert op, so fastData() holds point positions.
         bool hasFastData() const { return m_fast_points && m_N > 0; }
 
@@ -212,7 +221,6 @@ class LBVH : public Tunable<unsigned int>
         static constexpr size_t kSmallLiveCount = 8208;    // 1 word
         static constexpr size_t kSmallFrame = 8212;        // QuantFrame (9 floats), 16-byte aligned
         static constexpr size_t kSmallWords = 8224;
-        static constexpr int kClimbBlock = 512;        // sorted leaves per block of the climb
 
         int m_root;
         unsigned int m_N;
@@ -224,6 +232,7 @@ class LBVH : public Tunable<unsigned int>
         bool m_fast_points;
         unsigned int m_epoch;
         unsigned int m_block;
+        unsigned int m_climb_block;
         cudaStream_t m_stream;
         mutable bool m_ref_valid;  // reference-layout arrays match the last build
 
@@ -333,7 +342,7 @@ inline void LBVH::allocate(unsigned int N)
     m_nmeta.reserve(N);
     m_kids.reserve(2 * (size_t)N);
     // at most one pending node per split of a block plus two per block edge
-    m_items.reserve((size_t)N + 2 * (size_t)detail::ceil_div(N, kClimbBlock) + 16);
+    m_items.reserve((size_t)N + 2 * (size_t)detail::ceil_div(N, 128) + 16);
     m_live.reserve((size_t)N + 1 + gpu::kScanTile);
     if (m_locks.size() < N)
         {
@@ -491,8 +500,14 @@ void LBVH::build(const LaunchParameters& params, const InsertOpT& insert, const 
     c.frame_out = reinterpret_cast<QuantFrame*>(small + kSmallFrame);
     c.leaf_size = m_leaf_size;
     c.error = small + kSmallStatus;
-    gpu::k_climb<InsertOpT, kClimbBlock><<<detail::ceil_div(N, kClimbBlock), kClimbBlock, 0, stream>>>(insert, c);
-    if (N > (unsigned int)kClimbBlock)
+    const unsigned int T = m_climb_block;
+    if (T == 128)
+        gpu::k_climb<InsertOpT, 128><<<detail::ceil_div(N, 128), 128, 0, stream>>>(insert, c);
+    else if (T == 256)
+        gpu::k_climb<InsertOpT, 256><<<detail::ceil_div(N, 256), 256, 0, stream>>>(insert, c);
+    else
+        gpu::k_climb<InsertOpT, 512><<<detail::ceil_div(N, 512), 512, 0, stream>>>(insert, c);
+    if (N > T)
         gpu::k_climb_global<InsertOpT><<<std::min(detail::ceil_div(N, 2048), 152u * 8u), 256, 0, stream>>>(insert, c);
 
     // pre-order positions of the box records

@@ -186,8 +186,6 @@ class LBVHTraverser : public Tunable<unsigned int>
         unsigned long long* m_stats;
         bool m_symmetric;
         device_array<unsigned int> m_own;
-        device_array<unsigned int> m_long_rows;
-        device_array<unsigned int> m_n_long;
 
         template<class TransformOpT>
         void compress(const LaunchParameters& params, const LBVH& lbvh, const TransformOpT& transform)
@@ -357,10 +355,13 @@ void LBVHTraverser::traverseSelf(const LaunchParameters& params, const LBVH& lbv
     a.pad = pad;
     detail::set_output(a, out);
     const unsigned int longest = detail::max_row(out);
+    // Counts always take the symmetric kernel; fills only while every row fits the one-thread
+    // ordering (longer rows cost more to order than the whole-tree walk costs, and that walk
+    // writes every row already in order).
     if (detail::is_symmetric_images<TranslateOpT>::value && m_symmetric && m_mode == kThreadTraversal
         && !m_stats && lbvh.getN() < gpu::kHalfMaxN
         && (output_kind<OutputOpT>::value == gpu::kFastCount
-            || (longest > 0u && longest <= gpu::kHalfRowMax)
+            || (longest > 0u && longest <= gpu::kHalfRowThread)
             || (output_kind<OutputOpT>::value == gpu::kFastList && longest == 0u)))
         launch_half(params, lbvh, a, out, transform);
     else
@@ -421,8 +422,6 @@ void LBVHTraverser::launch_half(const LaunchParameters& params, const LBVH& lbvh
     if (kind != gpu::kFastCount)
         {
         m_own.reserve(N);
-        m_long_rows.reserve(N);
-        m_n_long.reserve(1);
         h.own = m_own.get();
         }
     detail::check_cuda(cudaMemsetAsync(a.nneigh, 0, (size_t)N * sizeof(unsigned int), stream), "memset");
@@ -438,12 +437,8 @@ void LBVHTraverser::launch_half(const LaunchParameters& params, const LBVH& lbvh
         o.caps = a.caps;
         o.own = m_own.get();
         o.primitive = lbvh.fastData().primitive;
-        o.long_rows = m_long_rows.get();
-        o.n_long = m_n_long.get();
         o.status = lbvh.getStatusPointer();
-        detail::check_cuda(cudaMemsetAsync(o.n_long, 0, sizeof(unsigned int), stream), "memset");
         gpu::k_half_order_rows<TransformOpT><<<detail::ceil_div(N, 256), 256, 0, stream>>>(o, transform);
-        gpu::k_half_order_long<TransformOpT><<<152u * 4u, 256, 0, stream>>>(o, transform);
         }
     detail::check_cuda(cudaGetLastError(), "half traversal launch");
     }

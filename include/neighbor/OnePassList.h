@@ -83,8 +83,10 @@ class OnePassNeighborList
             return m_caps.get();
             }
 
-        // Exclusive scan of n 32-bit values into 64-bit offsets; returns the total (synchronises).
-        unsigned long long scan(const unsigned int* in, unsigned int n, unsigned long long* out, cudaStream_t stream)
+        // Exclusive scan of n 32-bit values into 64-bit offsets; returns the total (synchronises)
+        // unless read_total is false (the total then stays on the device).
+        unsigned long long scan(const unsigned int* in, unsigned int n, unsigned long long* out, cudaStream_t stream,
+                                bool read_total = true)
             {
             const unsigned int tiles = detail::ceil_div(n, gpu::kScan64Tile);
             m_tiles.reserve((size_t)tiles + 1);
@@ -92,6 +94,7 @@ class OnePassNeighborList
             gpu::k_scan64_sums<<<1, 1024, 0, stream>>>(m_tiles.get(), tiles, m_tiles.get() + tiles);
             gpu::k_scan64_apply<<<tiles, gpu::kScan64Block, 0, stream>>>(in, n, m_tiles.get(), out);
             detail::check_cuda(cudaGetLastError(), "scan launch");
+            if (!read_total) return 0ull;
             unsigned long long total = 0;
             detail::check_cuda(cudaMemcpyAsync(&total, m_tiles.get() + tiles, sizeof(total), cudaMemcpyDeviceToHost,
                                                stream), "copy");
@@ -114,8 +117,13 @@ class OnePassNeighborList
             m_caps.reserve(N);
             m_nneigh.reserve(N);
             m_offsets.reserve(N);
-            st.slots = scan(m_caps.get(), N, m_offsets.get(), stream);
-            m_list.grow(st.slots + 1, 0, stream);
+            // With small capacities the list is sized N * cap_max up front and the total stays on the
+            // device until the overflow check (no wait for the GPU before the traversal).
+            const unsigned long long bound = (unsigned long long)N * cap_max;
+            const bool presized = bound <= kPresizeSlots;
+            if (presized) m_list.grow(bound + 1, 0, stream);
+            st.slots = scan(m_caps.get(), N, m_offsets.get(), stream, !presized);
+            if (!presized) m_list.grow(st.slots + 1, 0, stream);
             const CSRNeighborListOp out(m_list.get(), m_nneigh.get(), m_offsets.get(), m_caps.get(), cap_max);
             if (periodic)
                 trav.traverseSelf(params, lbvh, rc, box, pad, out, PeriodicImagesOp(box), transform, rows_sorted);
@@ -138,6 +146,13 @@ class OnePassNeighborList
                                "copy");
             detail::check_cuda(cudaStreamSynchronize(stream), "sync");
             st.overflow_rows = n_ovf;
+            if (presized)
+                {
+                // the stream is idle here (synchronised above)
+                const unsigned int tiles = detail::ceil_div(N, gpu::kScan64Tile);
+                detail::check_cuda(cudaMemcpy(&st.slots, m_tiles.get() + tiles, sizeof(st.slots),
+                                              cudaMemcpyDeviceToHost), "copy");
+                }
             m_total = st.slots;
             if (n_ovf)
                 {
@@ -166,6 +181,7 @@ class OnePassNeighborList
         unsigned long long totalSlots() const { return m_total; }
 
     private:
+        static constexpr unsigned long long kPresizeSlots = 1ull << 29;  // 2 GB of entries
         unsigned int m_N;
         unsigned long long m_total;
         device_array<unsigned int> m_caps;

@@ -11,15 +11,18 @@
 //   27..29 position inside its own cell along x, y, z, in [0, 1]
 //   30     log1p(sum of the 27 occupancies)
 //   31     1
-// Network: 32 -> 64 (ReLU) -> 64 (ReLU) -> 1 (softplus), weights in BF16, inputs and hidden
-// activations rounded to BF16, every product accumulated in FP32, biases FP32.  The output
+// Network: 32 -> 64 (ReLU) -> 64 (ReLU) -> 1 (softplus), weights in BF16, inputs and first
+// hidden activations rounded to BF16 (the operands of the two tensor-core layers), the second
+// hidden layer kept in FP32 for the output dot product, every product accumulated in FP32,
+// biases FP32.  The output
 // approximates log1p(count); capacity = ceil(expm1(y + margin)), clamped to [1, cap_max].
 //
 //   k_cap_occupancy      occupancy grid from the sorted Morton codes (warp-aggregated atomics)
 //   k_cap_features       the 32 features of every sorted point (training data, tests)
-//   k_cap_infer          features + network + capacity fused, one warp per 32 queries; the three
-//                        layers are BF16 mma.sync m16n8k16 tiles with FP32 accumulators, and a
-//                        layer's accumulator fragments are the next layer's A fragments
+//   k_cap_infer          features + network + capacity fused, one warp per 32 queries; the two
+//                        hidden layers are BF16 mma.sync m16n8k16 tiles with FP32 accumulators (a
+//                        layer's accumulator fragments are the next layer's A fragments) and the
+//                        output layer is folded into the second layer's accumulators
 //   k_cap_train_step     forward + backward of a mini-batch on CUDA cores (one thread per sample,
 //                        block tiles in shared memory), gradients summed in FP32
 //   k_cap_adam           Adam update of the FP32 master weights and their BF16 copies
@@ -82,9 +85,69 @@ __global__ void __launch_bounds__(256) k_cap_occupancy(const unsigned int* __res
     if (valid && (threadIdx.x & 31u) == 31u - __clz(peers)) atomicAdd(occ + c, __popc(peers));
     }
 
-// Features of sorted point s (see the file comment).
+// log1pf of small occupancies, shared by a block (the same values log1pf gives).
+constexpr int kCapLogTable = 256;
+__device__ __forceinline__ void cap_fill_log_table(float* table)
+    {
+    for (int i = threadIdx.x; i < kCapLogTable; i += blockDim.x) table[i] = log1pf((float)i);
+    }
+__device__ __forceinline__ float cap_log1p(const float* table, unsigned int o)
+    {
+    return o < (unsigned int)kCapLogTable ? table[o] : log1pf((float)o);
+    }
+
+// Spread Morton bits of the three cells c-1, c, c+1 of one axis (wrapped around the grid when
+// periodic; a cell outside an open grid gets valid = 0).
+__device__ __forceinline__ void cap_axis(int c, int G, int periodic, unsigned int (&part)[3], unsigned int (&valid)[3])
+    {
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+        {
+        int n = c + d - 1;
+        bool ok = true;
+        if (periodic)
+            {
+            if (n < 0) n += G;
+            if (n >= G) n -= G;
+            }
+        else
+            {
+            ok = n >= 0 && n < G;
+            }
+        part[d] = ok ? part1by2((unsigned int)n) : 0u;
+        valid[d] = ok ? 1u : 0u;
+        }
+    }
+
+// Occupancy of neighbor cell k = 9(dx+1) + 3(dy+1) + (dz+1).
+__device__ __forceinline__ unsigned int cap_occ(const unsigned int* __restrict__ occ, int k,
+                                                const unsigned int (&px)[3], const unsigned int (&vx)[3],
+                                                const unsigned int (&py)[3], const unsigned int (&vy)[3],
+                                                const unsigned int (&pz)[3], const unsigned int (&vz)[3])
+    {
+    const int a = k / 9, b = (k / 3) % 3, c = k % 3;
+    return (vx[a] & vy[b] & vz[c]) ? __ldg(occ + ((px[a] << 2) | (py[b] << 1) | pz[c])) : 0u;
+    }
+
+// Position of a point inside its coarse cell along the three axes (features 27..29).
+__device__ __forceinline__ void cap_frac(const CapFrame& fr, const float3& p, int cx, int cy, int cz, float* f)
+    {
+    const unsigned int sh = fr.shift;
+    const float inv = 1.0f / (float)(1u << sh);
+    const float tx = fminf(fmaxf(__fmul_rn(__fdiv_rn(__fsub_rn(p.x, fr.lo.x), fr.ext.x), 1023.f), 0.f), 1023.f);
+    const float ty = fminf(fmaxf(__fmul_rn(__fdiv_rn(__fsub_rn(p.y, fr.lo.y), fr.ext.y), 1023.f), 0.f), 1023.f);
+    const float tz = fminf(fmaxf(__fmul_rn(__fdiv_rn(__fsub_rn(p.z, fr.lo.z), fr.ext.z), 1023.f), 0.f), 1023.f);
+    f[0] = fminf(fmaxf((tx - (float)(cx << sh)) * inv, 0.f), 1.f);
+    f[1] = fminf(fmaxf((ty - (float)(cy << sh)) * inv, 0.f), 1.f);
+    f[2] = fminf(fmaxf((tz - (float)(cz << sh)) * inv, 0.f), 1.f);
+    }
+
+// Features of sorted point s (see the file comment); `table` is a block's log1p table.  emit(k, v)
+// receives feature k.
+template<class EmitF>
 __device__ __forceinline__ void cap_features(const CapFrame& fr, unsigned int code, const float3& p,
-                                             const unsigned int* __restrict__ occ, float* f)
+                                             const unsigned int* __restrict__ occ, const float* table,
+                                             const EmitF& emit)
     {
     const unsigned int sh = fr.shift;
     const int G = 1024 >> sh;
@@ -92,51 +155,39 @@ __device__ __forceinline__ void cap_features(const CapFrame& fr, unsigned int co
     const int cx = (int)compact1by2(c >> 2);
     const int cy = (int)compact1by2(c >> 1);
     const int cz = (int)compact1by2(c);
-    float sum = 0.f;
+    unsigned int px[3], py[3], pz[3], vx[3], vy[3], vz[3];
+    cap_axis(cx, G, fr.periodic, px, vx);
+    cap_axis(cy, G, fr.periodic, py, vy);
+    cap_axis(cz, G, fr.periodic, pz, vz);
+    unsigned int sum = 0u;
 #pragma unroll
     for (int k = 0; k < 27; ++k)
         {
-        int nx = cx + k / 9 - 1;
-        int ny = cy + (k / 3) % 3 - 1;
-        int nz = cz + k % 3 - 1;
-        unsigned int o = 0u;
-        bool inside = true;
-        if (fr.periodic)
-            {
-            nx = (nx + G) % G;
-            ny = (ny + G) % G;
-            nz = (nz + G) % G;
-            }
-        else
-            {
-            inside = nx >= 0 && nx < G && ny >= 0 && ny < G && nz >= 0 && nz < G;
-            }
-        if (inside)
-            o = __ldg(occ + ((part1by2((unsigned int)nx) << 2) | (part1by2((unsigned int)ny) << 1)
-                             | part1by2((unsigned int)nz)));
-        sum += (float)o;
-        f[k] = log1pf((float)o);
+        const unsigned int o = cap_occ(occ, k, px, vx, py, vy, pz, vz);
+        sum += o;
+        emit(k, cap_log1p(table, o));
         }
-    const float inv = 1.0f / (float)(1u << sh);
-    const float tx = fminf(fmaxf(__fmul_rn(__fdiv_rn(__fsub_rn(p.x, fr.lo.x), fr.ext.x), 1023.f), 0.f), 1023.f);
-    const float ty = fminf(fmaxf(__fmul_rn(__fdiv_rn(__fsub_rn(p.y, fr.lo.y), fr.ext.y), 1023.f), 0.f), 1023.f);
-    const float tz = fminf(fmaxf(__fmul_rn(__fdiv_rn(__fsub_rn(p.z, fr.lo.z), fr.ext.z), 1023.f), 0.f), 1023.f);
-    f[27] = fminf(fmaxf((tx - (float)(cx << sh)) * inv, 0.f), 1.f);
-    f[28] = fminf(fmaxf((ty - (float)(cy << sh)) * inv, 0.f), 1.f);
-    f[29] = fminf(fmaxf((tz - (float)(cz << sh)) * inv, 0.f), 1.f);
-    f[30] = log1pf(sum);
-    f[31] = 1.f;
+    float fr3[3];
+    cap_frac(fr, p, cx, cy, cz, fr3);
+    emit(27, fr3[0]);
+    emit(28, fr3[1]);
+    emit(29, fr3[2]);
+    emit(30, log1pf((float)sum));
+    emit(31, 1.f);
     }
 
 __global__ void __launch_bounds__(256) k_cap_features(const CapFrame fr, const unsigned int* __restrict__ codes,
                                                       const float4* __restrict__ points, unsigned int N,
                                                       const unsigned int* __restrict__ occ, float* __restrict__ out)
     {
+    __shared__ float s_log[kCapLogTable];
+    cap_fill_log_table(s_log);
+    __syncthreads();
     const unsigned int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= N) return;
     const float4 p = points[s];
     float f[kCapIn];
-    cap_features(fr, codes[s], make_float3(p.x, p.y, p.z), occ, f);
+    cap_features(fr, codes[s], make_float3(p.x, p.y, p.z), occ, s_log, [&f](int k, float v) { f[k] = v; });
     float4* o = reinterpret_cast<float4*>(out + (size_t)s * kCapIn);
 #pragma unroll
     for (int k = 0; k < kCapIn / 4; ++k) o[k] = make_float4(f[4 * k], f[4 * k + 1], f[4 * k + 2], f[4 * k + 3]);
@@ -156,11 +207,12 @@ __device__ __forceinline__ unsigned int cap_from_output(float y, float margin, u
 
 // ---------------------------------------------------------------------------------------------
 // Inference: features, network and capacity fused.  A warp takes 32 consecutive queries (two
-// m16 tiles): each lane computes one query's features into shared memory (BF16), then the warp
-// runs  H1 = relu(X W1^T + b1), H2 = relu(H1 W2^T + b2), z = H2 W3^T + b3  as mma.sync
-// m16n8k16 BF16 tiles with FP32 accumulators.  The accumulator fragment of N-tiles 2t and 2t+1
-// is exactly the A fragment of K-tile t of the next layer (rows: groupID, groupID + 8; columns:
-// 2*tig + {0,1} (+8)), so activations never leave registers between layers.
+// m16 tiles): each lane writes one query's features to shared memory (BF16), then the warp runs
+// H1 = relu(X W1^T + b1) and H2 = relu(H1 W2^T + b2) as mma.sync m16n8k16 BF16 tiles with FP32
+// accumulators.  The accumulator fragment of N-tiles 2t and 2t+1 is exactly the A fragment of
+// K-tile t of the next layer (rows: groupID, groupID + 8; columns: 2*tig + {0,1} (+8)), so H1
+// never leaves registers; each H2 fragment is multiplied into the output weights at once, and the
+// four lanes of a group add their columns with two shuffles.
 // ---------------------------------------------------------------------------------------------
 struct CapInferArgs
     {
@@ -194,25 +246,43 @@ __device__ __forceinline__ void mma_bf16_16816(float (&d)[4], const unsigned int
     }
 
 constexpr int kCapInferWarps = 8;
+// Row stride (32-bit words) of a warp's feature tile: 16 words of BF16 pairs + 4 of padding, so
+// the A-fragment reads (rows groupID, columns tig) of a warp fall in 32 distinct banks.
+constexpr int kCapXStride = 20;
+// Weights in shared memory in fragment order: for output row n, k-tile kt and thread-in-group t
+// the two words of the B fragment (B[2t..2t+1][n], B[8+2t..8+2t+1][n]) are one 64-bit word at
+// (kt * 4 + t) * kCapWStride + n; the stride of 72 spreads a warp's words over all bank pairs.
+constexpr int kCapWStride = 72;
 
-__global__ void __launch_bounds__(kCapInferWarps * 32) k_cap_infer(const CapInferArgs a)
+__global__ void __launch_bounds__(kCapInferWarps * 32, 4) k_cap_infer(const CapInferArgs a)
     {
-    // weights as 32-bit pairs of BF16: W1 [64][16], W2 [64][32], W3 [8][32] (rows 1..7 zero)
-    __shared__ unsigned int s_w1[kCapHidden * kCapIn / 2];
-    __shared__ unsigned int s_w2[kCapHidden * kCapHidden / 2];
-    __shared__ unsigned int s_w3[8 * kCapHidden / 2];
+    __shared__ uint2 s_w1[2 * 4 * kCapWStride];   // 2 k-tiles x 4 x 64 rows (+pad)
+    __shared__ uint2 s_w2[4 * 4 * kCapWStride];   // 4 k-tiles x 4 x 64 rows (+pad)
+    __shared__ float s_w3[kCapHidden];
     __shared__ float s_b1[kCapHidden];
     __shared__ float s_b2[kCapHidden];
-    __shared__ unsigned int s_x[kCapInferWarps][32 * (kCapIn / 2 + 1)];  // per warp: 32 queries x 16 pairs (+1 pad)
+    __shared__ float s_log[kCapLogTable];
+    __shared__ unsigned int s_x[kCapInferWarps][32 * kCapXStride];
     const unsigned int* wsrc = reinterpret_cast<const unsigned int*>(a.w);
-    for (int i = threadIdx.x; i < kCapHidden * kCapIn / 2; i += blockDim.x) s_w1[i] = wsrc[kCapBfW1 / 2 + i];
-    for (int i = threadIdx.x; i < kCapHidden * kCapHidden / 2; i += blockDim.x) s_w2[i] = wsrc[kCapBfW2 / 2 + i];
-    for (int i = threadIdx.x; i < 8 * kCapHidden / 2; i += blockDim.x) s_w3[i] = i < kCapHidden / 2 ? wsrc[kCapBfW3 / 2 + i] : 0u;
+    for (int i = threadIdx.x; i < kCapHidden * 2 * 4; i += blockDim.x)
+        {
+        const int n = i % kCapHidden, t = (i / kCapHidden) % 4, kt = i / (kCapHidden * 4);
+        s_w1[(kt * 4 + t) * kCapWStride + n] = make_uint2(wsrc[kCapBfW1 / 2 + n * (kCapIn / 2) + kt * 8 + t],
+                                                          wsrc[kCapBfW1 / 2 + n * (kCapIn / 2) + kt * 8 + 4 + t]);
+        }
+    for (int i = threadIdx.x; i < kCapHidden * 4 * 4; i += blockDim.x)
+        {
+        const int n = i % kCapHidden, t = (i / kCapHidden) % 4, kt = i / (kCapHidden * 4);
+        s_w2[(kt * 4 + t) * kCapWStride + n] = make_uint2(wsrc[kCapBfW2 / 2 + n * (kCapHidden / 2) + kt * 8 + t],
+                                                          wsrc[kCapBfW2 / 2 + n * (kCapHidden / 2) + kt * 8 + 4 + t]);
+        }
     for (int i = threadIdx.x; i < kCapHidden; i += blockDim.x)
         {
+        s_w3[i] = __bfloat162float(a.w[kCapBfW3 + i]);
         s_b1[i] = a.p[kCapOffB1 + i];
         s_b2[i] = a.p[kCapOffB2 + i];
         }
+    cap_fill_log_table(s_log);
     __syncthreads();
     const float b3 = a.p[kCapOffB3];
     const unsigned int lane = threadIdx.x & 31u;
@@ -220,116 +290,95 @@ __global__ void __launch_bounds__(kCapInferWarps * 32) k_cap_infer(const CapInfe
     const unsigned int g = lane >> 2;   // groupID
     const unsigned int t = lane & 3u;   // thread in group
     unsigned int* xs = s_x[warp];
-    constexpr int XS = kCapIn / 2 + 1;  // row stride of xs in 32-bit words
+    constexpr int XS = kCapXStride;
     const unsigned int n_tiles = (a.N + 31u) / 32u;
     for (unsigned int tile = blockIdx.x * kCapInferWarps + warp; tile < n_tiles; tile += gridDim.x * kCapInferWarps)
         {
         const unsigned int base = tile * 32u;
-        // features of query base + lane
         {
         const unsigned int s = base + lane;
-        float f[kCapIn];
+        unsigned int* row = xs + lane * XS;
         if (s < a.N)
             {
             const float4 p = a.points[s];
-            cap_features(a.frame, a.codes[s], make_float3(p.x, p.y, p.z), a.occ, f);
+            float prev = 0.f;
+            cap_features(a.frame, a.codes[s], make_float3(p.x, p.y, p.z), a.occ, s_log,
+                         [row, &prev](int k, float v) {
+                             if (k & 1) row[k >> 1] = pack_bf16x2(prev, v);
+                             prev = v;
+                         });
             }
         else
             {
 #pragma unroll
-            for (int k = 0; k < kCapIn; ++k) f[k] = 0.f;
+            for (int k = 0; k < kCapIn / 2; ++k) row[k] = 0u;
             }
-#pragma unroll
-        for (int k = 0; k < kCapIn / 2; ++k) xs[lane * XS + k] = pack_bf16x2(f[2 * k], f[2 * k + 1]);
         }
         __syncwarp();
-#pragma unroll
+#pragma unroll 1
         for (int mt = 0; mt < 2; ++mt)
             {
             const unsigned int r0 = mt * 16u + g;  // rows r0 and r0 + 8 of this lane
-            // layer 1: K = 32 (2 k-tiles), N = 64 (8 n-tiles)
-            float h1[8][4];
+            unsigned int a1[2][4];
+#pragma unroll
+            for (int kt = 0; kt < 2; ++kt)
+                {
+                a1[kt][0] = xs[r0 * XS + kt * 8 + t];
+                a1[kt][1] = xs[(r0 + 8) * XS + kt * 8 + t];
+                a1[kt][2] = xs[r0 * XS + kt * 8 + 4 + t];
+                a1[kt][3] = xs[(r0 + 8) * XS + kt * 8 + 4 + t];
+                }
+            // layer 1 -> BF16 A fragments of layer 2 (k-tile j = n-tiles 2j, 2j+1)
+            unsigned int a2[4][4];
 #pragma unroll
             for (int nt = 0; nt < 8; ++nt)
                 {
-                h1[nt][0] = h1[nt][1] = h1[nt][2] = h1[nt][3] = 0.f;
+                float acc[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
                 for (int kt = 0; kt < 2; ++kt)
                     {
-                    unsigned int af[4];
-                    af[0] = xs[r0 * XS + kt * 8 + t];
-                    af[1] = xs[(r0 + 8) * XS + kt * 8 + t];
-                    af[2] = xs[r0 * XS + kt * 8 + 4 + t];
-                    af[3] = xs[(r0 + 8) * XS + kt * 8 + 4 + t];
-                    const unsigned int n = nt * 8 + g;
-                    const unsigned int b0 = s_w1[n * (kCapIn / 2) + kt * 8 + t];
-                    const unsigned int b1 = s_w1[n * (kCapIn / 2) + kt * 8 + 4 + t];
-                    mma_bf16_16816(h1[nt], af, b0, b1);
+                    const uint2 b = s_w1[(kt * 4 + t) * kCapWStride + nt * 8 + g];
+                    mma_bf16_16816(acc, a1[kt], b.x, b.y);
                     }
                 const float bl = s_b1[nt * 8 + 2 * t];
                 const float bh = s_b1[nt * 8 + 2 * t + 1];
-                h1[nt][0] = fmaxf(h1[nt][0] + bl, 0.f);
-                h1[nt][1] = fmaxf(h1[nt][1] + bh, 0.f);
-                h1[nt][2] = fmaxf(h1[nt][2] + bl, 0.f);
-                h1[nt][3] = fmaxf(h1[nt][3] + bh, 0.f);
+                a2[nt >> 1][(nt & 1) * 2 + 0] = pack_bf16x2(fmaxf(acc[0] + bl, 0.f), fmaxf(acc[1] + bh, 0.f));
+                a2[nt >> 1][(nt & 1) * 2 + 1] = pack_bf16x2(fmaxf(acc[2] + bl, 0.f), fmaxf(acc[3] + bh, 0.f));
                 }
-            // layer 2: A fragments from h1 (k-tile kt = n-tiles 2kt, 2kt+1)
-            unsigned int a2[4][4];
-#pragma unroll
-            for (int kt = 0; kt < 4; ++kt)
-                {
-                a2[kt][0] = pack_bf16x2(h1[2 * kt][0], h1[2 * kt][1]);
-                a2[kt][1] = pack_bf16x2(h1[2 * kt][2], h1[2 * kt][3]);
-                a2[kt][2] = pack_bf16x2(h1[2 * kt + 1][0], h1[2 * kt + 1][1]);
-                a2[kt][3] = pack_bf16x2(h1[2 * kt + 1][2], h1[2 * kt + 1][3]);
-                }
-            float h2[8][4];
+            // layer 2 with the output layer folded in: z(row) = sum over columns of relu(h2) * w3
+            float z0 = 0.f, z1 = 0.f;
 #pragma unroll
             for (int nt = 0; nt < 8; ++nt)
                 {
-                h2[nt][0] = h2[nt][1] = h2[nt][2] = h2[nt][3] = 0.f;
+                float acc[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
                 for (int kt = 0; kt < 4; ++kt)
                     {
-                    const unsigned int n = nt * 8 + g;
-                    const unsigned int b0 = s_w2[n * (kCapHidden / 2) + kt * 8 + t];
-                    const unsigned int b1 = s_w2[n * (kCapHidden / 2) + kt * 8 + 4 + t];
-                    mma_bf16_16816(h2[nt], a2[kt], b0, b1);
+                    const uint2 b = s_w2[(kt * 4 + t) * kCapWStride + nt * 8 + g];
+                    mma_bf16_16816(acc, a2[kt], b.x, b.y);
                     }
-                const float bl = s_b2[nt * 8 + 2 * t];
-                const float bh = s_b2[nt * 8 + 2 * t + 1];
-                h2[nt][0] = fmaxf(h2[nt][0] + bl, 0.f);
-                h2[nt][1] = fmaxf(h2[nt][1] + bh, 0.f);
-                h2[nt][2] = fmaxf(h2[nt][2] + bl, 0.f);
-                h2[nt][3] = fmaxf(h2[nt][3] + bh, 0.f);
+                const int c0 = nt * 8 + 2 * t;
+                const float w0 = s_w3[c0], w1 = s_w3[c0 + 1];
+                const float bl = s_b2[c0], bh = s_b2[c0 + 1];
+                z0 = fmaf(fmaxf(acc[0] + bl, 0.f), w0, z0);
+                z0 = fmaf(fmaxf(acc[1] + bh, 0.f), w1, z0);
+                z1 = fmaf(fmaxf(acc[2] + bl, 0.f), w0, z1);
+                z1 = fmaf(fmaxf(acc[3] + bh, 0.f), w1, z1);
                 }
-            // layer 3: one n-tile (column 0 = the output)
-            float z[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-            for (int kt = 0; kt < 4; ++kt)
+            // the four lanes of a group hold disjoint columns of rows r0 and r0 + 8
+            z0 += __shfl_xor_sync(0xffffffffu, z0, 1);
+            z0 += __shfl_xor_sync(0xffffffffu, z0, 2);
+            z1 += __shfl_xor_sync(0xffffffffu, z1, 1);
+            z1 += __shfl_xor_sync(0xffffffffu, z1, 2);
+            if (t < 2u)
                 {
-                unsigned int af[4];
-                af[0] = pack_bf16x2(h2[2 * kt][0], h2[2 * kt][1]);
-                af[1] = pack_bf16x2(h2[2 * kt][2], h2[2 * kt][3]);
-                af[2] = pack_bf16x2(h2[2 * kt + 1][0], h2[2 * kt + 1][1]);
-                af[3] = pack_bf16x2(h2[2 * kt + 1][2], h2[2 * kt + 1][3]);
-                const unsigned int b0 = s_w3[g * (kCapHidden / 2) + kt * 8 + t];
-                const unsigned int b1 = s_w3[g * (kCapHidden / 2) + kt * 8 + 4 + t];
-                mma_bf16_16816(z, af, b0, b1);
-                }
-            if (t == 0u)
-                {
-#pragma unroll
-                for (int h = 0; h < 2; ++h)
+                const unsigned int s = base + r0 + 8u * t;
+                if (s < a.N)
                     {
-                    const unsigned int s = base + r0 + 8u * h;
-                    if (s < a.N)
-                        {
-                        const float y = cap_softplus(z[2 * h] + b3);
-                        const unsigned int row = a.rows_sorted ? s : __float_as_uint(a.points[s].w);
-                        if (a.y_out) a.y_out[row] = y;
-                        a.cap_out[row] = cap_from_output(y, a.margin, a.cap_max);
-                        }
+                    const float y = cap_softplus((t == 0u ? z0 : z1) + b3);
+                    const unsigned int row = a.rows_sorted ? s : __float_as_uint(a.points[s].w);
+                    if (a.y_out) a.y_out[row] = y;
+                    a.cap_out[row] = cap_from_output(y, a.margin, a.cap_max);
                     }
                 }
             }
@@ -415,7 +464,7 @@ __global__ void __launch_bounds__(kCapTrainTile) k_cap_train_step(const CapTrain
                 {
                 float acc = 0.f;
                 for (int k = 0; k < kCapHidden; ++k) acc = fmaf(S.w2[j * kCapHidden + k], S.h1[tid][k], acc);
-                S.h2[tid][j] = bf16_round(fmaxf(acc + S.b2[j], 0.f));
+                S.h2[tid][j] = fmaxf(acc + S.b2[j], 0.f);
                 }
             float z = 0.f;
             for (int k = 0; k < kCapHidden; ++k) z = fmaf(S.w3[k], S.h2[tid][k], z);

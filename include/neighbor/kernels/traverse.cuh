@@ -17,8 +17,7 @@
 //                      no pair is reported twice when buckets straddle images.
 //   k_traverse_half    self queries with a symmetric image set: each query walks only the records
 //                      after its own point record and a pair counts for both rows;
-//                      k_half_order_rows / k_half_order_long give each list row the reference's
-//                      order.
+//                      k_half_order_rows gives each list row the reference's order.
 #ifndef NEIGHBOR_KERNELS_TRAVERSE_CUH_
 #define NEIGHBOR_KERNELS_TRAVERSE_CUH_
 
@@ -396,14 +395,13 @@ __global__ void k_traverse_fast(const FastLBVHData tree, const FastQueryArgs a,
 // within an image), independent of the order of the atomics.  The image through which a partner
 // finds the query is the mirror image (26 - image on the lattice).  A row with more entries than
 // its capacity (max_neigh, or its own capacity in a CSR list) keeps that many of them (which
-// ones is unspecified) and its full count.  Rows longer than kHalfRowMax must not be ordered
-// here: the caller sizes capacities (or routes to the whole-tree walk) so that they are not.
+// ones is unspecified) and its full count.  Capacities are at most kHalfRowThread, so that one
+// thread orders a row; longer rows are filled by the whole-tree walk, which writes them in order.
 // ---------------------------------------------------------------------------------------------
 constexpr unsigned int kHalfKeyBits = 27;
 constexpr unsigned int kHalfKeyMask = (1u << kHalfKeyBits) - 1u;
 constexpr unsigned int kHalfMaxN = 1u << kHalfKeyBits;   // sorted positions must fit the key
-constexpr unsigned int kHalfRowThread = 32;              // rows up to this long: one thread
-constexpr unsigned int kHalfRowMax = 4096;               // longest row ordered (one block)
+constexpr unsigned int kHalfRowThread = 32;              // longest row a symmetric fill may write
 
 struct HalfArgs
     {
@@ -537,8 +535,6 @@ struct HalfOrderArgs
     const unsigned int* caps;
     const unsigned int* own;
     const unsigned int* primitive;
-    unsigned int* long_rows;    // rows longer than kHalfRowThread, for k_half_order_long
-    unsigned int* n_long;       // zero on entry
     const unsigned int* status;
     };
 
@@ -565,11 +561,8 @@ __global__ void __launch_bounds__(256) k_half_order_rows(const HalfOrderArgs a, 
     const unsigned int cap = a.offsets ? a.caps[r] : a.max_neigh;
     const unsigned int m = min(total, cap);
     if (m == 0u) return;
-    if (m > kHalfRowThread)
-        {
-        a.long_rows[atomicAdd(a.n_long, 1u)] = r;
-        return;
-        }
+    // callers route fills with rows longer than kHalfRowThread to the whole-tree walk
+    if (m > kHalfRowThread) return;
     unsigned int* row = a.list + first;
     unsigned int key[kHalfRowThread];
     for (unsigned int k = 0; k < m; ++k)
@@ -584,54 +577,6 @@ __global__ void __launch_bounds__(256) k_half_order_rows(const HalfOrderArgs a, 
         key[j] = v;
         }
     for (unsigned int k = 0; k < m; ++k) row[k] = transform(a.primitive[key[k] & kHalfKeyMask]);
-    }
-
-// Rows longer than kHalfRowThread entries: one block per row, bitonic sort in shared memory.
-template<class TransformOpT>
-__global__ void __launch_bounds__(256) k_half_order_long(const HalfOrderArgs a, const TransformOpT transform)
-    {
-    __shared__ unsigned int s_key[kHalfRowMax];
-    const unsigned int n_long = min(*a.n_long, a.Q);
-    for (unsigned int b = blockIdx.x; b < n_long; b += gridDim.x)
-        {
-        const unsigned int r = a.long_rows[b];
-        const unsigned int total = a.nneigh[r];
-        const unsigned int appended = total - a.own[r];
-        const unsigned long long first = a.offsets ? a.offsets[r] : (unsigned long long)r * a.max_neigh;
-        const unsigned int cap = a.offsets ? a.caps[r] : a.max_neigh;
-        const unsigned int m = min(min(total, cap), kHalfRowMax);
-        unsigned int* row = a.list + first;
-        unsigned int n2 = 1u;
-        while (n2 < m) n2 <<= 1;
-        for (unsigned int k = threadIdx.x; k < n2; k += blockDim.x)
-            s_key[k] = k < m ? half_row_key(row, k, appended, total, cap) : 0xffffffffu;
-        __syncthreads();
-        for (unsigned int size = 2u; size <= n2; size <<= 1)
-            {
-            for (unsigned int stride = size >> 1; stride > 0u; stride >>= 1)
-                {
-                for (unsigned int k = threadIdx.x; k < n2; k += blockDim.x)
-                    {
-                    const unsigned int o = k ^ stride;
-                    if (o > k)
-                        {
-                        const bool up = (k & size) == 0u;
-                        const unsigned int x = s_key[k];
-                        const unsigned int y = s_key[o];
-                        if ((x > y) == up)
-                            {
-                            s_key[k] = y;
-                            s_key[o] = x;
-                            }
-                        }
-                    }
-                __syncthreads();
-                }
-            }
-        for (unsigned int k = threadIdx.x; k < m; k += blockDim.x)
-            row[k] = transform(a.primitive[s_key[k] & kHalfKeyMask]);
-        __syncthreads();
-        }
     }
 
 // ---------------------------------------------------------------------------------------------

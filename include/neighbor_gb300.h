@@ -51,6 +51,8 @@ int nbr_lbvh_destroy(nbr_lbvh h);
 /* Additions: leaf bucket size of the traversal tree (1..64) and sort digit width (8 or 10). */
 int nbr_lbvh_set_leaf_size(nbr_lbvh h, unsigned int leaf_size);
 int nbr_lbvh_set_radix_bits(nbr_lbvh h, unsigned int bits);
+/* Addition: sorted leaves per block of the build's agglomerative climb (128, 256 or 512). */
+int nbr_lbvh_set_climb_block(nbr_lbvh h, unsigned int leaves);
 
 /* LBVH::build(LaunchParameters, PointInsertOp, lo, hi) (LBVH.h:242-318, InsertOps.h:18-54).
  * points: float3[N]; lo/hi: scene bounds for Morton binning (host float[3]). */

@@ -80,6 +80,7 @@ def _declare(L):
     sig("nbr_lbvh_destroy", [_P])
     sig("nbr_lbvh_set_leaf_size", [_P, _U])
     sig("nbr_lbvh_set_radix_bits", [_P, _U])
+    sig("nbr_lbvh_set_climb_block", [_P, _U])
     sig("nbr_lbvh_build_points", [_P, _P, _U, _P, _P, _U, _P])
     sig("nbr_lbvh_build_spheres", [_P, _P, _F, _U, _P, _P, _U, _P])
     sig("nbr_lbvh_get_sizes", [_P, ctypes.POINTER(_I), ctypes.POINTER(_U), ctypes.POINTER(_U),
@@ -128,7 +129,8 @@ def _declare(L):
 
 # C-ABI symbols declared in include/neighbor_gb300.h (checked by the CPU tests).
 EXPORTED = ["nbr_last_error", "nbr_version", "nbr_lbvh_create", "nbr_lbvh_destroy",
-            "nbr_lbvh_set_leaf_size", "nbr_lbvh_set_radix_bits", "nbr_lbvh_build_points",
+            "nbr_lbvh_set_leaf_size", "nbr_lbvh_set_radix_bits", "nbr_lbvh_set_climb_block",
+            "nbr_lbvh_build_points",
             "nbr_lbvh_build_spheres", "nbr_lbvh_get_sizes", "nbr_lbvh_get_arrays",
             "nbr_lbvh_get_codes", "nbr_lbvh_get_fast", "nbr_lbvh_num_fast_nodes",
             "nbr_lbvh_check_status", "nbr_traverser_create", "nbr_traverser_destroy",
@@ -249,7 +251,8 @@ def images27(L: Sequence[float], device="cuda"):
 class LBVH:
     """neighbor::LBVH (include/neighbor/LBVH.h) through the C ABI."""
 
-    def __init__(self, leaf_size: Optional[int] = None, radix_bits: Optional[int] = None):
+    def __init__(self, leaf_size: Optional[int] = None, radix_bits: Optional[int] = None,
+                 climb_block: Optional[int] = None):
         L = load()
         h = ctypes.c_void_p()
         _check(L.nbr_lbvh_create(ctypes.byref(h)))
@@ -259,6 +262,8 @@ class LBVH:
             self.set_leaf_size(leaf_size)
         if radix_bits is not None:
             self.set_radix_bits(radix_bits)
+        if climb_block is not None:
+            self.set_climb_block(climb_block)
 
     def __del__(self):
         h = getattr(self, "_h", None)
@@ -278,6 +283,10 @@ class LBVH:
 
     def set_radix_bits(self, bits: int):
         _check(self._L.nbr_lbvh_set_radix_bits(self._h, int(bits)))
+
+    def set_climb_block(self, leaves: int):
+        """Sorted leaves per block of the build's agglomerative climb (128, 256 or 512)."""
+        _check(self._L.nbr_lbvh_set_climb_block(self._h, int(leaves)))
 
     def build(self, points, lo, hi, radius: Optional[float] = None, block_size: int = 32,
               stream=None):

@@ -138,6 +138,12 @@ int nbr_lbvh_set_radix_bits(nbr_lbvh h, unsigned int bits)
     return guarded([&] { h->lbvh.setRadixBits(bits); });
     }
 
+int nbr_lbvh_set_climb_block(nbr_lbvh h, unsigned int leaves)
+    {
+    if (!h) return fail(NBR_ERR_INVALID, "null handle");
+    return guarded([&] { h->lbvh.setClimbBlock(leaves); });
+    }
+
 int nbr_lbvh_build_points(nbr_lbvh h, const float* points, unsigned int N, const float lo[3],
                           const float hi[3], unsigned int block_size, void* stream)
     {

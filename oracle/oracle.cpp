@@ -851,7 +851,7 @@ void cap_sample(const float* P, const float* xf, float target, R round, T* g, T&
     for (int j = 0; j < kH; ++j) {
         T acc = 0;
         for (int k = 0; k < kH; ++k) acc = std::fma(w2[j * kH + k], h1[k], acc);
-        h2[j] = round(std::max(acc + (T)P[oB2 + j], (T)0));
+        h2[j] = std::max(acc + (T)P[oB2 + j], (T)0);
     }
     T z = 0;
     for (int k = 0; k < kH; ++k) z = std::fma(w3[k], h2[k], z);

@@ -157,9 +157,9 @@ void orc_cap_features(const uint32_t* codes, const float* points4, uint32_t N, c
                       float* out);
 
 /* Forward and backward of the network for rows (offset + b*stride) mod N, b < batch:
- * 32 -> 64 ReLU -> 64 ReLU -> 1 softplus; when bf16 != 0 weights, inputs and hidden activations
- * are rounded to BF16 (round to nearest even) as on the GPU, products accumulated with fmaf in
- * ascending index order.  grad[6337] = summed dL/dparams, *loss = summed 0.5 (y - t)^2,
+ * 32 -> 64 ReLU -> 64 ReLU -> 1 softplus; when bf16 != 0 weights, inputs and the first hidden
+ * activations are rounded to BF16 (round to nearest even) as on the GPU, products accumulated
+ * with fmaf in ascending index order.  grad[6337] = summed dL/dparams, *loss = summed 0.5 (y - t)^2,
  * y[batch] = outputs (either may be NULL).  Double precision when bf16 < 0 (for finite-difference
  * checks of the restated backward). */
 void orc_cap_forward_backward(const float* params, const float* features, const float* targets,

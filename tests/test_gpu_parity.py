@@ -130,6 +130,21 @@ def test_fast_nodes_clustered(leaf):
     assert np.array_equal(fast["nodes"].cpu().numpy().view(np.uint32), want)
 
 
+@pytest.mark.parametrize("climb", [128, 256, 512])
+@pytest.mark.parametrize("N", [5000, 70001])
+def test_climb_block_sizes_give_the_same_tree(climb, N):
+    # the block size of the agglomerative climb changes which splits meet in shared memory and
+    # which across blocks, never the tree
+    L = 40.0
+    P = _clustered(N, 6, L)
+    lbvh = nb.LBVH(leaf_size=4, climb_block=climb)
+    lbvh.build(_t(P), [0, 0, 0], [L, L, L])
+    lbvh.check_status()
+    T = _check_tree(lbvh, P, [0, 0, 0], [L, L, L])
+    want, _ = O.fast_nodes(T, 4)
+    assert np.array_equal(lbvh.fast()["nodes"].cpu().numpy().view(np.uint32), want)
+
+
 def _csr_rows(off, nbrs, i):
     return nbrs[off[i]:off[i + 1]]
 

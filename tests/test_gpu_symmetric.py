@@ -4,8 +4,9 @@ With the self image or the 27-image lattice, a self traversal finds each unorder
 writes it to both rows; the rows are then ordered by (image, sorted position), the order of a
 whole-tree walk (and of the reference's rope traversal).  So the full outputs -- counts and every
 list row -- must be bit-identical to the whole-tree walk's, and the sets must equal the oracle's
-cell list.  Rows longer than 32 entries take the block-per-row ordering kernel; rows that overflow
-max_neigh keep their full count and a subset of their true neighbors.
+cell list.  Counts always take the symmetric kernel; fills with rows longer than 32 entries take
+the whole-tree walk (checked on clustered inputs); rows that overflow max_neigh keep their full
+count and a subset of their true neighbors.
 """
 import numpy as np
 import pytest
@@ -87,7 +88,7 @@ def test_symmetric_equals_whole_tree_walk(leaf, dist, images, rows_sorted):
     assert np.array_equal(cs, cf)
     assert np.array_equal(ls, lf)  # same entries in the same order
     if dist == "clustered":
-        assert mx > 32  # the block-per-row ordering kernel ran
+        assert mx > 32  # rows too long for the symmetric fill
     # the sets are the oracle's (open box: a periodic grid three times wider never wraps a pair)
     if images == "periodic":
         off, nbrs = O.celllist_csr(P, P, rc, [0, 0, 0], box)
@@ -123,7 +124,8 @@ def test_symmetric_overflow_keeps_counts_and_a_subset():
 
 
 def test_symmetric_transform_and_long_rows():
-    # dense clusters: rows of several hundred entries, a map transform on the ids
+    # dense clusters: rows of several hundred entries (the fill takes the whole-tree walk, the
+    # count the symmetric kernel), a map transform on the ids
     N = 20000
     L = 30.0
     P = _clustered(N, 44, L, per=2000)

@@ -50,7 +50,7 @@ def test_bf16_forward_matches_numpy():
     b3 = float(P[6336])
     x = _bf16(F).astype(np.float64)
     h1 = _bf16(np.maximum(x @ W1.T + b1, 0)).astype(np.float64)
-    h2 = _bf16(np.maximum(h1 @ W2.T + b2, 0)).astype(np.float64)
+    h2 = np.maximum(h1 @ W2.T + b2, 0)
     z = h2 @ W3 + b3
     want = np.maximum(z, 0) + np.log1p(np.exp(-np.abs(z)))
     np.testing.assert_allclose(y, want, rtol=2e-3, atol=2e-3)

@@ -272,12 +272,10 @@ def learned_uniform(nb, n, L, frames, warmup, plain_ms, pairs_step, args, stream
     model, train_s, loss = train_capacity_model(nb, lbvh, trav, train, L, RC, args.train_steps)
     del train
     op = nb.OnePassList()
-    caps = op.capacity(n)
 
     def step(p):
-        lbvh.build(p, [0, 0, 0], box, block_size=args.block)
-        model.predict(lbvh, [0, 0, 0], box, RC, caps=caps, cap_max=UNIFORM_CAP_MAX)
-        return op.build(trav, lbvh, RC, box, pad, cap_max=UNIFORM_CAP_MAX, block_size=args.block)
+        return op.build_learned(model, trav, lbvh, p, [0, 0, 0], box, RC, box, pad, cap_max=UNIFORM_CAP_MAX,
+                                block_size=args.block)
 
     ms, stats = time_steps(step, frames, warmup, stream)
     # exactness of the last frame: counts equal to the plain count pass
@@ -337,12 +335,10 @@ def clustered_c3(nb, args, stream, n=4_000_000, rc=1.0, steps=5, warmup=2):
         return total
 
     op = nb.OnePassList()
-    caps = op.capacity(n)
 
     def learned(p):
-        lbvh.build(p, [0, 0, 0], box, block_size=args.block)
-        model.predict(lbvh, [0, 0, 0], box, rc, caps=caps, cap_max=CLUSTERED_CAP_MAX)
-        return op.build(trav, lbvh, rc, box, pad, cap_max=CLUSTERED_CAP_MAX, block_size=args.block)
+        return op.build_learned(model, trav, lbvh, p, [0, 0, 0], box, rc, box, pad, cap_max=CLUSTERED_CAP_MAX,
+                                block_size=args.block)
 
     ms_plain, totals = time_steps(plain, frames, warmup, stream)
     ms_learned, stats = time_steps(learned, frames, warmup, stream)
@@ -359,7 +355,8 @@ def clustered_c3(nb, args, stream, n=4_000_000, rc=1.0, steps=5, warmup=2):
             "overflow_rows_mean": sum(s["overflow_rows"] for s in stats) / len(stats),
             "counts_equal_plain": exact, "margin": model.margin, "train_s": round(train_s, 2),
             "train_loss": loss, "plain": "count + exclusive scan + exact CSR fill",
-            "learned": "capacity network + one CSR fill + exact re-run of overflowed rows"}
+            "learned": "capacity network (overlapping the build after its sort) + one CSR fill + exact "
+                       "re-run of overflowed rows"}
 
 
 def reference_cuda(n, our_ms):

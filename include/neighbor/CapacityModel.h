@@ -87,13 +87,15 @@ class CapacityModel
         // Occupancy grid of the tree's points at the frame's level.
         void occupancy(const LBVH& lbvh, const gpu::CapFrame& fr, cudaStream_t stream)
             {
-            const unsigned int N = lbvh.getN();
+            occupancy(lbvh.getCodes().get(), lbvh.getN(), fr, stream);
+            }
+        void occupancy(const unsigned int* codes, unsigned int N, const gpu::CapFrame& fr, cudaStream_t stream)
+            {
             const size_t G = 1024u >> fr.shift;
             m_occ.reserve(G * G * G);
             detail::check_cuda(cudaMemsetAsync(m_occ.get(), 0, G * G * G * sizeof(unsigned int), stream), "memset");
             if (N < 2) return;
-            gpu::k_cap_occupancy<<<detail::ceil_div(N, 256), 256, 0, stream>>>(lbvh.getCodes().get(), N, fr.shift,
-                                                                               m_occ.get());
+            gpu::k_cap_occupancy<<<detail::ceil_div(N, 256), 256, 0, stream>>>(codes, N, fr.shift, m_occ.get());
             detail::check_cuda(cudaGetLastError(), "occupancy launch");
             }
 
@@ -120,7 +122,36 @@ class CapacityModel
             a.frame = fr;
             a.codes = lbvh.getCodes().get();
             a.points = lbvh.fastData().points;
+            a.points3 = nullptr;
+            a.primitive = nullptr;
             a.N = N;
+            infer(a, rows_sorted, cap_max, caps, y, stream);
+            }
+
+        // The same prediction from the sort's output alone (sorted codes, primitive order, the
+        // original points), so that it can run while the rest of a build is still forming the
+        // tree (LBVH::sortedEvent()).
+        void predictSorted(const unsigned int* codes, const unsigned int* primitive, const float3* points,
+                           unsigned int N, const gpu::CapFrame& fr, bool rows_sorted, unsigned int cap_max,
+                           unsigned int* caps, float* y, cudaStream_t stream)
+            {
+            if (N < 2) throw std::runtime_error("capacity prediction needs a tree of at least two points");
+            occupancy(codes, N, fr, stream);
+            gpu::CapInferArgs a;
+            a.frame = fr;
+            a.codes = codes;
+            a.points = nullptr;
+            a.points3 = points;
+            a.primitive = primitive;
+            a.N = N;
+            infer(a, rows_sorted, cap_max, caps, y, stream);
+            }
+
+    private:
+        void infer(gpu::CapInferArgs& a, bool rows_sorted, unsigned int cap_max, unsigned int* caps, float* y,
+                   cudaStream_t stream)
+            {
+            const unsigned int N = a.N;
             a.occ = m_occ.get();
             a.w = m_w.get();
             a.p = m_p.get();
@@ -135,6 +166,7 @@ class CapacityModel
             detail::check_cuda(cudaGetLastError(), "capacity inference launch");
             }
 
+    public:
         // log1p(count) targets from exact counts.
         static void targets(const unsigned int* counts, unsigned int N, float* out, cudaStream_t stream)
             {

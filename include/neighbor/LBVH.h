@@ -67,8 +67,16 @@ class LBVH : public Tunable<unsigned int>
         LBVH()
             : Tunable<unsigned int>(32, 1024, 32), m_root(LBVHSentinel), m_N(0), m_N_internal(0),
               m_N_nodes(0), m_capacity(0), m_leaf_size(4), m_radix_bits(8), m_fast_points(false),
-              m_epoch(0), m_block(256), m_climb_block(512), m_stream(0), m_ref_valid(true)
+              m_epoch(0), m_block(256), m_climb_block(512), m_stream(0), m_ref_valid(true),
+              m_sorted_event(nullptr)
             {}
+
+        ~LBVH()
+            {
+            if (m_sorted_event) cudaEventDestroy(m_sorted_event);
+            }
+        LBVH(const LBVH&) = delete;
+        LBVH& operator=(const LBVH&) = delete;
 
         template<class InsertOpT>
         void setup(const LaunchParameters& params, const InsertOpT& insert)
@@ -182,6 +190,11 @@ class LBVH : public Tunable<unsigned int>
             return f;
             }
 
+        // Event recorded on the build's stream once the sorted codes and primitive order of the
+        // last build are final (before the tree is formed): work that needs only those -- such as
+        // capacity prediction -- can start on another stream while the rest of the build runs.
+        cudaEvent_t sortedEvent() const { return m_sorted_event; }
+
         // Device status word (0 = all waits completed).
         const unsigned int* getStatusPointer() const { return m_small.get() + kSmallStatus; }
 
@@ -234,7 +247,8 @@ class LBVH : public Tunable<unsigned int>
         unsigned int m_block;
         unsigned int m_climb_block;
         cudaStream_t m_stream;
-        mutable bool m_ref_valid;  // reference-layout arrays match the last build
+        mutable bool m_ref_valid;
+        cudaEvent_t m_sorted_event;  // reference-layout arrays match the last build
 
         mutable shared_array<int> m_parent;
         mutable shared_array<int> m_left;
@@ -480,6 +494,9 @@ void LBVH::build(const LaunchParameters& params, const InsertOpT& insert, const 
         sort_codes<InsertOpT, 10>(insert, lo, ext, stream, epoch);
     else
         sort_codes<InsertOpT, 8>(insert, lo, ext, stream, epoch);
+    if (!m_sorted_event)
+        detail::check_cuda(cudaEventCreateWithFlags(&m_sorted_event, cudaEventDisableTiming), "event create");
+    detail::check_cuda(cudaEventRecord(m_sorted_event, stream), "event record");
 
     // radix tree, packed boxes, box-record counts
     gpu::ClimbArgs c;

@@ -12,6 +12,7 @@
 
 #include <cuda_runtime.h>
 
+#include "CapacityModel.h"
 #include "LBVH.h"
 #include "LBVHTraverser.h"
 #include "Memory.h"
@@ -24,22 +25,60 @@ namespace neighbor
 {
 namespace gpu
 {
-// Sorted positions whose row overflowed, with their exact counts.
-static __global__ void __launch_bounds__(256) k_overflow_rows(unsigned int N, int rows_sorted,
-                                                              const unsigned int* __restrict__ primitive,
-                                                              const unsigned int* __restrict__ nneigh,
-                                                              const unsigned int* __restrict__ caps,
-                                                              unsigned int* __restrict__ ovf_q,
-                                                              unsigned int* __restrict__ ovf_count,
-                                                              unsigned int* __restrict__ n_ovf)
+// Sorted positions whose row overflowed, with their exact counts, in ascending order (so the
+// appended space is laid out the same way on every run): k_overflow_count counts them per block,
+// k_scan64_sums turns the counts into block offsets, k_overflow_write writes them in order.
+constexpr int kOverflowBlock = 256;
+
+__device__ __forceinline__ bool row_overflows(unsigned int q, unsigned int N, int rows_sorted,
+                                              const unsigned int* __restrict__ primitive,
+                                              const unsigned int* __restrict__ nneigh,
+                                              const unsigned int* __restrict__ caps, unsigned int& count)
     {
-    const unsigned int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= N) return;
+    if (q >= N) return false;
     const unsigned int row = rows_sorted ? q : primitive[q];
-    const unsigned int c = nneigh[row];
-    if (c > caps[row])
+    count = nneigh[row];
+    return count > caps[row];
+    }
+
+static __global__ void __launch_bounds__(kOverflowBlock) k_overflow_count(unsigned int N, int rows_sorted,
+                                                                          const unsigned int* __restrict__ primitive,
+                                                                          const unsigned int* __restrict__ nneigh,
+                                                                          const unsigned int* __restrict__ caps,
+                                                                          unsigned long long* __restrict__ block_count)
+    {
+    __shared__ unsigned int s_n;
+    if (threadIdx.x == 0) s_n = 0u;
+    __syncthreads();
+    unsigned int c;
+    const bool ovf = row_overflows(blockIdx.x * blockDim.x + threadIdx.x, N, rows_sorted, primitive, nneigh, caps, c);
+    const unsigned int w = __ballot_sync(0xffffffffu, ovf);
+    if ((threadIdx.x & 31u) == 0u && w) atomicAdd(&s_n, (unsigned int)__popc(w));
+    __syncthreads();
+    if (threadIdx.x == 0) block_count[blockIdx.x] = s_n;
+    }
+
+static __global__ void __launch_bounds__(kOverflowBlock) k_overflow_write(unsigned int N, int rows_sorted,
+                                                                          const unsigned int* __restrict__ primitive,
+                                                                          const unsigned int* __restrict__ nneigh,
+                                                                          const unsigned int* __restrict__ caps,
+                                                                          const unsigned long long* __restrict__ block_base,
+                                                                          unsigned int* __restrict__ ovf_q,
+                                                                          unsigned int* __restrict__ ovf_count)
+    {
+    __shared__ unsigned int s_warp[kOverflowBlock / 32];
+    const unsigned int q = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned int c = 0;
+    const bool ovf = row_overflows(q, N, rows_sorted, primitive, nneigh, caps, c);
+    const unsigned int w = __ballot_sync(0xffffffffu, ovf);
+    const unsigned int lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    if (lane == 0u) s_warp[warp] = __popc(w);
+    __syncthreads();
+    unsigned int before = 0;
+    for (unsigned int k = 0; k < warp; ++k) before += s_warp[k];
+    if (ovf)
         {
-        const unsigned int k = atomicAdd(n_ovf, 1u);
+        const unsigned int k = (unsigned int)block_base[blockIdx.x] + before + __popc(w & lanemask_lt());
         ovf_q[k] = q;
         ovf_count[k] = c;
         }
@@ -74,7 +113,14 @@ class OnePassNeighborList
             unsigned long long overflow_slots;  // slots appended for them
             };
 
-        OnePassNeighborList() : m_N(0), m_total(0) {}
+        OnePassNeighborList() : m_N(0), m_total(0), m_side(nullptr), m_pred_done(nullptr) {}
+        ~OnePassNeighborList()
+            {
+            if (m_pred_done) cudaEventDestroy(m_pred_done);
+            if (m_side) cudaStreamDestroy(m_side);
+            }
+        OnePassNeighborList(const OnePassNeighborList&) = delete;
+        OnePassNeighborList& operator=(const OnePassNeighborList&) = delete;
 
         // Capacity array of N rows for the caller (or a CapacityModel) to fill before build().
         unsigned int* capacity(unsigned int N)
@@ -135,16 +181,20 @@ class OnePassNeighborList
             m_ovf_q.reserve(N);
             m_ovf_count.reserve(N);
             m_ovf_off.reserve(N);
-            m_small.reserve(1);
-            detail::check_cuda(cudaMemsetAsync(m_small.get(), 0, sizeof(unsigned int), stream), "memset");
-            gpu::k_overflow_rows<<<detail::ceil_div(N, 256), 256, 0, stream>>>(
-                N, rows_sorted ? 1 : 0, lbvh.fastData().primitive, m_nneigh.get(), m_caps.get(), m_ovf_q.get(),
-                m_ovf_count.get(), m_small.get());
+            const unsigned int blocks = detail::ceil_div(N, gpu::kOverflowBlock);
+            m_ovf_blocks.reserve((size_t)blocks + 1);
+            gpu::k_overflow_count<<<blocks, gpu::kOverflowBlock, 0, stream>>>(
+                N, rows_sorted ? 1 : 0, lbvh.fastData().primitive, m_nneigh.get(), m_caps.get(), m_ovf_blocks.get());
+            gpu::k_scan64_sums<<<1, 1024, 0, stream>>>(m_ovf_blocks.get(), blocks, m_ovf_blocks.get() + blocks);
+            gpu::k_overflow_write<<<blocks, gpu::kOverflowBlock, 0, stream>>>(
+                N, rows_sorted ? 1 : 0, lbvh.fastData().primitive, m_nneigh.get(), m_caps.get(), m_ovf_blocks.get(),
+                m_ovf_q.get(), m_ovf_count.get());
             detail::check_cuda(cudaGetLastError(), "overflow launch");
-            unsigned int n_ovf = 0;
-            detail::check_cuda(cudaMemcpyAsync(&n_ovf, m_small.get(), sizeof(n_ovf), cudaMemcpyDeviceToHost, stream),
-                               "copy");
+            unsigned long long n_ovf64 = 0;
+            detail::check_cuda(cudaMemcpyAsync(&n_ovf64, m_ovf_blocks.get() + blocks, sizeof(n_ovf64),
+                                               cudaMemcpyDeviceToHost, stream), "copy");
             detail::check_cuda(cudaStreamSynchronize(stream), "sync");
+            const unsigned int n_ovf = (unsigned int)n_ovf64;
             st.overflow_rows = n_ovf;
             if (presized)
                 {
@@ -174,6 +224,44 @@ class OnePassNeighborList
             return st;
             }
 
+        // The learned one-pass step in one call: build the tree of `points`, predict every row's
+        // capacity with `model`, fill the list.  The prediction needs only the sort's output, so it
+        // runs on a second stream from LBVH::sortedEvent() on, alongside the rest of the build.
+        template<class TransformOpT = NullTransformOp>
+        Stats buildLearned(const LBVHTraverser::LaunchParameters& params, LBVH& lbvh, LBVHTraverser& trav,
+                           CapacityModel& model, const float3* points, unsigned int N, const float3& lo,
+                           const float3& hi, float rc, float3 box, float pad, bool periodic, bool rows_sorted,
+                           unsigned int cap_max, const TransformOpT& transform = TransformOpT())
+            {
+            cudaStream_t stream = params.stream;
+            lbvh.build(params, PointInsertOp(points, N), lo, hi);
+            if (N == 0) return build(params, lbvh, trav, rc, box, pad, periodic, rows_sorted, cap_max, transform);
+            unsigned int* caps = capacity(N);
+            if (N < 2)
+                {
+                const unsigned int one = 1u;
+                detail::check_cuda(cudaMemcpy(caps, &one, sizeof(one), cudaMemcpyHostToDevice), "copy");
+                return build(params, lbvh, trav, rc, box, pad, periodic, rows_sorted, cap_max, transform);
+                }
+            if (!m_side)
+                {
+                // highest priority: the prediction's blocks take SMs as soon as blocks of the build's
+                // later kernels retire, instead of queueing behind all of them
+                int least = 0, greatest = 0;
+                detail::check_cuda(cudaDeviceGetStreamPriorityRange(&least, &greatest), "priority range");
+                detail::check_cuda(cudaStreamCreateWithPriority(&m_side, cudaStreamNonBlocking, greatest),
+                                   "stream create");
+                detail::check_cuda(cudaEventCreateWithFlags(&m_pred_done, cudaEventDisableTiming), "event create");
+                }
+            detail::check_cuda(cudaStreamWaitEvent(m_side, lbvh.sortedEvent(), 0), "wait");
+            model.predictSorted(lbvh.getCodes().get(), lbvh.getPrimitives().get(), points, N,
+                                CapacityModel::frame(lo, hi, rc, periodic), rows_sorted, cap_max, caps, nullptr,
+                                m_side);
+            detail::check_cuda(cudaEventRecord(m_pred_done, m_side), "event record");
+            detail::check_cuda(cudaStreamWaitEvent(stream, m_pred_done, 0), "wait");
+            return build(params, lbvh, trav, rc, box, pad, periodic, rows_sorted, cap_max, transform);
+            }
+
         const unsigned int* list() const { return m_list.get(); }
         const unsigned long long* offsets() const { return m_offsets.get(); }
         const unsigned int* capacities() const { return m_caps.get(); }
@@ -192,7 +280,9 @@ class OnePassNeighborList
         device_array<unsigned int> m_ovf_count;
         device_array<unsigned long long> m_ovf_off;
         device_array<unsigned long long> m_tiles;
-        device_array<unsigned int> m_small;
+        device_array<unsigned long long> m_ovf_blocks;
+        cudaStream_t m_side;
+        cudaEvent_t m_pred_done;
     };
 
 } // namespace neighbor

@@ -218,7 +218,9 @@ struct CapInferArgs
     {
     CapFrame frame;
     const unsigned int* codes;      // sorted Morton codes
-    const float4* points;           // sorted payload
+    const float4* points;           // sorted payload (x, y, z, primitive id), or NULL and then:
+    const float3* points3;          //   the original points, gathered through
+    const unsigned int* primitive;  //   the sorted primitive order
     unsigned int N;
     const unsigned int* occ;
     const __nv_bfloat16* w;         // BF16 weights (kCapBfWeights)
@@ -243,6 +245,21 @@ __device__ __forceinline__ void mma_bf16_16816(float (&d)[4], const unsigned int
                  "{%0,%1,%2,%3};"
                  : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
                  : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+    }
+
+// Position and output row of sorted point s.
+__device__ __forceinline__ float3 cap_position(const CapInferArgs& a, unsigned int s)
+    {
+    if (a.points) {
+        const float4 p = a.points[s];
+        return make_float3(p.x, p.y, p.z);
+    }
+    return a.points3[a.primitive[s]];
+    }
+__device__ __forceinline__ unsigned int cap_row(const CapInferArgs& a, unsigned int s)
+    {
+    if (a.rows_sorted) return s;
+    return a.points ? __float_as_uint(a.points[s].w) : a.primitive[s];
     }
 
 constexpr int kCapInferWarps = 8;
@@ -300,9 +317,9 @@ __global__ void __launch_bounds__(kCapInferWarps * 32, 4) k_cap_infer(const CapI
         unsigned int* row = xs + lane * XS;
         if (s < a.N)
             {
-            const float4 p = a.points[s];
+            const float3 pos = cap_position(a, s);
             float prev = 0.f;
-            cap_features(a.frame, a.codes[s], make_float3(p.x, p.y, p.z), a.occ, s_log,
+            cap_features(a.frame, a.codes[s], pos, a.occ, s_log,
                          [row, &prev](int k, float v) {
                              if (k & 1) row[k >> 1] = pack_bf16x2(prev, v);
                              prev = v;
@@ -376,7 +393,7 @@ __global__ void __launch_bounds__(kCapInferWarps * 32, 4) k_cap_infer(const CapI
                 if (s < a.N)
                     {
                     const float y = cap_softplus((t == 0u ? z0 : z1) + b3);
-                    const unsigned int row = a.rows_sorted ? s : __float_as_uint(a.points[s].w);
+                    const unsigned int row = cap_row(a, s);
                     if (a.y_out) a.y_out[row] = y;
                     a.cap_out[row] = cap_from_output(y, a.margin, a.cap_max);
                     }

@@ -239,6 +239,16 @@ int nbr_onepass_build(nbr_onepass op, nbr_traverser t, nbr_lbvh h, float rc, con
                       int periodic, int rows_sorted, unsigned int cap_max, const unsigned int* map,
                       unsigned int block_size, void* stream, unsigned long long* slots,
                       unsigned int* overflow_rows, unsigned long long* overflow_slots);
+/* The learned one-pass step in one call: build h from points (as nbr_lbvh_build_points, scene
+ * bounds lo/hi), predict every row's capacity with m (features in the frame lo/hi), and fill the
+ * list as nbr_onepass_build.  The prediction runs on a second stream as soon as the build's sort
+ * is done, alongside the rest of the build.  Synchronises the stream. */
+int nbr_onepass_build_learned(nbr_onepass op, nbr_capmodel m, nbr_traverser t, nbr_lbvh h, const float* points,
+                              unsigned int N, const float lo[3], const float hi[3], float rc, const float box[3],
+                              float pad, int periodic, int rows_sorted, unsigned int cap_max,
+                              const unsigned int* map, unsigned int block_size, void* stream,
+                              unsigned long long* slots, unsigned int* overflow_rows,
+                              unsigned long long* overflow_slots);
 /* The list of the last build: entries, row offsets (uint64[N]), capacities, counts, total slots. */
 int nbr_onepass_get(nbr_onepass op, const unsigned int** list, const unsigned long long** offsets,
                     const unsigned int** caps, const unsigned int** nneigh, unsigned long long* total);

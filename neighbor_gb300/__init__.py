@@ -124,6 +124,8 @@ def _declare(L):
     sig("nbr_onepass_build", [_P, _P, _P, _F, _P, _F, _I, _I, _U, _P, _U, _P,
                               ctypes.POINTER(_ULL), ctypes.POINTER(_U), ctypes.POINTER(_ULL)])
     sig("nbr_onepass_get", [_P, _PP, _PP, _PP, _PP, ctypes.POINTER(_ULL)])
+    sig("nbr_onepass_build_learned", [_P, _P, _P, _P, _P, _U, _P, _P, _F, _P, _F, _I, _I, _U, _P, _U, _P,
+                                      ctypes.POINTER(_ULL), ctypes.POINTER(_U), ctypes.POINTER(_ULL)])
     sig("nbr_onepass_scan", [_P, _P, _U, _P, ctypes.POINTER(_ULL), _P])
 
 
@@ -143,7 +145,7 @@ EXPORTED = ["nbr_last_error", "nbr_version", "nbr_lbvh_create", "nbr_lbvh_destro
             "nbr_capmodel_level", "nbr_capmodel_features", "nbr_capmodel_predict",
             "nbr_capmodel_targets", "nbr_capmodel_gradient", "nbr_capmodel_train",
             "nbr_onepass_create", "nbr_onepass_destroy", "nbr_onepass_capacity",
-            "nbr_onepass_build", "nbr_onepass_get", "nbr_onepass_scan"]
+            "nbr_onepass_build", "nbr_onepass_get", "nbr_onepass_scan", "nbr_onepass_build_learned"]
 
 CAP_PARAMS = 6337
 CAP_FEATURES = 32
@@ -633,6 +635,22 @@ class OnePassList:
                                          1 if periodic else 0, 1 if rows_sorted else 0, int(cap_max), _ptr(m),
                                          block_size, _stream_ptr(stream), ctypes.byref(slots),
                                          ctypes.byref(ovf), ctypes.byref(ovf_slots)))
+        return dict(slots=slots.value, overflow_rows=ovf.value, overflow_slots=ovf_slots.value)
+
+    def build_learned(self, model: "CapacityModel", trav: "LBVHTraverser", lbvh: "LBVH", points, lo, hi,
+                      rc: float, box, pad: float, periodic: bool = True, rows_sorted: bool = True,
+                      cap_max: int = 32, map=None, block_size: int = 256, stream=None):
+        """Build the tree of `points`, predict capacities with `model` (on a second stream from the
+        end of the sort on) and fill the list, in one call."""
+        torch = _torch()
+        p = _dev(points, torch.float32, 3)
+        m = None if map is None else _dev(map, torch.int32)
+        slots, ovf, ovf_slots = ctypes.c_ulonglong(), ctypes.c_uint(), ctypes.c_ulonglong()
+        _check(self._L.nbr_onepass_build_learned(self._h, model.handle, trav._h, lbvh.handle, _ptr(p), p.shape[0],
+                                                 _f3(lo), _f3(hi), float(rc), _f3(box), float(pad),
+                                                 1 if periodic else 0, 1 if rows_sorted else 0, int(cap_max),
+                                                 _ptr(m), block_size, _stream_ptr(stream), ctypes.byref(slots),
+                                                 ctypes.byref(ovf), ctypes.byref(ovf_slots)))
         return dict(slots=slots.value, overflow_rows=ovf.value, overflow_slots=ovf_slots.value)
 
     def result(self, N: int):

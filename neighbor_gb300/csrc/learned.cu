@@ -202,6 +202,32 @@ int nbr_onepass_build(nbr_onepass op, nbr_traverser t, nbr_lbvh h, float rc, con
     });
     }
 
+int nbr_onepass_build_learned(nbr_onepass op, nbr_capmodel m, nbr_traverser t, nbr_lbvh h, const float* points,
+                              unsigned int N, const float lo[3], const float hi[3], float rc, const float box[3],
+                              float pad, int periodic, int rows_sorted, unsigned int cap_max,
+                              const unsigned int* map, unsigned int block_size, void* stream,
+                              unsigned long long* slots, unsigned int* overflow_rows,
+                              unsigned long long* overflow_slots)
+    {
+    if (!op || !m || !t || !h || !lo || !hi || !box || (N > 0 && !points)) return fail(NBR_ERR_INVALID, "null argument");
+    if (!valid_block(block_size)) return fail(NBR_ERR_INVALID, "Invalid tuning parameter.");
+    if (cap_max == 0) return fail(NBR_ERR_INVALID, "cap_max must be positive");
+    return guarded([&] {
+        const neighbor::LBVHTraverser::LaunchParameters p(block_size, as_stream(stream));
+        const float3* pts = reinterpret_cast<const float3*>(points);
+        neighbor::OnePassNeighborList::Stats st;
+        if (map)
+            st = op->list.buildLearned(p, h->lbvh, t->trav, m->model, pts, N, f3(lo), f3(hi), rc, f3(box), pad,
+                                       periodic != 0, rows_sorted != 0, cap_max, neighbor::MapTransformOp(map));
+        else
+            st = op->list.buildLearned(p, h->lbvh, t->trav, m->model, pts, N, f3(lo), f3(hi), rc, f3(box), pad,
+                                       periodic != 0, rows_sorted != 0, cap_max, neighbor::NullTransformOp());
+        if (slots) *slots = st.slots;
+        if (overflow_rows) *overflow_rows = st.overflow_rows;
+        if (overflow_slots) *overflow_slots = st.overflow_slots;
+    });
+    }
+
 int nbr_onepass_get(nbr_onepass op, const unsigned int** list, const unsigned long long** offsets,
                     const unsigned int** caps, const unsigned int** nneigh, unsigned long long* total)
     {

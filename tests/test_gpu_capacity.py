@@ -214,3 +214,35 @@ def test_trained_capacities_are_exact_and_beat_a_constant_capacity():
     assert plain["slots"] <= learned["slots"]
     assert learned["overflow_rows"] * 5 < plain["overflow_rows"], (learned, plain)
     assert learned["overflow_rows"] < 0.05 * N
+
+
+@pytest.mark.parametrize("rows_sorted", [True, False])
+def test_learned_step_in_one_call_matches_separate_calls(rows_sorted):
+    # the one-call form predicts on a second stream from the end of the sort on; capacities,
+    # counts and every row must equal those of build + predict + one-pass fill done in sequence
+    P, L = _clustered(80000, 12)
+    rc = 1.0
+    box = [L, L, L]
+    pad = nb.exact_pad(rc, 2 * L)
+    model = nb.CapacityModel(seed=13)
+    rng = np.random.default_rng(14)
+    model.set_params(model.params() + (rng.normal(size=nb.CAP_PARAMS) * 0.05).astype(np.float32))
+    model.margin = 0.3
+    N = len(P)
+    trav = nb.LBVHTraverser()
+    lbvh = _tree(P, L)
+    op_a = nb.OnePassList()
+    model.predict(lbvh, [0, 0, 0], box, rc, rows_sorted=rows_sorted, cap_max=32, caps=op_a.capacity(N))
+    st_a = op_a.build(trav, lbvh, rc, box, pad, rows_sorted=rows_sorted, cap_max=32)
+    lbvh_b = nb.LBVH(leaf_size=4)
+    op_b = nb.OnePassList()
+    for _ in range(2):  # twice: the second call reuses the side stream and buffers
+        st_b = op_b.build_learned(model, trav, lbvh_b, _t(P), [0, 0, 0], box, rc, box, pad,
+                                  rows_sorted=rows_sorted, cap_max=32)
+        assert st_b == st_a
+        a, b = op_a.result(N), op_b.result(N)
+        assert torch.equal(a["nneigh"], b["nneigh"])
+        assert torch.equal(a["offsets"], b["offsets"])
+        assert torch.equal(a["caps"], b["caps"])
+        cnt, lst = _plain_rows(lbvh, rc, L, rows_sorted=rows_sorted)
+        _csr_equals_rows(b, cnt, lst)

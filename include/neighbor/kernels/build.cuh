@@ -479,13 +479,13 @@ static __global__ void __launch_bounds__(kScanBlock) k_scan_exclusive(const unsi
     }
 
 // ---------------------------------------------------------------------------------------------
-// Root-box frame of the record bins from the bounds words.
+// Root-box frame of the record bins from the root box (or from the bounds words).
 // ---------------------------------------------------------------------------------------------
-__device__ __forceinline__ QuantFrame frame_from_bounds(const unsigned int* bounds)
+__device__ __forceinline__ QuantFrame frame_from_box(const float3& lo, const float3& hi)
     {
     QuantFrame f;
-    f.lo = make_float3(ordered_to_float(~bounds[0]), ordered_to_float(~bounds[1]), ordered_to_float(~bounds[2]));
-    f.hi = make_float3(ordered_to_float(bounds[3]), ordered_to_float(bounds[4]), ordered_to_float(bounds[5]));
+    f.lo = lo;
+    f.hi = hi;
     float ex = approx::fsub_ru(f.hi.x, f.lo.x);
     float ey = approx::fsub_ru(f.hi.y, f.lo.y);
     float ez = approx::fsub_ru(f.hi.z, f.lo.z);
@@ -495,6 +495,13 @@ __device__ __forceinline__ QuantFrame frame_from_bounds(const unsigned int* boun
     f.scale = make_float3(approx::fdiv_rd((float)kBinMax, ex), approx::fdiv_rd((float)kBinMax, ey),
                           approx::fdiv_rd((float)kBinMax, ez));
     return f;
+    }
+
+__device__ __forceinline__ QuantFrame frame_from_bounds(const unsigned int* bounds)
+    {
+    return frame_from_box(
+        make_float3(ordered_to_float(~bounds[0]), ordered_to_float(~bounds[1]), ordered_to_float(~bounds[2])),
+        make_float3(ordered_to_float(bounds[3]), ordered_to_float(bounds[4]), ordered_to_float(bounds[5])));
     }
 
 // ---------------------------------------------------------------------------------------------

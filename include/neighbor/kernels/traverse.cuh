@@ -266,21 +266,24 @@ __device__ __forceinline__ unsigned int axis_images(float p, float rs, float L, 
     return m;
     }
 
+// Lattice images (bit i = 9*(ix+1) + 3*(iy+1) + (iz+1) of the 27) whose padded query box meets
+// the root box: the per-axis masks replicated into 27 bits.
+__device__ __forceinline__ unsigned int lattice_flags(const float3& L, const QuantFrame& f, const float3& p, float rs)
+    {
+    const unsigned int mx = axis_images(p.x, rs, L.x, f.lo.x, f.hi.x);
+    const unsigned int my = axis_images(p.y, rs, L.y, f.lo.y, f.hi.y);
+    const unsigned int mz = axis_images(p.z, rs, L.z, f.lo.z, f.hi.z);
+    const unsigned int X = ((mx & 1u) ? 0x1ffu : 0u) | ((mx & 2u) ? 0x3fe00u : 0u) | ((mx & 4u) ? 0x7fc0000u : 0u);
+    const unsigned int Y = (((my & 1u) ? 0x7u : 0u) | ((my & 2u) ? 0x38u : 0u) | ((my & 4u) ? 0x1c0u : 0u)) * 0x40201u;
+    const unsigned int Z = mz * 0x1249249u;
+    return X & Y & Z;
+    }
+
 // Images whose padded query box meets the root box.
 __device__ __forceinline__ unsigned int image_flags(const FastQueryArgs& a, const QuantFrame& f,
                                                     const float3& p, float rs)
     {
-    if (a.lattice)
-        {
-        // image i = 9*(ix+1) + 3*(iy+1) + (iz+1): replicate the per-axis masks into 27 bits
-        const unsigned int mx = axis_images(p.x, rs, a.lattice_L.x, f.lo.x, f.hi.x);
-        const unsigned int my = axis_images(p.y, rs, a.lattice_L.y, f.lo.y, f.hi.y);
-        const unsigned int mz = axis_images(p.z, rs, a.lattice_L.z, f.lo.z, f.hi.z);
-        const unsigned int X = ((mx & 1u) ? 0x1ffu : 0u) | ((mx & 2u) ? 0x3fe00u : 0u) | ((mx & 4u) ? 0x7fc0000u : 0u);
-        const unsigned int Y = (((my & 1u) ? 0x7u : 0u) | ((my & 2u) ? 0x38u : 0u) | ((my & 4u) ? 0x1c0u : 0u)) * 0x40201u;
-        const unsigned int Z = mz * 0x1249249u;
-        return X & Y & Z;
-        }
+    if (a.lattice) return lattice_flags(a.lattice_L, f, p, rs);
     const unsigned int nimg = a.images ? min(a.n_images, 32u) : 1u;
     unsigned int flags = 0;
     for (unsigned int i = 0; i < nimg; ++i)
@@ -425,16 +428,7 @@ struct HalfArgs
 __device__ __forceinline__ unsigned int half_image_flags(const HalfArgs& a, const QuantFrame& f,
                                                          const float3& p, float rs)
     {
-    if (a.lattice)
-        {
-        const unsigned int mx = axis_images(p.x, rs, a.lattice_L.x, f.lo.x, f.hi.x);
-        const unsigned int my = axis_images(p.y, rs, a.lattice_L.y, f.lo.y, f.hi.y);
-        const unsigned int mz = axis_images(p.z, rs, a.lattice_L.z, f.lo.z, f.hi.z);
-        const unsigned int X = ((mx & 1u) ? 0x1ffu : 0u) | ((mx & 2u) ? 0x3fe00u : 0u) | ((mx & 4u) ? 0x7fc0000u : 0u);
-        const unsigned int Y = (((my & 1u) ? 0x7u : 0u) | ((my & 2u) ? 0x38u : 0u) | ((my & 4u) ? 0x1c0u : 0u)) * 0x40201u;
-        const unsigned int Z = mz * 0x1249249u;
-        return X & Y & Z;
-        }
+    if (a.lattice) return lattice_flags(a.lattice_L, f, p, rs);
     const bool hit = approx::fsub_rd(p.x, rs) <= f.hi.x && approx::fadd_ru(p.x, rs) >= f.lo.x
                      && approx::fsub_rd(p.y, rs) <= f.hi.y && approx::fadd_ru(p.y, rs) >= f.lo.y
                      && approx::fsub_rd(p.z, rs) <= f.hi.z && approx::fadd_ru(p.z, rs) >= f.lo.z;

@@ -256,6 +256,39 @@ int nbr_onepass_get(nbr_onepass op, const unsigned int** list, const unsigned lo
 int nbr_onepass_scan(nbr_onepass op, const unsigned int* counts, unsigned int n,
                      unsigned long long* offsets, unsigned long long* total, void* stream);
 
+/* ---- Addition with no counterpart in the reference: batched ensembles of small systems. ----
+ * Many independent periodic systems (at most NBR_BATCH_MAX_N points each) built and listed in
+ * one launch.  start: host uint[S+1] (system s = points [start[s], start[s+1])), box: host
+ * float[3S] periodic lengths (system s's scene is [0, box)), rc cutoff, max_neigh list capacity
+ * per point.  Outputs per point of the batch: nneigh[T] and list[T * max_neigh] with global
+ * point indices; each system's result equals nbr_lbvh_build_points + nbr_traverse_self (27
+ * periodic images, rows by primitive) on that system alone. */
+#define NBR_BATCH_MAX_N 16384
+typedef struct nbr_batch_s* nbr_batch;
+int nbr_batch_create(nbr_batch* out);
+int nbr_batch_destroy(nbr_batch b);
+int nbr_batch_setup(nbr_batch b, const unsigned int* start, const float* box, unsigned int S, float rc,
+                    unsigned int max_neigh);
+/* Leaf size (1..64) and threads per block (512 or 1024) of the batched kernel. */
+int nbr_batch_set_config(nbr_batch b, unsigned int leaf_size, unsigned int block);
+int nbr_batch_get_config(nbr_batch b, unsigned int* leaf_size, unsigned int* block);
+int nbr_batch_run(nbr_batch b, const float* points, unsigned int* nneigh, unsigned int* list, void* stream);
+/* Autotuner: times every configuration on this batch and keeps the fastest (synchronises). */
+int nbr_batch_tune(nbr_batch b, const float* points, unsigned int* nneigh, unsigned int* list, void* stream,
+                   unsigned int* leaf_size, unsigned int* block);
+/* Capture a run (current configuration, these buffers) in a CUDA graph on `stream` (not the
+ * legacy default stream); nbr_batch_replay launches the graph. */
+int nbr_batch_capture(nbr_batch b, const float* points, unsigned int* nneigh, unsigned int* list, void* stream);
+int nbr_batch_replay(nbr_batch b, void* stream);
+/* After a run (synchronises): status bits (1 = a system above NBR_BATCH_MAX_N was skipped) and the
+ * largest count (rows with more than max_neigh entries keep max_neigh). */
+int nbr_batch_status(nbr_batch b, unsigned int* bits, unsigned int* largest, void* stream);
+/* The same work as one plain call per system: build, count, host read of the largest count, fill
+ * (for comparison with the batched form).  List entries are system-local primitive ids. */
+int nbr_batch_sequential_plain(nbr_lbvh h, nbr_traverser t, const float* points, const unsigned int* start,
+                               const float* box, unsigned int S, float rc, unsigned int* nneigh, unsigned int* list,
+                               unsigned int max_neigh, unsigned int block_size, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

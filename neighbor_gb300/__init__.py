@@ -124,6 +124,17 @@ def _declare(L):
     sig("nbr_onepass_build", [_P, _P, _P, _F, _P, _F, _I, _I, _U, _P, _U, _P,
                               ctypes.POINTER(_ULL), ctypes.POINTER(_U), ctypes.POINTER(_ULL)])
     sig("nbr_onepass_get", [_P, _PP, _PP, _PP, _PP, ctypes.POINTER(_ULL)])
+    sig("nbr_batch_create", [_PP])
+    sig("nbr_batch_destroy", [_P])
+    sig("nbr_batch_setup", [_P, _P, _P, _U, _F, _U])
+    sig("nbr_batch_set_config", [_P, _U, _U])
+    sig("nbr_batch_get_config", [_P, ctypes.POINTER(_U), ctypes.POINTER(_U)])
+    sig("nbr_batch_run", [_P, _P, _P, _P, _P])
+    sig("nbr_batch_tune", [_P, _P, _P, _P, _P, ctypes.POINTER(_U), ctypes.POINTER(_U)])
+    sig("nbr_batch_capture", [_P, _P, _P, _P, _P])
+    sig("nbr_batch_replay", [_P, _P])
+    sig("nbr_batch_status", [_P, ctypes.POINTER(_U), ctypes.POINTER(_U), _P])
+    sig("nbr_batch_sequential_plain", [_P, _P, _P, _P, _P, _U, _F, _P, _P, _U, _U, _P])
     sig("nbr_onepass_build_learned", [_P, _P, _P, _P, _P, _U, _P, _P, _F, _P, _F, _I, _I, _U, _P, _U, _P,
                                       ctypes.POINTER(_ULL), ctypes.POINTER(_U), ctypes.POINTER(_ULL)])
     sig("nbr_onepass_scan", [_P, _P, _U, _P, ctypes.POINTER(_ULL), _P])
@@ -145,7 +156,12 @@ EXPORTED = ["nbr_last_error", "nbr_version", "nbr_lbvh_create", "nbr_lbvh_destro
             "nbr_capmodel_level", "nbr_capmodel_features", "nbr_capmodel_predict",
             "nbr_capmodel_targets", "nbr_capmodel_gradient", "nbr_capmodel_train",
             "nbr_onepass_create", "nbr_onepass_destroy", "nbr_onepass_capacity",
-            "nbr_onepass_build", "nbr_onepass_get", "nbr_onepass_scan", "nbr_onepass_build_learned"]
+            "nbr_onepass_build", "nbr_onepass_get", "nbr_onepass_scan", "nbr_onepass_build_learned",
+            "nbr_batch_create", "nbr_batch_destroy", "nbr_batch_setup", "nbr_batch_set_config",
+            "nbr_batch_get_config", "nbr_batch_run", "nbr_batch_tune", "nbr_batch_capture",
+            "nbr_batch_replay", "nbr_batch_status", "nbr_batch_sequential_plain"]
+
+BATCH_MAX_N = 16384
 
 CAP_PARAMS = 6337
 CAP_FEATURES = 32
@@ -675,3 +691,72 @@ class OnePassList:
         _check(self._L.nbr_onepass_scan(self._h, _ptr(c), c.shape[0], _ptr(out), ctypes.byref(total),
                                         _stream_ptr(stream)))
         return out, total.value
+
+
+class BatchedList:
+    """Many independent small periodic systems, built and listed in one launch."""
+
+    def __init__(self):
+        self._L = load()
+        h = ctypes.c_void_p()
+        _check(self._L.nbr_batch_create(ctypes.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            self._L.nbr_batch_destroy(self._h)
+            self._h = None
+
+    def setup(self, start, boxes, rc: float, max_neigh: int):
+        """start: S + 1 point offsets, boxes: S x 3 periodic lengths (host sequences)."""
+        import numpy as np
+        st = np.ascontiguousarray(start, np.uint32)
+        bx = np.ascontiguousarray(boxes, np.float32).reshape(-1)
+        S = len(st) - 1
+        self.S, self.T, self.max_neigh = S, int(st[-1]), int(max_neigh)
+        self._start, self._boxes = st, bx
+        _check(self._L.nbr_batch_setup(self._h, st.ctypes.data_as(ctypes.c_void_p),
+                                       bx.ctypes.data_as(ctypes.c_void_p), S, float(rc), int(max_neigh)))
+
+    def outputs(self):
+        torch = _torch()
+        return (torch.empty(max(self.T, 1), dtype=torch.int32, device="cuda"),
+                torch.empty(max(self.T, 1) * max(self.max_neigh, 1), dtype=torch.int32, device="cuda"))
+
+    def set_config(self, leaf_size: int, block: int):
+        _check(self._L.nbr_batch_set_config(self._h, int(leaf_size), int(block)))
+
+    def config(self):
+        leaf, block = ctypes.c_uint(), ctypes.c_uint()
+        _check(self._L.nbr_batch_get_config(self._h, ctypes.byref(leaf), ctypes.byref(block)))
+        return leaf.value, block.value
+
+    def run(self, points, nneigh, lst, stream=None):
+        _check(self._L.nbr_batch_run(self._h, _ptr(points), _ptr(nneigh), _ptr(lst), _stream_ptr(stream)))
+
+    def tune(self, points, nneigh, lst, stream=None):
+        leaf, block = ctypes.c_uint(), ctypes.c_uint()
+        _check(self._L.nbr_batch_tune(self._h, _ptr(points), _ptr(nneigh), _ptr(lst), _stream_ptr(stream),
+                                      ctypes.byref(leaf), ctypes.byref(block)))
+        return leaf.value, block.value
+
+    def capture(self, points, nneigh, lst, stream):
+        _check(self._L.nbr_batch_capture(self._h, _ptr(points), _ptr(nneigh), _ptr(lst), _stream_ptr(stream)))
+
+    def replay(self, stream):
+        _check(self._L.nbr_batch_replay(self._h, _stream_ptr(stream)))
+
+    def status(self, stream=None):
+        bits, largest = ctypes.c_uint(), ctypes.c_uint()
+        _check(self._L.nbr_batch_status(self._h, ctypes.byref(bits), ctypes.byref(largest), _stream_ptr(stream)))
+        return bits.value, largest.value
+
+    def sequential_plain(self, lbvh: "LBVH", trav: "LBVHTraverser", points, rc: float, nneigh, lst,
+                         block_size: int = 256, stream=None):
+        """The same lists by one plain two-pass call per system (build, count, max, fill); list
+        entries are system-local primitive ids."""
+        _check(self._L.nbr_batch_sequential_plain(lbvh.handle, trav._h, _ptr(points),
+                                                  self._start.ctypes.data_as(ctypes.c_void_p),
+                                                  self._boxes.ctypes.data_as(ctypes.c_void_p), self.S,
+                                                  float(rc), _ptr(nneigh), _ptr(lst), self.max_neigh,
+                                                  block_size, _stream_ptr(stream)))

@@ -10,7 +10,7 @@ INCLUDE = os.path.join(ROOT, "include")
 BUILD_DIR = os.path.join(PKG, "_build")
 LIB_NAME = "libneighbor_gb300.so"
 LIB_PATH = os.path.join(BUILD_DIR, LIB_NAME)
-SOURCES = [os.path.join(PKG, "csrc", n) for n in ("capi.cu", "noalloc.cu", "learned.cu")]
+SOURCES = [os.path.join(PKG, "csrc", n) for n in ("capi.cu", "noalloc.cu", "learned.cu", "batched.cu")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

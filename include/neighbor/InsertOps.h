@@ -51,6 +51,25 @@ struct SphereInsertOp
     const unsigned int N;
     };
 
+// Addition: points given in double precision (HOOMD-blue's Scalar = double); each leaf box is
+// the point rounded outward to FP32 (BoundingBox(double3, double3),
+// include/neighbor/BoundingVolumes.h:54-58 of the reference), so it always contains the point.
+struct PointInsertOpF64
+    {
+    PointInsertOpF64(const double3* points_, unsigned int N_) : points(points_), N(N_) {}
+
+    __device__ __forceinline__ BoundingBox get(const unsigned int idx) const
+        {
+        const double3 p = points[idx];
+        return BoundingBox(p, p);
+        }
+
+    __host__ __device__ __forceinline__ unsigned int size() const { return N; }
+
+    const double3* points;
+    const unsigned int N;
+    };
+
 // Trait: does this insert op store bare points, so that the leaf payload (sorted positions) can
 // serve the exact-sphere fast traversal?  User ops default to "no".
 template<class InsertOpT>

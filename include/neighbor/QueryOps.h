@@ -93,6 +93,74 @@ inline float exact_query_pad(float rc, float coord_max)
     return 16.0f * std::ldexp(1.0f, e - 24) + std::fabs(rc) * 1.0e-6f;
     }
 
+// Addition: the exact predicate in double precision -- d = pj - pi, wrapped once by +-L when
+// |d| >= L/2, ((dx*dx + dy*dy) + dz*dz) <= rc*rc, every operation rounded to nearest and none
+// contracted -- for double positions (PointInsertOpF64 trees).
+__device__ __forceinline__ double min_image_component_f64(double d, double L)
+    {
+    if (L > 0.0)
+        {
+        const double h = __dmul_rn(0.5, L);
+        if (d >= h)
+            d = __dsub_rn(d, L);
+        else if (d < -h)
+            d = __dadd_rn(d, L);
+        }
+    return d;
+    }
+
+__device__ __forceinline__ bool exact_pair_f64(const double3& pi, const double3& pj, double rc, const double3& L)
+    {
+    const double dx = min_image_component_f64(__dsub_rn(pj.x, pi.x), L.x);
+    const double dy = min_image_component_f64(__dsub_rn(pj.y, pi.y), L.y);
+    const double dz = min_image_component_f64(__dsub_rn(pj.z, pi.z), L.z);
+    const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+    return d2 <= __dmul_rn(rc, rc);
+    }
+
+// Addition: exact sphere query on double positions.  The traversal volume is the double sphere
+// (radius + pad) enclosed by an FP32 sphere (BoundingSphere(double3, double)); refine applies
+// exact_pair_f64.  Image translations are FP32 (the translate ops' type), so pad must cover their
+// rounding as well: exact_query_pad(rc, 2 * largest coordinate) does.  With box lengths above
+// 2 (rc + pad) every neighbor is found through exactly one image.
+struct ExactSphereQueryOpF64
+    {
+    ExactSphereQueryOpF64(const double4* spheres_, unsigned int N_, const double3* points_, double3 box_,
+                          float pad_)
+        : spheres(spheres_), N(N_), points(points_), box(box_), pad(pad_)
+        {}
+
+    typedef double4 ThreadData;
+    typedef BoundingSphere Volume;
+
+    __device__ __forceinline__ ThreadData setup(const unsigned int idx) const { return spheres[idx]; }
+
+    __device__ __forceinline__ Volume get(const ThreadData& q, const float3& image) const
+        {
+        const double3 t = make_double3(__dadd_rn(q.x, (double)image.x), __dadd_rn(q.y, (double)image.y),
+                                       __dadd_rn(q.z, (double)image.z));
+        return BoundingSphere(t, __dadd_ru(q.w, (double)pad));
+        }
+
+    __device__ __forceinline__ bool overlap(const Volume& v, const BoundingBox& box_) const
+        {
+        return v.overlap(box_);
+        }
+
+    __device__ __forceinline__ bool refine(const ThreadData& q, const int primitive) const
+        {
+        return exact_pair_f64(make_double3(q.x, q.y, q.z), points[primitive], q.w, box);
+        }
+
+    __host__ __device__ __forceinline__ unsigned int size() const { return N; }
+
+    const double4* spheres;
+    const unsigned int N;
+    const double3* points;
+    const double3 box;
+    const float pad;
+    };
+
 struct ExactSphereQueryOp
     {
     // spheres: (x, y, z, cutoff) per query.  points: positions indexed by the primitive id that

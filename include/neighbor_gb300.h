@@ -172,6 +172,21 @@ int nbr_morton_sort_noalloc(const float* points, unsigned int N, const float lo[
                             const float hi[3], unsigned int* codes_out, unsigned int* order_out,
                             void* stream);
 
+/* Addition (double-precision inputs, e.g. HOOMD-blue built with Scalar = double): LBVH::build
+ * with PointInsertOpF64 -- each point's box is the point rounded outward to FP32
+ * (BoundingBox(double3, double3), include/neighbor/BoundingVolumes.h:54-58). */
+int nbr_lbvh_build_points_f64(nbr_lbvh h, const double* points, unsigned int N, const float lo[3],
+                              const float hi[3], unsigned int block_size, void* stream);
+
+/* Addition: LBVHTraverser::traverse with ExactSphereQueryOpF64 over a tree of double points:
+ * spheres double[4Q] (x, y, z, cutoff), points double[3N] indexed by the reported id, box double[3]
+ * periodic lengths (0 = open), pad as nbr_exact_pad; images, map and outputs as nbr_traverse.
+ * Runs the reference-layout rope traversal with the exact double predicate. */
+int nbr_traverse_f64(nbr_traverser t, nbr_lbvh h, const double* spheres, unsigned int Q, const double* points,
+                     const double box[3], float pad, const float* images, unsigned int n_images,
+                     const unsigned int* map, unsigned int* nneigh, unsigned int* list, unsigned int max_neigh,
+                     unsigned int block_size, void* stream);
+
 /* Radius padding for the exact query: 16 ulps of twice the largest coordinate magnitude
  * (centres, points and image translations) plus 1e-6 * rc. */
 float nbr_exact_pad(float rc, float coord_max);

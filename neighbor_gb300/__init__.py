@@ -102,6 +102,8 @@ def _declare(L):
     sig("nbr_traverse", [_P, _P, _I, _P, _U, _P, _P, _F, _P, _U, _P, _P, _P, _U, _U, _P])
     sig("nbr_traverse_self", [_P, _P, _F, _P, _F, _P, _U, _P, _P, _P, _U, _I, _U, _P])
     sig("nbr_exact_pad", [_F, _F], _F)
+    sig("nbr_lbvh_build_points_f64", [_P, _P, _U, _P, _P, _U, _P])
+    sig("nbr_traverse_f64", [_P, _P, _P, _U, _P, _P, _F, _P, _U, _P, _P, _P, _U, _U, _P])
     sig("nbr_debug_wait_timeout", [ctypes.POINTER(_U), _P])
     sig("nbr_morton_sort_noalloc", [_P, _U, _P, _P, _P, _P, _P])
     _ULL = ctypes.c_ulonglong
@@ -159,7 +161,8 @@ EXPORTED = ["nbr_last_error", "nbr_version", "nbr_lbvh_create", "nbr_lbvh_destro
             "nbr_onepass_build", "nbr_onepass_get", "nbr_onepass_scan", "nbr_onepass_build_learned",
             "nbr_batch_create", "nbr_batch_destroy", "nbr_batch_setup", "nbr_batch_set_config",
             "nbr_batch_get_config", "nbr_batch_run", "nbr_batch_tune", "nbr_batch_capture",
-            "nbr_batch_replay", "nbr_batch_status", "nbr_batch_sequential_plain"]
+            "nbr_batch_replay", "nbr_batch_status", "nbr_batch_sequential_plain",
+            "nbr_lbvh_build_points_f64", "nbr_traverse_f64"]
 
 BATCH_MAX_N = 16384
 
@@ -301,6 +304,13 @@ class LBVH:
 
     def set_radix_bits(self, bits: int):
         _check(self._L.nbr_lbvh_set_radix_bits(self._h, int(bits)))
+
+    def build_f64(self, points, lo, hi, block_size: int = 32, stream=None):
+        """LBVH::build with PointInsertOpF64: points is a CUDA float64 [N, 3] tensor."""
+        torch = _torch()
+        p = _dev(points, torch.float64, 3)
+        _check(self._L.nbr_lbvh_build_points_f64(self._h, _ptr(p), p.shape[0], _f3(lo), _f3(hi), block_size,
+                                                 _stream_ptr(stream)))
 
     def set_climb_block(self, leaves: int):
         """Sorted leaves per block of the build's agglomerative climb (128, 256 or 512)."""
@@ -473,6 +483,32 @@ class LBVHTraverser:
                                     _ptr(m), _ptr(nneigh), _ptr(lst),
                                     0 if max_neigh is None else int(max_neigh), block_size,
                                     _stream_ptr(stream)))
+        if max_neigh is None:
+            return nneigh
+        return nneigh, lst
+
+    def traverse_f64(self, lbvh: LBVH, spheres, points, box, pad: float, images=None, map=None,
+                     max_neigh: Optional[int] = None, nneigh=None, neigh_list=None, block_size: int = 32,
+                     stream=None):
+        """Exact sphere queries on double positions (ExactSphereQueryOpF64): spheres float64 [Q, 4],
+        points float64 [N, 3], box the periodic lengths (0 = open), images as traverse()."""
+        torch = _torch()
+        sph = _dev(spheres, torch.float64, 4)
+        pts = _dev(points, torch.float64, 3)
+        Q = sph.shape[0]
+        lattice = isinstance(images, str) and images == "periodic"
+        img = None if images is None or lattice else _dev(images, torch.float32, 3)
+        m = None if map is None else _dev(map, torch.int32)
+        if nneigh is None:
+            nneigh = torch.empty(Q, dtype=torch.int32, device=sph.device)
+        lst = neigh_list
+        if max_neigh is not None and lst is None:
+            lst = torch.full((Q, max(max_neigh, 1)), -1, dtype=torch.int32, device=sph.device)
+        b = (ctypes.c_double * 3)(*[float(x) for x in box])
+        _check(self._L.nbr_traverse_f64(self._h, lbvh.handle, _ptr(sph), Q, _ptr(pts), b, float(pad), _ptr(img),
+                                        27 if lattice else (0 if img is None else img.shape[0]), _ptr(m),
+                                        _ptr(nneigh), _ptr(lst), 0 if max_neigh is None else int(max_neigh),
+                                        block_size, _stream_ptr(stream)))
         if max_neigh is None:
             return nneigh
         return nneigh, lst

@@ -341,6 +341,56 @@ int nbr_traverse_self(nbr_traverser t, nbr_lbvh h, float rc, const float box[3],
 
 float nbr_exact_pad(float rc, float coord_max) { return neighbor::exact_query_pad(rc, coord_max); }
 
+int nbr_lbvh_build_points_f64(nbr_lbvh h, const double* points, unsigned int N, const float lo[3],
+                              const float hi[3], unsigned int block_size, void* stream)
+    {
+    if (!h || !lo || !hi || (N > 0 && !points)) return fail(NBR_ERR_INVALID, "null argument");
+    if (!valid_block(block_size)) return fail(NBR_ERR_INVALID, "Invalid tuning parameter.");
+    return guarded([&] {
+        h->lbvh.build(neighbor::LBVH::LaunchParameters(block_size, as_stream(stream)),
+                      neighbor::PointInsertOpF64(reinterpret_cast<const double3*>(points), N), f3(lo), f3(hi));
+    });
+    }
+
+int nbr_traverse_f64(nbr_traverser t, nbr_lbvh h, const double* spheres, unsigned int Q, const double* points,
+                     const double box[3], float pad, const float* images, unsigned int n_images,
+                     const unsigned int* map, unsigned int* nneigh, unsigned int* list, unsigned int max_neigh,
+                     unsigned int block_size, void* stream)
+    {
+    if (!t || !h || !box) return fail(NBR_ERR_INVALID, "null argument");
+    if (Q > 0 && (!spheres || !points || !nneigh)) return fail(NBR_ERR_INVALID, "null argument");
+    if (list && max_neigh == 0) return fail(NBR_ERR_INVALID, "max_neigh must be positive with a list");
+    if (images && n_images > 32) return fail(NBR_ERR_INVALID, "A maximum of 32 image vectors are supported by LBVH traversers.");
+    if (!valid_block(block_size)) return fail(NBR_ERR_INVALID, "Invalid tuning parameter.");
+    return guarded([&] {
+        const neighbor::LBVHTraverser::LaunchParameters p(block_size, as_stream(stream));
+        const double3 b = make_double3(box[0], box[1], box[2]);
+        const neighbor::ExactSphereQueryOpF64 q(reinterpret_cast<const double4*>(spheres), Q,
+                                                reinterpret_cast<const double3*>(points), b, pad);
+        const float3 bf = make_float3((float)box[0], (float)box[1], (float)box[2]);
+        auto go = [&](const auto& out) {
+            auto with_images = [&](const auto& transform) {
+                if (images)
+                    t->trav.traverse(p, h->lbvh, q, out,
+                                     neighbor::ImageListOp<float3>(reinterpret_cast<const float3*>(images), n_images),
+                                     transform);
+                else if (n_images == 27)
+                    t->trav.traverse(p, h->lbvh, q, out, neighbor::PeriodicImagesOp(bf), transform);
+                else
+                    t->trav.traverse(p, h->lbvh, q, out, neighbor::SelfOp(), transform);
+            };
+            if (map)
+                with_images(neighbor::MapTransformOp(map));
+            else
+                with_images(neighbor::NullTransformOp());
+        };
+        if (list)
+            go(neighbor::NeighborListOp(list, nneigh, max_neigh));
+        else
+            go(neighbor::CountNeighborsOp(nneigh));
+    });
+    }
+
 int nbr_debug_wait_timeout(unsigned int* status_out, void* stream)
     {
     if (!status_out) return fail(NBR_ERR_INVALID, "null argument");

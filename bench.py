@@ -59,6 +59,17 @@ def parse():
     return ap.parse_args()
 
 
+def stage_traffic(stage, n):
+    """DRAM bytes of one stage per launch, scaled from the committed ncu summary (bytes per point
+    of an 8M-point capture; the traffic grows with the points), or None."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "stage_traffic.json")) as f:
+            t = json.load(f)
+        return t[stage]["dram_bytes_per_point"] * n / 1e9
+    except Exception:
+        return None
+
+
 def load_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -612,8 +623,7 @@ def run_ours(args):
     t_start = ev()
     t_end = ev()
     t_start.record(stream)
-    for k in range(args.steps):
-        step(frames[args.warmup + k], recs[k])
+    step_max = [step(frames[args.warmup + k], recs[k]) for k in range(args.steps)]
     t_end.record(stream)
     torch.cuda.synchronize()
     barrier(ws)
@@ -687,6 +697,10 @@ def run_ours(args):
     # (16 B payload) and writes a count (4 B); fill additionally writes 4 B per pair
     alg = {"build": 12.0 * n, "count": 20.0 * n, "fill": 20.0 * n + 4.0 * pairs_step}
     dom = max(stages, key=stages.get)
+    passes = (30 + args.radix_bits - 1) // args.radix_bits
+    build_launches = 2 + passes + 1 + (1 if n > args.climb else 0) + 2
+    launches_per_step = [build_launches + 1 + (2 if 0 < m <= 32 and args.mode == 0 else 1)
+                         for m in step_max]
     achieved = alg[dom] / (stages[dom] * 1e-3) / 1e9
     step_bytes = 12.0 * n + 16.0 * n + 4.0 * n + 4.0 * pairs_step
     line = {
@@ -714,11 +728,11 @@ def run_ours(args):
         "pairs_per_step": pairs_step,
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
-                     "traffic": None,
+                     "traffic": stage_traffic(dom, n),
                      "step_achieved": step_bytes / (ms_max / args.steps * 1e-3) / 1e9},
-        # per step: histogram, digit offsets, one onesweep per pass, root, hierarchy, scan,
-        # bubble (build) + count traversal + fill traversal
-        "gpu_launches": args.steps * (9 + (4 if args.radix_bits == 8 else 3)),
+        # per step: histogram, digit offsets, one onesweep per pass, climb, climb across blocks,
+        # scan, emit (build) + count traversal + fill traversal (+ row ordering for rows <= 32)
+        "gpu_launches": sum(launches_per_step),
         "clocks": clocks,
         "e2e": e2e,
         "check_vs_oracle": check,

@@ -77,6 +77,10 @@ int nbr_lbvh_get_arrays(nbr_lbvh h, const int** parent, const int** left, const 
 /* Addition: sorted Morton codes of the last build (managed pointer). */
 int nbr_lbvh_get_codes(nbr_lbvh h, const unsigned int** codes);
 
+/* getPrimitives (LBVH.h:135-169) alone: the sorted primitive order (managed pointer), without
+ * forming the reference-layout tree arrays that nbr_lbvh_get_arrays makes current. */
+int nbr_lbvh_get_primitives(nbr_lbvh h, const unsigned int** primitive);
+
 /* Addition: the traversal tree (device pointers): records uint32[4*n] in depth-first pre-order
  * (box record {16-bit bins, skip} or point record {x, y, z, 0x80000000 | primitive id}),
  * points float4[N] (sorted x, y, z, primitive id bits), frame float[9] (root lo, root hi,

@@ -87,6 +87,7 @@ def _declare(L):
                                ctypes.POINTER(_U)])
     sig("nbr_lbvh_get_arrays", [_P, _PP, _PP, _PP, _PP, _PP, _PP])
     sig("nbr_lbvh_get_codes", [_P, _PP])
+    sig("nbr_lbvh_get_primitives", [_P, _PP])
     sig("nbr_lbvh_get_fast", [_P, _PP, _PP, _PP, ctypes.POINTER(_U)])
     sig("nbr_lbvh_num_fast_nodes", [_P, ctypes.POINTER(_U), _P])
     sig("nbr_lbvh_check_status", [_P, _P])
@@ -147,7 +148,7 @@ EXPORTED = ["nbr_last_error", "nbr_version", "nbr_lbvh_create", "nbr_lbvh_destro
             "nbr_lbvh_set_leaf_size", "nbr_lbvh_set_radix_bits", "nbr_lbvh_set_climb_block",
             "nbr_lbvh_build_points",
             "nbr_lbvh_build_spheres", "nbr_lbvh_get_sizes", "nbr_lbvh_get_arrays",
-            "nbr_lbvh_get_codes", "nbr_lbvh_get_fast", "nbr_lbvh_num_fast_nodes",
+            "nbr_lbvh_get_codes", "nbr_lbvh_get_primitives", "nbr_lbvh_get_fast", "nbr_lbvh_num_fast_nodes",
             "nbr_lbvh_check_status", "nbr_traverser_create", "nbr_traverser_destroy",
             "nbr_traverser_setup", "nbr_traverser_reset", "nbr_traverser_set_fast_path",
             "nbr_traverser_set_mode", "nbr_traverser_set_stats", "nbr_traverser_set_symmetric",
@@ -368,9 +369,12 @@ class LBVH:
         )
 
     def primitives(self):
+        """View of the sorted primitive order (getPrimitives())."""
         torch = _torch()
         _, N, _, _ = self.sizes()
-        return _view(self._arrays()[3], (N,), "<u4", torch.int32)
+        p = ctypes.c_void_p()
+        _check(self._L.nbr_lbvh_get_primitives(self._h, ctypes.byref(p)))
+        return _view(p.value, (N,), "<u4", torch.int32)
 
     def codes(self):
         torch = _torch()

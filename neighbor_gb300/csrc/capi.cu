@@ -192,6 +192,13 @@ int nbr_lbvh_get_arrays(nbr_lbvh h, const int** parent, const int** left, const 
     return NBR_OK;
     }
 
+int nbr_lbvh_get_primitives(nbr_lbvh h, const unsigned int** primitive)
+    {
+    if (!h || !primitive) return fail(NBR_ERR_INVALID, "null argument");
+    *primitive = h->lbvh.getPrimitives().get();
+    return NBR_OK;
+    }
+
 int nbr_lbvh_get_codes(nbr_lbvh h, const unsigned int** codes)
     {
     if (!h || !codes) return fail(NBR_ERR_INVALID, "null argument");

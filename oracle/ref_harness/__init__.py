@@ -73,8 +73,9 @@ def run_bench(n, steps=5, warmup=2, rc=1.3, timeout=600):
 
 
 def run_dump(points, lo, hi, rc, box, timeout=300):
-    """The reference's tree arrays, compressed nodes and counts (stock and exact query, 27
-    periodic images of `box`, queries = the points in input order) for the given points."""
+    """The reference's tree arrays, compressed nodes, counts (stock and exact query, 27 periodic
+    images of `box`, queries = the points in input order) and the exact query's neighbor list
+    (stride = the largest count) for the given points."""
     P = np.ascontiguousarray(points, np.float32).reshape(-1, 3)
     n = len(P)
     with tempfile.TemporaryDirectory() as d:
@@ -95,4 +96,9 @@ def run_dump(points, lo, hi, rc, box, timeout=300):
             path = prefix + "." + name
             if os.path.exists(path):
                 out[name] = np.fromfile(path, dt).reshape(shape)
+        lpath = prefix + ".list_exact"
+        if os.path.exists(lpath) and "count_exact" in out and n:
+            stride = max(1, int(out["count_exact"].max()))
+            out["list_exact"] = np.fromfile(lpath, np.uint32).reshape(n, stride)
+            out["count_list"] = np.fromfile(prefix + ".count_list", np.uint32)
         return out

@@ -379,6 +379,7 @@ int run_dump(const Kernels& K, const char* in_path, unsigned int n, float3 slo, 
     check(cudaMemcpy(P, hp.data(), (size_t)n * 12, cudaMemcpyHostToDevice), "copy");
     RefTree T;
     T.allocate(n);
+    unsigned int list_stride = 0;
     T.build(K, P, slo, shi, 32, 0);
     LBVHCompressedData c = T.compress(K, 32, 0);
     std::vector<float3> himg;
@@ -387,8 +388,9 @@ int run_dump(const Kernels& K, const char* in_path, unsigned int n, float3 slo, 
     check(cudaMalloc(&img, 27 * 12), "alloc");
     check(cudaMemcpy(img, himg.data(), 27 * 12, cudaMemcpyHostToDevice), "copy");
     float4* sph;
-    unsigned int *c_stock, *c_exact;
+    unsigned int *c_stock, *c_exact, *c_list, *list;
     check(cudaMalloc(&sph, (size_t)n * 16), "alloc");
+    check(cudaMalloc(&c_list, (size_t)n * 4), "alloc");
     check(cudaMalloc(&c_stock, (size_t)n * 4), "alloc");
     check(cudaMalloc(&c_exact, (size_t)n * 4), "alloc");
     // queries: the points in input order
@@ -408,6 +410,18 @@ int run_dump(const Kernels& K, const char* in_path, unsigned int n, float3 slo, 
         CountNeighborsOp out{c_exact};
         void* a[] = {&out, &c, &q, &im};
         launch(K.count_exact, n, 32, 0, a);
+        check(cudaDeviceSynchronize(), "sync");
+        // the exact neighbor list with the stride of the largest count
+        std::vector<unsigned int> hc(n);
+        check(cudaMemcpy(hc.data(), c_exact, (size_t)n * 4, cudaMemcpyDeviceToHost), "copy");
+        unsigned int mx = 1;
+        for (unsigned int v : hc) mx = std::max(mx, v);
+        check(cudaMalloc(&list, (size_t)n * mx * 4), "alloc");
+        check(cudaMemset(list, 0xff, (size_t)n * mx * 4), "memset");
+        NeighborListOp lout{list, c_list, mx};
+        void* b[] = {&lout, &c, &q, &im};
+        launch(K.list_exact, n, 32, 0, b);
+        list_stride = mx;
         }
     check(cudaDeviceSynchronize(), "sync");
     auto dump = [&](const char* name, const void* ptr, size_t bytes) {
@@ -432,7 +446,9 @@ int run_dump(const Kernels& K, const char* in_path, unsigned int n, float3 slo, 
     dump("data", T.data, nodes * 16);
     dump("count_stock", c_stock, (size_t)n * 4);
     dump("count_exact", c_exact, (size_t)n * 4);
-    printf("{\"dumped\": %u}\n", n);
+    dump("count_list", c_list, (size_t)n * 4);
+    dump("list_exact", list, (size_t)n * list_stride * 4);
+    printf("{\"dumped\": %u, \"list_stride\": %u}\n", n, list_stride);
     return 0;
     }
 } // namespace

@@ -3,8 +3,10 @@
 The reference harness (oracle/ref_harness) compiles mphowardlab/neighbor's kernels from its
 headers and replays its build / setup / traverse sequence.  Its outputs must equal this
 library's bit for bit: sorted codes and primitive order, hierarchy, FP32 boxes, the 10-bit int4
-nodes of getData(), the stock query's superset counts, and the exact query's counts (which also
-equal the oracle's cell list).  Skipped where the reference kernels were not built.
+nodes of getData(), the stock query's superset counts, the exact query's counts (which also
+equal the oracle's cell list), and the exact query's neighbor lists, row by row in the
+reference's order, from the general traversal, the whole-tree self walk and the symmetric self
+walk.  Skipped where the reference kernels were not built.
 """
 import numpy as np
 import pytest
@@ -72,3 +74,21 @@ def test_library_matches_reference_kernels(name, P, L, rc):
     assert np.array_equal(exact, ref["count_exact"])
     want, _ = O.celllist_counts(P, P, rc, [0, 0, 0], box)
     assert np.array_equal(exact, want)
+
+    # neighbor lists: every row equal to the reference's, entries in the reference's order
+    ref_list = ref["list_exact"]
+    mx = ref_list.shape[1]
+    assert np.array_equal(ref["count_list"], ref["count_exact"])
+    valid = np.arange(mx)[None, :] < ref["count_exact"][:, None]
+    _, lst = trav.traverse(lbvh, sph, query=nb.QUERY_EXACT, points=_t(P), box=box, pad=pad,
+                           images="periodic", max_neigh=mx)
+    got = lst.cpu().numpy().view(np.uint32)
+    assert np.array_equal(np.where(valid, got, 0), np.where(valid, ref_list, 0))
+    for symmetric in (False, True):
+        trav.set_symmetric(symmetric)
+        nn, lst = trav.traverse_self(lbvh, rc, box, pad, images="periodic", max_neigh=mx,
+                                     rows_sorted=False)
+        assert np.array_equal(nn.cpu().numpy().view(np.uint32), ref["count_exact"])
+        got = lst.cpu().numpy().view(np.uint32)
+        assert np.array_equal(np.where(valid, got, 0), np.where(valid, ref_list, 0)), symmetric
+    trav.set_symmetric(True)

@@ -82,6 +82,25 @@ __device__ __forceinline__ bool exact_pair(const float3& pi, const float3& pj, f
     return exact_dist2(pi, pj, L) <= __fmul_rn(rc, rc);
     }
 
+// exact_pair() without the minimum-image wrap (rc2 = rc * rc rounded).  It gives the same answer
+// for a query whose only periodic image meeting the scene is the query itself: a point accepted
+// through a wrap lies within rc of another image of the query, whose padded box would then meet
+// the scene too; and where no axis wraps both compute the same numbers.  Valid while no distance
+// inside the padded query box can wrap: wrap_free(L, rs) with rs the padded radius.
+__device__ __forceinline__ bool plain_pair(const float3& pi, const float3& pj, float rc2)
+    {
+    const float dx = __fsub_rn(pj.x, pi.x);
+    const float dy = __fsub_rn(pj.y, pi.y);
+    const float dz = __fsub_rn(pj.z, pi.z);
+    return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)) <= rc2;
+    }
+
+__device__ __forceinline__ bool wrap_free(const float3& L, float rs)
+    {
+    const float r = fabsf(rs);
+    return (L.x == 0.f || r < 0.45f * L.x) && (L.y == 0.f || r < 0.45f * L.y) && (L.z == 0.f || r < 0.45f * L.z);
+    }
+
 // Radius padding that keeps a conservative traversal from missing any pair the predicate
 // accepts: 16 ulps of twice the largest coordinate magnitude (query centres, points and image
 // translations included) plus 1e-6 relative to the cutoff.

@@ -330,6 +330,9 @@ __global__ void k_traverse_fast(const FastLBVHData tree, const FastQueryArgs a,
     const FastQuery Q = load_fast_query(tree, a, q);
     const float rs = approx::fadd_ru(Q.rc, a.pad);
     unsigned int flags = n_rec ? image_flags(a, f, Q.p, rs) : 0u;
+    // a point inside the padded box of the query's own image needs no minimum-image wrap
+    const bool no_wrap = wrap_free(a.box, rs);
+    const float rc2 = __fmul_rn(Q.rc, Q.rc);
     unsigned long long row_first = 0;
     unsigned int cap = 0;
     if (OUT != kFastCount) row_layout<OUT>(a.offsets, a.caps, a.max_neigh, Q.row, row_first, cap);
@@ -345,6 +348,7 @@ __global__ void k_traverse_fast(const FastLBVHData tree, const FastQueryArgs a,
         const float3 qlo = make_float3(approx::fsub_rd(c.x, rs), approx::fsub_rd(c.y, rs), approx::fsub_rd(c.z, rs));
         const float3 qhi = make_float3(approx::fadd_ru(c.x, rs), approx::fadd_ru(c.y, rs), approx::fadd_ru(c.z, rs));
         const uint3 qb = pack_query_box(f, qlo, qhi);
+        const bool plain = no_wrap && t.x == 0.f && t.y == 0.f && t.z == 0.f;
         if (STATS) ++walks;
         unsigned int i = 0;
         while (i < n_rec)
@@ -357,7 +361,7 @@ __global__ void k_traverse_fast(const FastLBVHData tree, const FastQueryArgs a,
                 if (point_in_box(x, qlo, qhi))
                     {
                     if (STATS) ++tests;
-                    if (exact_pair(Q.p, x, Q.rc, a.box))
+                    if (plain ? plain_pair(Q.p, x, rc2) : exact_pair(Q.p, x, Q.rc, a.box))
                         {
                         if (OUT != kFastCount && count < cap)
                             a.list[row_first + count] = transform(tree.primitive[n.w & ~kLeafFlag]);
@@ -456,6 +460,9 @@ __global__ void __launch_bounds__(256) k_traverse_half(const FastLBVHData tree, 
     const float rs = approx::fadd_ru(a.rc, a.pad);
     unsigned int flags = n_rec ? half_image_flags(a, f, P, rs) : 0u;
     const bool multi = __popc(flags) > 1;
+    // a query meeting the scene through its own image only needs no minimum-image wrap
+    const bool plain = !multi && wrap_free(a.box, rs);
+    const float rc2 = __fmul_rn(a.rc, a.rc);
     const unsigned int start = n_rec ? tree.pre[q + 1] + q : 0u;
     unsigned long long row_first = 0;
     unsigned int cap = 0;
@@ -478,7 +485,12 @@ __global__ void __launch_bounds__(256) k_traverse_half(const FastLBVHData tree, 
             if ((int)n.w < 0)
                 {
                 const float3 x = make_float3(__uint_as_float(n.x), __uint_as_float(n.y), __uint_as_float(n.z));
-                if ((!multi || point_in_box(x, qlo, qhi)) && exact_pair(P, x, a.rc, a.box))
+                bool accept;
+                if (plain)
+                    accept = plain_pair(P, x, rc2);
+                else
+                    accept = (!multi || point_in_box(x, qlo, qhi)) && exact_pair(P, x, a.rc, a.box);
+                if (accept)
                     {
                     const unsigned int j = n.w & ~kLeafFlag;
                     if (OUT == kFastCount)

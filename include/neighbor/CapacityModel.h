@@ -161,7 +161,11 @@ class CapacityModel
             a.y_out = y;
             a.cap_out = caps;
             const unsigned int tiles = detail::ceil_div(N, 32);
-            const unsigned int grid = std::min(detail::ceil_div(tiles, gpu::kCapInferWarps), 152u * 8u);
+            int dev = 0, sms = 152;
+            detail::check_cuda(cudaGetDevice(&dev), "device");
+            detail::check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "attribute");
+            // persistent: two blocks per SM (the kernel's register budget) walk all tiles
+            const unsigned int grid = std::min(detail::ceil_div(tiles, gpu::kCapInferWarps), (unsigned int)sms * 2u);
             gpu::k_cap_infer<<<grid, gpu::kCapInferWarps * 32, 0, stream>>>(a);
             detail::check_cuda(cudaGetLastError(), "capacity inference launch");
             }

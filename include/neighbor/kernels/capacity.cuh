@@ -263,15 +263,15 @@ __device__ __forceinline__ unsigned int cap_row(const CapInferArgs& a, unsigned 
     }
 
 constexpr int kCapInferWarps = 8;
-// Row stride (32-bit words) of a warp's feature tile: 16 words of BF16 pairs + 4 of padding, so
-// the A-fragment reads (rows groupID, columns tig) of a warp fall in 32 distinct banks.
-constexpr int kCapXStride = 20;
+// Row stride (BF16 values) of a warp's per-cell feature rows: 32 features + 2 of padding, so that
+// rows of different cells start in different banks (17 words apart).
+constexpr int kCapCellStride = 34;
 // Weights in shared memory in fragment order: for output row n, k-tile kt and thread-in-group t
 // the two words of the B fragment (B[2t..2t+1][n], B[8+2t..8+2t+1][n]) are one 64-bit word at
 // (kt * 4 + t) * kCapWStride + n; the stride of 72 spreads a warp's words over all bank pairs.
 constexpr int kCapWStride = 72;
 
-__global__ void __launch_bounds__(kCapInferWarps * 32, 4) k_cap_infer(const CapInferArgs a)
+__global__ void __launch_bounds__(kCapInferWarps * 32, 2) k_cap_infer(const CapInferArgs a)
     {
     __shared__ uint2 s_w1[2 * 4 * kCapWStride];   // 2 k-tiles x 4 x 64 rows (+pad)
     __shared__ uint2 s_w2[4 * 4 * kCapWStride];   // 4 k-tiles x 4 x 64 rows (+pad)
@@ -279,7 +279,14 @@ __global__ void __launch_bounds__(kCapInferWarps * 32, 4) k_cap_infer(const CapI
     __shared__ float s_b1[kCapHidden];
     __shared__ float s_b2[kCapHidden];
     __shared__ float s_log[kCapLogTable];
-    __shared__ unsigned int s_x[kCapInferWarps][32 * kCapXStride];
+    // per warp: the distinct coarse cells of its 32 points -- spread Morton parts of the 3 x 3
+    // neighbor coordinates (0xffffffff outside an open grid), occupancy sums, BF16 feature rows --
+    // and per point its cell and its two point-specific feature words
+    __shared__ unsigned int s_part[kCapInferWarps][32 * 9];
+    __shared__ unsigned int s_sum[kCapInferWarps][32];
+    __shared__ unsigned short s_cell[kCapInferWarps][32 * kCapCellStride];
+    __shared__ unsigned int s_ci[kCapInferWarps][32];
+    __shared__ uint2 s_pt[kCapInferWarps][32];
     const unsigned int* wsrc = reinterpret_cast<const unsigned int*>(a.w);
     for (int i = threadIdx.x; i < kCapHidden * 2 * 4; i += blockDim.x)
         {
@@ -306,90 +313,152 @@ __global__ void __launch_bounds__(kCapInferWarps * 32, 4) k_cap_infer(const CapI
     const unsigned int warp = threadIdx.x >> 5;
     const unsigned int g = lane >> 2;   // groupID
     const unsigned int t = lane & 3u;   // thread in group
-    unsigned int* xs = s_x[warp];
-    constexpr int XS = kCapXStride;
+    unsigned int* part = s_part[warp];
+    unsigned int* csum = s_sum[warp];
+    unsigned short* cell = s_cell[warp];
+    unsigned int* cidx = s_ci[warp];
+    uint2* pt = s_pt[warp];
+    const unsigned int sh = a.frame.shift;
+    const int G = 1024 >> sh;
+    const unsigned int lane_le = lanemask_lt() | (1u << lane);
     const unsigned int n_tiles = (a.N + 31u) / 32u;
     for (unsigned int tile = blockIdx.x * kCapInferWarps + warp; tile < n_tiles; tile += gridDim.x * kCapInferWarps)
         {
         const unsigned int base = tile * 32u;
-        {
-        const unsigned int s = base + lane;
-        unsigned int* row = xs + lane * XS;
-        if (s < a.N)
+        // Features as cap_features() gives them, gathered once per distinct coarse cell: sorted
+        // points of one cell are consecutive, so a warp's 32 points lie in m (typically a few)
+        // cells, and the warp's lanes share the 27 m occupancy lookups.  Lanes past the end
+        // repeat the last point (their outputs are not written).
+        const unsigned int s = base + min(lane, a.N - 1u - base);
+        const unsigned int c = a.codes[s] >> (3u * sh);
+        const unsigned int c_prev = __shfl_up_sync(0xffffffffu, c, 1);
+        const unsigned int heads = __ballot_sync(0xffffffffu, lane == 0u || c != c_prev);
+        const unsigned int m = __popc(heads);
+        const unsigned int ci = __popc(heads & lane_le) - 1u;
+        const int cx = (int)compact1by2(c >> 2);
+        const int cy = (int)compact1by2(c >> 1);
+        const int cz = (int)compact1by2(c);
+        cidx[lane] = ci;
+        if ((heads >> lane) & 1u)
             {
-            const float3 pos = cap_position(a, s);
-            float prev = 0.f;
-            cap_features(a.frame, a.codes[s], pos, a.occ, s_log,
-                         [row, &prev](int k, float v) {
-                             if (k & 1) row[k >> 1] = pack_bf16x2(prev, v);
-                             prev = v;
-                         });
-            }
-        else
-            {
+            unsigned int p[3], v[3];
+            cap_axis(cx, G, a.frame.periodic, p, v);
 #pragma unroll
-            for (int k = 0; k < kCapIn / 2; ++k) row[k] = 0u;
+            for (int d = 0; d < 3; ++d) part[ci * 9 + d] = v[d] ? p[d] : 0xffffffffu;
+            cap_axis(cy, G, a.frame.periodic, p, v);
+#pragma unroll
+            for (int d = 0; d < 3; ++d) part[ci * 9 + 3 + d] = v[d] ? p[d] : 0xffffffffu;
+            cap_axis(cz, G, a.frame.periodic, p, v);
+#pragma unroll
+            for (int d = 0; d < 3; ++d) part[ci * 9 + 6 + d] = v[d] ? p[d] : 0xffffffffu;
+            csum[ci] = 0u;
             }
+        __syncwarp();
+        // neighbor cell k = 9(dx+1) + 3(dy+1) + (dz+1) of every distinct cell; a spread part of
+        // 0xffffffff (outside an open grid) makes the index >= 2^30
+        for (unsigned int job = lane; job < 27u * m; job += 32u)
+            {
+            const unsigned int k = job / 27u;
+            const unsigned int nb = job - 27u * k;
+            const unsigned int* pk = part + k * 9u;
+            const unsigned int idx = (pk[nb / 9u] << 2) | (pk[3u + (nb / 3u) % 3u] << 1) | pk[6u + nb % 3u];
+            const unsigned int o = idx < (1u << 30) ? __ldg(a.occ + idx) : 0u;
+            cell[k * kCapCellStride + nb] = __bfloat16_as_ushort(__float2bfloat16_rn(cap_log1p(s_log, o)));
+            atomicAdd(csum + k, o);
+            }
+        __syncwarp();
+        if (lane < m)
+            {
+            cell[lane * kCapCellStride + 30] = __bfloat16_as_ushort(__float2bfloat16_rn(log1pf((float)csum[lane])));
+            cell[lane * kCapCellStride + 31] = __bfloat16_as_ushort(__float2bfloat16_rn(1.f));
+            }
+        {
+        // the point's own words: 13 = (feature 26 of its cell, x fraction), 14 = (y, z fractions)
+        float fr3[3];
+        cap_frac(a.frame, cap_position(a, s), cx, cy, cz, fr3);
+        const unsigned int f26 = cell[ci * kCapCellStride + 26];
+        pt[lane] = make_uint2(f26 | ((unsigned int)__bfloat16_as_ushort(__float2bfloat16_rn(fr3[0])) << 16),
+                              pack_bf16x2(fr3[1], fr3[2]));
         }
         __syncwarp();
-#pragma unroll 1
+        // Both m16 tiles (rows g, g + 8, g + 16, g + 24 of this lane) go through the layers together:
+        // every B fragment read from shared memory feeds two independent MMAs.
+        unsigned int a1[2][2][4];
+#pragma unroll
         for (int mt = 0; mt < 2; ++mt)
             {
-            const unsigned int r0 = mt * 16u + g;  // rows r0 and r0 + 8 of this lane
-            unsigned int a1[2][4];
+            const unsigned int r0 = mt * 16u + g;
+            // feature words of rows r0 and r0 + 8: the cell's row, except words 13 and 14
+            const unsigned int* x0 = reinterpret_cast<const unsigned int*>(cell + cidx[r0] * kCapCellStride);
+            const unsigned int* x1 = reinterpret_cast<const unsigned int*>(cell + cidx[r0 + 8u] * kCapCellStride);
+            a1[mt][0][0] = x0[t];
+            a1[mt][0][1] = x1[t];
+            a1[mt][0][2] = x0[4 + t];
+            a1[mt][0][3] = x1[4 + t];
+            a1[mt][1][0] = x0[8 + t];
+            a1[mt][1][1] = x1[8 + t];
+            a1[mt][1][2] = t == 1u ? pt[r0].x : (t == 2u ? pt[r0].y : x0[12 + t]);
+            a1[mt][1][3] = t == 1u ? pt[r0 + 8u].x : (t == 2u ? pt[r0 + 8u].y : x1[12 + t]);
+            }
+        // layer 1 -> BF16 A fragments of layer 2 (k-tile j = n-tiles 2j, 2j+1)
+        unsigned int a2[2][4][4];
+#pragma unroll
+        for (int nt = 0; nt < 8; ++nt)
+            {
+            float acc[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
 #pragma unroll
             for (int kt = 0; kt < 2; ++kt)
                 {
-                a1[kt][0] = xs[r0 * XS + kt * 8 + t];
-                a1[kt][1] = xs[(r0 + 8) * XS + kt * 8 + t];
-                a1[kt][2] = xs[r0 * XS + kt * 8 + 4 + t];
-                a1[kt][3] = xs[(r0 + 8) * XS + kt * 8 + 4 + t];
+                const uint2 b = s_w1[(kt * 4 + t) * kCapWStride + nt * 8 + g];
+                mma_bf16_16816(acc[0], a1[0][kt], b.x, b.y);
+                mma_bf16_16816(acc[1], a1[1][kt], b.x, b.y);
                 }
-            // layer 1 -> BF16 A fragments of layer 2 (k-tile j = n-tiles 2j, 2j+1)
-            unsigned int a2[4][4];
+            const float bl = s_b1[nt * 8 + 2 * t];
+            const float bh = s_b1[nt * 8 + 2 * t + 1];
 #pragma unroll
-            for (int nt = 0; nt < 8; ++nt)
+            for (int mt = 0; mt < 2; ++mt)
                 {
-                float acc[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-                for (int kt = 0; kt < 2; ++kt)
-                    {
-                    const uint2 b = s_w1[(kt * 4 + t) * kCapWStride + nt * 8 + g];
-                    mma_bf16_16816(acc, a1[kt], b.x, b.y);
-                    }
-                const float bl = s_b1[nt * 8 + 2 * t];
-                const float bh = s_b1[nt * 8 + 2 * t + 1];
-                a2[nt >> 1][(nt & 1) * 2 + 0] = pack_bf16x2(fmaxf(acc[0] + bl, 0.f), fmaxf(acc[1] + bh, 0.f));
-                a2[nt >> 1][(nt & 1) * 2 + 1] = pack_bf16x2(fmaxf(acc[2] + bl, 0.f), fmaxf(acc[3] + bh, 0.f));
+                a2[mt][nt >> 1][(nt & 1) * 2 + 0] = pack_bf16x2(fmaxf(acc[mt][0] + bl, 0.f), fmaxf(acc[mt][1] + bh, 0.f));
+                a2[mt][nt >> 1][(nt & 1) * 2 + 1] = pack_bf16x2(fmaxf(acc[mt][2] + bl, 0.f), fmaxf(acc[mt][3] + bh, 0.f));
                 }
-            // layer 2 with the output layer folded in: z(row) = sum over columns of relu(h2) * w3
-            float z0 = 0.f, z1 = 0.f;
+            }
+        // layer 2 with the output layer folded in: z(row) = sum over columns of relu(h2) * w3
+        float z[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
 #pragma unroll
-            for (int nt = 0; nt < 8; ++nt)
+        for (int nt = 0; nt < 8; ++nt)
+            {
+            float acc[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
+#pragma unroll
+            for (int kt = 0; kt < 4; ++kt)
                 {
-                float acc[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-                for (int kt = 0; kt < 4; ++kt)
-                    {
-                    const uint2 b = s_w2[(kt * 4 + t) * kCapWStride + nt * 8 + g];
-                    mma_bf16_16816(acc, a2[kt], b.x, b.y);
-                    }
-                const int c0 = nt * 8 + 2 * t;
-                const float w0 = s_w3[c0], w1 = s_w3[c0 + 1];
-                const float bl = s_b2[c0], bh = s_b2[c0 + 1];
-                z0 = fmaf(fmaxf(acc[0] + bl, 0.f), w0, z0);
-                z0 = fmaf(fmaxf(acc[1] + bh, 0.f), w1, z0);
-                z1 = fmaf(fmaxf(acc[2] + bl, 0.f), w0, z1);
-                z1 = fmaf(fmaxf(acc[3] + bh, 0.f), w1, z1);
+                const uint2 b = s_w2[(kt * 4 + t) * kCapWStride + nt * 8 + g];
+                mma_bf16_16816(acc[0], a2[0][kt], b.x, b.y);
+                mma_bf16_16816(acc[1], a2[1][kt], b.x, b.y);
                 }
+            const int c0 = nt * 8 + 2 * t;
+            const float w0 = s_w3[c0], w1 = s_w3[c0 + 1];
+            const float bl = s_b2[c0], bh = s_b2[c0 + 1];
+#pragma unroll
+            for (int mt = 0; mt < 2; ++mt)
+                {
+                z[mt][0] = fmaf(fmaxf(acc[mt][0] + bl, 0.f), w0, z[mt][0]);
+                z[mt][0] = fmaf(fmaxf(acc[mt][1] + bh, 0.f), w1, z[mt][0]);
+                z[mt][1] = fmaf(fmaxf(acc[mt][2] + bl, 0.f), w0, z[mt][1]);
+                z[mt][1] = fmaf(fmaxf(acc[mt][3] + bh, 0.f), w1, z[mt][1]);
+                }
+            }
+#pragma unroll
+        for (int mt = 0; mt < 2; ++mt)
+            {
             // the four lanes of a group hold disjoint columns of rows r0 and r0 + 8
+            float z0 = z[mt][0], z1 = z[mt][1];
             z0 += __shfl_xor_sync(0xffffffffu, z0, 1);
             z0 += __shfl_xor_sync(0xffffffffu, z0, 2);
             z1 += __shfl_xor_sync(0xffffffffu, z1, 1);
             z1 += __shfl_xor_sync(0xffffffffu, z1, 2);
             if (t < 2u)
                 {
-                const unsigned int s = base + r0 + 8u * t;
+                const unsigned int s = base + mt * 16u + g + 8u * t;
                 if (s < a.N)
                     {
                     const float y = cap_softplus((t == 0u ? z0 : z1) + b3);

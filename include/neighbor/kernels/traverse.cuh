@@ -440,7 +440,7 @@ __device__ __forceinline__ unsigned int half_image_flags(const HalfArgs& a, cons
     }
 
 template<int OUT>
-__global__ void __launch_bounds__(256) k_traverse_half(const FastLBVHData tree, const HalfArgs a)
+__global__ void __launch_bounds__(256, 6) k_traverse_half(const FastLBVHData tree, const HalfArgs a)
     {
     __shared__ QuantFrame s_frame;
     __shared__ unsigned int s_records;
@@ -468,6 +468,11 @@ __global__ void __launch_bounds__(256) k_traverse_half(const FastLBVHData tree, 
     unsigned int cap = 0;
     if (OUT != kFastCount) row_layout<OUT>(a.offsets, a.caps, a.max_neigh, row, row_first, cap);
     unsigned int own = 0;
+    // A partner's entry is stored once its slot (the atomic's old value) is known, at the next
+    // partner the query finds or after the walk, so the atomic's round trip overlaps the walk.
+    bool pending = false;
+    unsigned int p_slot = 0, p_cap = 0, p_key = 0;
+    unsigned long long p_first = 0;
     while (flags)
         {
         const int bit = __ffs(flags) - 1;
@@ -503,12 +508,12 @@ __global__ void __launch_bounds__(256) k_traverse_half(const FastLBVHData tree, 
                             a.list[row_first + (cap - 1u - own)] = ((unsigned int)bit << kHalfKeyBits) | j;
                         if (j != q)
                             {
+                            if (pending && p_slot < p_cap) a.list[p_first + p_slot] = p_key;
                             const unsigned int rj = a.rows_sorted ? j : tree.primitive[j];
-                            const unsigned int slot = atomicAdd(a.nneigh + rj, 1u);
-                            unsigned long long jfirst;
-                            unsigned int jcap;
-                            row_layout<OUT>(a.offsets, a.caps, a.max_neigh, rj, jfirst, jcap);
-                            if (slot < jcap) a.list[jfirst + slot] = (mirror << kHalfKeyBits) | q;
+                            p_slot = atomicAdd(a.nneigh + rj, 1u);
+                            row_layout<OUT>(a.offsets, a.caps, a.max_neigh, rj, p_first, p_cap);
+                            p_key = (mirror << kHalfKeyBits) | q;
+                            pending = true;
                             }
                         }
                     ++own;
@@ -527,6 +532,7 @@ __global__ void __launch_bounds__(256) k_traverse_half(const FastLBVHData tree, 
         }
     else
         {
+        if (pending && p_slot < p_cap) a.list[p_first + p_slot] = p_key;
         a.own[row] = own;
         }
     }
@@ -571,9 +577,12 @@ __global__ void __launch_bounds__(256) k_half_order_rows(const HalfOrderArgs a, 
     if (m > kHalfRowThread) return;
     unsigned int* row = a.list + first;
     unsigned int key[kHalfRowThread];
-    for (unsigned int k = 0; k < m; ++k)
+    // loads first (independent, several in flight), then the insertion sort, then the ids
+#pragma unroll 8
+    for (unsigned int k = 0; k < m; ++k) key[k] = half_row_key(row, k, appended, total, cap);
+    for (unsigned int k = 1; k < m; ++k)
         {
-        const unsigned int v = half_row_key(row, k, appended, total, cap);
+        const unsigned int v = key[k];
         unsigned int j = k;
         while (j > 0u && key[j - 1u] > v)
             {
@@ -582,7 +591,10 @@ __global__ void __launch_bounds__(256) k_half_order_rows(const HalfOrderArgs a, 
             }
         key[j] = v;
         }
-    for (unsigned int k = 0; k < m; ++k) row[k] = transform(a.primitive[key[k] & kHalfKeyMask]);
+#pragma unroll 8
+    for (unsigned int k = 0; k < m; ++k) key[k] = a.primitive[key[k] & kHalfKeyMask];
+#pragma unroll 8
+    for (unsigned int k = 0; k < m; ++k) row[k] = transform(key[k]);
     }
 
 // ---------------------------------------------------------------------------------------------

@@ -145,6 +145,9 @@ class LBVH : public Tunable<unsigned int>
 
         // ---- additions of this library ----
 
+        // Number of builds so far (identifies the current tree).
+        unsigned long long getBuildCount() const { return m_builds; }
+
         // Primitives per leaf bucket of the traversal tree (1..64; rounded to a power of two).
         void setLeafSize(unsigned int leaf_size)
             {
@@ -244,6 +247,7 @@ class LBVH : public Tunable<unsigned int>
         unsigned int m_radix_bits;
         bool m_fast_points;
         unsigned int m_epoch;
+        unsigned long long m_builds = 0;
         unsigned int m_block;
         unsigned int m_climb_block;
         cudaStream_t m_stream;
@@ -283,6 +287,7 @@ class LBVH : public Tunable<unsigned int>
 
         unsigned int next_epoch()
             {
+            ++m_builds;
             ++m_epoch;
             if (m_epoch >= (1u << 27))
                 {

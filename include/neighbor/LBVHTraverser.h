@@ -157,6 +157,12 @@ class LBVHTraverser : public Tunable<unsigned int>
         void setSymmetric(bool enabled) { m_symmetric = enabled; }
         bool getSymmetric() const { return m_symmetric; }
 
+        // A symmetric count records how many records each query visited; a symmetric fill over the
+        // same tree with the same cutoff then hands each block's queries to its lanes in order of
+        // those lengths (true, default), or in sorted order (false).  Results do not depend on it.
+        void setWorkOrder(bool enabled) { m_work_order = enabled; }
+        bool getWorkOrder() const { return m_work_order; }
+
         // Self queries on the fast path: every primitive of the tree queries the tree with cutoff
         // rc.  Queries run in the tree's sorted order; rows_sorted selects whether row s of the
         // output belongs to sorted slot s (the reference benchmark's layout) or to the original
@@ -185,6 +191,14 @@ class LBVHTraverser : public Tunable<unsigned int>
         int m_mode;
         unsigned long long* m_stats;
         bool m_symmetric;
+        bool m_work_order = true;
+        // walk lengths of the last symmetric count and what they were measured on
+        device_array<unsigned short> m_walk;
+        const LBVH* m_walk_tree = nullptr;
+        unsigned long long m_walk_build = 0;
+        float m_walk_rc = 0.f, m_walk_pad = 0.f;
+        int m_walk_lattice = -1;
+        float3 m_walk_L = make_float3(0.f, 0.f, 0.f);
         device_array<unsigned int> m_own;
 
         template<class TransformOpT>
@@ -424,8 +438,28 @@ void LBVHTraverser::launch_half(const LaunchParameters& params, const LBVH& lbvh
         m_own.reserve(N);
         h.own = m_own.get();
         }
+    h.walk_out = nullptr;
+    h.walk_in = nullptr;
+    const bool same_walk = m_walk_tree == &lbvh && m_walk_build == lbvh.getBuildCount() && m_walk_rc == a.self_rc
+                           && m_walk_pad == a.pad && m_walk_lattice == a.lattice && m_walk_L.x == a.lattice_L.x
+                           && m_walk_L.y == a.lattice_L.y && m_walk_L.z == a.lattice_L.z;
+    if (kind == gpu::kFastCount)
+        {
+        m_walk.reserve(N);
+        h.walk_out = m_walk.get();
+        m_walk_tree = &lbvh;
+        m_walk_build = lbvh.getBuildCount();
+        m_walk_rc = a.self_rc;
+        m_walk_pad = a.pad;
+        m_walk_lattice = a.lattice;
+        m_walk_L = a.lattice_L;
+        }
+    else if (m_work_order && same_walk)
+        {
+        h.walk_in = m_walk.get();
+        }
     detail::check_cuda(cudaMemsetAsync(a.nneigh, 0, (size_t)N * sizeof(unsigned int), stream), "memset");
-    gpu::k_traverse_half<kind><<<detail::ceil_div(N, 256), 256, 0, stream>>>(lbvh.fastData(), h);
+    gpu::k_traverse_half<kind><<<detail::ceil_div(N, gpu::kHalfBlock), gpu::kHalfBlock, 0, stream>>>(lbvh.fastData(), h);
     if (kind != gpu::kFastCount)
         {
         gpu::HalfOrderArgs o;

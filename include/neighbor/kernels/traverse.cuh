@@ -425,7 +425,12 @@ struct HalfArgs
     const unsigned long long* offsets;
     const unsigned int* caps;
     unsigned int* own;       // fill only: entries each row found itself
+    unsigned short* walk_out;       // optional: records each query visited (saturated at 65535)
+    const unsigned short* walk_in;  // optional: walk lengths of an earlier pass over the same tree
     };
+
+constexpr unsigned int kHalfBlock = 256;
+constexpr unsigned int kHalfWorkClasses = 64;  // walk-length classes of 8 records
 
 // Images (bits of the 27-image lattice, or bit 0 for the self image) whose padded query box
 // meets the root box.
@@ -440,18 +445,59 @@ __device__ __forceinline__ unsigned int half_image_flags(const HalfArgs& a, cons
     }
 
 template<int OUT>
-__global__ void __launch_bounds__(256, 6) k_traverse_half(const FastLBVHData tree, const HalfArgs a)
+__global__ void __launch_bounds__(kHalfBlock, 6) k_traverse_half(const FastLBVHData tree, const HalfArgs a)
     {
     __shared__ QuantFrame s_frame;
     __shared__ unsigned int s_records;
+    __shared__ unsigned int s_class[kHalfWorkClasses];
+    __shared__ unsigned int s_order[kHalfBlock];
     if (threadIdx.x == 0)
         {
         s_frame = *tree.frame;
         s_records = ld_status(tree.status) != 0u ? 0u : *tree.n_boxes + tree.N;
         }
-    __syncthreads();
-    const unsigned int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= a.Q) return;
+    unsigned int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a.walk_in)
+        {
+        // Work order: the block's queries go to its lanes by walk length (classes of 8 records,
+        // from an earlier pass over the same tree), so that a warp's lanes walk about as long as
+        // each other.  Results do not depend on which lane takes which query.
+        if (threadIdx.x < kHalfWorkClasses) s_class[threadIdx.x] = 0u;
+        __syncthreads();
+        unsigned int cls = 0, rank = 0;
+        if (q < a.Q)
+            {
+            cls = min((unsigned int)a.walk_in[q] >> 3, kHalfWorkClasses - 1u);
+            rank = atomicAdd(s_class + cls, 1u);
+            }
+        __syncthreads();
+        if (threadIdx.x < 32)
+            {
+            // exclusive scan of the 64 class sizes, two per lane
+            const unsigned int c0 = s_class[2 * threadIdx.x], c1 = s_class[2 * threadIdx.x + 1];
+            unsigned int incl = c0 + c1;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1)
+                {
+                const unsigned int v = __shfl_up_sync(0xffffffffu, incl, o);
+                if ((int)threadIdx.x >= o) incl += v;
+                }
+            const unsigned int excl = incl - c0 - c1;
+            s_class[2 * threadIdx.x] = excl;
+            s_class[2 * threadIdx.x + 1] = excl + c0;
+            }
+        __syncthreads();
+        if (q < a.Q) s_order[s_class[cls] + rank] = q;
+        __syncthreads();
+        const unsigned int first = blockIdx.x * blockDim.x;
+        if (threadIdx.x >= min(a.Q - first, blockDim.x)) return;
+        q = s_order[threadIdx.x];
+        }
+    else
+        {
+        __syncthreads();
+        if (q >= a.Q) return;
+        }
     const QuantFrame f = s_frame;
     const unsigned int n_rec = s_records;
     const float4 me = tree.points[q];
@@ -468,6 +514,7 @@ __global__ void __launch_bounds__(256, 6) k_traverse_half(const FastLBVHData tre
     unsigned int cap = 0;
     if (OUT != kFastCount) row_layout<OUT>(a.offsets, a.caps, a.max_neigh, row, row_first, cap);
     unsigned int own = 0;
+    unsigned int visits = 0;
     // A partner's entry is stored once its slot (the atomic's old value) is known, at the next
     // partner the query finds or after the walk, so the atomic's round trip overlaps the walk.
     bool pending = false;
@@ -487,6 +534,7 @@ __global__ void __launch_bounds__(256, 6) k_traverse_half(const FastLBVHData tre
         while (i < n_rec)
             {
             const uint4 n = __ldg(tree.nodes + i);
+            ++visits;
             if ((int)n.w < 0)
                 {
                 const float3 x = make_float3(__uint_as_float(n.x), __uint_as_float(n.y), __uint_as_float(n.z));
@@ -535,6 +583,7 @@ __global__ void __launch_bounds__(256, 6) k_traverse_half(const FastLBVHData tre
         if (pending && p_slot < p_cap) a.list[p_first + p_slot] = p_key;
         a.own[row] = own;
         }
+    if (a.walk_out) a.walk_out[q] = (unsigned short)min(visits, 65535u);
     }
 
 struct HalfOrderArgs

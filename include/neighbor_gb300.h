@@ -125,6 +125,11 @@ int nbr_traverser_set_stats(nbr_traverser t, unsigned long long* counters);
  * query (0).  Counts, neighbor sets and the order of each row are the same either way. */
 int nbr_traverser_set_symmetric(nbr_traverser t, int enabled);
 
+/* Addition: a symmetric count records each query's walk length, and a symmetric fill over the same
+ * tree and cutoff gives each block's queries to its lanes in order of those lengths (1, default)
+ * or in sorted order (0).  Results are the same either way. */
+int nbr_traverser_set_work_order(nbr_traverser t, int enabled);
+
 /* getData() (LBVHTraverser.h:326-329): int4 nodes in the reference's 10-bit layout (managed),
  * plus the compression frame (lo, hi, bins: managed float[3] each). */
 int nbr_traverser_get_data(nbr_traverser t, const int** data, const float** lo, const float** hi,

@@ -99,6 +99,7 @@ def _declare(L):
     sig("nbr_traverser_set_mode", [_P, _I])
     sig("nbr_traverser_set_stats", [_P, _P])
     sig("nbr_traverser_set_symmetric", [_P, _I])
+    sig("nbr_traverser_set_work_order", [_P, _I])
     sig("nbr_traverser_get_data", [_P, _PP, _PP, _PP, _PP])
     sig("nbr_traverse", [_P, _P, _I, _P, _U, _P, _P, _F, _P, _U, _P, _P, _P, _U, _U, _P])
     sig("nbr_traverse_self", [_P, _P, _F, _P, _F, _P, _U, _P, _P, _P, _U, _I, _U, _P])
@@ -152,6 +153,7 @@ EXPORTED = ["nbr_last_error", "nbr_version", "nbr_lbvh_create", "nbr_lbvh_destro
             "nbr_lbvh_check_status", "nbr_traverser_create", "nbr_traverser_destroy",
             "nbr_traverser_setup", "nbr_traverser_reset", "nbr_traverser_set_fast_path",
             "nbr_traverser_set_mode", "nbr_traverser_set_stats", "nbr_traverser_set_symmetric",
+            "nbr_traverser_set_work_order",
             "nbr_traverser_get_data", "nbr_traverse", "nbr_traverse_self", "nbr_exact_pad",
             "nbr_debug_wait_timeout", "nbr_morton_sort_noalloc", "nbr_traverse_self_csr",
             "nbr_capmodel_create", "nbr_capmodel_destroy", "nbr_capmodel_get_params",
@@ -444,6 +446,11 @@ class LBVHTraverser:
     def set_symmetric(self, enabled: bool):
         """Self traversals: find each pair once and write both rows (True, default)."""
         _check(self._L.nbr_traverser_set_symmetric(self._h, 1 if enabled else 0))
+
+    def set_work_order(self, enabled: bool):
+        """Symmetric fills take each block's queries in order of the walk lengths of the last
+        symmetric count over the same tree (True, default)."""
+        _check(self._L.nbr_traverser_set_work_order(self._h, 1 if enabled else 0))
 
     def set_mode(self, mode: int):
         """0 = one thread per query, 1 = one warp per 32 consecutive queries."""

@@ -289,6 +289,13 @@ int nbr_traverser_set_symmetric(nbr_traverser t, int enabled)
     return NBR_OK;
     }
 
+int nbr_traverser_set_work_order(nbr_traverser t, int enabled)
+    {
+    if (!t) return fail(NBR_ERR_INVALID, "null handle");
+    t->trav.setWorkOrder(enabled != 0);
+    return NBR_OK;
+    }
+
 int nbr_traverser_get_data(nbr_traverser t, const int** data, const float** lo, const float** hi,
                            const float** bins)
     {

@@ -144,3 +144,24 @@ def test_symmetric_transform_and_long_rows():
     cf, lf = _rows(cf, lf)
     assert np.array_equal(cs, cf)
     assert np.array_equal(ls, lf)
+
+
+@pytest.mark.parametrize("images", ["periodic", "self"])
+@pytest.mark.parametrize("N", [1, 37, 300, 20000])
+def test_work_order_does_not_change_results(N, images):
+    P, L = _uniform(N, 7)
+    box = [L, L, L] if images == "periodic" else [0, 0, 0]
+    imgs = "periodic" if images == "periodic" else None
+    rc = 1.3
+    lbvh = nb.LBVH()
+    lbvh.build(_t(P), [0, 0, 0], [L, L, L])
+    pad = nb.exact_pad(rc, 2 * L)
+    out = []
+    for ordered in (False, True):
+        trav = nb.LBVHTraverser()
+        trav.set_work_order(ordered)
+        cnt = trav.traverse_self(lbvh, rc, box, pad, images=imgs)   # records the walk lengths
+        mx = max(1, int(cnt.max().item()))
+        out.append(_rows(*trav.traverse_self(lbvh, rc, box, pad, images=imgs, max_neigh=mx)))
+    assert np.array_equal(out[0][0], out[1][0])
+    assert np.array_equal(out[0][1], out[1][1])

@@ -56,6 +56,8 @@ def parse():
     ap.add_argument("--no-polydisperse", action="store_true")
     ap.add_argument("--train-steps", type=int, default=400)
     ap.add_argument("--climb", type=int, default=512)
+    ap.add_argument("--no-work-order", action="store_true",
+                    help="fills take queries in sorted order instead of by walk length / capacity")
     return ap.parse_args()
 
 
@@ -281,6 +283,7 @@ def learned_uniform(nb, n, L, frames, warmup, plain_ms, pairs_step, args, stream
     pad = nb.exact_pad(RC, 2 * L)
     lbvh = nb.LBVH(leaf_size=args.leaf, radix_bits=args.radix_bits, climb_block=args.climb)
     trav = nb.LBVHTraverser()
+    trav.set_work_order(not args.no_work_order)
     train = make_frames(n, L, 1, seed=4242)
     model, train_s, loss = train_capacity_model(nb, lbvh, trav, train, L, RC, args.train_steps)
     del train
@@ -326,6 +329,7 @@ def clustered_c3(nb, args, stream, n=4_000_000, rc=1.0, steps=5, warmup=2):
 
     lbvh = nb.LBVH(leaf_size=args.leaf, radix_bits=args.radix_bits, climb_block=args.climb)
     trav = nb.LBVHTraverser()
+    trav.set_work_order(not args.no_work_order)
     model, train_s, loss = train_capacity_model(nb, lbvh, trav, [frame(500), frame(501)], L, rc,
                                                 args.train_steps)
     frames = [frame(600 + k) for k in range(warmup + steps)]
@@ -414,6 +418,7 @@ def batched_ensemble(nb, args, stream, S=4096, rc=1.3, steps=5, max_neigh=48, se
     cnt2, lst2 = b.outputs()
     lbvh = nb.LBVH()
     trav = nb.LBVHTraverser()
+    trav.set_work_order(not args.no_work_order)
     b.sequential_plain(lbvh, trav, pts, rc, cnt2, lst2)  # warm-up (allocations grow to the largest system)
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -484,6 +489,7 @@ def polydisperse_c2(nb, args, stream, steps=5, warmup=2):
     frames = [polydisperse_frame(n_small, n_large, L, 900 + k) for k in range(warmup + steps)]
     trees = [nb.LBVH(), nb.LBVH()]
     trav = nb.LBVHTraverser()
+    trav.set_work_order(not args.no_work_order)
     ms, outs = time_steps(lambda fr: polydisperse_step(nb, trees, trav, fr, L), frames, warmup, stream)
     out = outs[-1]
     species = frames[-1]
@@ -577,6 +583,7 @@ def run_ours(args):
     pad = nb.exact_pad(RC, 2 * L)
     lbvh = nb.LBVH(leaf_size=args.leaf, radix_bits=args.radix_bits, climb_block=args.climb)
     trav = nb.LBVHTraverser()
+    trav.set_work_order(not args.no_work_order)
     trav.set_mode(args.mode)
     counts = torch.empty(n, dtype=torch.int32, device="cuda")
     cap = 64

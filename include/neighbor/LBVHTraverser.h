@@ -157,9 +157,10 @@ class LBVHTraverser : public Tunable<unsigned int>
         void setSymmetric(bool enabled) { m_symmetric = enabled; }
         bool getSymmetric() const { return m_symmetric; }
 
-        // A symmetric count records how many records each query visited; a symmetric fill over the
-        // same tree with the same cutoff then hands each block's queries to its lanes in order of
-        // those lengths (true, default), or in sorted order (false).  Results do not depend on it.
+        // Work order of fills (true, default): a symmetric count records how many records each
+        // query visited, and a symmetric fill over the same tree with the same cutoff hands each
+        // block's queries to its lanes in order of those lengths; a whole-tree CSR fill orders them
+        // by row capacity.  false: sorted order.  Results do not depend on it.
         void setWorkOrder(bool enabled) { m_work_order = enabled; }
         bool getWorkOrder() const { return m_work_order; }
 
@@ -289,6 +290,7 @@ void LBVHTraverser::launch_fast(const LaunchParameters& params, const LBVH& lbvh
     {
     detail::set_output(a, out);
     a.stats = m_stats;
+    a.work_order = (output_kind<OutputOpT>::value == gpu::kFastCSR && !a.subset && m_work_order) ? 1 : 0;
     const unsigned int bs = params.tunable;
     constexpr int kind = output_kind<OutputOpT>::value;
     if (m_mode == kPacketTraversal && kind != gpu::kFastCSR && !a.subset)

@@ -184,6 +184,7 @@ struct FastQueryArgs
     const unsigned int* caps = nullptr;           // kFastCSR: capacity of each row
     const unsigned int* subset = nullptr;         // optional: thread t runs query subset[t] (Q threads)
     unsigned long long* stats = nullptr;  // optional counters: records visited, point tests, walks
+    int work_order = 0;                   // CSR fills: a block's rows go to lanes by capacity class
     };
 
 // First slot and capacity of an output row.
@@ -303,6 +304,46 @@ __device__ __forceinline__ bool point_in_box(const float3& x, const float3& lo, 
     return x.x >= lo.x && x.x <= hi.x && x.y >= lo.y && x.y <= hi.y && x.z >= lo.z && x.z <= hi.z;
     }
 
+// Work order of a block: a counting sort of the block's items (one per thread) by a work class
+// in [0, 64).  Returns the item the calling thread takes -- a warp then gets items of similar work
+// -- or 0xffffffff when the block has fewer items than threads.  All threads of the block call it.
+constexpr unsigned int kWorkClasses = 64;
+__device__ __forceinline__ unsigned int block_work_order(unsigned int item, bool valid, unsigned int cls,
+                                                         unsigned int* s_class, unsigned int* s_order)
+    {
+    if (threadIdx.x < kWorkClasses) s_class[threadIdx.x] = 0u;
+    __syncthreads();
+    unsigned int rank = 0;
+    if (valid) rank = atomicAdd(s_class + cls, 1u);
+    const unsigned int n = __syncthreads_count(valid ? 1 : 0);
+    if (threadIdx.x < 32)
+        {
+        // exclusive scan of the 64 class sizes, two per lane
+        const unsigned int c0 = s_class[2 * threadIdx.x], c1 = s_class[2 * threadIdx.x + 1];
+        unsigned int incl = c0 + c1;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1)
+            {
+            const unsigned int v = __shfl_up_sync(0xffffffffu, incl, o);
+            if ((int)threadIdx.x >= o) incl += v;
+            }
+        const unsigned int excl = incl - c0 - c1;
+        s_class[2 * threadIdx.x] = excl;
+        s_class[2 * threadIdx.x + 1] = excl + c0;
+        }
+    __syncthreads();
+    if (valid) s_order[s_class[cls] + rank] = item;
+    __syncthreads();
+    return threadIdx.x < n ? s_order[threadIdx.x] : 0xffffffffu;
+    }
+
+// Work class of a row capacity (or count): about four classes per octave, 0..63.
+__device__ __forceinline__ unsigned int capacity_class(unsigned int c)
+    {
+    const unsigned int bits = __float_as_uint((float)min(c, 65535u) + 1.f);
+    return min((bits >> 21) - (127u << 2), kWorkClasses - 1u);
+    }
+
 // One thread per query, stackless: a box record is tested against the query's box (hit: the next
 // record, miss: the skip link); a point record inside the query's padded box goes to the exact
 // predicate.  Images are walked one after the other in the same loop.  When a query visits more
@@ -314,15 +355,33 @@ __global__ void k_traverse_fast(const FastLBVHData tree, const FastQueryArgs a,
     {
     __shared__ QuantFrame s_frame;
     __shared__ unsigned int s_records;
+    __shared__ unsigned int s_class[kWorkClasses];
+    __shared__ unsigned int s_order[1024];
     if (threadIdx.x == 0)
         {
         s_frame = *tree.frame;
         // a failed build leaves no tree to walk
         s_records = ld_status(tree.status) != 0u ? 0u : *tree.n_boxes + tree.N;
         }
-    __syncthreads();
-    const unsigned int tq = blockIdx.x * blockDim.x + threadIdx.x;
-    if (tq >= a.Q) return;
+    unsigned int tq = blockIdx.x * blockDim.x + threadIdx.x;
+    if (OUT == kFastCSR && a.work_order)
+        {
+        // rows with capacities of similar size (their predicted or counted lengths) share warps
+        const bool valid = tq < a.Q;
+        unsigned int cls = 0;
+        if (valid)
+            {
+            const unsigned int row = a.spheres || a.self_rows_sorted ? tq : __float_as_uint(tree.points[tq].w);
+            cls = capacity_class(a.caps[row]);
+            }
+        tq = block_work_order(tq, valid, cls, s_class, s_order);
+        if (tq == 0xffffffffu) return;
+        }
+    else
+        {
+        __syncthreads();
+        if (tq >= a.Q) return;
+        }
     const unsigned int q = a.subset ? a.subset[tq] : tq;
     const QuantFrame f = s_frame;
     const unsigned int n_rec = s_records;
@@ -430,7 +489,6 @@ struct HalfArgs
     };
 
 constexpr unsigned int kHalfBlock = 256;
-constexpr unsigned int kHalfWorkClasses = 64;  // walk-length classes of 8 records
 
 // Images (bits of the 27-image lattice, or bit 0 for the self image) whose padded query box
 // meets the root box.
@@ -449,7 +507,7 @@ __global__ void __launch_bounds__(kHalfBlock, 6) k_traverse_half(const FastLBVHD
     {
     __shared__ QuantFrame s_frame;
     __shared__ unsigned int s_records;
-    __shared__ unsigned int s_class[kHalfWorkClasses];
+    __shared__ unsigned int s_class[kWorkClasses];
     __shared__ unsigned int s_order[kHalfBlock];
     if (threadIdx.x == 0)
         {
@@ -462,36 +520,10 @@ __global__ void __launch_bounds__(kHalfBlock, 6) k_traverse_half(const FastLBVHD
         // Work order: the block's queries go to its lanes by walk length (classes of 8 records,
         // from an earlier pass over the same tree), so that a warp's lanes walk about as long as
         // each other.  Results do not depend on which lane takes which query.
-        if (threadIdx.x < kHalfWorkClasses) s_class[threadIdx.x] = 0u;
-        __syncthreads();
-        unsigned int cls = 0, rank = 0;
-        if (q < a.Q)
-            {
-            cls = min((unsigned int)a.walk_in[q] >> 3, kHalfWorkClasses - 1u);
-            rank = atomicAdd(s_class + cls, 1u);
-            }
-        __syncthreads();
-        if (threadIdx.x < 32)
-            {
-            // exclusive scan of the 64 class sizes, two per lane
-            const unsigned int c0 = s_class[2 * threadIdx.x], c1 = s_class[2 * threadIdx.x + 1];
-            unsigned int incl = c0 + c1;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1)
-                {
-                const unsigned int v = __shfl_up_sync(0xffffffffu, incl, o);
-                if ((int)threadIdx.x >= o) incl += v;
-                }
-            const unsigned int excl = incl - c0 - c1;
-            s_class[2 * threadIdx.x] = excl;
-            s_class[2 * threadIdx.x + 1] = excl + c0;
-            }
-        __syncthreads();
-        if (q < a.Q) s_order[s_class[cls] + rank] = q;
-        __syncthreads();
-        const unsigned int first = blockIdx.x * blockDim.x;
-        if (threadIdx.x >= min(a.Q - first, blockDim.x)) return;
-        q = s_order[threadIdx.x];
+        const bool valid = q < a.Q;
+        const unsigned int cls = valid ? min((unsigned int)a.walk_in[q] >> 3, kWorkClasses - 1u) : 0u;
+        q = block_work_order(q, valid, cls, s_class, s_order);
+        if (q == 0xffffffffu) return;
         }
     else
         {

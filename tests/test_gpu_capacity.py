@@ -246,3 +246,26 @@ def test_learned_step_in_one_call_matches_separate_calls(rows_sorted):
         assert torch.equal(a["caps"], b["caps"])
         cnt, lst = _plain_rows(lbvh, rc, L, rows_sorted=rows_sorted)
         _csr_equals_rows(b, cnt, lst)
+
+
+def test_csr_fill_work_order_does_not_change_results():
+    P, L = _clustered(50000, 16)
+    lbvh = _tree(P, L)
+    rc = 1.0
+    box = [L, L, L]
+    pad = nb.exact_pad(rc, 2 * L)
+    op = nb.OnePassList()
+    out = []
+    for ordered in (False, True):
+        trav = nb.LBVHTraverser()
+        trav.set_work_order(ordered)
+        cnt = trav.traverse_self(lbvh, rc, box, pad, images="periodic", rows_sorted=False)
+        mx = int(cnt.max().item())
+        assert mx > 32  # rows too long for the symmetric fill: the whole-tree walk fills them
+        offsets, total = op.scan(cnt)
+        lst = torch.full((total + 1,), -1, dtype=torch.int32, device="cuda")
+        nn = trav.traverse_self_csr(lbvh, rc, box, pad, offsets, cnt, lst, max_capacity=mx,
+                                    images="periodic", rows_sorted=False)
+        out.append((nn.cpu().numpy(), lst.cpu().numpy()))
+    assert np.array_equal(out[0][0], out[1][0])
+    assert np.array_equal(out[0][1], out[1][1])

@@ -299,6 +299,11 @@ void LBVHTraverser::launch_fast(const LaunchParameters& params, const LBVH& lbvh
     else if (m_stats)
         gpu::k_traverse_fast<kind, true, TransformOpT><<<detail::ceil_div(Q, bs), bs, 0, params.stream>>>(
             lbvh.fastData(), a, transform);
+    else if (a.subset)
+        // a subset is a few rows (those that overflowed a one-pass list): one warp walks each
+        gpu::k_traverse_warp<kind, TransformOpT><<<(unsigned int)(((unsigned long long)Q * 32u + gpu::kWarpWalkBlock - 1u)
+                                                                  / gpu::kWarpWalkBlock),
+                                                   gpu::kWarpWalkBlock, 0, params.stream>>>(lbvh.fastData(), a, transform);
     else
         gpu::k_traverse_fast<kind, false, TransformOpT><<<detail::ceil_div(Q, bs), bs, 0, params.stream>>>(
             lbvh.fastData(), a, transform);

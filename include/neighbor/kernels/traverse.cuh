@@ -441,6 +441,99 @@ __global__ void k_traverse_fast(const FastLBVHData tree, const FastQueryArgs a,
     }
 
 // ---------------------------------------------------------------------------------------------
+// One warp per query (long rows, few queries).  The warp takes the records in chunks of 32 in
+// pre-order: lane k tests record i + k.  A box that misses covers the records up to its skip link,
+// so a record is live when no earlier live-or-not missed box of the chunk covers it (a prefix
+// maximum of the missed boxes' skip links over the lanes); live points go to the exact predicate,
+// and the accepted ones are written in record order (ballot + rank), which is the order of the
+// one-thread walk.  The next chunk starts past the chunk and past every live missed subtree.
+// Many lanes test records that a one-thread walk skips, but the walk's latency is about 32
+// times shorter, which is what a handful of long rows needs.
+// ---------------------------------------------------------------------------------------------
+constexpr unsigned int kWarpWalkBlock = 256;
+
+template<int OUT, class TransformOpT>
+__global__ void __launch_bounds__(kWarpWalkBlock) k_traverse_warp(const FastLBVHData tree, const FastQueryArgs a,
+                                                                  const TransformOpT transform)
+    {
+    __shared__ QuantFrame s_frame;
+    __shared__ unsigned int s_records;
+    if (threadIdx.x == 0)
+        {
+        s_frame = *tree.frame;
+        s_records = ld_status(tree.status) != 0u ? 0u : *tree.n_boxes + tree.N;
+        }
+    __syncthreads();
+    const unsigned int lane = threadIdx.x & 31u;
+    const unsigned int tq = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (tq >= a.Q) return;   // whole warps
+    const unsigned int q = a.subset ? a.subset[tq] : tq;
+    const QuantFrame f = s_frame;
+    const unsigned int n_rec = s_records;
+    const unsigned int lt = lanemask_lt();
+
+    const FastQuery Q = load_fast_query(tree, a, q);
+    const float rs = approx::fadd_ru(Q.rc, a.pad);
+    unsigned int flags = n_rec ? image_flags(a, f, Q.p, rs) : 0u;
+    const bool no_wrap = wrap_free(a.box, rs);
+    const float rc2 = __fmul_rn(Q.rc, Q.rc);
+    unsigned long long row_first = 0;
+    unsigned int cap = 0;
+    if (OUT != kFastCount) row_layout<OUT>(a.offsets, a.caps, a.max_neigh, Q.row, row_first, cap);
+
+    unsigned int count = 0;   // warp-uniform
+    while (flags)
+        {
+        const int bit = __ffs(flags) - 1;
+        flags &= flags - 1u;
+        const float3 t = image_vector(a, bit);
+        const float3 c = make_float3(__fadd_rn(Q.p.x, t.x), __fadd_rn(Q.p.y, t.y), __fadd_rn(Q.p.z, t.z));
+        const float3 qlo = make_float3(approx::fsub_rd(c.x, rs), approx::fsub_rd(c.y, rs), approx::fsub_rd(c.z, rs));
+        const float3 qhi = make_float3(approx::fadd_ru(c.x, rs), approx::fadd_ru(c.y, rs), approx::fadd_ru(c.z, rs));
+        const uint3 qb = pack_query_box(f, qlo, qhi);
+        const bool plain = no_wrap && t.x == 0.f && t.y == 0.f && t.z == 0.f;
+        unsigned int i = 0;
+        while (i < n_rec)   // warp-uniform
+            {
+            const unsigned int k = i + lane;
+            const bool valid = k < n_rec;
+            const uint4 n = valid ? __ldg(tree.nodes + k) : make_uint4(0u, 0u, 0u, 0u);
+            const bool is_point = valid && (int)n.w < 0;
+            const bool miss = valid && !is_point && !node_overlaps(n, qb);
+            const unsigned int kill = miss ? max(n.w, k + 1u) : 0u;   // [k + 1, kill) lies under it
+            unsigned int cover = kill;   // inclusive prefix maximum over the lanes
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1)
+                {
+                const unsigned int v = __shfl_up_sync(0xffffffffu, cover, o);
+                if ((int)lane >= o) cover = max(cover, v);
+                }
+            const unsigned int before = __shfl_up_sync(0xffffffffu, cover, 1);
+            const bool live = valid && (lane == 0u || before <= k);
+            bool accept = false;
+            if (live && is_point)
+                {
+                const float3 x = make_float3(__uint_as_float(n.x), __uint_as_float(n.y), __uint_as_float(n.z));
+                if (point_in_box(x, qlo, qhi)) accept = plain ? plain_pair(Q.p, x, rc2) : exact_pair(Q.p, x, Q.rc, a.box);
+                }
+            const unsigned int hits = __ballot_sync(0xffffffffu, accept);
+            if (OUT != kFastCount && accept)
+                {
+                const unsigned int pos = count + __popc(hits & lt);
+                if (pos < cap) a.list[row_first + pos] = transform(tree.primitive[n.w & ~kLeafFlag]);
+                }
+            count += __popc(hits);
+            // past the chunk and past every live missed subtree
+            unsigned int next = (live && miss) ? kill : 0u;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) next = max(next, __shfl_xor_sync(0xffffffffu, next, o));
+            i = max(i + 32u, next);
+            }
+        }
+    if (lane == 0u) a.nneigh[Q.row] = count;
+    }
+
+// ---------------------------------------------------------------------------------------------
 // Symmetric (half) self traversal.  When the queries are the tree's own points with one cutoff
 // and the image set is symmetric (the self image, or the 27-image lattice), the FP32
 // minimum-image predicate is symmetric too (d(j,i) = -d(i,j) exactly, and the wrap keeps |d|), so

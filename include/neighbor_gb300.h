@@ -218,6 +218,16 @@ int nbr_traverse_self_csr(nbr_traverser t, nbr_lbvh h, float rc, const float box
                           const unsigned int* caps, unsigned int max_capacity, int rows_sorted,
                           unsigned int block_size, void* stream);
 
+/* Addition: traverseSelfSubset -- the rows of the sorted positions subset[0..count) of a point
+ * tree re-run into a CSR list (offsets/caps as nbr_traverse_self_csr; only those rows and their
+ * counts are written), one warp per row.  For rows that overflowed a one-pass list, or a few rows
+ * whose capacity changed. */
+int nbr_traverse_self_subset_csr(nbr_traverser t, nbr_lbvh h, float rc, const float box[3], float pad,
+                                 const float* images, unsigned int n_images, const unsigned int* map,
+                                 const unsigned int* subset, unsigned int count, unsigned int* nneigh,
+                                 unsigned int* list, const unsigned long long* offsets, const unsigned int* caps,
+                                 int rows_sorted, void* stream);
+
 /* Capacity network (32 -> 64 -> 64 -> 1, BF16 weights, FP32 accumulation): create with a seed for
  * the initial weights; parameters as FP32[NBR_CAP_PARAMS] on the host (W1[64][32], b1[64],
  * W2[64][64], b2[64], W3[64], b3). */

@@ -110,6 +110,7 @@ def _declare(L):
     sig("nbr_morton_sort_noalloc", [_P, _U, _P, _P, _P, _P, _P])
     _ULL = ctypes.c_ulonglong
     sig("nbr_traverse_self_csr", [_P, _P, _F, _P, _F, _P, _U, _P, _P, _P, _P, _P, _U, _I, _U, _P])
+    sig("nbr_traverse_self_subset_csr", [_P, _P, _F, _P, _F, _P, _U, _P, _P, _U, _P, _P, _P, _P, _I, _P])
     sig("nbr_capmodel_create", [_PP, _ULL])
     sig("nbr_capmodel_destroy", [_P])
     sig("nbr_capmodel_get_params", [_P, _P])
@@ -156,6 +157,7 @@ EXPORTED = ["nbr_last_error", "nbr_version", "nbr_lbvh_create", "nbr_lbvh_destro
             "nbr_traverser_set_work_order",
             "nbr_traverser_get_data", "nbr_traverse", "nbr_traverse_self", "nbr_exact_pad",
             "nbr_debug_wait_timeout", "nbr_morton_sort_noalloc", "nbr_traverse_self_csr",
+            "nbr_traverse_self_subset_csr",
             "nbr_capmodel_create", "nbr_capmodel_destroy", "nbr_capmodel_get_params",
             "nbr_capmodel_set_params", "nbr_capmodel_set_margin", "nbr_capmodel_get_margin",
             "nbr_capmodel_level", "nbr_capmodel_features", "nbr_capmodel_predict",
@@ -568,6 +570,25 @@ class LBVHTraverser:
                                              _ptr(m), _ptr(nneigh), _ptr(list_out), _ptr(offsets),
                                              _ptr(caps), int(max_capacity), 1 if rows_sorted else 0,
                                              block_size, _stream_ptr(stream)))
+        return nneigh
+
+    def traverse_self_subset_csr(self, lbvh: LBVH, rc: float, box, pad: float, subset, offsets, caps, list_out,
+                                 images=None, map=None, rows_sorted: bool = True, nneigh=None, stream=None):
+        """traverseSelfSubset: only the rows of the sorted positions in `subset` (CUDA int32) are
+        written into the CSR list (one warp per row); returns nneigh."""
+        torch = _torch()
+        _, N, _, _ = lbvh.sizes()
+        sub = _dev(subset, torch.int32)
+        lattice = isinstance(images, str) and images == "periodic"
+        img = None if images is None or lattice else _dev(images, torch.float32, 3)
+        m = None if map is None else _dev(map, torch.int32)
+        if nneigh is None:
+            nneigh = torch.zeros(N, dtype=torch.int32, device="cuda")
+        _check(self._L.nbr_traverse_self_subset_csr(self._h, lbvh.handle, float(rc), _f3(box), float(pad), _ptr(img),
+                                                     27 if lattice else (0 if img is None else img.shape[0]), _ptr(m),
+                                                     _ptr(sub), sub.shape[0], _ptr(nneigh), _ptr(list_out),
+                                                     _ptr(offsets), _ptr(caps), 1 if rows_sorted else 0,
+                                                     _stream_ptr(stream)))
         return nneigh
 
 

@@ -37,6 +37,18 @@ void self_csr(neighbor::LBVHTraverser& t, const neighbor::LBVH& h, const neighbo
     else
         t.traverseSelf(p, h, rc, box, pad, out, img, neighbor::NullTransformOp(), rows_sorted);
     }
+
+template<class TranslateOpT>
+void self_subset_csr(neighbor::LBVHTraverser& t, const neighbor::LBVH& h,
+                     const neighbor::LBVHTraverser::LaunchParameters& p, float rc, float3 box, float pad,
+                     const TranslateOpT& img, const unsigned int* map, const neighbor::CSRNeighborListOp& out,
+                     bool rows_sorted, const unsigned int* subset, unsigned int count)
+    {
+    if (map)
+        t.traverseSelfSubset(p, h, rc, box, pad, out, img, neighbor::MapTransformOp(map), rows_sorted, subset, count);
+    else
+        t.traverseSelfSubset(p, h, rc, box, pad, out, img, neighbor::NullTransformOp(), rows_sorted, subset, count);
+    }
 } // namespace
 
 extern "C" {
@@ -63,6 +75,33 @@ int nbr_traverse_self_csr(nbr_traverser t, nbr_lbvh h, float rc, const float box
             self_csr(t->trav, h->lbvh, p, rc, b, pad, neighbor::PeriodicImagesOp(b), map, out, rows_sorted != 0);
         else
             self_csr(t->trav, h->lbvh, p, rc, b, pad, neighbor::SelfOp(), map, out, rows_sorted != 0);
+    });
+    }
+
+int nbr_traverse_self_subset_csr(nbr_traverser t, nbr_lbvh h, float rc, const float box[3], float pad,
+                                 const float* images, unsigned int n_images, const unsigned int* map,
+                                 const unsigned int* subset, unsigned int count, unsigned int* nneigh,
+                                 unsigned int* list, const unsigned long long* offsets, const unsigned int* caps,
+                                 int rows_sorted, void* stream)
+    {
+    if (!t || !h || !box) return fail(NBR_ERR_INVALID, "null argument");
+    if (count > 0 && (!subset || !nneigh || !list || !offsets || !caps)) return fail(NBR_ERR_INVALID, "null argument");
+    if (count > h->lbvh.getN()) return fail(NBR_ERR_INVALID, "subset larger than the tree");
+    if (images && n_images > 32) return fail(NBR_ERR_INVALID, "A maximum of 32 image vectors are supported by LBVH traversers.");
+    return guarded([&] {
+        const neighbor::LBVHTraverser::LaunchParameters p(256, as_stream(stream));
+        const neighbor::CSRNeighborListOp out(list, nneigh, offsets, caps, 0u);
+        const float3 b = f3(box);
+        if (images)
+            self_subset_csr(t->trav, h->lbvh, p, rc, b, pad,
+                            neighbor::ImageListOp<float3>(reinterpret_cast<const float3*>(images), n_images), map,
+                            out, rows_sorted != 0, subset, count);
+        else if (n_images == 27)
+            self_subset_csr(t->trav, h->lbvh, p, rc, b, pad, neighbor::PeriodicImagesOp(b), map, out,
+                            rows_sorted != 0, subset, count);
+        else
+            self_subset_csr(t->trav, h->lbvh, p, rc, b, pad, neighbor::SelfOp(), map, out, rows_sorted != 0,
+                            subset, count);
     });
     }
 

@@ -269,3 +269,35 @@ def test_csr_fill_work_order_does_not_change_results():
         out.append((nn.cpu().numpy(), lst.cpu().numpy()))
     assert np.array_equal(out[0][0], out[1][0])
     assert np.array_equal(out[0][1], out[1][1])
+
+
+@pytest.mark.parametrize("rows_sorted", [True, False])
+def test_subset_rows_equal_full_traversal(rows_sorted):
+    P, L = _clustered(40000, 21)
+    lbvh = _tree(P, L)
+    rc = 1.0
+    box = [L, L, L]
+    pad = nb.exact_pad(rc, 2 * L)
+    trav = nb.LBVHTraverser()
+    cnt = trav.traverse_self(lbvh, rc, box, pad, images="periodic", rows_sorted=rows_sorted)
+    op = nb.OnePassList()
+    offsets, total = op.scan(cnt)
+    full = torch.full((total + 1,), -1, dtype=torch.int32, device="cuda")
+    nn_full = trav.traverse_self_csr(lbvh, rc, box, pad, offsets, cnt, full, max_capacity=int(cnt.max().item()),
+                                     images="periodic", rows_sorted=rows_sorted)
+    rng = np.random.default_rng(3)
+    sub = np.sort(rng.choice(len(P), 3000, replace=False)).astype(np.int32)
+    sub = np.concatenate([sub, np.arange(0, len(P), 997, dtype=np.int32)])
+    part = torch.full((total + 1,), -1, dtype=torch.int32, device="cuda")
+    nn = trav.traverse_self_subset_csr(lbvh, rc, box, pad, torch.tensor(sub, device="cuda"), offsets, cnt, part,
+                                       images="periodic", rows_sorted=rows_sorted)
+    prim = lbvh.primitives().cpu().numpy()
+    rows = sub if rows_sorted else prim[sub]
+    off = offsets.cpu().numpy()
+    c = cnt.cpu().numpy()
+    f = full.cpu().numpy()
+    p = part.cpu().numpy()
+    got = nn.cpu().numpy()
+    assert np.array_equal(got[rows], nn_full.cpu().numpy()[rows])
+    for r in rows:
+        assert np.array_equal(p[off[r]:off[r] + c[r]], f[off[r]:off[r] + c[r]])

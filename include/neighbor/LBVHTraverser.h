@@ -299,8 +299,9 @@ void LBVHTraverser::launch_fast(const LaunchParameters& params, const LBVH& lbvh
     else if (m_stats)
         gpu::k_traverse_fast<kind, true, TransformOpT><<<detail::ceil_div(Q, bs), bs, 0, params.stream>>>(
             lbvh.fastData(), a, transform);
-    else if (a.subset)
-        // a subset is a few rows (those that overflowed a one-pass list): one warp walks each
+    else if (a.subset || Q <= gpu::kWarpWalkMaxQueries)
+        // few queries (a subset is the rows that overflowed a one-pass list): one warp walks each,
+        // so the walks' latency, not the GPU's width, sets the time
         gpu::k_traverse_warp<kind, TransformOpT><<<(unsigned int)(((unsigned long long)Q * 32u + gpu::kWarpWalkBlock - 1u)
                                                                   / gpu::kWarpWalkBlock),
                                                    gpu::kWarpWalkBlock, 0, params.stream>>>(lbvh.fastData(), a, transform);

@@ -451,6 +451,9 @@ __global__ void k_traverse_fast(const FastLBVHData tree, const FastQueryArgs a,
 // times shorter, which is what a handful of long rows needs.
 // ---------------------------------------------------------------------------------------------
 constexpr unsigned int kWarpWalkBlock = 256;
+// Up to this many queries, a traversal walks one warp per query: one thread per query would
+// leave most of the GPU's SMs idle.
+constexpr unsigned int kWarpWalkMaxQueries = 16384;
 
 template<int OUT, class TransformOpT>
 __global__ void __launch_bounds__(kWarpWalkBlock) k_traverse_warp(const FastLBVHData tree, const FastQueryArgs a,

@@ -193,13 +193,30 @@ class LBVHTraverser : public Tunable<unsigned int>
         unsigned long long* m_stats;
         bool m_symmetric;
         bool m_work_order = true;
-        // walk lengths of the last symmetric count and what they were measured on
+        // What a symmetric count ran on; a fill with the same tag reuses its results.
+        struct PassTag
+            {
+            const LBVH* tree = nullptr;
+            unsigned long long build = 0;
+            unsigned int N = 0;
+            float rc = 0.f, pad = 0.f;
+            int lattice = -1;
+            float3 L = make_float3(0.f, 0.f, 0.f);
+            float3 box = make_float3(0.f, 0.f, 0.f);
+            int rows_sorted = -1;
+            bool operator==(const PassTag& o) const
+                {
+                return tree == o.tree && build == o.build && N == o.N && rc == o.rc && pad == o.pad
+                       && lattice == o.lattice && L.x == o.L.x && L.y == o.L.y && L.z == o.L.z && box.x == o.box.x
+                       && box.y == o.box.y && box.z == o.box.z && rows_sorted == o.rows_sorted;
+                }
+            };
+        // results of the last symmetric count: walk lengths (by sorted position), own counts and
+        // row totals (by row)
+        PassTag m_count_tag;
         device_array<unsigned short> m_walk;
-        const LBVH* m_walk_tree = nullptr;
-        unsigned long long m_walk_build = 0;
-        float m_walk_rc = 0.f, m_walk_pad = 0.f;
-        int m_walk_lattice = -1;
-        float3 m_walk_L = make_float3(0.f, 0.f, 0.f);
+        device_array<unsigned int> m_count_own;
+        device_array<unsigned int> m_totals;
         device_array<unsigned int> m_own;
 
         template<class TransformOpT>
@@ -448,26 +465,32 @@ void LBVHTraverser::launch_half(const LaunchParameters& params, const LBVH& lbvh
         }
     h.walk_out = nullptr;
     h.walk_in = nullptr;
-    const bool same_walk = m_walk_tree == &lbvh && m_walk_build == lbvh.getBuildCount() && m_walk_rc == a.self_rc
-                           && m_walk_pad == a.pad && m_walk_lattice == a.lattice && m_walk_L.x == a.lattice_L.x
-                           && m_walk_L.y == a.lattice_L.y && m_walk_L.z == a.lattice_L.z;
+    h.totals = nullptr;
+    h.own_counted = nullptr;
+    // what the last symmetric count ran on: this tree and build, cutoff, images, box and rows
+    const PassTag tag{&lbvh, lbvh.getBuildCount(), N, a.self_rc, a.pad, a.lattice, a.lattice_L, a.box,
+                      a.self_rows_sorted};
     if (kind == gpu::kFastCount)
         {
         m_walk.reserve(N);
+        m_count_own.reserve(N);
+        m_totals.reserve(N);
         h.walk_out = m_walk.get();
-        m_walk_tree = &lbvh;
-        m_walk_build = lbvh.getBuildCount();
-        m_walk_rc = a.self_rc;
-        m_walk_pad = a.pad;
-        m_walk_lattice = a.lattice;
-        m_walk_L = a.lattice_L;
+        h.own = m_count_own.get();
+        m_count_tag = tag;
         }
-    else if (m_work_order && same_walk)
+    else if (tag == m_count_tag)
         {
-        h.walk_in = m_walk.get();
+        if (m_work_order) h.walk_in = m_walk.get();
+        h.totals = m_totals.get();
+        h.own_counted = m_count_own.get();
         }
     detail::check_cuda(cudaMemsetAsync(a.nneigh, 0, (size_t)N * sizeof(unsigned int), stream), "memset");
-    gpu::k_traverse_half<kind><<<detail::ceil_div(N, gpu::kHalfBlock), gpu::kHalfBlock, 0, stream>>>(lbvh.fastData(), h);
+    gpu::k_traverse_half<kind, TransformOpT><<<detail::ceil_div(N, gpu::kHalfBlock), gpu::kHalfBlock, 0, stream>>>(
+        lbvh.fastData(), h, transform);
+    if (kind == gpu::kFastCount)
+        detail::check_cuda(cudaMemcpyAsync(m_totals.get(), a.nneigh, (size_t)N * sizeof(unsigned int),
+                                           cudaMemcpyDeviceToDevice, stream), "copy");
     if (kind != gpu::kFastCount)
         {
         gpu::HalfOrderArgs o;

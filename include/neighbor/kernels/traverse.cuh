@@ -582,7 +582,15 @@ struct HalfArgs
     unsigned int* own;       // fill only: entries each row found itself
     unsigned short* walk_out;       // optional: records each query visited (saturated at 65535)
     const unsigned short* walk_in;  // optional: walk lengths of an earlier pass over the same tree
+    // fill only, optional: row totals and own counts of a symmetric count over the same tree and
+    // rows; a query that met the scene through its own image only then writes its entries as
+    // final ids straight after the row's appended entries
+    const unsigned int* totals;
+    const unsigned int* own_counted;
     };
+
+// own[] flag of a row whose own entries were written as final ids after its appended entries
+constexpr unsigned int kOwnPlaced = 0x80000000u;
 
 constexpr unsigned int kHalfBlock = 256;
 
@@ -598,8 +606,9 @@ __device__ __forceinline__ unsigned int half_image_flags(const HalfArgs& a, cons
     return hit ? 1u : 0u;
     }
 
-template<int OUT>
-__global__ void __launch_bounds__(kHalfBlock, 6) k_traverse_half(const FastLBVHData tree, const HalfArgs a)
+template<int OUT, class TransformOpT>
+__global__ void __launch_bounds__(kHalfBlock, 6) k_traverse_half(const FastLBVHData tree, const HalfArgs a,
+                                                                  const TransformOpT transform)
     {
     __shared__ QuantFrame s_frame;
     __shared__ unsigned int s_records;
@@ -641,6 +650,9 @@ __global__ void __launch_bounds__(kHalfBlock, 6) k_traverse_half(const FastLBVHD
     unsigned long long row_first = 0;
     unsigned int cap = 0;
     if (OUT != kFastCount) row_layout<OUT>(a.offsets, a.caps, a.max_neigh, row, row_first, cap);
+    // own entries as final ids from slot own_base on (the row's appended entries come first)
+    const bool placed = OUT != kFastCount && a.totals != nullptr && !multi;
+    const unsigned int own_base = placed ? a.totals[row] - a.own_counted[row] : 0u;
     unsigned int own = 0;
     unsigned int visits = 0;
     // A partner's entry is stored once its slot (the atomic's old value) is known, at the next
@@ -680,8 +692,14 @@ __global__ void __launch_bounds__(kHalfBlock, 6) k_traverse_half(const FastLBVHD
                         }
                     else
                         {
-                        if (own < cap)
+                        if (placed)
+                            {
+                            if (own_base + own < cap) a.list[row_first + own_base + own] = transform(tree.primitive[j]);
+                            }
+                        else if (own < cap)
+                            {
                             a.list[row_first + (cap - 1u - own)] = ((unsigned int)bit << kHalfKeyBits) | j;
+                            }
                         if (j != q)
                             {
                             if (pending && p_slot < p_cap) a.list[p_first + p_slot] = p_key;
@@ -705,11 +723,12 @@ __global__ void __launch_bounds__(kHalfBlock, 6) k_traverse_half(const FastLBVHD
     if (OUT == kFastCount)
         {
         if (own) atomicAdd(a.nneigh + row, own);
+        if (a.own) a.own[row] = own;
         }
     else
         {
         if (pending && p_slot < p_cap) a.list[p_first + p_slot] = p_key;
-        a.own[row] = own;
+        a.own[row] = own | (placed ? kOwnPlaced : 0u);
         }
     if (a.walk_out) a.walk_out[q] = (unsigned short)min(visits, 65535u);
     }
@@ -744,10 +763,37 @@ __global__ void __launch_bounds__(256) k_half_order_rows(const HalfOrderArgs a, 
     const unsigned int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= a.Q || ld_status(a.status) != 0u) return;
     const unsigned int appended = a.nneigh[r];
-    const unsigned int total = appended + a.own[r];
+    const unsigned int own_word = a.own[r];
+    const unsigned int total = appended + (own_word & ~kOwnPlaced);
     a.nneigh[r] = total;
     const unsigned long long first = a.offsets ? a.offsets[r] : (unsigned long long)r * a.max_neigh;
     const unsigned int cap = a.offsets ? a.caps[r] : a.max_neigh;
+    if (own_word & kOwnPlaced)
+        {
+        // own entries are final ids already (after the appended ones): order the appended keys
+        const unsigned int ma = min(appended, min(cap, kHalfRowThread));
+        if (ma == 0u) return;
+        unsigned int* row = a.list + first;
+        unsigned int key[kHalfRowThread];
+#pragma unroll 8
+        for (unsigned int k = 0; k < ma; ++k) key[k] = row[k];
+        for (unsigned int k = 1; k < ma; ++k)
+            {
+            const unsigned int v = key[k];
+            unsigned int j = k;
+            while (j > 0u && key[j - 1u] > v)
+                {
+                key[j] = key[j - 1u];
+                --j;
+                }
+            key[j] = v;
+            }
+#pragma unroll 8
+        for (unsigned int k = 0; k < ma; ++k) key[k] = a.primitive[key[k] & kHalfKeyMask];
+#pragma unroll 8
+        for (unsigned int k = 0; k < ma; ++k) row[k] = transform(key[k]);
+        return;
+        }
     const unsigned int m = min(total, cap);
     if (m == 0u) return;
     // callers route fills with rows longer than kHalfRowThread to the whole-tree walk

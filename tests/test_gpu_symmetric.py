@@ -47,11 +47,18 @@ def _clustered(N, seed, L, per=200):
     return np.mod(p, L).astype(np.float32)
 
 
-def _both(lbvh, rc, box, pad, images, rows_sorted, max_neigh=None, map=None):
+def _both(lbvh, rc, box, pad, images, rows_sorted, max_neigh=None, map=None, travs=None):
+    """(symmetric, whole-tree) results; `travs` keeps the two traversers across calls, so that a
+    fill follows the count of the same traverser (the fill then reuses that count's results)."""
     out = []
-    for sym in (True, False):
-        trav = nb.LBVHTraverser()
-        trav.set_symmetric(sym)
+    for k, sym in enumerate((True, False)):
+        if travs is not None and len(travs) > k:
+            trav = travs[k]
+        else:
+            trav = nb.LBVHTraverser()
+            trav.set_symmetric(sym)
+            if travs is not None:
+                travs.append(trav)
         out.append(trav.traverse_self(lbvh, rc, box, pad, images=images, rows_sorted=rows_sorted,
                                       max_neigh=max_neigh, map=map))
     return out
@@ -79,14 +86,20 @@ def test_symmetric_equals_whole_tree_walk(leaf, dist, images, rows_sorted):
     lbvh.build(_t(P), [0, 0, 0], [L, L, L])
     pad = nb.exact_pad(rc, 2 * L)
     imgs = "periodic" if images == "periodic" else None
-    c_sym, c_full = _both(lbvh, rc, box, pad, imgs, rows_sorted)
+    travs = []
+    c_sym, c_full = _both(lbvh, rc, box, pad, imgs, rows_sorted, travs=travs)
     assert torch.equal(c_sym, c_full)
     mx = int(c_full.max().item())
-    (cs, ls), (cf, lf) = _both(lbvh, rc, box, pad, imgs, rows_sorted, max_neigh=mx)
+    (cs, ls), (cf, lf) = _both(lbvh, rc, box, pad, imgs, rows_sorted, max_neigh=mx, travs=travs)
+    # the same fill without the count's results (a fresh traverser)
+    (cs2, ls2), _ = _both(lbvh, rc, box, pad, imgs, rows_sorted, max_neigh=mx)
+    cs2, ls2 = _rows(cs2, ls2)
     cs, ls = _rows(cs, ls)
     cf, lf = _rows(cf, lf)
     assert np.array_equal(cs, cf)
     assert np.array_equal(ls, lf)  # same entries in the same order
+    assert np.array_equal(cs2, cf)
+    assert np.array_equal(ls2, lf)
     if dist == "clustered":
         assert mx > 32  # rows too long for the symmetric fill
     # the sets are the oracle's (open box: a periodic grid three times wider never wraps a pair)
@@ -165,3 +178,40 @@ def test_work_order_does_not_change_results(N, images):
         out.append(_rows(*trav.traverse_self(lbvh, rc, box, pad, images=imgs, max_neigh=mx)))
     assert np.array_equal(out[0][0], out[1][0])
     assert np.array_equal(out[0][1], out[1][1])
+
+
+@pytest.mark.parametrize("count_rows_sorted,fill_rows_sorted", [(True, True), (False, False), (True, False),
+                                                                (False, True)])
+def test_fill_after_count_with_map_transform(count_rows_sorted, fill_rows_sorted):
+    # the fill reuses the count's row totals only when both ran on the same rows
+    N = 30000
+    P, L = _uniform(N, 52)
+    box = [L, L, L]
+    rc = 1.3
+    lbvh = nb.LBVH()
+    lbvh.build(_t(P), [0, 0, 0], box)
+    pad = nb.exact_pad(rc, 2 * L)
+    m = _t(np.random.default_rng(53).permutation(N).astype(np.int32), torch.int32)
+    whole = nb.LBVHTraverser()
+    whole.set_symmetric(False)
+    cnt_w = whole.traverse_self(lbvh, rc, box, pad, images="periodic", rows_sorted=fill_rows_sorted)
+    mx = int(cnt_w.max().item())
+    cf, lf = _rows(*whole.traverse_self(lbvh, rc, box, pad, images="periodic", rows_sorted=fill_rows_sorted,
+                                        max_neigh=mx, map=m))
+    trav = nb.LBVHTraverser()
+    trav.traverse_self(lbvh, rc, box, pad, images="periodic", rows_sorted=count_rows_sorted)
+    cs, ls = _rows(*trav.traverse_self(lbvh, rc, box, pad, images="periodic", rows_sorted=fill_rows_sorted,
+                                       max_neigh=mx, map=m))
+    assert np.array_equal(cs, cf)
+    assert np.array_equal(ls, lf)
+    # a rebuild invalidates the count's results
+    P2 = np.mod(P + np.random.default_rng(54).normal(size=P.shape).astype(np.float32) * 0.3, L).astype(np.float32)
+    lbvh.build(_t(P2), [0, 0, 0], box)
+    cnt2 = whole.traverse_self(lbvh, rc, box, pad, images="periodic", rows_sorted=fill_rows_sorted)
+    mx2 = int(cnt2.max().item())
+    cf2, lf2 = _rows(*whole.traverse_self(lbvh, rc, box, pad, images="periodic", rows_sorted=fill_rows_sorted,
+                                          max_neigh=mx2))
+    cs2, ls2 = _rows(*trav.traverse_self(lbvh, rc, box, pad, images="periodic", rows_sorted=fill_rows_sorted,
+                                         max_neigh=mx2))
+    assert np.array_equal(cs2, cf2)
+    assert np.array_equal(ls2, lf2)

@@ -227,6 +227,9 @@ class LBVH : public Tunable<unsigned int>
             }
 
     private:
+        // tile shape of the onesweep sort: threads per block, keys per thread
+        static constexpr int kSortBlock = 256;
+        static constexpr int kSortItems = 8;
         // layout of the small scratch buffer (uint32 words)
         static constexpr size_t kSmallHist = 0;            // 4 passes x 1024
         static constexpr size_t kSmallOffsets = 4096;      // 4 passes x 1024
@@ -370,9 +373,9 @@ inline void LBVH::allocate(unsigned int N)
         }
     m_nodes.reserve(nodes);
     m_payload.reserve(N);
-    // one status word per (tile, digit, pass) at the widest configuration: 4 passes x 256 digits
-    // of 4096-key tiles, or 3 passes x 1024 digits of 4096-key tiles
-    const size_t tiles = detail::ceil_div(N, 4096);
+    // one status word per (tile, digit, pass), enough for the widest configuration (4 passes x 256
+    // digits, or 3 passes x 1024 digits) of the sort's tiles
+    const size_t tiles = detail::ceil_div((size_t)N, (size_t)kSortBlock * kSortItems);
     const size_t need = tiles * 4 * 1024;
     if (m_sort_status.size() < need)
         {
@@ -394,8 +397,8 @@ void LBVH::sort_codes(const InsertOpT& insert, const float3& lo, const float3& e
     {
     constexpr int R = gpu::RadixConfig<RB>::kRadix;
     constexpr int P = gpu::RadixConfig<RB>::kPasses;
-    constexpr int BLOCK = 256;
-    constexpr int ITEMS = 16;
+    constexpr int BLOCK = kSortBlock;
+    constexpr int ITEMS = kSortItems;
     typedef gpu::OnesweepConfig<RB, BLOCK, ITEMS> Cfg;
     const unsigned int N = m_N;
     unsigned int* small = m_small.get();
@@ -418,6 +421,13 @@ void LBVH::sort_codes(const InsertOpT& insert, const float3& lo, const float3& e
         detail::check_cuda(cudaFuncSetAttribute(gpu::k_onesweep<InsertOpT, RB, BLOCK, ITEMS, false>,
                                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                 (int)Cfg::kSmemBytes), "onesweep attribute");
+        // all of L1 that can be shared memory: tiles are staged there, several blocks per SM
+        detail::check_cuda(cudaFuncSetAttribute(gpu::k_onesweep<InsertOpT, RB, BLOCK, ITEMS, true>,
+                                                cudaFuncAttributePreferredSharedMemoryCarveout,
+                                                (int)cudaSharedmemCarveoutMaxShared), "onesweep attribute");
+        detail::check_cuda(cudaFuncSetAttribute(gpu::k_onesweep<InsertOpT, RB, BLOCK, ITEMS, false>,
+                                                cudaFuncAttributePreferredSharedMemoryCarveout,
+                                                (int)cudaSharedmemCarveoutMaxShared), "onesweep attribute");
         attr_set[0] = true;
         }
 

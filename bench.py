@@ -686,16 +686,22 @@ def run_ours(args):
         done = [torch.cuda.Event() for _ in range(2)]
         computed = torch.cuda.Event()
 
+        rows_b = [torch.empty(n, dtype=torch.int32, device="cuda") for _ in range(2)]
+        scan_op = nb.OnePassList()
+
         def e2e_step(b, p):
+            # the plain two-pass step with the list in CSR form (count, scan, fill), so that only
+            # the valid entries travel to the host
             lbvh.build(p, [0, 0, 0], box, block_size=args.block)
             trav.traverse_self(lbvh, RC, box, pad, images=imgs, nneigh=cnt_b[b], rows_sorted=True,
                                block_size=args.block)
             mx = int(cnt_b[b].max().item())
-            if mx > cap:
-                raise RuntimeError(f"max neighbors {mx} exceeds the list capacity {cap}")
-            trav.traverse_self(lbvh, RC, box, pad, images=imgs, max_neigh=mx, nneigh=cnt_b[b],
-                               neigh_list=lst_b[b], rows_sorted=True, block_size=args.block)
-            return mx
+            offsets, total = scan_op.scan(cnt_b[b])
+            if total > n * cap:
+                raise RuntimeError(f"{total} pairs exceed the list buffer")
+            trav.traverse_self_csr(lbvh, RC, box, pad, offsets, cnt_b[b], lst_b[b], max_capacity=mx,
+                                   images=imgs, nneigh=rows_b[b], block_size=args.block)
+            return total
 
         e_steps = max(4, min(args.steps, 10))
         h2d = d2h = 0
@@ -708,15 +714,15 @@ def run_ours(args):
             if k >= 2:
                 stream.wait_event(done[b])   # buffers b are free once step k-2's results are home
             dev_in[b].copy_(host_in[k % 2], non_blocking=True)
-            mx = e2e_step(b, dev_in[b])
+            total = e2e_step(b, dev_in[b])
             computed.record(stream)
             with torch.cuda.stream(copy_stream):
                 copy_stream.wait_event(computed)
-                host_counts[b].copy_(cnt_b[b], non_blocking=True)
-                host_list[b][: n * mx].copy_(lst_b[b][: n * mx], non_blocking=True)
+                host_counts[b].copy_(rows_b[b], non_blocking=True)
+                host_list[b][:total].copy_(lst_b[b][:total], non_blocking=True)
                 done[b].record(copy_stream)
             h2d += n * 12
-            d2h += n * 4 + n * mx * 4
+            d2h += n * 4 + total * 4
             e_pairs += pairs_of[k % 2]
         stream.wait_event(done[(e_steps - 1) % 2])
         stream.wait_event(done[e_steps % 2])
@@ -727,7 +733,8 @@ def run_ours(args):
         e2e = {"value": sum_over_ranks(e_pairs, ws) / (max_over_ranks(ems, ws) / 1e3),
                "unit": "pairs/s", "h2d_bytes_per_step": h2d // e_steps,
                "d2h_bytes_per_step": d2h // e_steps, "steps": e_steps,
-               "overlap": "results of step k copied to the host while step k+1 computes"}
+               "overlap": "results of step k copied to the host while step k+1 computes",
+               "list": "CSR (counts + the valid entries), filled by the same two passes"}
 
     if rank != 0:
         return 0

@@ -294,8 +294,9 @@ __global__ void __launch_bounds__(BLOCK) k_batch_systems(const BatchArgs a)
         for (unsigned int s = tid; s < N; s += BLOCK)
             {
             const float4 pl = __ldcg(a.payload + o + s);
+            // point records hold the primitive id (local to the system): the list entries
             records[__ldcg(pre + s + 1u) + s] = make_uint4(__float_as_uint(pl.x), __float_as_uint(pl.y),
-                                                          __float_as_uint(pl.z), kLeafFlag | s);
+                                                          __float_as_uint(pl.z), kLeafFlag | __float_as_uint(pl.w));
             if (s + 1u < N)
                 {
                 const uint2 m = __ldcg(A.nmeta + s);
@@ -326,6 +327,9 @@ __global__ void __launch_bounds__(BLOCK) k_batch_systems(const BatchArgs a)
             const unsigned long long row_first = (unsigned long long)row * a.max_neigh;
             unsigned int flags = lattice_flags(L, f, P, rs);
             const bool multi = __popc(flags) > 1;
+            // a query meeting the scene through its own image only needs no minimum-image wrap
+            const bool plain = !multi && wrap_free(L, rs);
+            const float rc2 = __fmul_rn(rc, rc);
             unsigned int count = 0u;
             while (flags)
                 {
@@ -343,13 +347,11 @@ __global__ void __launch_bounds__(BLOCK) k_batch_systems(const BatchArgs a)
                     if ((int)n.w < 0)
                         {
                         const float3 x = make_float3(__uint_as_float(n.x), __uint_as_float(n.y), __uint_as_float(n.z));
-                        if ((!multi || point_in_box(x, qlo, qhi)) && exact_pair(P, x, rc, L))
+                        const bool accept = plain ? plain_pair(P, x, rc2)
+                                                  : ((!multi || point_in_box(x, qlo, qhi)) && exact_pair(P, x, rc, L));
+                        if (accept)
                             {
-                            if (count < a.max_neigh)
-                                {
-                                const float4 pj = __ldcg(a.payload + o + (n.w & ~kLeafFlag));
-                                a.list[row_first + count] = o + __float_as_uint(pj.w);
-                                }
+                            if (count < a.max_neigh) a.list[row_first + count] = o + (n.w & ~kLeafFlag);
                             ++count;
                             }
                         ++i;

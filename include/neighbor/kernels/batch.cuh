@@ -340,27 +340,35 @@ __global__ void __launch_bounds__(BLOCK) k_batch_systems(const BatchArgs a)
                 const float3 qlo = make_float3(approx::fsub_rd(c.x, rs), approx::fsub_rd(c.y, rs), approx::fsub_rd(c.z, rs));
                 const float3 qhi = make_float3(approx::fadd_ru(c.x, rs), approx::fadd_ru(c.y, rs), approx::fadd_ru(c.z, rs));
                 const uint3 qb = pack_query_box(f, qlo, qhi);
-                unsigned int i = 0u;
-                while (i < n_rec)
-                    {
-                    const uint4 n = records[i];
-                    if ((int)n.w < 0)
+                // the walk, compiled twice: with the no-wrap predicate and with the general one
+                const auto walk = [&](auto plain_tag) {
+                    constexpr bool kPlain = decltype(plain_tag)::value;
+                    unsigned int i = 0u;
+                    while (i < n_rec)
                         {
-                        const float3 x = make_float3(__uint_as_float(n.x), __uint_as_float(n.y), __uint_as_float(n.z));
-                        const bool accept = plain ? plain_pair(P, x, rc2)
-                                                  : ((!multi || point_in_box(x, qlo, qhi)) && exact_pair(P, x, rc, L));
-                        if (accept)
+                        const uint4 n = records[i];
+                        if ((int)n.w < 0)
                             {
-                            if (count < a.max_neigh) a.list[row_first + count] = o + (n.w & ~kLeafFlag);
-                            ++count;
+                            const float3 x = make_float3(__uint_as_float(n.x), __uint_as_float(n.y), __uint_as_float(n.z));
+                            const bool accept = kPlain ? plain_pair(P, x, rc2)
+                                                       : ((!multi || point_in_box(x, qlo, qhi)) && exact_pair(P, x, rc, L));
+                            if (accept)
+                                {
+                                if (count < a.max_neigh) a.list[row_first + count] = o + (n.w & ~kLeafFlag);
+                                ++count;
+                                }
+                            ++i;
                             }
-                        ++i;
+                        else
+                            {
+                            i = node_overlaps(n, qb) ? i + 1u : max(n.w, i + 1u);
+                            }
                         }
-                    else
-                        {
-                        i = node_overlaps(n, qb) ? i + 1u : max(n.w, i + 1u);
-                        }
-                    }
+                };
+                if (plain)
+                    walk(std::true_type());
+                else
+                    walk(std::false_type());
                 }
             a.nneigh[row] = count;
             largest = max(largest, count);

@@ -21,6 +21,8 @@
 #ifndef NEIGHBOR_KERNELS_TRAVERSE_CUH_
 #define NEIGHBOR_KERNELS_TRAVERSE_CUH_
 
+#include <type_traits>
+
 #include "../QueryOps.h"
 #include "../LBVHTraverserData.h"
 #include "common.cuh"
@@ -409,32 +411,40 @@ __global__ void k_traverse_fast(const FastLBVHData tree, const FastQueryArgs a,
         const uint3 qb = pack_query_box(f, qlo, qhi);
         const bool plain = no_wrap && t.x == 0.f && t.y == 0.f && t.z == 0.f;
         if (STATS) ++walks;
-        unsigned int i = 0;
-        while (i < n_rec)
-            {
-            const uint4 n = __ldg(tree.nodes + i);
-            if (STATS) ++visits;
-            if ((int)n.w < 0)
+        // the walk, compiled twice: with the no-wrap predicate and with the general one
+        const auto walk = [&](auto plain_tag) {
+            constexpr bool kPlain = decltype(plain_tag)::value;
+            unsigned int i = 0;
+            while (i < n_rec)
                 {
-                const float3 x = make_float3(__uint_as_float(n.x), __uint_as_float(n.y), __uint_as_float(n.z));
-                if (point_in_box(x, qlo, qhi))
+                const uint4 n = __ldg(tree.nodes + i);
+                if (STATS) ++visits;
+                if ((int)n.w < 0)
                     {
-                    if (STATS) ++tests;
-                    if (plain ? plain_pair(Q.p, x, rc2) : exact_pair(Q.p, x, Q.rc, a.box))
+                    const float3 x = make_float3(__uint_as_float(n.x), __uint_as_float(n.y), __uint_as_float(n.z));
+                    if (point_in_box(x, qlo, qhi))
                         {
-                        if (OUT != kFastCount && count < cap)
-                            a.list[row_first + count] = transform(tree.primitive[n.w & ~kLeafFlag]);
-                        ++count;
+                        if (STATS) ++tests;
+                        if (kPlain ? plain_pair(Q.p, x, rc2) : exact_pair(Q.p, x, Q.rc, a.box))
+                            {
+                            if (OUT != kFastCount && count < cap)
+                                a.list[row_first + count] = transform(tree.primitive[n.w & ~kLeafFlag]);
+                            ++count;
+                            }
                         }
+                    ++i;
                     }
-                ++i;
+                else
+                    {
+                    // skip links point forward in a valid tree; max() keeps a damaged one from looping
+                    i = node_overlaps(n, qb) ? i + 1u : max(n.w, i + 1u);
+                    }
                 }
-            else
-                {
-                // skip links point forward in a valid tree; max() keeps a damaged one from looping
-                i = node_overlaps(n, qb) ? i + 1u : max(n.w, i + 1u);
-                }
-            }
+        };
+        if (plain)
+            walk(std::true_type());
+        else
+            walk(std::false_type());
         }
     a.nneigh[Q.row] = count;
     if (STATS) add_stats(a.stats, visits, tests, walks);
@@ -670,55 +680,60 @@ __global__ void __launch_bounds__(kHalfBlock, 6) k_traverse_half(const FastLBVHD
         const float3 qlo = make_float3(approx::fsub_rd(c.x, rs), approx::fsub_rd(c.y, rs), approx::fsub_rd(c.z, rs));
         const float3 qhi = make_float3(approx::fadd_ru(c.x, rs), approx::fadd_ru(c.y, rs), approx::fadd_ru(c.z, rs));
         const uint3 qb = pack_query_box(f, qlo, qhi);
-        unsigned int i = start;
-        while (i < n_rec)
-            {
-            const uint4 n = __ldg(tree.nodes + i);
-            ++visits;
-            if ((int)n.w < 0)
+        // the walk, compiled twice: with the no-wrap predicate and with the general one
+        const auto walk = [&](auto plain_tag) {
+            constexpr bool kPlain = decltype(plain_tag)::value;
+            unsigned int i = start;
+            while (i < n_rec)
                 {
-                const float3 x = make_float3(__uint_as_float(n.x), __uint_as_float(n.y), __uint_as_float(n.z));
-                bool accept;
-                if (plain)
-                    accept = plain_pair(P, x, rc2);
-                else
-                    accept = (!multi || point_in_box(x, qlo, qhi)) && exact_pair(P, x, a.rc, a.box);
-                if (accept)
+                const uint4 n = __ldg(tree.nodes + i);
+                if (OUT == kFastCount) ++visits;
+                if ((int)n.w < 0)
                     {
-                    const unsigned int j = n.w & ~kLeafFlag;
-                    if (OUT == kFastCount)
+                    const float3 x = make_float3(__uint_as_float(n.x), __uint_as_float(n.y), __uint_as_float(n.z));
+                    const bool accept = kPlain ? plain_pair(P, x, rc2)
+                                               : ((!multi || point_in_box(x, qlo, qhi)) && exact_pair(P, x, a.rc, a.box));
+                    if (accept)
                         {
-                        if (j != q) atomicAdd(a.nneigh + (a.rows_sorted ? j : tree.primitive[j]), 1u);
+                        const unsigned int j = n.w & ~kLeafFlag;
+                        if (OUT == kFastCount)
+                            {
+                            if (j != q) atomicAdd(a.nneigh + (a.rows_sorted ? j : tree.primitive[j]), 1u);
+                            }
+                        else
+                            {
+                            if (placed)
+                                {
+                                if (own_base + own < cap) a.list[row_first + own_base + own] = transform(tree.primitive[j]);
+                                }
+                            else if (own < cap)
+                                {
+                                a.list[row_first + (cap - 1u - own)] = ((unsigned int)bit << kHalfKeyBits) | j;
+                                }
+                            if (j != q)
+                                {
+                                if (pending && p_slot < p_cap) a.list[p_first + p_slot] = p_key;
+                                const unsigned int rj = a.rows_sorted ? j : tree.primitive[j];
+                                p_slot = atomicAdd(a.nneigh + rj, 1u);
+                                row_layout<OUT>(a.offsets, a.caps, a.max_neigh, rj, p_first, p_cap);
+                                p_key = (mirror << kHalfKeyBits) | q;
+                                pending = true;
+                                }
+                            }
+                        ++own;
                         }
-                    else
-                        {
-                        if (placed)
-                            {
-                            if (own_base + own < cap) a.list[row_first + own_base + own] = transform(tree.primitive[j]);
-                            }
-                        else if (own < cap)
-                            {
-                            a.list[row_first + (cap - 1u - own)] = ((unsigned int)bit << kHalfKeyBits) | j;
-                            }
-                        if (j != q)
-                            {
-                            if (pending && p_slot < p_cap) a.list[p_first + p_slot] = p_key;
-                            const unsigned int rj = a.rows_sorted ? j : tree.primitive[j];
-                            p_slot = atomicAdd(a.nneigh + rj, 1u);
-                            row_layout<OUT>(a.offsets, a.caps, a.max_neigh, rj, p_first, p_cap);
-                            p_key = (mirror << kHalfKeyBits) | q;
-                            pending = true;
-                            }
-                        }
-                    ++own;
+                    ++i;
                     }
-                ++i;
+                else
+                    {
+                    i = node_overlaps(n, qb) ? i + 1u : max(n.w, i + 1u);
+                    }
                 }
-            else
-                {
-                i = node_overlaps(n, qb) ? i + 1u : max(n.w, i + 1u);
-                }
-            }
+        };
+        if (plain)
+            walk(std::true_type());
+        else
+            walk(std::false_type());
         }
     if (OUT == kFastCount)
         {

@@ -233,8 +233,9 @@ CLUSTERED_CAP_MAX = 1 << 16
 
 
 def train_capacity_model(nb, lbvh, trav, frames, L, rc, steps, periodic=True, quantile=0.999):
-    """Train the capacity network on exact counts of the given frames (plain method) and set its
-    margin to the quantile of the training residuals.  Returns (model, seconds, final loss)."""
+    """Train the capacity network on exact counts of the given frames (plain method) and calibrate
+    its margins: per bin of the output, the quantile of the training residuals.  Returns (model,
+    seconds, final loss)."""
     import torch
     t0 = time.perf_counter()
     model = nb.CapacityModel(seed=7)
@@ -250,13 +251,12 @@ def train_capacity_model(nb, lbvh, trav, frames, L, rc, steps, periodic=True, qu
     F = torch.cat(feats)
     T = torch.cat(targs)
     loss = model.train(F, T, steps=steps, batch=16384, lr=3e-3, seed=3)
-    resid = []
-    for p, t in zip(frames, targs):
+    ys = []
+    for p in frames:
         lbvh.build(p, [0, 0, 0], box)
         _, y = model.predict(lbvh, [0, 0, 0], box, rc, periodic=periodic, want_y=True)
-        resid.append(t - y)
-    r, _ = torch.sort(torch.cat(resid))
-    model.margin = float(r[min(len(r) - 1, int(quantile * len(r)))].item())
+        ys.append(y)
+    model.calibrate(T, torch.cat(ys), quantile=quantile)
     torch.cuda.synchronize()
     return model, time.perf_counter() - t0, loss
 
@@ -302,7 +302,7 @@ def learned_uniform(nb, n, L, frames, warmup, plain_ms, pairs_step, args, stream
     return {"ms_per_step": ms, "value": pairs_step / (ms * 1e-3), "unit": "pairs/s",
             "vs_plain": plain_ms / ms, "slots_per_point": stats[-1]["slots"] / n,
             "overflow_rows_mean": sum(ovf) / len(ovf), "counts_equal_plain": exact,
-            "margin": model.margin, "cap_max": UNIFORM_CAP_MAX, "train_s": round(train_s, 2),
+            "margin": model.margin, "margins": [round(v, 3) for v in model.margins], "cap_max": UNIFORM_CAP_MAX, "train_s": round(train_s, 2),
             "train_loss": loss, "train_frames": "1 frame, seed distinct from the timed frames"}
 
 
@@ -370,7 +370,8 @@ def clustered_c3(nb, args, stream, n=4_000_000, rc=1.0, steps=5, warmup=2):
             "pairs_per_step": pairs, "max_count": int(cnt.max().item()),
             "learned_slots_per_point": stats[-1]["slots"] / n,
             "overflow_rows_mean": sum(s["overflow_rows"] for s in stats) / len(stats),
-            "counts_equal_plain": exact, "margin": model.margin, "train_s": round(train_s, 2),
+            "counts_equal_plain": exact, "margin": model.margin,
+            "margins": [round(v, 3) for v in model.margins], "train_s": round(train_s, 2),
             "train_loss": loss, "plain": "count + exclusive scan + exact CSR fill",
             "learned": "capacity network (overlapping the build after its sort) + one CSR fill + exact "
                        "re-run of overflowed rows"}

@@ -30,8 +30,9 @@ class CapacityModel
         static constexpr int kParams = gpu::kCapParams;
         static constexpr int kFeatures = gpu::kCapIn;
 
-        explicit CapacityModel(unsigned long long seed = 1) : m_step(0), m_margin(0.f)
+        explicit CapacityModel(unsigned long long seed = 1) : m_step(0)
             {
+            setMargin(0.f);
             m_p.reserve(kParams);
             m_m.reserve(kParams);
             m_v.reserve(kParams);
@@ -155,7 +156,7 @@ class CapacityModel
             a.occ = m_occ.get();
             a.w = m_w.get();
             a.p = m_p.get();
-            a.margin = m_margin;
+            for (int b = 0; b < gpu::kCapMarginBins; ++b) a.margins[b] = m_margins[b];
             a.cap_max = cap_max;
             a.rows_sorted = rows_sorted ? 1 : 0;
             a.y_out = y;
@@ -250,8 +251,29 @@ class CapacityModel
             detail::check_cuda(cudaGetLastError(), "adam launch");
             }
 
-        void setMargin(float margin) { m_margin = margin; }
-        float getMargin() const { return m_margin; }
+        // One margin for every output (capacity = ceil(expm1(y + margin))).
+        void setMargin(float margin)
+            {
+            for (int b = 0; b < gpu::kCapMarginBins; ++b) m_margins[b] = margin;
+            }
+        // The largest margin of the table.
+        float getMargin() const
+            {
+            float m = m_margins[0];
+            for (int b = 1; b < gpu::kCapMarginBins; ++b) m = std::fmax(m, m_margins[b]);
+            return m;
+            }
+        // Calibration table: margin of the outputs y in [b/2, (b+1)/2) for b < kMarginBins - 1, the
+        // last bin open-ended.
+        static constexpr int kMarginBins = gpu::kCapMarginBins;
+        void setMargins(const float* margins)
+            {
+            for (int b = 0; b < gpu::kCapMarginBins; ++b) m_margins[b] = margins[b];
+            }
+        void getMargins(float* margins) const
+            {
+            for (int b = 0; b < gpu::kCapMarginBins; ++b) margins[b] = m_margins[b];
+            }
 
         void getParams(float* host) const
             {
@@ -281,7 +303,7 @@ class CapacityModel
         device_array<__nv_bfloat16> m_w;
         device_array<unsigned int> m_occ;
         unsigned int m_step;
-        float m_margin;
+        float m_margins[gpu::kCapMarginBins];
 
         void launch_train(const float* features, const float* targets, unsigned int N, unsigned int batch,
                           unsigned int offset, unsigned int stride, float* grad, float* loss, cudaStream_t stream)

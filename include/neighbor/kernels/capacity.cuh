@@ -15,7 +15,8 @@
 // hidden activations rounded to BF16 (the operands of the two tensor-core layers), the second
 // hidden layer kept in FP32 for the output dot product, every product accumulated in FP32,
 // biases FP32.  The output
-// approximates log1p(count); capacity = ceil(expm1(y + margin)), clamped to [1, cap_max].
+// approximates log1p(count); capacity = ceil(expm1(y + margin(y))), clamped to [1, cap_max], where
+// margin(y) is a calibration table over bins of 0.5 in y (kCapMarginBins bins, the last open).
 //
 //   k_cap_occupancy      occupancy grid from the sorted Morton codes (warp-aggregated atomics)
 //   k_cap_features       the 32 features of every sorted point (training data, tests)
@@ -197,6 +198,13 @@ __global__ void __launch_bounds__(256) k_cap_features(const CapFrame fr, const u
 __device__ __forceinline__ float cap_softplus(float z) { return fmaxf(z, 0.f) + log1pf(expf(-fabsf(z))); }
 __device__ __forceinline__ float cap_sigmoid(float z) { return 1.f / (1.f + expf(-z)); }
 
+constexpr int kCapMarginBins = 16;
+__host__ __device__ __forceinline__ int cap_margin_bin(float y)
+    {
+    const float b = floorf(y * 2.f);
+    return b <= 0.f ? 0 : (b >= (float)(kCapMarginBins - 1) ? kCapMarginBins - 1 : (int)b);
+    }
+
 __device__ __forceinline__ unsigned int cap_from_output(float y, float margin, unsigned int cap_max)
     {
     const float c = ceilf(expm1f(y + margin));
@@ -225,7 +233,7 @@ struct CapInferArgs
     const unsigned int* occ;
     const __nv_bfloat16* w;         // BF16 weights (kCapBfWeights)
     const float* p;                 // FP32 parameters (biases read from here)
-    float margin;
+    float margins[kCapMarginBins];  // calibration: margin of each bin of y
     unsigned int cap_max;
     int rows_sorted;                // row of sorted position s: s or primitive id
     float* y_out;                   // optional: network output per row
@@ -464,7 +472,7 @@ __global__ void __launch_bounds__(kCapInferWarps * 32, 2) k_cap_infer(const CapI
                     const float y = cap_softplus((t == 0u ? z0 : z1) + b3);
                     const unsigned int row = cap_row(a, s);
                     if (a.y_out) a.y_out[row] = y;
-                    a.cap_out[row] = cap_from_output(y, a.margin, a.cap_max);
+                    a.cap_out[row] = cap_from_output(y, a.margins[cap_margin_bin(y)], a.cap_max);
                     }
                 }
             }

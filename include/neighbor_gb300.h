@@ -237,9 +237,14 @@ int nbr_capmodel_create(nbr_capmodel* out, unsigned long long seed);
 int nbr_capmodel_destroy(nbr_capmodel m);
 int nbr_capmodel_get_params(nbr_capmodel m, float* host_params);
 int nbr_capmodel_set_params(nbr_capmodel m, const float* host_params);
-/* Capacity = ceil(expm1(output + margin)) clamped to [1, cap_max]. */
+/* Capacity = ceil(expm1(output + margin(output))) clamped to [1, cap_max].  set_margin sets one
+ * margin for every output, get_margin returns the largest; set/get_margins the calibration table of
+ * NBR_CAP_MARGIN_BINS margins over bins of 0.5 in the output (the last bin open-ended). */
+#define NBR_CAP_MARGIN_BINS 16
 int nbr_capmodel_set_margin(nbr_capmodel m, float margin);
 int nbr_capmodel_get_margin(nbr_capmodel m, float* margin);
+int nbr_capmodel_set_margins(nbr_capmodel m, const float* margins);
+int nbr_capmodel_get_margins(nbr_capmodel m, float* margins);
 /* Coarse-cell level the features use for cutoff rc in a scene of extent hi - lo. */
 int nbr_capmodel_level(float rc, const float lo[3], const float hi[3], unsigned int* level);
 /* Features (float[N][32]) of every sorted point of a built point tree; lo/hi = the build's scene

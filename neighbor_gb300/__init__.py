@@ -117,6 +117,8 @@ def _declare(L):
     sig("nbr_capmodel_set_params", [_P, _P])
     sig("nbr_capmodel_set_margin", [_P, _F])
     sig("nbr_capmodel_get_margin", [_P, ctypes.POINTER(_F)])
+    sig("nbr_capmodel_set_margins", [_P, _P])
+    sig("nbr_capmodel_get_margins", [_P, _P])
     sig("nbr_capmodel_level", [_F, _P, _P, ctypes.POINTER(_U)])
     sig("nbr_capmodel_features", [_P, _P, _P, _P, _F, _I, _P, _P])
     sig("nbr_capmodel_predict", [_P, _P, _P, _P, _F, _I, _I, _U, _P, _P, _P])
@@ -160,6 +162,7 @@ EXPORTED = ["nbr_last_error", "nbr_version", "nbr_lbvh_create", "nbr_lbvh_destro
             "nbr_traverse_self_subset_csr",
             "nbr_capmodel_create", "nbr_capmodel_destroy", "nbr_capmodel_get_params",
             "nbr_capmodel_set_params", "nbr_capmodel_set_margin", "nbr_capmodel_get_margin",
+            "nbr_capmodel_set_margins", "nbr_capmodel_get_margins",
             "nbr_capmodel_level", "nbr_capmodel_features", "nbr_capmodel_predict",
             "nbr_capmodel_targets", "nbr_capmodel_gradient", "nbr_capmodel_train",
             "nbr_onepass_create", "nbr_onepass_destroy", "nbr_onepass_capacity",
@@ -173,6 +176,7 @@ BATCH_MAX_N = 16384
 
 CAP_PARAMS = 6337
 CAP_FEATURES = 32
+CAP_MARGIN_BINS = 16
 
 NOALLOC_MAX_POINTS = 1 << 20
 
@@ -632,6 +636,40 @@ class CapacityModel:
     @margin.setter
     def margin(self, value: float):
         _check(self._L.nbr_capmodel_set_margin(self._h, float(value)))
+
+    @property
+    def margins(self):
+        """Calibration table: margin of each bin of 0.5 in the output (the last bin open)."""
+        t = (ctypes.c_float * CAP_MARGIN_BINS)()
+        _check(self._L.nbr_capmodel_get_margins(self._h, ctypes.cast(t, ctypes.c_void_p)))
+        return list(t)
+
+    @margins.setter
+    def margins(self, table):
+        t = (ctypes.c_float * CAP_MARGIN_BINS)(*[float(v) for v in table])
+        _check(self._L.nbr_capmodel_set_margins(self._h, ctypes.cast(t, ctypes.c_void_p)))
+
+    def calibrate(self, targets, y, quantile: float = 0.999, min_rows: int = 1000):
+        """Set the calibration table from residuals: bin b gets the `quantile` of target - y over the
+        rows whose output y falls in bin b (width 0.5, the last bin open, as the inference bins
+        it); a bin with fewer than min_rows rows gets the quantile over all rows.  Returns it."""
+        torch = _torch()
+        t = _dev(targets, torch.float32).reshape(-1)
+        yy = _dev(y, torch.float32).reshape(-1)
+        r = t - yy
+        b = torch.clamp(torch.floor(yy * 2.0), 0, CAP_MARGIN_BINS - 1).to(torch.int64)
+
+        def q(v):
+            s, _ = torch.sort(v)
+            return float(s[min(s.numel() - 1, int(quantile * s.numel()))].item())
+
+        overall = q(r)
+        table = []
+        for k in range(CAP_MARGIN_BINS):
+            sel = r[b == k]
+            table.append(q(sel) if sel.numel() >= min_rows else overall)
+        self.margins = table
+        return table
 
     @staticmethod
     def level(rc, lo, hi) -> int:

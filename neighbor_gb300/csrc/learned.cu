@@ -8,6 +8,8 @@
 #include "neighbor/CapacityModel.h"
 #include "neighbor/OnePassList.h"
 
+static_assert(NBR_CAP_MARGIN_BINS == neighbor::CapacityModel::kMarginBins, "margin table size");
+
 struct nbr_capmodel_s
     {
     explicit nbr_capmodel_s(unsigned long long seed) : model(seed) {}
@@ -139,6 +141,20 @@ int nbr_capmodel_get_margin(nbr_capmodel m, float* margin)
     {
     if (!m || !margin) return fail(NBR_ERR_INVALID, "null argument");
     *margin = m->model.getMargin();
+    return NBR_OK;
+    }
+
+int nbr_capmodel_set_margins(nbr_capmodel m, const float* margins)
+    {
+    if (!m || !margins) return fail(NBR_ERR_INVALID, "null argument");
+    m->model.setMargins(margins);
+    return NBR_OK;
+    }
+
+int nbr_capmodel_get_margins(nbr_capmodel m, float* margins)
+    {
+    if (!m || !margins) return fail(NBR_ERR_INVALID, "null argument");
+    m->model.getMargins(margins);
     return NBR_OK;
     }
 

@@ -301,3 +301,27 @@ def test_subset_rows_equal_full_traversal(rows_sorted):
     assert np.array_equal(got[rows], nn_full.cpu().numpy()[rows])
     for r in rows:
         assert np.array_equal(p[off[r]:off[r] + c[r]], f[off[r]:off[r] + c[r]])
+
+
+def test_margin_table_bins_outputs():
+    # each row's capacity uses the margin of its output's bin (bins of 0.5, the last open)
+    P, L = _clustered(40000, 31)
+    lbvh = _tree(P, L)
+    rc = 1.0
+    model = nb.CapacityModel(seed=11)
+    table = [0.05 * k for k in range(nb.CAP_MARGIN_BINS)]
+    model.margins = table
+    assert np.allclose(model.margins, table)
+    assert model.margin == pytest.approx(max(table))
+    caps, y = model.predict(lbvh, [0, 0, 0], [L, L, L], rc, cap_max=4096, want_y=True)
+    yv = y.cpu().numpy().astype(np.float32)
+    b = np.clip(np.floor(yv * np.float32(2.0)), 0, nb.CAP_MARGIN_BINS - 1).astype(int)
+    m = np.asarray(table, np.float32)[b]
+    want = np.clip(np.ceil(np.expm1((yv + m).astype(np.float64))), 1, 4096)
+    assert np.mean(caps.cpu().numpy().view(np.uint32) == want) > 0.999
+    # calibration: residuals of a bin land in that bin's margin
+    t = torch.tensor((yv + 0.1 + (b >= 4) * 0.5).astype(np.float32), device="cuda")
+    got = model.calibrate(t, y, quantile=0.5, min_rows=1)
+    for k in range(nb.CAP_MARGIN_BINS):
+        if np.any(b == k):
+            assert got[k] == pytest.approx(0.1 + (0.5 if k >= 4 else 0.0), abs=1e-3)

@@ -54,7 +54,7 @@ def parse():
     ap.add_argument("--no-clustered", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-polydisperse", action="store_true")
-    ap.add_argument("--train-steps", type=int, default=400)
+    ap.add_argument("--train-steps", type=int, default=4000)
     ap.add_argument("--climb", type=int, default=512)
     ap.add_argument("--no-work-order", action="store_true",
                     help="fills take queries in sorted order instead of by walk length / capacity")

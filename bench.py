@@ -35,7 +35,7 @@ RC = 1.3
 SIGMA = 0.05
 
 
-def parse():
+def parse(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
@@ -58,7 +58,7 @@ def parse():
     ap.add_argument("--climb", type=int, default=512)
     ap.add_argument("--no-work-order", action="store_true",
                     help="fills take queries in sorted order instead of by walk length / capacity")
-    return ap.parse_args()
+    return ap.parse_args(argv)
 
 
 def stage_traffic(stage, n):
@@ -166,12 +166,18 @@ def barrier(ws):
         dist.barrier()
 
 
+def _reduce_device():
+    """Where the process group reduces: the GPU under NCCL, the host under gloo."""
+    import torch.distributed as dist
+    return "cuda" if dist.get_backend() == "nccl" else "cpu"
+
+
 def max_over_ranks(x, ws):
     if ws == 1:
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    t = torch.tensor([x], dtype=torch.float64, device=_reduce_device())
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
@@ -181,9 +187,17 @@ def sum_over_ranks(x, ws):
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    t = torch.tensor([x], dtype=torch.float64, device=_reduce_device())
     dist.all_reduce(t, op=dist.ReduceOp.SUM)
     return float(t.item())
+
+
+def replica_throughput(pairs_local, ms_local, ws):
+    """Whole-job throughput of independent replicas: the pairs of every rank over the slowest
+    rank's time (weak scaling).  Returns (pairs/s, pairs of all ranks, max ms)."""
+    ms = max_over_ranks(ms_local, ws)
+    pairs = sum_over_ranks(pairs_local, ws)
+    return pairs / (ms / 1e3), pairs, ms
 
 
 def make_frames(n, L, count, seed):
@@ -646,8 +660,7 @@ def run_ours(args):
                            block_size=args.block)
         pair_counts.append(int(counts.cpu().numpy().astype(np.int64).sum()))
     pairs_local = float(sum(pair_counts))
-    ms_max = max_over_ranks(ms, ws)
-    pairs_all = sum_over_ranks(pairs_local, ws)
+    value, pairs_all, ms_max = replica_throughput(pairs_local, ms, ws)
     gap_max_ms = [r[2].elapsed_time(r[3]) for r in recs]
     gap_step_ms = [recs[k][4].elapsed_time(recs[k + 1][0]) for k in range(len(recs) - 1)]
     build_ms = [r[0].elapsed_time(r[1]) for r in recs]
@@ -755,7 +768,7 @@ def run_ours(args):
     step_bytes = 12.0 * n + 16.0 * n + 4.0 * n + 4.0 * pairs_step
     line = {
         "metric": "neighbor pairs/s (build+traverse) at 16M pts",
-        "value": pairs_all / (ms_max / 1e3),
+        "value": value,
         "unit": "pairs/s",
         "n_gpus": ws,
         "steps": args.steps,

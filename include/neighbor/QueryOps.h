@@ -144,12 +144,12 @@ __device__ __forceinline__ bool exact_pair_f64(const double3& pi, const double3&
 // 2 (rc + pad) every neighbor is found through exactly one image.
 struct ExactSphereQueryOpF64
     {
-    ExactSphereQueryOpF64(const double4* spheres_, unsigned int N_, const double3* points_, double3 box_,
+    ExactSphereQueryOpF64(const double4_16a* spheres_, unsigned int N_, const double3* points_, double3 box_,
                           float pad_)
         : spheres(spheres_), N(N_), points(points_), box(box_), pad(pad_)
         {}
 
-    typedef double4 ThreadData;
+    typedef double4_16a ThreadData;
     typedef BoundingSphere Volume;
 
     __device__ __forceinline__ ThreadData setup(const unsigned int idx) const { return spheres[idx]; }
@@ -173,7 +173,7 @@ struct ExactSphereQueryOpF64
 
     __host__ __device__ __forceinline__ unsigned int size() const { return N; }
 
-    const double4* spheres;
+    const double4_16a* spheres;
     const unsigned int N;
     const double3* points;
     const double3 box;

@@ -379,7 +379,7 @@ int nbr_traverse_f64(nbr_traverser t, nbr_lbvh h, const double* spheres, unsigne
     return guarded([&] {
         const neighbor::LBVHTraverser::LaunchParameters p(block_size, as_stream(stream));
         const double3 b = make_double3(box[0], box[1], box[2]);
-        const neighbor::ExactSphereQueryOpF64 q(reinterpret_cast<const double4*>(spheres), Q,
+        const neighbor::ExactSphereQueryOpF64 q(reinterpret_cast<const double4_16a*>(spheres), Q,
                                                 reinterpret_cast<const double3*>(points), b, pad);
         const float3 bf = make_float3((float)box[0], (float)box[1], (float)box[2]);
         auto go = [&](const auto& out) {

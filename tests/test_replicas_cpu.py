@@ -38,7 +38,7 @@ def _worker(rank, ws, port, out):
 
 def test_replica_throughput_two_ranks():
     ws = 2
-    out = mp.Manager().dict()
+    out = mp.get_context("spawn").Manager().dict()
     mp.spawn(_worker, args=(ws, _free_port(), out), nprocs=ws, join=True)
     for r in range(ws):
         value, pairs, ms = out[r]

@@ -21,7 +21,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(os.path.dirname(HERE), "_ref")
 CUBIN = os.path.join(OUT, "ref_kernels.cubin")
 DRIVER = os.path.join(OUT, "ref_driver")
-REFERENCE_INCLUDE = "/root/reference/include"  # the reference sources (development container only)
+REFERENCE_INCLUDE = "/root/reference/include"  # the reference sources, where they exist
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

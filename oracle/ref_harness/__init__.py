@@ -2,8 +2,8 @@
 
 Builds and runs the reference's own CUDA kernels (mphowardlab/neighbor v0.3.2) on the GPU:
 ``ref_kernels.cu`` instantiates them from the reference headers into
-``oracle/_ref/ref_kernels.cubin`` (only where the reference sources exist, i.e. the development
-container), and ``ref_driver.cu`` -- compiled wherever that cubin exists -- loads it and replays
+``oracle/_ref/ref_kernels.cubin`` (only where the reference sources exist), and
+``ref_driver.cu`` -- compiled wherever that cubin exists -- loads it and replays
 the reference's build / setup / traverse sequence.  Used by the parity tests (to pin the oracle
 and the library against the real reference) and by bench.py (to time the reference on the same
 GPU).  The product never touches it.

@@ -61,15 +61,20 @@ def parse(argv=None):
     return ap.parse_args(argv)
 
 
+def stage_profile(stage):
+    """The committed ncu figures of a stage (an 8M-point capture), or {}."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "stage_traffic.json")) as f:
+            return json.load(f).get(stage, {})
+    except Exception:
+        return {}
+
+
 def stage_traffic(stage, n):
     """DRAM bytes of one stage per launch, scaled from the committed ncu summary (bytes per point
     of an 8M-point capture; the traffic grows with the points), or None."""
-    try:
-        with open(os.path.join(ROOT, "profiles", "stage_traffic.json")) as f:
-            t = json.load(f)
-        return t[stage]["dram_bytes_per_point"] * n / 1e9
-    except Exception:
-        return None
+    t = stage_profile(stage).get("dram_bytes_per_point")
+    return None if t is None else t * n / 1e9
 
 
 def load_peaks():
@@ -792,6 +797,9 @@ def run_ours(args):
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
                      "traffic": stage_traffic(dom, n),
+                     # what bounds the traversal instead: instruction issue (ncu, 8M capture)
+                     "issue_active_pct": stage_profile(dom).get("issue_active_pct"),
+                     "lanes_active": stage_profile(dom).get("lanes_active_per_warp_instruction"),
                      "step_achieved": step_bytes / (ms_max / args.steps * 1e-3) / 1e9},
         # per step: histogram, digit offsets, one onesweep per pass, climb, climb across blocks,
         # scan, emit (build) + count traversal + fill traversal (+ row ordering for rows <= 32)

@@ -43,6 +43,9 @@ def _cases():
     out.append(("clustered", p, L, 1.0))
     out.append(("duplicates", np.tile(np.float32([[3.0, 4.0, 5.0]]), (300, 1)), 8.0, 0.7))
     out.append(("small", (rng.random((5, 3)) * 6).astype(np.float32), 6.0, 2.0))
+    # the small plain configuration: 32,768 uniform points at density 0.85, cutoff 1.3
+    Lc = float((32768 / 0.85) ** (1.0 / 3.0))
+    out.append(("uniform32k", (rng.random((32768, 3)) * Lc).astype(np.float32), Lc, 1.3))
     return out
 
 

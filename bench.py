@@ -701,9 +701,12 @@ def run_ours(args):
         lst_b = [lst, torch.empty(n * cap, dtype=torch.int32, device="cuda")]
         host_counts = [torch.empty(n, dtype=torch.int32).pin_memory() for _ in range(2)]
         host_list = [torch.empty(n * cap, dtype=torch.int32).pin_memory() for _ in range(2)]
-        copy_stream = torch.cuda.Stream()
+        copy_stream = torch.cuda.Stream()   # results to the host
+        load_stream = torch.cuda.Stream()   # inputs to the device
         done = [torch.cuda.Event() for _ in range(2)]
-        computed = torch.cuda.Event()
+        computed = [torch.cuda.Event() for _ in range(2)]
+        loaded = [torch.cuda.Event() for _ in range(2)]
+        started = torch.cuda.Event()
 
         rows_b = [torch.empty(n, dtype=torch.int32, device="cuda") for _ in range(2)]
         scan_op = nb.OnePassList()
@@ -728,15 +731,28 @@ def run_ours(args):
         torch.cuda.synchronize()
         e0, e1 = ev(), ev()
         e0.record(stream)
+        started.record(stream)
+
+        def load(k):
+            # step k's frame into input buffer k % 2, once step k - 2 (its last user) has computed
+            bb = k % 2
+            with torch.cuda.stream(load_stream):
+                load_stream.wait_event(started if k < 2 else computed[bb])
+                dev_in[bb].copy_(host_in[k % 2], non_blocking=True)
+                loaded[bb].record(load_stream)
+
+        load(0)
         for k in range(e_steps):
             b = k % 2
+            if k + 1 < e_steps:
+                load(k + 1)                  # the next frame travels while this step computes
+            stream.wait_event(loaded[b])
             if k >= 2:
                 stream.wait_event(done[b])   # buffers b are free once step k-2's results are home
-            dev_in[b].copy_(host_in[k % 2], non_blocking=True)
             total = e2e_step(b, dev_in[b])
-            computed.record(stream)
+            computed[b].record(stream)
             with torch.cuda.stream(copy_stream):
-                copy_stream.wait_event(computed)
+                copy_stream.wait_event(computed[b])
                 host_counts[b].copy_(rows_b[b], non_blocking=True)
                 host_list[b][:total].copy_(lst_b[b][:total], non_blocking=True)
                 done[b].record(copy_stream)
@@ -752,7 +768,7 @@ def run_ours(args):
         e2e = {"value": sum_over_ranks(e_pairs, ws) / (max_over_ranks(ems, ws) / 1e3),
                "unit": "pairs/s", "h2d_bytes_per_step": h2d // e_steps,
                "d2h_bytes_per_step": d2h // e_steps, "steps": e_steps,
-               "overlap": "results of step k copied to the host while step k+1 computes",
+               "overlap": "step k+1's frame copied in and step k's results copied out while steps compute",
                "list": "CSR (counts + the valid entries), filled by the same two passes"}
 
     if rank != 0:

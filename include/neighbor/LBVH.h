@@ -407,8 +407,9 @@ void LBVH::sort_codes(const InsertOpT& insert, const float3& lo, const float3& e
     // digit histograms of every pass + bounds
     {
     const unsigned int grid = std::min(detail::ceil_div(N, 256), 152u * 8u);
+    // the codes also go to the buffer the first sort pass reads
     gpu::k_codes_histogram<InsertOpT, RB><<<grid, 256, 0, stream>>>(insert, N, lo, ext, small + kSmallHist,
-                                                                    small + kSmallBounds);
+                                                                    small + kSmallBounds, m_codes.current().get());
     gpu::k_digit_offsets<RB><<<P, 1024, 0, stream>>>(small + kSmallHist, small + kSmallOffsets);
     }
 

@@ -91,14 +91,16 @@ __device__ __forceinline__ unsigned int block_exclusive_scan_smem(unsigned int* 
     }
 
 // ---------------------------------------------------------------------------------------------
-// Morton codes -> histograms of every pass, and the bounds of all leaf boxes.
+// Morton codes -> histograms of every pass, and the bounds of all leaf boxes; the codes go to
+// codes_out too when it is given (the first sort pass then reads them instead of recomputing).
 // bounds[0..2] = max of ~ordered(lo), bounds[3..5] = max of ordered(hi); all start at zero.
 // ---------------------------------------------------------------------------------------------
 template<class InsertOpT, int RB>
 __global__ void __launch_bounds__(256) k_codes_histogram(const InsertOpT insert, unsigned int N,
                                                          float3 scene_lo, float3 scene_ext,
                                                          unsigned int* __restrict__ hist,
-                                                         unsigned int* __restrict__ bounds)
+                                                         unsigned int* __restrict__ bounds,
+                                                         unsigned int* __restrict__ codes_out = nullptr)
     {
     constexpr int R = RadixConfig<RB>::kRadix;
     constexpr int P = RadixConfig<RB>::kPasses;
@@ -120,6 +122,7 @@ __global__ void __launch_bounds__(256) k_codes_histogram(const InsertOpT insert,
         bmax.y = fmaxf(bmax.y, b.hi.y);
         bmax.z = fmaxf(bmax.z, b.hi.z);
         const unsigned int code = morton_code(b, scene_lo, scene_ext);
+        if (codes_out) codes_out[i] = code;
 #pragma unroll
         for (int p = 0; p < P; ++p) atomicAdd(&s_hist[p * R + ((code >> (p * RB)) & (R - 1))], 1u);
         }
@@ -250,7 +253,8 @@ __global__ void __launch_bounds__(BLOCK, ITEMS <= 8 ? 4 : 2) k_onesweep(const In
             {
             if (FIRST)
                 {
-                keys[j] = morton_code(insert.get(idx), scene_lo, scene_ext);
+                // the codes of the histogram pass when given, else computed here
+                keys[j] = keys_in ? keys_in[idx] : morton_code(insert.get(idx), scene_lo, scene_ext);
                 vals[j] = idx;
                 }
             else

@@ -101,4 +101,8 @@ def run_dump(points, lo, hi, rc, box, timeout=300):
             stride = max(1, int(out["count_exact"].max()))
             out["list_exact"] = np.fromfile(lpath, np.uint32).reshape(n, stride)
             out["count_list"] = np.fromfile(prefix + ".count_list", np.uint32)
+        spath = prefix + ".list_stock"
+        if os.path.exists(spath) and "count_stock" in out and n:
+            stride = max(1, int(out["count_stock"].max()))
+            out["list_stock"] = np.fromfile(spath, np.uint32).reshape(n, stride)
         return out

@@ -62,7 +62,7 @@ void checkd(CUresult e, const char* what)
 struct Kernels
     {
     CUfunction gen_codes = nullptr, gen_tree = nullptr, bubble = nullptr, one = nullptr, compress = nullptr;
-    CUfunction count_stock = nullptr, count_exact = nullptr, list_exact = nullptr;
+    CUfunction count_stock = nullptr, count_exact = nullptr, list_exact = nullptr, list_stock = nullptr;
     };
 
 Kernels load_kernels(const char* cubin)
@@ -91,8 +91,10 @@ Kernels load_kernels(const char* cubin)
         else if (has("lbvh_traverse_ropes") && has("CountNeighborsOp") && has("SphereQueryOp")) k.count_stock = f;
         else if (has("lbvh_traverse_ropes") && has("CountNeighborsOp") && has("RefExactQueryOp")) k.count_exact = f;
         else if (has("lbvh_traverse_ropes") && has("NeighborListOp") && has("RefExactQueryOp")) k.list_exact = f;
+        else if (has("lbvh_traverse_ropes") && has("NeighborListOp") && has("SphereQueryOp")) k.list_stock = f;
         }
-    if (!k.gen_codes || !k.gen_tree || !k.bubble || !k.one || !k.compress || !k.count_stock || !k.count_exact || !k.list_exact)
+    if (!k.gen_codes || !k.gen_tree || !k.bubble || !k.one || !k.compress || !k.count_stock || !k.count_exact || !k.list_exact
+        || !k.list_stock)
         { fprintf(stderr, "reference kernels missing from %s\n", cubin); exit(3); }
     return k;
     }
@@ -379,7 +381,8 @@ int run_dump(const Kernels& K, const char* in_path, unsigned int n, float3 slo, 
     check(cudaMemcpy(P, hp.data(), (size_t)n * 12, cudaMemcpyHostToDevice), "copy");
     RefTree T;
     T.allocate(n);
-    unsigned int list_stride = 0;
+    unsigned int list_stride = 0, stock_stride = 0;
+    unsigned int *list_s = nullptr, *c_list_s = nullptr;
     T.build(K, P, slo, shi, 32, 0);
     LBVHCompressedData c = T.compress(K, 32, 0);
     std::vector<float3> himg;
@@ -403,6 +406,19 @@ int run_dump(const Kernels& K, const char* in_path, unsigned int n, float3 slo, 
         CountNeighborsOp out{c_stock};
         void* a[] = {&out, &c, &q, &im};
         launch(K.count_stock, n, 32, 0, a);
+        // the stock query's neighbor list (a superset of the exact one), stride its largest count
+        check(cudaDeviceSynchronize(), "sync");
+        std::vector<unsigned int> hs_c(n);
+        check(cudaMemcpy(hs_c.data(), c_stock, (size_t)n * 4, cudaMemcpyDeviceToHost), "copy");
+        unsigned int ms = 1;
+        for (unsigned int v : hs_c) ms = std::max(ms, v);
+        check(cudaMalloc(&list_s, (size_t)n * ms * 4), "alloc");
+        check(cudaMalloc(&c_list_s, (size_t)n * 4), "alloc");
+        check(cudaMemset(list_s, 0xff, (size_t)n * ms * 4), "memset");
+        NeighborListOp lout{list_s, c_list_s, ms};
+        void* b[] = {&lout, &c, &q, &im};
+        launch(K.list_stock, n, 32, 0, b);
+        stock_stride = ms;
         }
         {
         float cm = std::max(std::max(std::fabs(slo.x), std::fabs(shi.x)), std::max(box.x, std::max(box.y, box.z)));
@@ -448,6 +464,7 @@ int run_dump(const Kernels& K, const char* in_path, unsigned int n, float3 slo, 
     dump("count_exact", c_exact, (size_t)n * 4);
     dump("count_list", c_list, (size_t)n * 4);
     dump("list_exact", list, (size_t)n * list_stride * 4);
+    dump("list_stock", list_s, (size_t)n * stock_stride * 4);
     printf("{\"dumped\": %u, \"list_stride\": %u}\n", n, list_stride);
     return 0;
     }

@@ -83,6 +83,8 @@ template __global__ void lbvh_traverse_ropes<CountNeighborsOp, RefExactQueryOp, 
     const CountNeighborsOp, const LBVHCompressedData, const RefExactQueryOp, const ImageListOp<float3>);
 template __global__ void lbvh_traverse_ropes<NeighborListOp, RefExactQueryOp, ImageListOp<float3>>(
     const NeighborListOp, const LBVHCompressedData, const RefExactQueryOp, const ImageListOp<float3>);
+template __global__ void lbvh_traverse_ropes<NeighborListOp, SphereQueryOp, ImageListOp<float3>>(
+    const NeighborListOp, const LBVHCompressedData, const SphereQueryOp, const ImageListOp<float3>);
 } // namespace kernel
 } // namespace gpu
 } // namespace neighbor

@@ -4,8 +4,8 @@ The reference harness (oracle/ref_harness) compiles mphowardlab/neighbor's kerne
 headers and replays its build / setup / traverse sequence.  Its outputs must equal this
 library's bit for bit: sorted codes and primitive order, hierarchy, FP32 boxes, the 10-bit int4
 nodes of getData(), the stock query's superset counts, the exact query's counts (which also
-equal the oracle's cell list), and the exact query's neighbor lists, row by row in the
-reference's order, from the general traversal, the whole-tree self walk and the symmetric self
+equal the oracle's cell list), the stock query's neighbor lists, and the exact query's neighbor
+lists, row by row in the reference's order, from the general traversal, the whole-tree self walk and the symmetric self
 walk.  Skipped where the reference kernels were not built.
 """
 import numpy as np
@@ -71,6 +71,12 @@ def test_library_matches_reference_kernels(name, P, L, rc):
     sph = _t(np.concatenate([P, np.full((len(P), 1), rc, np.float32)], 1))
     stock = trav.traverse(lbvh, sph, images=nb.images27(box)).cpu().numpy().view(np.uint32)
     assert np.array_equal(stock, ref["count_stock"])
+    # the stock query's lists (the reference's default path): every row equal, in order
+    ms = ref["list_stock"].shape[1]
+    _, lst_s = trav.traverse(lbvh, sph, images=nb.images27(box), max_neigh=ms)
+    vs = np.arange(ms)[None, :] < ref["count_stock"][:, None]
+    got_s = lst_s.cpu().numpy().view(np.uint32)
+    assert np.array_equal(np.where(vs, got_s, 0), np.where(vs, ref["list_stock"], 0))
     pad = nb.exact_pad(rc, 2 * L)
     exact = trav.traverse(lbvh, sph, query=nb.QUERY_EXACT, points=_t(P), box=box, pad=pad,
                           images="periodic").cpu().numpy().view(np.uint32)

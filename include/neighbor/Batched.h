@@ -20,6 +20,7 @@
 
 #include "LBVH.h"
 #include "Memory.h"
+#include "Trace.h"
 #include "QueryOps.h"
 #include "kernels/batch.cuh"
 
@@ -103,6 +104,7 @@ class BatchedNeighborList
         // Every system's build and self list in one launch (plus one memset of its counters).
         void run(const float3* points, unsigned int* nneigh, unsigned int* list, cudaStream_t stream, const Config& cfg)
             {
+            const detail::TraceRange trace_range("neighbor::BatchedNeighborList::run");
             if (cfg.block != 512 && cfg.block != 1024) throw std::runtime_error("Batch block must be 512 or 1024.");
             if (cfg.leaf_size < 1 || cfg.leaf_size > 64) throw std::runtime_error("Leaf size must be in [1, 64].");
             detail::check_cuda(cudaMemsetAsync(m_small.get(), 0, 4 * sizeof(unsigned int), stream), "memset");

@@ -11,7 +11,10 @@
 
 #include <cmath>
 #include <cstdint>
+#include <cstdio>
+#include <cstring>
 #include <stdexcept>
+#include <string>
 #include <vector>
 
 #include <cuda_bf16.h>
@@ -19,6 +22,7 @@
 
 #include "LBVH.h"
 #include "Memory.h"
+#include "Trace.h"
 #include "kernels/capacity.cuh"
 
 namespace neighbor
@@ -116,6 +120,7 @@ class CapacityModel
         void predict(const LBVH& lbvh, const gpu::CapFrame& fr, bool rows_sorted, unsigned int cap_max,
                      unsigned int* caps, float* y, cudaStream_t stream)
             {
+            const detail::TraceRange trace_range("neighbor::CapacityModel::predict");
             const unsigned int N = lbvh.getN();
             if (N < 2) throw std::runtime_error("capacity prediction needs a tree of at least two points");
             occupancy(lbvh, fr, stream);
@@ -136,6 +141,7 @@ class CapacityModel
                            unsigned int N, const gpu::CapFrame& fr, bool rows_sorted, unsigned int cap_max,
                            unsigned int* caps, float* y, cudaStream_t stream)
             {
+            const detail::TraceRange trace_range("neighbor::CapacityModel::predictSorted");
             if (N < 2) throw std::runtime_error("capacity prediction needs a tree of at least two points");
             occupancy(codes, N, fr, stream);
             gpu::CapInferArgs a;
@@ -193,6 +199,7 @@ class CapacityModel
         float train(const float* features, const float* targets, unsigned int N, unsigned int steps,
                     unsigned int batch, float lr, unsigned long long seed, cudaStream_t stream)
             {
+            const detail::TraceRange trace_range("neighbor::CapacityModel::train");
             if (N == 0 || batch == 0) return 0.f;
             unsigned long long s = seed * 0xbf58476d1ce4e5b9ull + 1;
             const auto next = [&s]() {
@@ -291,6 +298,45 @@ class CapacityModel
             m_step = 0;
             }
 
+        // Weights file (little-endian): the 8 bytes "NBRCAPMD", u32 version (1), u32 parameters,
+        // u32 inputs, u32 hidden units, u32 margin bins, the FP32 parameters, the FP32 margin
+        // table, and a u64 FNV-1a hash of all the bytes before it.  load() rejects a file whose
+        // magic, version, shapes, size or hash differ.
+        void save(const char* path) const
+            {
+            std::vector<unsigned char> b = file_image();
+            const unsigned long long h = fnv1a(b.data(), b.size());
+            append(b, &h, sizeof(h));
+            FILE* f = std::fopen(path, "wb");
+            if (!f) throw std::runtime_error(std::string("Invalid path: cannot write capacity model file ") + path);
+            const size_t w = std::fwrite(b.data(), 1, b.size(), f);
+            const bool ok = std::fclose(f) == 0 && w == b.size();
+            if (!ok) throw std::runtime_error(std::string("Invalid path: cannot write capacity model file ") + path);
+            }
+        void load(const char* path)
+            {
+            FILE* f = std::fopen(path, "rb");
+            if (!f) throw std::runtime_error(std::string("Invalid capacity model file (cannot open) ") + path);
+            std::vector<unsigned char> b;
+            unsigned char chunk[4096];
+            size_t r;
+            while ((r = std::fread(chunk, 1, sizeof(chunk), f)) > 0) b.insert(b.end(), chunk, chunk + r);
+            std::fclose(f);
+            const std::vector<unsigned char> shape = file_image(false);
+            const size_t body = shape.size() + (size_t)kParams * 4 + (size_t)kMarginBins * 4;
+            if (b.size() != body + 8 || std::memcmp(b.data(), shape.data(), shape.size()) != 0)
+                throw std::runtime_error("Invalid capacity model file: magic, version or shapes differ");
+            unsigned long long h = 0;
+            std::memcpy(&h, b.data() + body, sizeof(h));
+            if (h != fnv1a(b.data(), body)) throw std::runtime_error("Invalid capacity model file: hash mismatch");
+            std::vector<float> p(kParams);
+            float margins[kMarginBins];
+            std::memcpy(p.data(), b.data() + shape.size(), (size_t)kParams * 4);
+            std::memcpy(margins, b.data() + shape.size() + (size_t)kParams * 4, sizeof(margins));
+            setParams(p.data());
+            setMargins(margins);
+            }
+
         const float* params() const { return m_p.get(); }
         const __nv_bfloat16* weights() const { return m_w.get(); }
 
@@ -304,6 +350,39 @@ class CapacityModel
         device_array<unsigned int> m_occ;
         unsigned int m_step;
         float m_margins[gpu::kCapMarginBins];
+
+        static void append(std::vector<unsigned char>& b, const void* p, size_t n)
+            {
+            const unsigned char* c = static_cast<const unsigned char*>(p);
+            b.insert(b.end(), c, c + n);
+            }
+        static unsigned long long fnv1a(const unsigned char* p, size_t n)
+            {
+            unsigned long long h = 0xcbf29ce484222325ull;
+            for (size_t i = 0; i < n; ++i)
+                {
+                h ^= p[i];
+                h *= 0x100000001b3ull;
+                }
+            return h;
+            }
+        // header, and (with_body) the parameters and margins
+        std::vector<unsigned char> file_image(bool with_body = true) const
+            {
+            std::vector<unsigned char> b;
+            append(b, "NBRCAPMD", 8);
+            const uint32_t head[5] = {1u, (uint32_t)kParams, (uint32_t)gpu::kCapIn, (uint32_t)gpu::kCapHidden,
+                                      (uint32_t)gpu::kCapMarginBins};
+            append(b, head, sizeof(head));
+            if (with_body)
+                {
+                std::vector<float> p(kParams);
+                getParams(p.data());
+                append(b, p.data(), p.size() * sizeof(float));
+                append(b, m_margins, sizeof(m_margins));
+                }
+            return b;
+            }
 
         void launch_train(const float* features, const float* targets, unsigned int N, unsigned int batch,
                           unsigned int offset, unsigned int stride, float* grad, float* loss, cudaStream_t stream)

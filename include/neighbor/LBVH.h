@@ -31,6 +31,7 @@
 #include "InsertOps.h"
 #include "LBVHData.h"
 #include "Memory.h"
+#include "Trace.h"
 #include "Tunable.h"
 #include "kernels/build.cuh"
 
@@ -482,6 +483,7 @@ void LBVH::reference_layout(const LeafBoxT& leaf_box, cudaStream_t stream) const
 template<class InsertOpT>
 void LBVH::build(const LaunchParameters& params, const InsertOpT& insert, const float3& lo, const float3& hi)
     {
+    const detail::TraceRange trace_range("neighbor::LBVH::build");
     setup(params, insert);
     m_fast_points = is_point_insert<InsertOpT>::value;
     m_ref_valid = true;

@@ -22,6 +22,7 @@
 #include "LBVH.h"
 #include "LBVHTraverserData.h"
 #include "Memory.h"
+#include "Trace.h"
 #include "OutputOps.h"
 #include "QueryOps.h"
 #include "TransformOps.h"
@@ -332,6 +333,7 @@ template<class QueryOpT, class OutputOpT, class TranslateOpT, class TransformOpT
 void LBVHTraverser::traverse(const LaunchParameters& params, const LBVH& lbvh, const QueryOpT& query,
                              const OutputOpT& out, const TranslateOpT& images, const TransformOpT& transform)
     {
+    const detail::TraceRange trace_range("neighbor::LBVHTraverser::traverse");
     if (lbvh.getN() == 0) return;
     if (query.size() == 0 || images.size() == 0) return;
     if (images.size() > 32)
@@ -372,6 +374,7 @@ void LBVHTraverser::traverseSelf(const LaunchParameters& params, const LBVH& lbv
                                  float pad, const OutputOpT& out, const TranslateOpT& images,
                                  const TransformOpT& transform, bool rows_sorted)
     {
+    const detail::TraceRange trace_range("neighbor::LBVHTraverser::traverseSelf");
     static_assert(output_kind<OutputOpT>::value != 0,
                   "traverseSelf needs CountNeighborsOp, NeighborListOp or CSRNeighborListOp");
     static_assert(detail::is_float3_images<TranslateOpT>::value,
@@ -413,6 +416,7 @@ void LBVHTraverser::traverseSelfSubset(const LaunchParameters& params, const LBV
                                        const TransformOpT& transform, bool rows_sorted,
                                        const unsigned int* subset, unsigned int count)
     {
+    const detail::TraceRange trace_range("neighbor::LBVHTraverser::traverseSelfSubset");
     static_assert(output_kind<OutputOpT>::value != 0,
                   "traverseSelfSubset needs CountNeighborsOp, NeighborListOp or CSRNeighborListOp");
     static_assert(detail::is_float3_images<TranslateOpT>::value,

@@ -12,6 +12,7 @@
 #define NEIGHBOR_MEMORY_H_
 
 #include <algorithm>
+#include <atomic>
 #include <cstddef>
 #include <memory>
 #include <stdexcept>
@@ -22,6 +23,29 @@
 
 namespace neighbor
 {
+namespace detail
+{
+// Fault injection for tests: the next n allocations of shared_array / device_array fail as if
+// the CUDA allocator had refused them (set through nbr_debug_inject_alloc_failures).
+inline std::atomic<unsigned int>& injected_alloc_failures()
+    {
+    static std::atomic<unsigned int> n(0u);
+    return n;
+    }
+inline bool take_injected_alloc_failure()
+    {
+    std::atomic<unsigned int>& n = injected_alloc_failures();
+    unsigned int v = n.load();
+    while (v > 0u && !n.compare_exchange_weak(v, v - 1u)) {}
+    return v > 0u;
+    }
+// cudaMalloc / cudaMallocManaged, or the injected failure
+inline cudaError_t device_malloc(void** p, size_t bytes, bool managed)
+    {
+    if (take_injected_alloc_failure()) return cudaErrorMemoryAllocation;
+    return managed ? cudaMallocManaged(p, bytes) : cudaMalloc(p, bytes);
+    }
+} // namespace detail
 
 template<typename T>
 class shared_array
@@ -86,7 +110,7 @@ class shared_array
                 return;
                 }
             T* ptr = nullptr;
-            const cudaError_t code = cudaMallocManaged(reinterpret_cast<void**>(&ptr), count * sizeof(T));
+            const cudaError_t code = detail::device_malloc(reinterpret_cast<void**>(&ptr), count * sizeof(T), true);
             if (code != cudaSuccess)
                 {
                 (void)cudaGetLastError();
@@ -145,7 +169,7 @@ class device_array
             if (count <= size_) return;
             release();
             T* p = nullptr;
-            const cudaError_t code = cudaMalloc(reinterpret_cast<void**>(&p), count * sizeof(T));
+            const cudaError_t code = detail::device_malloc(reinterpret_cast<void**>(&p), count * sizeof(T), false);
             if (code != cudaSuccess)
                 {
                 (void)cudaGetLastError();
@@ -161,7 +185,7 @@ class device_array
             {
             if (count <= size_) return;
             T* p = nullptr;
-            const cudaError_t code = cudaMalloc(reinterpret_cast<void**>(&p), count * sizeof(T));
+            const cudaError_t code = detail::device_malloc(reinterpret_cast<void**>(&p), count * sizeof(T), false);
             if (code != cudaSuccess)
                 {
                 (void)cudaGetLastError();

@@ -16,6 +16,7 @@
 #include "LBVH.h"
 #include "LBVHTraverser.h"
 #include "Memory.h"
+#include "Trace.h"
 #include "OutputOps.h"
 #include "TransformOps.h"
 #include "TranslateOps.h"
@@ -155,6 +156,7 @@ class OnePassNeighborList
                     float pad, bool periodic, bool rows_sorted, unsigned int cap_max,
                     const TransformOpT& transform = TransformOpT())
             {
+            const detail::TraceRange trace_range("neighbor::OnePassNeighborList::build");
             Stats st = {0, 0, 0};
             const unsigned int N = lbvh.getN();
             m_N = N;
@@ -233,6 +235,7 @@ class OnePassNeighborList
                            const float3& hi, float rc, float3 box, float pad, bool periodic, bool rows_sorted,
                            unsigned int cap_max, const TransformOpT& transform = TransformOpT())
             {
+            const detail::TraceRange trace_range("neighbor::OnePassNeighborList::buildLearned");
             cudaStream_t stream = params.stream;
             lbvh.build(params, PointInsertOp(points, N), lo, hi);
             if (N == 0) return build(params, lbvh, trav, rc, box, pad, periodic, rows_sorted, cap_max, transform);

@@ -166,6 +166,12 @@ int nbr_traverse_self(nbr_traverser t, nbr_lbvh h, float rc, const float box[3],
  * ended, the kernels finished and the context is still usable. */
 int nbr_debug_wait_timeout(unsigned int* status_out, void* stream);
 
+/* Fault injection for tests (no counterpart in the reference): the next `count` device
+ * allocations of the library fail as if the CUDA allocator had refused them; the call that hits
+ * one returns NBR_ERR_ALLOC, as the reference throws for a failed allocation
+ * (include/neighbor/Memory.h:182-186), and leaves its handle usable. */
+int nbr_debug_inject_alloc_failures(unsigned int count);
+
 /* No counterpart in the reference.  The Morton-code and stable-sort stage of the LBVH build for
  * callers that cannot allocate device memory (a host framework that owns every allocation, a
  * latency-critical loop that must not touch the allocator, a fully committed memory budget):
@@ -245,6 +251,12 @@ int nbr_capmodel_set_margin(nbr_capmodel m, float margin);
 int nbr_capmodel_get_margin(nbr_capmodel m, float* margin);
 int nbr_capmodel_set_margins(nbr_capmodel m, const float* margins);
 int nbr_capmodel_get_margins(nbr_capmodel m, float* margins);
+
+/* Weights file of a trained model: "NBRCAPMD", version 1, its shapes, the FP32 parameters and
+ * margin table, and an FNV-1a hash; load returns NBR_ERR_INVALID for a file whose magic,
+ * version, shapes, size or hash differ. */
+int nbr_capmodel_save(nbr_capmodel m, const char* path);
+int nbr_capmodel_load(nbr_capmodel m, const char* path);
 /* Coarse-cell level the features use for cutoff rc in a scene of extent hi - lo. */
 int nbr_capmodel_level(float rc, const float lo[3], const float hi[3], unsigned int* level);
 /* Features (float[N][32]) of every sorted point of a built point tree; lo/hi = the build's scene

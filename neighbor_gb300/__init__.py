@@ -99,6 +99,7 @@ def _declare(L):
     sig("nbr_traverser_set_mode", [_P, _I])
     sig("nbr_traverser_set_stats", [_P, _P])
     sig("nbr_traverser_set_symmetric", [_P, _I])
+    sig("nbr_debug_inject_alloc_failures", [_U])
     sig("nbr_traverser_set_work_order", [_P, _I])
     sig("nbr_traverser_get_data", [_P, _PP, _PP, _PP, _PP])
     sig("nbr_traverse", [_P, _P, _I, _P, _U, _P, _P, _F, _P, _U, _P, _P, _P, _U, _U, _P])
@@ -118,6 +119,8 @@ def _declare(L):
     sig("nbr_capmodel_set_margin", [_P, _F])
     sig("nbr_capmodel_get_margin", [_P, ctypes.POINTER(_F)])
     sig("nbr_capmodel_set_margins", [_P, _P])
+    sig("nbr_capmodel_save", [_P, ctypes.c_char_p])
+    sig("nbr_capmodel_load", [_P, ctypes.c_char_p])
     sig("nbr_capmodel_get_margins", [_P, _P])
     sig("nbr_capmodel_level", [_F, _P, _P, ctypes.POINTER(_U)])
     sig("nbr_capmodel_features", [_P, _P, _P, _P, _F, _I, _P, _P])
@@ -156,13 +159,15 @@ EXPORTED = ["nbr_last_error", "nbr_version", "nbr_lbvh_create", "nbr_lbvh_destro
             "nbr_lbvh_check_status", "nbr_traverser_create", "nbr_traverser_destroy",
             "nbr_traverser_setup", "nbr_traverser_reset", "nbr_traverser_set_fast_path",
             "nbr_traverser_set_mode", "nbr_traverser_set_stats", "nbr_traverser_set_symmetric",
+            "nbr_debug_inject_alloc_failures",
             "nbr_traverser_set_work_order",
             "nbr_traverser_get_data", "nbr_traverse", "nbr_traverse_self", "nbr_exact_pad",
             "nbr_debug_wait_timeout", "nbr_morton_sort_noalloc", "nbr_traverse_self_csr",
             "nbr_traverse_self_subset_csr",
             "nbr_capmodel_create", "nbr_capmodel_destroy", "nbr_capmodel_get_params",
             "nbr_capmodel_set_params", "nbr_capmodel_set_margin", "nbr_capmodel_get_margin",
-            "nbr_capmodel_set_margins", "nbr_capmodel_get_margins",
+            "nbr_capmodel_set_margins", "nbr_capmodel_get_margins", "nbr_capmodel_save",
+            "nbr_capmodel_load",
             "nbr_capmodel_level", "nbr_capmodel_features", "nbr_capmodel_predict",
             "nbr_capmodel_targets", "nbr_capmodel_gradient", "nbr_capmodel_train",
             "nbr_onepass_create", "nbr_onepass_destroy", "nbr_onepass_capacity",
@@ -265,6 +270,11 @@ def morton_sort_noalloc(points, lo, hi, codes_out, order_out, stream=None):
             raise TypeError("outputs must be contiguous 4-byte CUDA tensors of N elements")
     _check(load().nbr_morton_sort_noalloc(_ptr(p), n, _f3(lo), _f3(hi), _ptr(codes_out),
                                           _ptr(order_out), _stream_ptr(stream)))
+
+
+def inject_alloc_failures(count: int):
+    """Test hook: the library's next `count` device allocations fail (NBR_ERR_ALLOC)."""
+    _check(load().nbr_debug_inject_alloc_failures(int(count)))
 
 
 def images27(L: Sequence[float], device="cuda"):
@@ -648,6 +658,14 @@ class CapacityModel:
     def margins(self, table):
         t = (ctypes.c_float * CAP_MARGIN_BINS)(*[float(v) for v in table])
         _check(self._L.nbr_capmodel_set_margins(self._h, ctypes.cast(t, ctypes.c_void_p)))
+
+    def save(self, path: str):
+        """Write the weights file (parameters, margin table, shapes, hash)."""
+        _check(self._L.nbr_capmodel_save(self._h, os.fsencode(path)))
+
+    def load(self, path: str):
+        """Read a weights file written by save(); a damaged or foreign file raises."""
+        _check(self._L.nbr_capmodel_load(self._h, os.fsencode(path)))
 
     def calibrate(self, targets, y, quantile: float = 0.999, min_rows: int = 1000):
         """Set the calibration table from residuals: bin b gets the `quantile` of target - y over the

@@ -405,6 +405,12 @@ int nbr_traverse_f64(nbr_traverser t, nbr_lbvh h, const double* spheres, unsigne
     });
     }
 
+int nbr_debug_inject_alloc_failures(unsigned int count)
+    {
+    neighbor::detail::injected_alloc_failures().store(count);
+    return NBR_OK;
+    }
+
 int nbr_debug_wait_timeout(unsigned int* status_out, void* stream)
     {
     if (!status_out) return fail(NBR_ERR_INVALID, "null argument");

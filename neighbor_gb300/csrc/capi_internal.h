@@ -38,7 +38,7 @@ inline int from_exception(const std::exception& e)
     const std::string m = e.what();
     if (m.find("allocating") != std::string::npos) return fail(NBR_ERR_ALLOC, m);
     if (m.find("bounded device wait") != std::string::npos) return fail(NBR_ERR_DEVICE_WAIT, m);
-    if (m.find("Invalid tuning") != std::string::npos || m.find("maximum of 32") != std::string::npos
+    if (m.find("Invalid") != std::string::npos || m.find("maximum of 32") != std::string::npos
         || m.find("must be") != std::string::npos || m.find("need") != std::string::npos)
         return fail(NBR_ERR_INVALID, m);
     return fail(NBR_ERR_CUDA, m);

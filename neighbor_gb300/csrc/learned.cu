@@ -158,6 +158,18 @@ int nbr_capmodel_get_margins(nbr_capmodel m, float* margins)
     return NBR_OK;
     }
 
+int nbr_capmodel_save(nbr_capmodel m, const char* path)
+    {
+    if (!m || !path) return fail(NBR_ERR_INVALID, "null argument");
+    return guarded([&] { m->model.save(path); });
+    }
+
+int nbr_capmodel_load(nbr_capmodel m, const char* path)
+    {
+    if (!m || !path) return fail(NBR_ERR_INVALID, "null argument");
+    return guarded([&] { m->model.load(path); });
+    }
+
 int nbr_capmodel_level(float rc, const float lo[3], const float hi[3], unsigned int* level)
     {
     if (!lo || !hi || !level) return fail(NBR_ERR_INVALID, "null argument");

@@ -215,3 +215,31 @@ def test_fill_after_count_with_map_transform(count_rows_sorted, fill_rows_sorted
                                          max_neigh=mx2))
     assert np.array_equal(cs2, cf2)
     assert np.array_equal(ls2, lf2)
+
+
+@pytest.mark.parametrize("N", [300, 25000])
+def test_noncubic_offset_box(N):
+    # periodic box of unequal sides whose corner is not the origin: counts and sets equal the
+    # oracle's cell list, and the symmetric count + ordered fill equal the whole-tree walk row by row
+    rng = np.random.default_rng(71)
+    Lv = np.array([21.0, 14.5, 26.3]) * (N / 25000.0) ** (1.0 / 3.0)
+    lo = np.array([-5.0, 2.0, 10.0])
+    P = (lo + rng.random((N, 3)) * Lv).astype(np.float32)
+    box = [float(v) for v in Lv]
+    rc = 1.3
+    lbvh = nb.LBVH()
+    lbvh.build(_t(P), lo.tolist(), (lo + Lv).tolist())
+    pad = nb.exact_pad(rc, 2.0 * float(np.max(np.abs(lo + 2 * Lv))))
+    trav = nb.LBVHTraverser()
+    cnt = trav.traverse_self(lbvh, rc, box, pad, images="periodic", rows_sorted=False)
+    mx = max(1, int(cnt.max().item()))
+    cs, ls = _rows(*trav.traverse_self(lbvh, rc, box, pad, images="periodic", rows_sorted=False, max_neigh=mx))
+    whole = nb.LBVHTraverser()
+    whole.set_symmetric(False)
+    cf, lf = _rows(*whole.traverse_self(lbvh, rc, box, pad, images="periodic", rows_sorted=False, max_neigh=mx))
+    assert np.array_equal(cs, cf)
+    assert np.array_equal(ls, lf)
+    off, nbrs = O.celllist_csr(P, P, rc, lo.tolist(), box)
+    assert np.array_equal(cs, np.diff(off).astype(np.uint32))
+    for r in range(0, N, max(1, N // 97)):
+        assert np.array_equal(np.sort(ls[r, : cs[r]]), nbrs[off[r]:off[r + 1]])

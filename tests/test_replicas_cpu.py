@@ -61,3 +61,23 @@ def test_reference_arm_runs_on_rank_zero_only(monkeypatch, capsys):
     args = bench.parse(["--impl", "reference", "--gpus", "2"])
     assert bench.run_reference(args) == 0
     assert capsys.readouterr().out == ""
+
+
+def test_reference_arm_json_line(monkeypatch, capsys):
+    # the reference arm runs the oracle's cell list on the host cores: its JSON line carries the
+    # contract's keys (one rank)
+    import json
+    sys.path.insert(0, ROOT)
+    import bench
+    monkeypatch.delenv("WORLD_SIZE", raising=False)
+    monkeypatch.delenv("RANK", raising=False)
+    args = bench.parse(["--impl", "reference", "--steps", "2", "--warmup", "1", "--n", "32768",
+                        "--cpu-seconds", "0.2"])
+    assert bench.run_reference(args) == 0
+    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    assert line["impl"] == "reference"
+    assert line["unit"] == "pairs/s" and line["value"] > 0
+    assert line["steps"] == 2 and line["warmup"] == 1
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
+    assert line["e2e"] == {"value": line["value"], "unit": "pairs/s", "h2d_bytes_per_step": 0,
+                           "d2h_bytes_per_step": 0}

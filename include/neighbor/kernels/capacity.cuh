@@ -220,7 +220,8 @@ __device__ __forceinline__ unsigned int cap_from_output(float y, float margin, u
 // accumulators.  The accumulator fragment of N-tiles 2t and 2t+1 is exactly the A fragment of
 // K-tile t of the next layer (rows: groupID, groupID + 8; columns: 2*tig + {0,1} (+8)), so H1
 // never leaves registers; each H2 fragment is multiplied into the output weights at once, and the
-// four lanes of a group add their columns with two shuffles.
+// four lanes of a group add their columns with two shuffles, after which each of the four
+// finishes one of the group's four rows.  Accumulators start at the bias (the sum is still FP32).
 // ---------------------------------------------------------------------------------------------
 struct CapInferArgs
     {
@@ -244,6 +245,15 @@ __device__ __forceinline__ unsigned int pack_bf16x2(float lo, float hi)
     {
     const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
     return *reinterpret_cast<const unsigned int*>(&v);
+    }
+
+// pack_bf16x2(max(lo, 0), max(hi, 0)) in one conversion: rounding to nearest keeps the sign, so
+// clamping after the rounding gives the same values (a negative input becomes +0).
+__device__ __forceinline__ unsigned int pack_relu_bf16x2(float lo, float hi)
+    {
+    unsigned int d;
+    asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(hi), "f"(lo));
+    return d;
     }
 
 __device__ __forceinline__ void mma_bf16_16816(float (&d)[4], const unsigned int (&a)[4], unsigned int b0,
@@ -278,20 +288,24 @@ constexpr int kCapCellStride = 34;
 // the two words of the B fragment (B[2t..2t+1][n], B[8+2t..8+2t+1][n]) are one 64-bit word at
 // (kt * 4 + t) * kCapWStride + n; the stride of 72 spreads a warp's words over all bank pairs.
 constexpr int kCapWStride = 72;
+// m16 row tiles that go through the layers together, and the kernel's resident blocks per SM
+// (16M points: 2 tiles at 2 blocks 1.18 ms; 1 tile at 3 blocks (80 registers) 1.35 ms, at 4
+// blocks (64) 1.42 ms)
+constexpr int kCapInferTiles = 2;
+constexpr int kCapInferMinBlocks = 2;
 
-__global__ void __launch_bounds__(kCapInferWarps * 32, 2) k_cap_infer(const CapInferArgs a)
+__global__ void __launch_bounds__(kCapInferWarps * 32, kCapInferMinBlocks) k_cap_infer(const CapInferArgs a)
     {
     __shared__ uint2 s_w1[2 * 4 * kCapWStride];   // 2 k-tiles x 4 x 64 rows (+pad)
     __shared__ uint2 s_w2[4 * 4 * kCapWStride];   // 4 k-tiles x 4 x 64 rows (+pad)
-    __shared__ float s_w3[kCapHidden];
-    __shared__ float s_b1[kCapHidden];
-    __shared__ float s_b2[kCapHidden];
+    __shared__ float2 s_w3[kCapHidden / 2];        // (w3[2c], w3[2c + 1])
+    __shared__ float2 s_b1[kCapHidden / 2];        // (b1[2c], b1[2c + 1])
+    __shared__ float2 s_b2[kCapHidden / 2];
     __shared__ float s_log[kCapLogTable];
     // per warp: the distinct coarse cells of its 32 points -- spread Morton parts of the 3 x 3
-    // neighbor coordinates (0xffffffff outside an open grid), occupancy sums, BF16 feature rows --
-    // and per point its cell and its two point-specific feature words
+    // neighbor coordinates (0xffffffff outside an open grid), BF16 feature rows -- and per point
+    // its cell and its two point-specific feature words
     __shared__ unsigned int s_part[kCapInferWarps][32 * 9];
-    __shared__ unsigned int s_sum[kCapInferWarps][32];
     __shared__ unsigned short s_cell[kCapInferWarps][32 * kCapCellStride];
     __shared__ unsigned int s_ci[kCapInferWarps][32];
     __shared__ uint2 s_pt[kCapInferWarps][32];
@@ -308,11 +322,11 @@ __global__ void __launch_bounds__(kCapInferWarps * 32, 2) k_cap_infer(const CapI
         s_w2[(kt * 4 + t) * kCapWStride + n] = make_uint2(wsrc[kCapBfW2 / 2 + n * (kCapHidden / 2) + kt * 8 + t],
                                                           wsrc[kCapBfW2 / 2 + n * (kCapHidden / 2) + kt * 8 + 4 + t]);
         }
-    for (int i = threadIdx.x; i < kCapHidden; i += blockDim.x)
+    for (int i = threadIdx.x; i < kCapHidden / 2; i += blockDim.x)
         {
-        s_w3[i] = __bfloat162float(a.w[kCapBfW3 + i]);
-        s_b1[i] = a.p[kCapOffB1 + i];
-        s_b2[i] = a.p[kCapOffB2 + i];
+        s_w3[i] = make_float2(__bfloat162float(a.w[kCapBfW3 + 2 * i]), __bfloat162float(a.w[kCapBfW3 + 2 * i + 1]));
+        s_b1[i] = make_float2(a.p[kCapOffB1 + 2 * i], a.p[kCapOffB1 + 2 * i + 1]);
+        s_b2[i] = make_float2(a.p[kCapOffB2 + 2 * i], a.p[kCapOffB2 + 2 * i + 1]);
         }
     cap_fill_log_table(s_log);
     __syncthreads();
@@ -321,8 +335,9 @@ __global__ void __launch_bounds__(kCapInferWarps * 32, 2) k_cap_infer(const CapI
     const unsigned int warp = threadIdx.x >> 5;
     const unsigned int g = lane >> 2;   // groupID
     const unsigned int t = lane & 3u;   // thread in group
+    // lane nb < 27 gathers neighbor cell nb = 9(dx+1) + 3(dy+1) + (dz+1) of every distinct cell
+    const unsigned int nb_x = lane / 9u, nb_y = 3u + (lane / 3u) % 3u, nb_z = 6u + lane % 3u;
     unsigned int* part = s_part[warp];
-    unsigned int* csum = s_sum[warp];
     unsigned short* cell = s_cell[warp];
     unsigned int* cidx = s_ci[warp];
     uint2* pt = s_pt[warp];
@@ -339,6 +354,7 @@ __global__ void __launch_bounds__(kCapInferWarps * 32, 2) k_cap_infer(const CapI
         // repeat the last point (their outputs are not written).
         const unsigned int s = base + min(lane, a.N - 1u - base);
         const unsigned int c = a.codes[s] >> (3u * sh);
+        const float3 pos = cap_position(a, s);   // loaded early: used after the occupancy gather
         const unsigned int c_prev = __shfl_up_sync(0xffffffffu, c, 1);
         const unsigned int heads = __ballot_sync(0xffffffffu, lane == 0u || c != c_prev);
         const unsigned int m = __popc(heads);
@@ -359,123 +375,160 @@ __global__ void __launch_bounds__(kCapInferWarps * 32, 2) k_cap_infer(const CapI
             cap_axis(cz, G, a.frame.periodic, p, v);
 #pragma unroll
             for (int d = 0; d < 3; ++d) part[ci * 9 + 6 + d] = v[d] ? p[d] : 0xffffffffu;
-            csum[ci] = 0u;
             }
         __syncwarp();
-        // neighbor cell k = 9(dx+1) + 3(dy+1) + (dz+1) of every distinct cell; a spread part of
-        // 0xffffffff (outside an open grid) makes the index >= 2^30
-        for (unsigned int job = lane; job < 27u * m; job += 32u)
+        // one distinct cell per step: lanes 0..26 its 27 occupancies (a spread part of 0xffffffff,
+        // outside an open grid, makes the index >= 2^30), lane 30 the log of their sum (a warp
+        // reduction), lane 31 the constant; the loads of four cells are issued before their sums
+        for (unsigned int k0 = 0; k0 < m; k0 += 4u)
             {
-            const unsigned int k = job / 27u;
-            const unsigned int nb = job - 27u * k;
-            const unsigned int* pk = part + k * 9u;
-            const unsigned int idx = (pk[nb / 9u] << 2) | (pk[3u + (nb / 3u) % 3u] << 1) | pk[6u + nb % 3u];
-            const unsigned int o = idx < (1u << 30) ? __ldg(a.occ + idx) : 0u;
-            cell[k * kCapCellStride + nb] = __bfloat16_as_ushort(__float2bfloat16_rn(cap_log1p(s_log, o)));
-            atomicAdd(csum + k, o);
+            unsigned int o[4];
+#pragma unroll
+            for (unsigned int j = 0; j < 4u; ++j)
+                {
+                const unsigned int* pk = part + (k0 + j) * 9u;
+                o[j] = 0u;
+                if (lane < 27u && k0 + j < m)
+                    {
+                    const unsigned int idx = (pk[nb_x] << 2) | (pk[nb_y] << 1) | pk[nb_z];
+                    if (idx < (1u << 30)) o[j] = __ldg(a.occ + idx);
+                    }
+                }
+#pragma unroll
+            for (unsigned int j = 0; j < 4u; ++j)
+                {
+                const unsigned int k = k0 + j;
+                if (k >= m) break;   // uniform over the warp
+                const unsigned int sum = __reduce_add_sync(0xffffffffu, o[j]);
+                const float f = lane < 27u ? cap_log1p(s_log, o[j]) : (lane == 31u ? 1.f : cap_log1p(s_log, sum));
+                if (lane < 27u || lane >= 30u)
+                    cell[k * kCapCellStride + lane] = __bfloat16_as_ushort(__float2bfloat16_rn(f));
+                }
             }
         __syncwarp();
-        if (lane < m)
-            {
-            cell[lane * kCapCellStride + 30] = __bfloat16_as_ushort(__float2bfloat16_rn(log1pf((float)csum[lane])));
-            cell[lane * kCapCellStride + 31] = __bfloat16_as_ushort(__float2bfloat16_rn(1.f));
-            }
         {
         // the point's own words: 13 = (feature 26 of its cell, x fraction), 14 = (y, z fractions)
         float fr3[3];
-        cap_frac(a.frame, cap_position(a, s), cx, cy, cz, fr3);
+        cap_frac(a.frame, pos, cx, cy, cz, fr3);
         const unsigned int f26 = cell[ci * kCapCellStride + 26];
         pt[lane] = make_uint2(f26 | ((unsigned int)__bfloat16_as_ushort(__float2bfloat16_rn(fr3[0])) << 16),
                               pack_bf16x2(fr3[1], fr3[2]));
         }
         __syncwarp();
-        // Both m16 tiles (rows g, g + 8, g + 16, g + 24 of this lane) go through the layers together:
-        // every B fragment read from shared memory feeds two independent MMAs.
-        unsigned int a1[2][2][4];
-#pragma unroll
-        for (int mt = 0; mt < 2; ++mt)
-            {
-            const unsigned int r0 = mt * 16u + g;
-            // feature words of rows r0 and r0 + 8: the cell's row, except words 13 and 14
-            const unsigned int* x0 = reinterpret_cast<const unsigned int*>(cell + cidx[r0] * kCapCellStride);
-            const unsigned int* x1 = reinterpret_cast<const unsigned int*>(cell + cidx[r0 + 8u] * kCapCellStride);
-            a1[mt][0][0] = x0[t];
-            a1[mt][0][1] = x1[t];
-            a1[mt][0][2] = x0[4 + t];
-            a1[mt][0][3] = x1[4 + t];
-            a1[mt][1][0] = x0[8 + t];
-            a1[mt][1][1] = x1[8 + t];
-            a1[mt][1][2] = t == 1u ? pt[r0].x : (t == 2u ? pt[r0].y : x0[12 + t]);
-            a1[mt][1][3] = t == 1u ? pt[r0 + 8u].x : (t == 2u ? pt[r0 + 8u].y : x1[12 + t]);
-            }
-        // layer 1 -> BF16 A fragments of layer 2 (k-tile j = n-tiles 2j, 2j+1)
-        unsigned int a2[2][4][4];
-#pragma unroll
-        for (int nt = 0; nt < 8; ++nt)
-            {
-            float acc[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
-#pragma unroll
-            for (int kt = 0; kt < 2; ++kt)
-                {
-                const uint2 b = s_w1[(kt * 4 + t) * kCapWStride + nt * 8 + g];
-                mma_bf16_16816(acc[0], a1[0][kt], b.x, b.y);
-                mma_bf16_16816(acc[1], a1[1][kt], b.x, b.y);
-                }
-            const float bl = s_b1[nt * 8 + 2 * t];
-            const float bh = s_b1[nt * 8 + 2 * t + 1];
-#pragma unroll
-            for (int mt = 0; mt < 2; ++mt)
-                {
-                a2[mt][nt >> 1][(nt & 1) * 2 + 0] = pack_bf16x2(fmaxf(acc[mt][0] + bl, 0.f), fmaxf(acc[mt][1] + bh, 0.f));
-                a2[mt][nt >> 1][(nt & 1) * 2 + 1] = pack_bf16x2(fmaxf(acc[mt][2] + bl, 0.f), fmaxf(acc[mt][3] + bh, 0.f));
-                }
-            }
-        // layer 2 with the output layer folded in: z(row) = sum over columns of relu(h2) * w3
+        // The two m16 tiles (rows g, g + 8 and g + 16, g + 24 of this lane) go through the layers
+        // kCapInferTiles at a time: every B fragment read from shared memory feeds that many MMAs.
         float z[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
-#pragma unroll
-        for (int nt = 0; nt < 8; ++nt)
+#pragma unroll 1
+        for (int m0 = 0; m0 < 2; m0 += kCapInferTiles)
             {
-            float acc[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
+            float zc[kCapInferTiles][2];
 #pragma unroll
-            for (int kt = 0; kt < 4; ++kt)
+            for (int i = 0; i < kCapInferTiles; ++i) zc[i][0] = zc[i][1] = 0.f;
+            unsigned int a1[kCapInferTiles][2][4];
+#pragma unroll
+            for (int i = 0; i < kCapInferTiles; ++i)
                 {
-                const uint2 b = s_w2[(kt * 4 + t) * kCapWStride + nt * 8 + g];
-                mma_bf16_16816(acc[0], a2[0][kt], b.x, b.y);
-                mma_bf16_16816(acc[1], a2[1][kt], b.x, b.y);
+                const unsigned int r0 = (m0 + i) * 16u + g;
+                // feature words of rows r0 and r0 + 8: the cell's row, except words 13 and 14
+                const unsigned int* x0 = reinterpret_cast<const unsigned int*>(cell + cidx[r0] * kCapCellStride);
+                const unsigned int* x1 = reinterpret_cast<const unsigned int*>(cell + cidx[r0 + 8u] * kCapCellStride);
+                a1[i][0][0] = x0[t];
+                a1[i][0][1] = x1[t];
+                a1[i][0][2] = x0[4 + t];
+                a1[i][0][3] = x1[4 + t];
+                a1[i][1][0] = x0[8 + t];
+                a1[i][1][1] = x1[8 + t];
+                a1[i][1][2] = t == 1u ? pt[r0].x : (t == 2u ? pt[r0].y : x0[12 + t]);
+                a1[i][1][3] = t == 1u ? pt[r0 + 8u].x : (t == 2u ? pt[r0 + 8u].y : x1[12 + t]);
                 }
-            const int c0 = nt * 8 + 2 * t;
-            const float w0 = s_w3[c0], w1 = s_w3[c0 + 1];
-            const float bl = s_b2[c0], bh = s_b2[c0 + 1];
+            // layer 1 -> BF16 A fragments of layer 2 (k-tile j = n-tiles 2j, 2j+1); the accumulators
+            // start at the bias, and one conversion applies the ReLU and packs two columns
+            unsigned int a2[kCapInferTiles][4][4];
 #pragma unroll
-            for (int mt = 0; mt < 2; ++mt)
+            for (int nt = 0; nt < 8; ++nt)
                 {
-                z[mt][0] = fmaf(fmaxf(acc[mt][0] + bl, 0.f), w0, z[mt][0]);
-                z[mt][0] = fmaf(fmaxf(acc[mt][1] + bh, 0.f), w1, z[mt][0]);
-                z[mt][1] = fmaf(fmaxf(acc[mt][2] + bl, 0.f), w0, z[mt][1]);
-                z[mt][1] = fmaf(fmaxf(acc[mt][3] + bh, 0.f), w1, z[mt][1]);
-                }
-            }
+                const float2 bias = s_b1[nt * 4 + t];
+                float acc[kCapInferTiles][4];
 #pragma unroll
-        for (int mt = 0; mt < 2; ++mt)
-            {
-            // the four lanes of a group hold disjoint columns of rows r0 and r0 + 8
-            float z0 = z[mt][0], z1 = z[mt][1];
-            z0 += __shfl_xor_sync(0xffffffffu, z0, 1);
-            z0 += __shfl_xor_sync(0xffffffffu, z0, 2);
-            z1 += __shfl_xor_sync(0xffffffffu, z1, 1);
-            z1 += __shfl_xor_sync(0xffffffffu, z1, 2);
-            if (t < 2u)
-                {
-                const unsigned int s = base + mt * 16u + g + 8u * t;
-                if (s < a.N)
+                for (int i = 0; i < kCapInferTiles; ++i)
                     {
-                    const float y = cap_softplus((t == 0u ? z0 : z1) + b3);
-                    const unsigned int row = cap_row(a, s);
-                    if (a.y_out) a.y_out[row] = y;
-                    a.cap_out[row] = cap_from_output(y, a.margins[cap_margin_bin(y)], a.cap_max);
+                    acc[i][0] = bias.x; acc[i][1] = bias.y; acc[i][2] = bias.x; acc[i][3] = bias.y;
+                    }
+#pragma unroll
+                for (int kt = 0; kt < 2; ++kt)
+                    {
+                    const uint2 b = s_w1[(kt * 4 + t) * kCapWStride + nt * 8 + g];
+#pragma unroll
+                    for (int i = 0; i < kCapInferTiles; ++i) mma_bf16_16816(acc[i], a1[i][kt], b.x, b.y);
+                    }
+#pragma unroll
+                for (int i = 0; i < kCapInferTiles; ++i)
+                    {
+                    a2[i][nt >> 1][(nt & 1) * 2 + 0] = pack_relu_bf16x2(acc[i][0], acc[i][1]);
+                    a2[i][nt >> 1][(nt & 1) * 2 + 1] = pack_relu_bf16x2(acc[i][2], acc[i][3]);
                     }
                 }
+            // layer 2 with the output layer folded in: z(row) = sum over columns of relu(h2) * w3
+#pragma unroll
+            for (int nt = 0; nt < 8; ++nt)
+                {
+                const float2 bias = s_b2[nt * 4 + t];
+                float acc[kCapInferTiles][4];
+#pragma unroll
+                for (int i = 0; i < kCapInferTiles; ++i)
+                    {
+                    acc[i][0] = bias.x; acc[i][1] = bias.y; acc[i][2] = bias.x; acc[i][3] = bias.y;
+                    }
+#pragma unroll
+                for (int kt = 0; kt < 4; ++kt)
+                    {
+                    const uint2 b = s_w2[(kt * 4 + t) * kCapWStride + nt * 8 + g];
+#pragma unroll
+                    for (int i = 0; i < kCapInferTiles; ++i) mma_bf16_16816(acc[i], a2[i][kt], b.x, b.y);
+                    }
+                const float2 w = s_w3[nt * 4 + t];
+#pragma unroll
+                for (int i = 0; i < kCapInferTiles; ++i)
+                    {
+                    zc[i][0] = fmaf(fmaxf(acc[i][0], 0.f), w.x, zc[i][0]);
+                    zc[i][0] = fmaf(fmaxf(acc[i][1], 0.f), w.y, zc[i][0]);
+                    zc[i][1] = fmaf(fmaxf(acc[i][2], 0.f), w.x, zc[i][1]);
+                    zc[i][1] = fmaf(fmaxf(acc[i][3], 0.f), w.y, zc[i][1]);
+                    }
+                }
+            // (the loop is not unrolled, so that one pass's fragments are all that is live: the
+            // partial sums leave through selects, not through an index)
+#pragma unroll
+            for (int i = 0; i < kCapInferTiles; ++i)
+#pragma unroll
+                for (int mt = 0; mt < 2; ++mt)
+                    if (m0 + i == mt)
+                        {
+                        z[mt][0] = zc[i][0];
+                        z[mt][1] = zc[i][1];
+                        }
             }
+        // the four lanes of a group hold disjoint columns of rows g, g + 8 (tile 0) and g + 16,
+        // g + 24 (tile 1): after the sums lane t of the group finishes row g + 8t
+#pragma unroll
+        for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+            for (int h = 0; h < 2; ++h)
+                {
+                z[mt][h] += __shfl_xor_sync(0xffffffffu, z[mt][h], 1);
+                z[mt][h] += __shfl_xor_sync(0xffffffffu, z[mt][h], 2);
+                }
+        {
+        const float zr = t == 0u ? z[0][0] : (t == 1u ? z[0][1] : (t == 2u ? z[1][0] : z[1][1]));
+        const unsigned int s = base + g + 8u * t;
+        if (s < a.N)
+            {
+            const float y = cap_softplus(zr + b3);
+            const unsigned int row = cap_row(a, s);
+            if (a.y_out) a.y_out[row] = y;
+            a.cap_out[row] = cap_from_output(y, a.margins[cap_margin_bin(y)], a.cap_max);
+            }
+        }
         __syncwarp();
         }
     }

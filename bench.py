@@ -54,6 +54,7 @@ def parse(argv=None):
     ap.add_argument("--no-clustered", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-polydisperse", action="store_true")
+    ap.add_argument("--no-small", action="store_true")
     ap.add_argument("--train-steps", type=int, default=4000)
     ap.add_argument("--climb", type=int, default=512)
     ap.add_argument("--no-work-order", action="store_true",
@@ -532,6 +533,56 @@ def polydisperse_c2(nb, args, stream, steps=5, warmup=2):
             "step": "2 builds + 4 x (count, host read of the largest count, fill)"}
 
 
+def small_plain(nb, args, stream, n=32_768, steps=200, warmup=20):
+    """The small plain configuration: 32,768 uniform points at density 0.85, cutoff 1.3, 27
+    images, build + count + max read-back + fill.  It fits in L2 and is launch-bound, so it is
+    reported in microseconds per step (each step ends with a synchronisation, as the reference's
+    driver does), beside the reference's own kernels on the same size and GPU."""
+    import torch
+    L = (n / DENSITY) ** (1.0 / 3.0)
+    box = [L, L, L]
+    pad = nb.exact_pad(RC, 2 * L)
+    frames = make_frames(n, L, warmup + steps, seed=31)
+    lbvh = nb.LBVH(leaf_size=args.leaf, radix_bits=args.radix_bits, climb_block=args.climb)
+    trav = nb.LBVHTraverser()
+    trav.set_work_order(not args.no_work_order)
+    counts = torch.empty(n, dtype=torch.int32, device="cuda")
+    lst = torch.empty(n * 64, dtype=torch.int32, device="cuda")
+    times = []
+    for i, p in enumerate(frames):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        lbvh.build(p, [0, 0, 0], box, block_size=args.block)
+        trav.traverse_self(lbvh, RC, box, pad, images="periodic", nneigh=counts, rows_sorted=True,
+                           block_size=args.block)
+        mx = int(counts.max().item())
+        trav.traverse_self(lbvh, RC, box, pad, images="periodic", max_neigh=mx, nneigh=counts,
+                           neigh_list=lst, rows_sorted=True, block_size=args.block)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if i >= warmup:
+            times.append(e0.elapsed_time(e1))
+    times.sort()
+    out = {"workload": f"uniform N={n} density 0.85 L={L:.2f} rc={RC}, 27 images, build+count+max+fill",
+           "us_per_step_median": 1e3 * times[len(times) // 2], "us_per_step_mean": 1e3 * sum(times) / len(times),
+           "steps": steps, "pairs_per_step": int(counts.sum().item())}
+    lbvh.check_status()
+    if not args.no_ref_cuda:
+        try:
+            from oracle import ref_harness
+            if ref_harness.build_if_available() and ref_harness.available():
+                r = ref_harness.run_bench(n, steps=100, warmup=10, rc=RC)
+                best = min(r["results"], key=lambda x: x["step_ms"])
+                out["reference_us_per_step"] = 1e3 * best["step_ms"]
+                out["reference_block"] = best["block"]
+                out["speedup_vs_reference"] = best["step_ms"] * 1e3 / out["us_per_step_mean"]
+            else:
+                out["reference"] = "unavailable: reference kernels not built here"
+        except Exception as e:  # measurement aid only: never fails the bench
+            out["reference"] = f"unavailable: {type(e).__name__}: {e}"[:200]
+    return out
+
+
 def reference_cuda(n, our_ms):
     """The reference's own CUDA kernels on the same GPU and workload (oracle/ref_harness): the
     plain two-pass step (build, setup, count, max, fill) with the best block size of 32..512."""
@@ -833,6 +884,8 @@ def run_ours(args):
         line["polydisperse_1m"] = polydisperse_c2(nb, args, stream)
     if not args.no_batched:
         line["batched_4096"] = batched_ensemble(nb, args, stream)
+    if not args.no_small:
+        line["small_32k"] = small_plain(nb, args, stream)
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(n, L, args.cpu_seconds, os.cpu_count() or 1)
     if not args.no_ref_cuda:

@@ -542,7 +542,9 @@ void LBVH::build(const LaunchParameters& params, const InsertOpT& insert, const 
         gpu::k_climb<InsertOpT, 256><<<detail::ceil_div(N, 256), 256, 0, stream>>>(insert, c);
     else
         gpu::k_climb<InsertOpT, 512><<<detail::ceil_div(N, 512), 512, 0, stream>>>(insert, c);
-    if (N > T)
+    if (N > T && N <= gpu::kClimbOneBlockMaxN)
+        gpu::k_climb_global_block<InsertOpT><<<1, gpu::kClimbOneBlockThreads, 0, stream>>>(insert, c);
+    else if (N > T)
         gpu::k_climb_global<InsertOpT><<<std::min(detail::ceil_div(N, 2048), 152u * 8u), 256, 0, stream>>>(insert, c);
 
     // pre-order positions of the box records

@@ -165,6 +165,19 @@ class LBVHTraverser : public Tunable<unsigned int>
         void setWorkOrder(bool enabled) { m_work_order = enabled; }
         bool getWorkOrder() const { return m_work_order; }
 
+        // Routing by size (results do not depend on it).  With few queries the GPU is mostly idle
+        // and the longest walks set the time.  Traversals of at most getWarpWalkMaxQueries()
+        // queries walk one warp per query, which shortens a walk about 32 times; larger ones one
+        // thread per query.  Self traversals take the symmetric walk only above
+        // getSymmetricMinPoints() points: below it the whole-tree walk, with no partner atomics and
+        // no ordering pass, measured faster (32,768 points, count + fill: warp walk 237 us, thread
+        // walk 270 us, symmetric walk 290 us; 262,144 points: 337 / 351 us thread / symmetric;
+        // 1,048,576 points: 867 / 720 us).  0 turns a limit off.
+        void setWarpWalkMaxQueries(unsigned int q) { m_warp_walk_max = q; }
+        unsigned int getWarpWalkMaxQueries() const { return m_warp_walk_max; }
+        void setSymmetricMinPoints(unsigned int n) { m_symmetric_min = n; }
+        unsigned int getSymmetricMinPoints() const { return m_symmetric_min; }
+
         // Self queries on the fast path: every primitive of the tree queries the tree with cutoff
         // rc.  Queries run in the tree's sorted order; rows_sorted selects whether row s of the
         // output belongs to sorted slot s (the reference benchmark's layout) or to the original
@@ -194,6 +207,8 @@ class LBVHTraverser : public Tunable<unsigned int>
         unsigned long long* m_stats;
         bool m_symmetric;
         bool m_work_order = true;
+        unsigned int m_warp_walk_max = gpu::kWarpWalkMaxQueries;
+        unsigned int m_symmetric_min = gpu::kSymmetricMinPoints;
         // What a symmetric count ran on; a fill with the same tag reuses its results.
         struct PassTag
             {
@@ -317,7 +332,7 @@ void LBVHTraverser::launch_fast(const LaunchParameters& params, const LBVH& lbvh
     else if (m_stats)
         gpu::k_traverse_fast<kind, true, TransformOpT><<<detail::ceil_div(Q, bs), bs, 0, params.stream>>>(
             lbvh.fastData(), a, transform);
-    else if (a.subset || Q <= gpu::kWarpWalkMaxQueries)
+    else if (a.subset || Q <= m_warp_walk_max)
         // few queries (a subset is the rows that overflowed a one-pass list): one warp walks each,
         // so the walks' latency, not the GPU's width, sets the time
         gpu::k_traverse_warp<kind, TransformOpT><<<(unsigned int)(((unsigned long long)Q * 32u + gpu::kWarpWalkBlock - 1u)
@@ -397,11 +412,12 @@ void LBVHTraverser::traverseSelf(const LaunchParameters& params, const LBVH& lbv
     a.pad = pad;
     detail::set_output(a, out);
     const unsigned int longest = detail::max_row(out);
-    // Counts always take the symmetric kernel; fills only while every row fits the one-thread
-    // ordering (longer rows cost more to order than the whole-tree walk costs, and that walk
+    // Counts take the symmetric kernel above the size limits; fills only while every row also
+    // fits the one-thread ordering (longer rows cost more to order than the whole-tree walk costs, and that walk
     // writes every row already in order).
     if (detail::is_symmetric_images<TranslateOpT>::value && m_symmetric && m_mode == kThreadTraversal
-        && !m_stats && lbvh.getN() < gpu::kHalfMaxN
+        && !m_stats && lbvh.getN() < gpu::kHalfMaxN && lbvh.getN() > m_warp_walk_max
+        && lbvh.getN() > m_symmetric_min
         && (output_kind<OutputOpT>::value == gpu::kFastCount
             || (longest > 0u && longest <= gpu::kHalfRowThread)
             || (output_kind<OutputOpT>::value == gpu::kFastList && longest == 0u)))

@@ -634,10 +634,13 @@ __device__ __forceinline__ ClimbNode form_parent(const ClimbArgs& A, unsigned in
     return P;
     }
 
-// Continue a climb through the global arrival words from node X at split p.
-template<class InsertOpT>
+// Continue a climb from node X at split p.  Arrivals are counted in the global arrival words
+// (any number of blocks, GPU-scope fences), or with BLOCK in a shared bitmap of all splits when a
+// single block runs the whole stage (block-scope fences: the children's records are still in
+// global memory, but every reader is in the same block).
+template<bool BLOCK, class InsertOpT>
 __device__ void climb_global(const InsertOpT& insert, const ClimbArgs& A, const QuantFrame& f,
-                             ClimbNode X, unsigned int p)
+                             ClimbNode X, unsigned int p, unsigned int* s_arrived)
     {
     const unsigned int N = A.N;
     const unsigned int* codes = A.codes;
@@ -646,10 +649,20 @@ __device__ void climb_global(const InsertOpT& insert, const ClimbArgs& A, const 
         {
         const unsigned int side = (p == X.r) ? 0u : 1u;
         A.kids[2 * (size_t)p + side] = X.id;
-        __threadfence();
         // the first child to arrive leaves; the second finds the first's node complete
-        if (atomicMax(A.locks + p, A.tag) != A.tag) return;
-        __threadfence();
+        if (BLOCK)
+            {
+            __threadfence_block();
+            const unsigned int bit = 1u << (p & 31u);
+            if (!(atomicOr(s_arrived + (p >> 5), bit) & bit)) return;
+            __threadfence_block();
+            }
+        else
+            {
+            __threadfence();
+            if (atomicMax(A.locks + p, A.tag) != A.tag) return;
+            __threadfence();
+            }
         const unsigned int oid = __ldcg(A.kids + 2 * (size_t)p + (side ^ 1u));
         ClimbNode S;
         if (oid & kNodeLeaf)
@@ -772,6 +785,28 @@ __global__ void __launch_bounds__(T) k_climb(const InsertOpT insert, const Climb
 
 // Second stage of the climb: one thread per pending node, arrival words in global memory.
 template<class InsertOpT>
+__device__ __forceinline__ ClimbNode climb_item(const InsertOpT& insert, const ClimbArgs& A, const QuantFrame& f,
+                                                const uint2& it)
+    {
+    ClimbNode X;
+    if (it.x & kNodeLeaf)
+        {
+        X = climb_leaf(insert, A, f, it.x & ~kNodeLeaf, false);
+        }
+    else
+        {
+        const uint4 nb = A.nbox[it.x];
+        const uint2 nm = A.nmeta[it.x];
+        X.box = make_uint3(nb.x, nb.y, nb.z);
+        X.l = nb.w;
+        X.r = nm.x;
+        X.id = it.x;
+        X.db = nm.y & ~kMetaLive;
+        }
+    return X;
+    }
+
+template<class InsertOpT>
 __global__ void __launch_bounds__(256) k_climb_global(const InsertOpT insert, const ClimbArgs A)
     {
     __shared__ QuantFrame s_frame;
@@ -790,22 +825,40 @@ __global__ void __launch_bounds__(256) k_climb_global(const InsertOpT insert, co
     for (unsigned int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
         {
         const uint2 it = A.items[k];
-        ClimbNode X;
-        if (it.x & kNodeLeaf)
-            {
-            X = climb_leaf(insert, A, f, it.x & ~kNodeLeaf, false);
-            }
-        else
-            {
-            const uint4 nb = A.nbox[it.x];
-            const uint2 nm = A.nmeta[it.x];
-            X.box = make_uint3(nb.x, nb.y, nb.z);
-            X.l = nb.w;
-            X.r = nm.x;
-            X.id = it.x;
-            X.db = nm.y & ~kMetaLive;
-            }
-        climb_global(insert, A, f, X, it.y);
+        climb_global<false>(insert, A, f, climb_item(insert, A, f, it), it.y, nullptr);
+        }
+    }
+
+// The same stage in one block for trees of at most kClimbOneBlockMaxN points: the arrivals are a
+// shared bitmap over the splits, so a level of the climb costs a shared atomic and block-scope
+// fences instead of a global atomic and two GPU-scope fences.  Whole build: 32,768 points 148 ->
+// 125 us, 65,536 points 160 -> 139 us; at 131,072 points one block is slower (198 against 173 us).
+constexpr unsigned int kClimbOneBlockMaxN = 1u << 16;
+constexpr unsigned int kClimbOneBlockThreads = 1024;
+
+template<class InsertOpT>
+__global__ void __launch_bounds__(kClimbOneBlockThreads) k_climb_global_block(const InsertOpT insert, const ClimbArgs A)
+    {
+    __shared__ unsigned int s_arrived[kClimbOneBlockMaxN / 32];
+    __shared__ QuantFrame s_frame;
+    __shared__ unsigned int s_err;
+    __shared__ unsigned int s_n;
+    if (threadIdx.x == 0)
+        {
+        s_frame = frame_from_bounds(A.bounds);
+        s_err = ld_status(A.error);
+        s_n = min(*A.n_items, A.item_capacity);
+        }
+    const unsigned int words = min((A.N + 31u) / 32u, kClimbOneBlockMaxN / 32u);
+    for (unsigned int i = threadIdx.x; i < words; i += blockDim.x) s_arrived[i] = 0u;
+    __syncthreads();
+    if (s_err != 0u || A.N > kClimbOneBlockMaxN) return;
+    const QuantFrame f = s_frame;
+    const unsigned int n = s_n;
+    for (unsigned int k = threadIdx.x; k < n; k += blockDim.x)
+        {
+        const uint2 it = A.items[k];
+        climb_global<true>(insert, A, f, climb_item(insert, A, f, it), it.y, s_arrived);
         }
     }
 

@@ -463,7 +463,9 @@ __global__ void k_traverse_fast(const FastLBVHData tree, const FastQueryArgs a,
 constexpr unsigned int kWarpWalkBlock = 256;
 // Up to this many queries, a traversal walks one warp per query: one thread per query would
 // leave most of the GPU's SMs idle.
-constexpr unsigned int kWarpWalkMaxQueries = 16384;
+constexpr unsigned int kWarpWalkMaxQueries = 32768;
+// self traversals of at most this many points walk the whole tree (no symmetric walk)
+constexpr unsigned int kSymmetricMinPoints = 262144;
 
 template<int OUT, class TransformOpT>
 __global__ void __launch_bounds__(kWarpWalkBlock) k_traverse_warp(const FastLBVHData tree, const FastQueryArgs a,

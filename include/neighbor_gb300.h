@@ -130,6 +130,13 @@ int nbr_traverser_set_symmetric(nbr_traverser t, int enabled);
  * or in sorted order (0).  Results are the same either way. */
 int nbr_traverser_set_work_order(nbr_traverser t, int enabled);
 
+/* Addition, routing by size: traversals of at most max_queries queries (self traversals included)
+ * walk one warp per query, larger ones one thread per query (default 32,768; 0 = never).  Self
+ * traversals take the symmetric walk only above min_points points (default 262,144; 0 = any size
+ * above the warp limit).  Results are the same either way. */
+int nbr_traverser_set_warp_walk_max(nbr_traverser t, unsigned int max_queries);
+int nbr_traverser_set_symmetric_min_points(nbr_traverser t, unsigned int min_points);
+
 /* getData() (LBVHTraverser.h:326-329): int4 nodes in the reference's 10-bit layout (managed),
  * plus the compression frame (lo, hi, bins: managed float[3] each). */
 int nbr_traverser_get_data(nbr_traverser t, const int** data, const float** lo, const float** hi,

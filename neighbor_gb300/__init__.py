@@ -101,6 +101,8 @@ def _declare(L):
     sig("nbr_traverser_set_symmetric", [_P, _I])
     sig("nbr_debug_inject_alloc_failures", [_U])
     sig("nbr_traverser_set_work_order", [_P, _I])
+    sig("nbr_traverser_set_warp_walk_max", [_P, ctypes.c_uint])
+    sig("nbr_traverser_set_symmetric_min_points", [_P, ctypes.c_uint])
     sig("nbr_traverser_get_data", [_P, _PP, _PP, _PP, _PP])
     sig("nbr_traverse", [_P, _P, _I, _P, _U, _P, _P, _F, _P, _U, _P, _P, _P, _U, _U, _P])
     sig("nbr_traverse_self", [_P, _P, _F, _P, _F, _P, _U, _P, _P, _P, _U, _I, _U, _P])
@@ -160,7 +162,8 @@ EXPORTED = ["nbr_last_error", "nbr_version", "nbr_lbvh_create", "nbr_lbvh_destro
             "nbr_traverser_setup", "nbr_traverser_reset", "nbr_traverser_set_fast_path",
             "nbr_traverser_set_mode", "nbr_traverser_set_stats", "nbr_traverser_set_symmetric",
             "nbr_debug_inject_alloc_failures",
-            "nbr_traverser_set_work_order",
+            "nbr_traverser_set_work_order", "nbr_traverser_set_warp_walk_max",
+            "nbr_traverser_set_symmetric_min_points",
             "nbr_traverser_get_data", "nbr_traverse", "nbr_traverse_self", "nbr_exact_pad",
             "nbr_debug_wait_timeout", "nbr_morton_sort_noalloc", "nbr_traverse_self_csr",
             "nbr_traverse_self_subset_csr",
@@ -467,6 +470,20 @@ class LBVHTraverser:
         """Symmetric fills take each block's queries in order of the walk lengths of the last
         symmetric count over the same tree (True, default)."""
         _check(self._L.nbr_traverser_set_work_order(self._h, 1 if enabled else 0))
+
+    def set_warp_walk_max(self, max_queries: int):
+        """Traversals of at most max_queries queries walk one warp per query (0 = never)."""
+        _check(self._L.nbr_traverser_set_warp_walk_max(self._h, int(max_queries)))
+
+    def set_symmetric_min_points(self, min_points: int):
+        """Self traversals take the symmetric walk only above min_points points (0 = any)."""
+        _check(self._L.nbr_traverser_set_symmetric_min_points(self._h, int(min_points)))
+
+    def force_symmetric(self):
+        """The symmetric walk for self traversals of every size (no size routing)."""
+        self.set_symmetric(True)
+        self.set_warp_walk_max(0)
+        self.set_symmetric_min_points(0)
 
     def set_mode(self, mode: int):
         """0 = one thread per query, 1 = one warp per 32 consecutive queries."""

@@ -296,6 +296,20 @@ int nbr_traverser_set_work_order(nbr_traverser t, int enabled)
     return NBR_OK;
     }
 
+int nbr_traverser_set_warp_walk_max(nbr_traverser t, unsigned int max_queries)
+    {
+    if (!t) return fail(NBR_ERR_INVALID, "null handle");
+    t->trav.setWarpWalkMaxQueries(max_queries);
+    return NBR_OK;
+    }
+
+int nbr_traverser_set_symmetric_min_points(nbr_traverser t, unsigned int min_points)
+    {
+    if (!t) return fail(NBR_ERR_INVALID, "null handle");
+    t->trav.setSymmetricMinPoints(min_points);
+    return NBR_OK;
+    }
+
 int nbr_traverser_get_data(nbr_traverser t, const int** data, const float** lo, const float** hi,
                            const float** bins)
     {

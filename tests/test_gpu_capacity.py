@@ -141,6 +141,7 @@ def test_csr_two_pass_equals_stride_lists():
     assert total == int(cnt.sum())
     flat = torch.full((total,), -1, dtype=torch.int32, device="cuda")
     trav = nb.LBVHTraverser()
+    trav.force_symmetric()
     pad = nb.exact_pad(rc, 2 * L)
     for max_capacity in (int(cnt.max()), 0):  # symmetric kernels, then the whole-tree walk
         flat.fill_(-1)
@@ -150,8 +151,9 @@ def test_csr_two_pass_equals_stride_lists():
         _csr_equals_rows(res, cnt, lst)
 
 
+@pytest.mark.parametrize("symmetric", [False, True])
 @pytest.mark.parametrize("rows_sorted", [True, False])
-def test_one_pass_with_small_capacities_is_exact(rows_sorted):
+def test_one_pass_with_small_capacities_is_exact(rows_sorted, symmetric):
     P, L = _clustered(30000, 7)
     lbvh = _tree(P, L)
     rc = 1.0
@@ -160,6 +162,8 @@ def test_one_pass_with_small_capacities_is_exact(rows_sorted):
     caps = op.capacity(len(P))
     caps.fill_(3)  # most rows overflow and are re-run
     trav = nb.LBVHTraverser()
+    if symmetric:
+        trav.force_symmetric()
     st = op.build(trav, lbvh, rc, [L, L, L], nb.exact_pad(rc, 2 * L), rows_sorted=rows_sorted, cap_max=4096)
     assert st["overflow_rows"] == int((cnt > 3).sum())
     res = op.result(len(P))
@@ -230,6 +234,7 @@ def test_learned_step_in_one_call_matches_separate_calls(rows_sorted):
     model.margin = 0.3
     N = len(P)
     trav = nb.LBVHTraverser()
+    trav.force_symmetric()   # the path of large trees (the symmetric CSR fill)
     lbvh = _tree(P, L)
     op_a = nb.OnePassList()
     model.predict(lbvh, [0, 0, 0], box, rc, rows_sorted=rows_sorted, cap_max=32, caps=op_a.capacity(N))

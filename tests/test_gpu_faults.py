@@ -59,6 +59,7 @@ def test_failed_allocation_in_traversal_is_reported_and_recoverable():
     rc = 1.3
     pad = nb.exact_pad(rc, 2 * L)
     trav = nb.LBVHTraverser()
+    trav.force_symmetric()       # the symmetric count, which allocates work buffers
     nb.inject_alloc_failures(1)   # the count's first work buffer
     with pytest.raises(nb.NeighborError) as e:
         trav.traverse_self(lbvh, rc, [L, L, L], pad, images="periodic")

@@ -4,9 +4,10 @@ With the self image or the 27-image lattice, a self traversal finds each unorder
 writes it to both rows; the rows are then ordered by (image, sorted position), the order of a
 whole-tree walk (and of the reference's rope traversal).  So the full outputs -- counts and every
 list row -- must be bit-identical to the whole-tree walk's, and the sets must equal the oracle's
-cell list.  Counts always take the symmetric kernel; fills with rows longer than 32 entries take
-the whole-tree walk (checked on clustered inputs); rows that overflow max_neigh keep their full
-count and a subset of their true neighbors.
+cell list.  With the size routing off (force_symmetric), counts take the symmetric kernel at every
+size; fills with rows longer than 32 entries take the whole-tree walk (checked on clustered
+inputs); rows that overflow max_neigh keep their full count and a subset of their true neighbors.
+The whole-tree side keeps the default routing (one warp per query up to 32,768 points).
 """
 import numpy as np
 import pytest
@@ -57,6 +58,8 @@ def _both(lbvh, rc, box, pad, images, rows_sorted, max_neigh=None, map=None, tra
         else:
             trav = nb.LBVHTraverser()
             trav.set_symmetric(sym)
+            if sym:
+                trav.force_symmetric()   # the symmetric kernels at every size
             if travs is not None:
                 travs.append(trav)
         out.append(trav.traverse_self(lbvh, rc, box, pad, images=images, rows_sorted=rows_sorted,
@@ -125,6 +128,7 @@ def test_symmetric_overflow_keeps_counts_and_a_subset():
     lbvh.build(_t(P), [0, 0, 0], box)
     pad = nb.exact_pad(rc, 2 * L)
     trav = nb.LBVHTraverser()
+    trav.force_symmetric()
     full = trav.traverse_self(lbvh, rc, box, pad, images="periodic", rows_sorted=False)
     cnt, lst = trav.traverse_self(lbvh, rc, box, pad, images="periodic", rows_sorted=False, max_neigh=5)
     assert torch.equal(cnt, full)
@@ -173,6 +177,7 @@ def test_work_order_does_not_change_results(N, images):
     for ordered in (False, True):
         trav = nb.LBVHTraverser()
         trav.set_work_order(ordered)
+        trav.force_symmetric()   # the symmetric kernels at every size
         cnt = trav.traverse_self(lbvh, rc, box, pad, images=imgs)   # records the walk lengths
         mx = max(1, int(cnt.max().item()))
         out.append(_rows(*trav.traverse_self(lbvh, rc, box, pad, images=imgs, max_neigh=mx)))
@@ -231,6 +236,7 @@ def test_noncubic_offset_box(N):
     lbvh.build(_t(P), lo.tolist(), (lo + Lv).tolist())
     pad = nb.exact_pad(rc, 2.0 * float(np.max(np.abs(lo + 2 * Lv))))
     trav = nb.LBVHTraverser()
+    trav.force_symmetric()   # the symmetric kernels at every size
     cnt = trav.traverse_self(lbvh, rc, box, pad, images="periodic", rows_sorted=False)
     mx = max(1, int(cnt.max().item()))
     cs, ls = _rows(*trav.traverse_self(lbvh, rc, box, pad, images="periodic", rows_sorted=False, max_neigh=mx))

@@ -170,13 +170,22 @@ class LBVHTraverser : public Tunable<unsigned int>
         // queries walk one warp per query, which shortens a walk about 32 times; larger ones one
         // thread per query.  Self traversals take the symmetric walk only above
         // getSymmetricMinPoints() points: below it the whole-tree walk, with no partner atomics and
-        // no ordering pass, measured faster (32,768 points, count + fill: warp walk 237 us, thread
-        // walk 270 us, symmetric walk 290 us; 262,144 points: 337 / 351 us thread / symmetric;
-        // 1,048,576 points: 867 / 720 us).  0 turns a limit off.
+        // no ordering pass, measured faster (count + fill: 32,768 points lane groups 185 us, thread
+        // walk 269 us, symmetric walk 293 us; 65,536 points thread 262, groups of 8 269, symmetric
+        // 310 us; 262,144 points thread 338, symmetric 349 us; 1,048,576 points 867 / 720 us).
+        // 0 turns a limit off.
         void setWarpWalkMaxQueries(unsigned int q) { m_warp_walk_max = q; }
         unsigned int getWarpWalkMaxQueries() const { return m_warp_walk_max; }
         void setSymmetricMinPoints(unsigned int n) { m_symmetric_min = n; }
         unsigned int getSymmetricMinPoints() const { return m_symmetric_min; }
+        // Lanes per query of those small traversals: 4, 8, 16 or 32; 0 (default) picks by size.
+        void setWalkLanes(unsigned int lanes)
+            {
+            if (lanes != 0 && lanes != 4 && lanes != 8 && lanes != 16 && lanes != 32)
+                throw std::runtime_error("Invalid walk lanes (0, 4, 8, 16 or 32).");
+            m_walk_lanes = lanes;
+            }
+        unsigned int getWalkLanes() const { return m_walk_lanes; }
 
         // Self queries on the fast path: every primitive of the tree queries the tree with cutoff
         // rc.  Queries run in the tree's sorted order; rows_sorted selects whether row s of the
@@ -209,6 +218,15 @@ class LBVHTraverser : public Tunable<unsigned int>
         bool m_work_order = true;
         unsigned int m_warp_walk_max = gpu::kWarpWalkMaxQueries;
         unsigned int m_symmetric_min = gpu::kSymmetricMinPoints;
+        unsigned int m_walk_lanes = 0;
+        // self traversal, count + fill: 4,096 points 63 us with 32 lanes (16: 85, 8: 110);
+        // 16,384 points 120 us with 32 (8: 124, 4: 172); 32,768 points 185 us with 16 (8: 188,
+        // 32: 195, 4: 193; one thread per query 269)
+        unsigned int walk_lanes(unsigned int Q) const
+            {
+            if (m_walk_lanes) return m_walk_lanes;
+            return Q <= 16384u ? 32u : 16u;
+            }
         // What a symmetric count ran on; a fill with the same tag reuses its results.
         struct PassTag
             {
@@ -333,11 +351,25 @@ void LBVHTraverser::launch_fast(const LaunchParameters& params, const LBVH& lbvh
         gpu::k_traverse_fast<kind, true, TransformOpT><<<detail::ceil_div(Q, bs), bs, 0, params.stream>>>(
             lbvh.fastData(), a, transform);
     else if (a.subset || Q <= m_warp_walk_max)
-        // few queries (a subset is the rows that overflowed a one-pass list): one warp walks each,
-        // so the walks' latency, not the GPU's width, sets the time
-        gpu::k_traverse_warp<kind, TransformOpT><<<(unsigned int)(((unsigned long long)Q * 32u + gpu::kWarpWalkBlock - 1u)
-                                                                  / gpu::kWarpWalkBlock),
-                                                   gpu::kWarpWalkBlock, 0, params.stream>>>(lbvh.fastData(), a, transform);
+        {
+        // few queries (a subset is the rows that overflowed a one-pass list): a group of lanes
+        // walks each, so the walks' latency, not the GPU's width, sets the time
+        const unsigned int G = a.subset ? 32u : walk_lanes(Q);
+        const unsigned int grid = (unsigned int)(((unsigned long long)Q * G + gpu::kWarpWalkBlock - 1u)
+                                                 / gpu::kWarpWalkBlock);
+        if (G == 4)
+            gpu::k_traverse_warp<kind, TransformOpT, 4><<<grid, gpu::kWarpWalkBlock, 0, params.stream>>>(
+                lbvh.fastData(), a, transform);
+        else if (G == 8)
+            gpu::k_traverse_warp<kind, TransformOpT, 8><<<grid, gpu::kWarpWalkBlock, 0, params.stream>>>(
+                lbvh.fastData(), a, transform);
+        else if (G == 16)
+            gpu::k_traverse_warp<kind, TransformOpT, 16><<<grid, gpu::kWarpWalkBlock, 0, params.stream>>>(
+                lbvh.fastData(), a, transform);
+        else
+            gpu::k_traverse_warp<kind, TransformOpT, 32><<<grid, gpu::kWarpWalkBlock, 0, params.stream>>>(
+                lbvh.fastData(), a, transform);
+        }
     else
         gpu::k_traverse_fast<kind, false, TransformOpT><<<detail::ceil_div(Q, bs), bs, 0, params.stream>>>(
             lbvh.fastData(), a, transform);

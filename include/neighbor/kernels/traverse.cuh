@@ -467,10 +467,14 @@ constexpr unsigned int kWarpWalkMaxQueries = 32768;
 // self traversals of at most this many points walk the whole tree (no symmetric walk)
 constexpr unsigned int kSymmetricMinPoints = 262144;
 
-template<int OUT, class TransformOpT>
+// G < 32: the same walk by groups of G lanes, 32 / G queries per warp (chunks of G records).  A
+// group's shuffles and ballots name only its own lanes, so the groups of a warp may be at
+// different records or images.
+template<int OUT, class TransformOpT, int G = 32>
 __global__ void __launch_bounds__(kWarpWalkBlock) k_traverse_warp(const FastLBVHData tree, const FastQueryArgs a,
                                                                   const TransformOpT transform)
     {
+    static_assert(G == 4 || G == 8 || G == 16 || G == 32, "lane groups of 4, 8, 16 or 32");
     __shared__ QuantFrame s_frame;
     __shared__ unsigned int s_records;
     if (threadIdx.x == 0)
@@ -479,13 +483,15 @@ __global__ void __launch_bounds__(kWarpWalkBlock) k_traverse_warp(const FastLBVH
         s_records = ld_status(tree.status) != 0u ? 0u : *tree.n_boxes + tree.N;
         }
     __syncthreads();
-    const unsigned int lane = threadIdx.x & 31u;
-    const unsigned int tq = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (tq >= a.Q) return;   // whole warps
+    const unsigned int lane = threadIdx.x & (unsigned int)(G - 1);   // lane within the group
+    const unsigned int gmask = G == 32 ? 0xffffffffu
+                                       : (((1u << (G & 31)) - 1u) << ((threadIdx.x & 31u) & ~(unsigned int)(G - 1)));
+    const unsigned int tq = (blockIdx.x * blockDim.x + threadIdx.x) / (unsigned int)G;
+    if (tq >= a.Q) return;   // whole groups
     const unsigned int q = a.subset ? a.subset[tq] : tq;
     const QuantFrame f = s_frame;
     const unsigned int n_rec = s_records;
-    const unsigned int lt = lanemask_lt();
+    const unsigned int lt = lanemask_lt() & gmask;
 
     const FastQuery Q = load_fast_query(tree, a, q);
     const float rs = approx::fadd_ru(Q.rc, a.pad);
@@ -508,7 +514,7 @@ __global__ void __launch_bounds__(kWarpWalkBlock) k_traverse_warp(const FastLBVH
         const uint3 qb = pack_query_box(f, qlo, qhi);
         const bool plain = no_wrap && t.x == 0.f && t.y == 0.f && t.z == 0.f;
         unsigned int i = 0;
-        while (i < n_rec)   // warp-uniform
+        while (i < n_rec)   // group-uniform
             {
             const unsigned int k = i + lane;
             const bool valid = k < n_rec;
@@ -516,14 +522,14 @@ __global__ void __launch_bounds__(kWarpWalkBlock) k_traverse_warp(const FastLBVH
             const bool is_point = valid && (int)n.w < 0;
             const bool miss = valid && !is_point && !node_overlaps(n, qb);
             const unsigned int kill = miss ? max(n.w, k + 1u) : 0u;   // [k + 1, kill) lies under it
-            unsigned int cover = kill;   // inclusive prefix maximum over the lanes
+            unsigned int cover = kill;   // inclusive prefix maximum over the group's lanes
 #pragma unroll
-            for (int o = 1; o < 32; o <<= 1)
+            for (int o = 1; o < G; o <<= 1)
                 {
-                const unsigned int v = __shfl_up_sync(0xffffffffu, cover, o);
+                const unsigned int v = __shfl_up_sync(gmask, cover, o, G);
                 if ((int)lane >= o) cover = max(cover, v);
                 }
-            const unsigned int before = __shfl_up_sync(0xffffffffu, cover, 1);
+            const unsigned int before = __shfl_up_sync(gmask, cover, 1, G);
             const bool live = valid && (lane == 0u || before <= k);
             bool accept = false;
             if (live && is_point)
@@ -531,18 +537,17 @@ __global__ void __launch_bounds__(kWarpWalkBlock) k_traverse_warp(const FastLBVH
                 const float3 x = make_float3(__uint_as_float(n.x), __uint_as_float(n.y), __uint_as_float(n.z));
                 if (point_in_box(x, qlo, qhi)) accept = plain ? plain_pair(Q.p, x, rc2) : exact_pair(Q.p, x, Q.rc, a.box);
                 }
-            const unsigned int hits = __ballot_sync(0xffffffffu, accept);
+            const unsigned int hits = __ballot_sync(gmask, accept) & gmask;
             if (OUT != kFastCount && accept)
                 {
                 const unsigned int pos = count + __popc(hits & lt);
                 if (pos < cap) a.list[row_first + pos] = transform(tree.primitive[n.w & ~kLeafFlag]);
                 }
             count += __popc(hits);
-            // past the chunk and past every live missed subtree
-            unsigned int next = (live && miss) ? kill : 0u;
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) next = max(next, __shfl_xor_sync(0xffffffffu, next, o));
-            i = max(i + 32u, next);
+            // past the chunk and past every missed subtree: the last lane's prefix maximum (a
+            // missed box that is not live lies under an earlier one, and so does its skip link)
+            const unsigned int next = __shfl_sync(gmask, cover, G - 1, G);
+            i = max(i + (unsigned int)G, next);
             }
         }
     if (lane == 0u) a.nneigh[Q.row] = count;

@@ -136,6 +136,8 @@ int nbr_traverser_set_work_order(nbr_traverser t, int enabled);
  * above the warp limit).  Results are the same either way. */
 int nbr_traverser_set_warp_walk_max(nbr_traverser t, unsigned int max_queries);
 int nbr_traverser_set_symmetric_min_points(nbr_traverser t, unsigned int min_points);
+/* Addition: lanes per query of those small traversals (4, 8, 16 or 32; 0 = by size). */
+int nbr_traverser_set_walk_lanes(nbr_traverser t, unsigned int lanes);
 
 /* getData() (LBVHTraverser.h:326-329): int4 nodes in the reference's 10-bit layout (managed),
  * plus the compression frame (lo, hi, bins: managed float[3] each). */

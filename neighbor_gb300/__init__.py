@@ -103,6 +103,7 @@ def _declare(L):
     sig("nbr_traverser_set_work_order", [_P, _I])
     sig("nbr_traverser_set_warp_walk_max", [_P, ctypes.c_uint])
     sig("nbr_traverser_set_symmetric_min_points", [_P, ctypes.c_uint])
+    sig("nbr_traverser_set_walk_lanes", [_P, ctypes.c_uint])
     sig("nbr_traverser_get_data", [_P, _PP, _PP, _PP, _PP])
     sig("nbr_traverse", [_P, _P, _I, _P, _U, _P, _P, _F, _P, _U, _P, _P, _P, _U, _U, _P])
     sig("nbr_traverse_self", [_P, _P, _F, _P, _F, _P, _U, _P, _P, _P, _U, _I, _U, _P])
@@ -163,7 +164,7 @@ EXPORTED = ["nbr_last_error", "nbr_version", "nbr_lbvh_create", "nbr_lbvh_destro
             "nbr_traverser_set_mode", "nbr_traverser_set_stats", "nbr_traverser_set_symmetric",
             "nbr_debug_inject_alloc_failures",
             "nbr_traverser_set_work_order", "nbr_traverser_set_warp_walk_max",
-            "nbr_traverser_set_symmetric_min_points",
+            "nbr_traverser_set_symmetric_min_points", "nbr_traverser_set_walk_lanes",
             "nbr_traverser_get_data", "nbr_traverse", "nbr_traverse_self", "nbr_exact_pad",
             "nbr_debug_wait_timeout", "nbr_morton_sort_noalloc", "nbr_traverse_self_csr",
             "nbr_traverse_self_subset_csr",
@@ -478,6 +479,10 @@ class LBVHTraverser:
     def set_symmetric_min_points(self, min_points: int):
         """Self traversals take the symmetric walk only above min_points points (0 = any)."""
         _check(self._L.nbr_traverser_set_symmetric_min_points(self._h, int(min_points)))
+
+    def set_walk_lanes(self, lanes: int):
+        """Lanes per query of small traversals: 4, 8, 16 or 32 (0 = by size)."""
+        _check(self._L.nbr_traverser_set_walk_lanes(self._h, int(lanes)))
 
     def force_symmetric(self):
         """The symmetric walk for self traversals of every size (no size routing)."""

@@ -310,6 +310,12 @@ int nbr_traverser_set_symmetric_min_points(nbr_traverser t, unsigned int min_poi
     return NBR_OK;
     }
 
+int nbr_traverser_set_walk_lanes(nbr_traverser t, unsigned int lanes)
+    {
+    if (!t) return fail(NBR_ERR_INVALID, "null handle");
+    return guarded([&] { t->trav.setWalkLanes(lanes); });
+    }
+
 int nbr_traverser_get_data(nbr_traverser t, const int** data, const float** lo, const float** hi,
                            const float** bins)
     {

@@ -59,6 +59,8 @@ def parse(argv=None):
     ap.add_argument("--climb", type=int, default=512)
     ap.add_argument("--no-work-order", action="store_true",
                     help="fills take queries in sorted order instead of by walk length / capacity")
+    ap.add_argument("--no-pair-cache", action="store_true",
+                    help="symmetric fills walk again instead of replaying the count's pairs")
     return ap.parse_args(argv)
 
 
@@ -304,6 +306,7 @@ def learned_uniform(nb, n, L, frames, warmup, plain_ms, pairs_step, args, stream
     lbvh = nb.LBVH(leaf_size=args.leaf, radix_bits=args.radix_bits, climb_block=args.climb)
     trav = nb.LBVHTraverser()
     trav.set_work_order(not args.no_work_order)
+    trav.set_pair_cache(not args.no_pair_cache)
     train = make_frames(n, L, 1, seed=4242)
     model, train_s, loss = train_capacity_model(nb, lbvh, trav, train, L, RC, args.train_steps)
     del train
@@ -350,6 +353,7 @@ def clustered_c3(nb, args, stream, n=4_000_000, rc=1.0, steps=5, warmup=2):
     lbvh = nb.LBVH(leaf_size=args.leaf, radix_bits=args.radix_bits, climb_block=args.climb)
     trav = nb.LBVHTraverser()
     trav.set_work_order(not args.no_work_order)
+    trav.set_pair_cache(not args.no_pair_cache)
     model, train_s, loss = train_capacity_model(nb, lbvh, trav, [frame(500), frame(501)], L, rc,
                                                 args.train_steps)
     frames = [frame(600 + k) for k in range(warmup + steps)]
@@ -440,6 +444,7 @@ def batched_ensemble(nb, args, stream, S=4096, rc=1.3, steps=5, max_neigh=48, se
     lbvh = nb.LBVH()
     trav = nb.LBVHTraverser()
     trav.set_work_order(not args.no_work_order)
+    trav.set_pair_cache(not args.no_pair_cache)
     b.sequential_plain(lbvh, trav, pts, rc, cnt2, lst2)  # warm-up (allocations grow to the largest system)
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -511,6 +516,7 @@ def polydisperse_c2(nb, args, stream, steps=5, warmup=2):
     trees = [nb.LBVH(), nb.LBVH()]
     trav = nb.LBVHTraverser()
     trav.set_work_order(not args.no_work_order)
+    trav.set_pair_cache(not args.no_pair_cache)
     ms, outs = time_steps(lambda fr: polydisperse_step(nb, trees, trav, fr, L), frames, warmup, stream)
     out = outs[-1]
     species = frames[-1]
@@ -546,6 +552,7 @@ def small_plain(nb, args, stream, n=32_768, steps=200, warmup=20):
     lbvh = nb.LBVH(leaf_size=args.leaf, radix_bits=args.radix_bits, climb_block=args.climb)
     trav = nb.LBVHTraverser()
     trav.set_work_order(not args.no_work_order)
+    trav.set_pair_cache(not args.no_pair_cache)
     counts = torch.empty(n, dtype=torch.int32, device="cuda")
     lst = torch.empty(n * 64, dtype=torch.int32, device="cuda")
     times = []
@@ -655,6 +662,7 @@ def run_ours(args):
     lbvh = nb.LBVH(leaf_size=args.leaf, radix_bits=args.radix_bits, climb_block=args.climb)
     trav = nb.LBVHTraverser()
     trav.set_work_order(not args.no_work_order)
+    trav.set_pair_cache(not args.no_pair_cache)
     trav.set_mode(args.mode)
     counts = torch.empty(n, dtype=torch.int32, device="cuda")
     cap = 64

@@ -165,6 +165,13 @@ class LBVHTraverser : public Tunable<unsigned int>
         void setWorkOrder(bool enabled) { m_work_order = enabled; }
         bool getWorkOrder() const { return m_work_order; }
 
+        // Pair cache (true, default): a symmetric count also keeps the first 16 pairs each query
+        // found itself (64 bytes per point), and a symmetric fill over the same tree, cutoff,
+        // images and rows replays them instead of walking again (queries that found more walk).
+        // Results do not depend on it.
+        void setPairCache(bool enabled) { m_pair_cache = enabled; }
+        bool getPairCache() const { return m_pair_cache; }
+
         // Routing by size (results do not depend on it).  With few queries the GPU is mostly idle
         // and the longest walks set the time.  Traversals of at most getWarpWalkMaxQueries()
         // queries walk one warp per query, which shortens a walk about 32 times; larger ones one
@@ -219,6 +226,9 @@ class LBVHTraverser : public Tunable<unsigned int>
         unsigned int m_warp_walk_max = gpu::kWarpWalkMaxQueries;
         unsigned int m_symmetric_min = gpu::kSymmetricMinPoints;
         unsigned int m_walk_lanes = 0;
+        bool m_pair_cache = true;
+        bool m_count_cached = false;
+        device_array<unsigned int> m_cache;   // pair cache of the last symmetric count
         // self traversal, count + fill: 4,096 points 63 us with 32 lanes (16: 85, 8: 110);
         // 16,384 points 120 us with 32 (8: 124, 4: 172); 32,768 points 185 us with 16 (8: 188,
         // 32: 195, 4: 193; one thread per query 269)
@@ -519,6 +529,8 @@ void LBVHTraverser::launch_half(const LaunchParameters& params, const LBVH& lbvh
     h.walk_in = nullptr;
     h.totals = nullptr;
     h.own_counted = nullptr;
+    h.cache_out = nullptr;
+    h.cache_in = nullptr;
     // what the last symmetric count ran on: this tree and build, cutoff, images, box and rows
     const PassTag tag{&lbvh, lbvh.getBuildCount(), N, a.self_rc, a.pad, a.lattice, a.lattice_L, a.box,
                       a.self_rows_sorted};
@@ -529,17 +541,31 @@ void LBVHTraverser::launch_half(const LaunchParameters& params, const LBVH& lbvh
         m_totals.reserve(N);
         h.walk_out = m_walk.get();
         h.own = m_count_own.get();
+        if (m_pair_cache)
+            {
+            m_cache.reserve((size_t)N * gpu::kHalfCacheSlots);
+            h.cache_out = m_cache.get();
+            }
         m_count_tag = tag;
+        m_count_cached = m_pair_cache;
         }
     else if (tag == m_count_tag)
         {
-        if (m_work_order) h.walk_in = m_walk.get();
         h.totals = m_totals.get();
         h.own_counted = m_count_own.get();
+        if (m_count_cached && m_pair_cache)
+            h.cache_in = m_cache.get();   // (no work order: the walks are replayed pairs)
+        else if (m_work_order)
+            h.walk_in = m_walk.get();
         }
     detail::check_cuda(cudaMemsetAsync(a.nneigh, 0, (size_t)N * sizeof(unsigned int), stream), "memset");
-    gpu::k_traverse_half<kind, TransformOpT><<<detail::ceil_div(N, gpu::kHalfBlock), gpu::kHalfBlock, 0, stream>>>(
-        lbvh.fastData(), h, transform);
+    const unsigned int grid = detail::ceil_div(N, gpu::kHalfBlock);
+    if (h.cache_out || h.cache_in)
+        gpu::k_traverse_half<kind, TransformOpT, true><<<grid, gpu::kHalfBlock, 0, stream>>>(lbvh.fastData(), h,
+                                                                                             transform);
+    else
+        gpu::k_traverse_half<kind, TransformOpT, false><<<grid, gpu::kHalfBlock, 0, stream>>>(lbvh.fastData(), h,
+                                                                                              transform);
     if (kind == gpu::kFastCount)
         detail::check_cuda(cudaMemcpyAsync(m_totals.get(), a.nneigh, (size_t)N * sizeof(unsigned int),
                                            cudaMemcpyDeviceToDevice, stream), "copy");

@@ -604,7 +604,15 @@ struct HalfArgs
     // final ids straight after the row's appended entries
     const unsigned int* totals;
     const unsigned int* own_counted;
+    // Pair cache: a count writes the first kHalfCacheSlots keys (image << 27 | sorted position)
+    // each query found itself, in the order found (cache_out); a fill over the same tree and rows
+    // replays them instead of walking for every query that found at most that many (cache_in,
+    // with own_counted)
+    unsigned int* cache_out;
+    const unsigned int* cache_in;
     };
+
+constexpr unsigned int kHalfCacheSlots = 16;
 
 // own[] flag of a row whose own entries were written as final ids after its appended entries
 constexpr unsigned int kOwnPlaced = 0x80000000u;
@@ -623,7 +631,9 @@ __device__ __forceinline__ unsigned int half_image_flags(const HalfArgs& a, cons
     return hit ? 1u : 0u;
     }
 
-template<int OUT, class TransformOpT>
+// CACHE: a count writes the pair cache (cache_out), a fill replays it (cache_in); compiled
+// separately so that the walk without it carries no test for it.
+template<int OUT, class TransformOpT, bool CACHE = false>
 __global__ void __launch_bounds__(kHalfBlock, 6) k_traverse_half(const FastLBVHData tree, const HalfArgs a,
                                                                   const TransformOpT transform)
     {
@@ -677,6 +687,52 @@ __global__ void __launch_bounds__(kHalfBlock, 6) k_traverse_half(const FastLBVHD
     bool pending = false;
     unsigned int p_slot = 0, p_cap = 0, p_key = 0;
     unsigned long long p_first = 0;
+    // one pair (q, j) that the query found through image `bit` (mirror: the partner's image)
+    const auto take = [&](unsigned int j, unsigned int bit, unsigned int mirror) {
+        if (OUT == kFastCount)
+            {
+            if (j != q) atomicAdd(a.nneigh + (a.rows_sorted ? j : tree.primitive[j]), 1u);
+            if (CACHE && own < kHalfCacheSlots)
+                a.cache_out[(size_t)q * kHalfCacheSlots + own] = (bit << kHalfKeyBits) | j;
+            }
+        else
+            {
+            if (placed)
+                {
+                if (own_base + own < cap) a.list[row_first + own_base + own] = transform(tree.primitive[j]);
+                }
+            else if (own < cap)
+                {
+                a.list[row_first + (cap - 1u - own)] = (bit << kHalfKeyBits) | j;
+                }
+            if (j != q)
+                {
+                if (pending && p_slot < p_cap) a.list[p_first + p_slot] = p_key;
+                const unsigned int rj = a.rows_sorted ? j : tree.primitive[j];
+                p_slot = atomicAdd(a.nneigh + rj, 1u);
+                row_layout<OUT>(a.offsets, a.caps, a.max_neigh, rj, p_first, p_cap);
+                p_key = (mirror << kHalfKeyBits) | q;
+                pending = true;
+                }
+            }
+        ++own;
+    };
+    if (CACHE && OUT != kFastCount)
+        {
+        // the count's pairs of this query, replayed in the order it found them
+        const unsigned int n_cached = a.own_counted[row];
+        if (n_cached <= kHalfCacheSlots)
+            {
+            const unsigned int* keys = a.cache_in + (size_t)q * kHalfCacheSlots;
+            for (unsigned int k = 0; k < n_cached; ++k)
+                {
+                const unsigned int key = keys[k];
+                const unsigned int bit = key >> kHalfKeyBits;
+                take(key & kHalfKeyMask, bit, a.lattice ? 26u - bit : 0u);
+                }
+            flags = 0u;
+            }
+        }
     while (flags)
         {
         const int bit = __ffs(flags) - 1;
@@ -700,35 +756,7 @@ __global__ void __launch_bounds__(kHalfBlock, 6) k_traverse_half(const FastLBVHD
                     const float3 x = make_float3(__uint_as_float(n.x), __uint_as_float(n.y), __uint_as_float(n.z));
                     const bool accept = kPlain ? plain_pair(P, x, rc2)
                                                : ((!multi || point_in_box(x, qlo, qhi)) && exact_pair(P, x, a.rc, a.box));
-                    if (accept)
-                        {
-                        const unsigned int j = n.w & ~kLeafFlag;
-                        if (OUT == kFastCount)
-                            {
-                            if (j != q) atomicAdd(a.nneigh + (a.rows_sorted ? j : tree.primitive[j]), 1u);
-                            }
-                        else
-                            {
-                            if (placed)
-                                {
-                                if (own_base + own < cap) a.list[row_first + own_base + own] = transform(tree.primitive[j]);
-                                }
-                            else if (own < cap)
-                                {
-                                a.list[row_first + (cap - 1u - own)] = ((unsigned int)bit << kHalfKeyBits) | j;
-                                }
-                            if (j != q)
-                                {
-                                if (pending && p_slot < p_cap) a.list[p_first + p_slot] = p_key;
-                                const unsigned int rj = a.rows_sorted ? j : tree.primitive[j];
-                                p_slot = atomicAdd(a.nneigh + rj, 1u);
-                                row_layout<OUT>(a.offsets, a.caps, a.max_neigh, rj, p_first, p_cap);
-                                p_key = (mirror << kHalfKeyBits) | q;
-                                pending = true;
-                                }
-                            }
-                        ++own;
-                        }
+                    if (accept) take(n.w & ~kLeafFlag, (unsigned int)bit, mirror);
                     ++i;
                     }
                 else

@@ -130,6 +130,11 @@ int nbr_traverser_set_symmetric(nbr_traverser t, int enabled);
  * or in sorted order (0).  Results are the same either way. */
 int nbr_traverser_set_work_order(nbr_traverser t, int enabled);
 
+/* Addition: a symmetric count keeps the first 16 pairs each query found itself (64 bytes per
+ * point) and a symmetric fill over the same tree, cutoff, images and rows replays them instead of
+ * walking again (1, default), or every fill walks (0).  Results are the same either way. */
+int nbr_traverser_set_pair_cache(nbr_traverser t, int enabled);
+
 /* Addition, routing by size: traversals of at most max_queries queries (self traversals included)
  * walk one warp per query, larger ones one thread per query (default 32,768; 0 = never).  Self
  * traversals take the symmetric walk only above min_points points (default 262,144; 0 = any size

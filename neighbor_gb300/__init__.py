@@ -102,6 +102,7 @@ def _declare(L):
     sig("nbr_debug_inject_alloc_failures", [_U])
     sig("nbr_traverser_set_work_order", [_P, _I])
     sig("nbr_traverser_set_warp_walk_max", [_P, ctypes.c_uint])
+    sig("nbr_traverser_set_pair_cache", [_P, _I])
     sig("nbr_traverser_set_symmetric_min_points", [_P, ctypes.c_uint])
     sig("nbr_traverser_set_walk_lanes", [_P, ctypes.c_uint])
     sig("nbr_traverser_get_data", [_P, _PP, _PP, _PP, _PP])
@@ -165,6 +166,7 @@ EXPORTED = ["nbr_last_error", "nbr_version", "nbr_lbvh_create", "nbr_lbvh_destro
             "nbr_debug_inject_alloc_failures",
             "nbr_traverser_set_work_order", "nbr_traverser_set_warp_walk_max",
             "nbr_traverser_set_symmetric_min_points", "nbr_traverser_set_walk_lanes",
+            "nbr_traverser_set_pair_cache",
             "nbr_traverser_get_data", "nbr_traverse", "nbr_traverse_self", "nbr_exact_pad",
             "nbr_debug_wait_timeout", "nbr_morton_sort_noalloc", "nbr_traverse_self_csr",
             "nbr_traverse_self_subset_csr",
@@ -471,6 +473,10 @@ class LBVHTraverser:
         """Symmetric fills take each block's queries in order of the walk lengths of the last
         symmetric count over the same tree (True, default)."""
         _check(self._L.nbr_traverser_set_work_order(self._h, 1 if enabled else 0))
+
+    def set_pair_cache(self, enabled: bool):
+        """A symmetric count keeps each query's first 16 pairs for the next fill (True, default)."""
+        _check(self._L.nbr_traverser_set_pair_cache(self._h, 1 if enabled else 0))
 
     def set_warp_walk_max(self, max_queries: int):
         """Traversals of at most max_queries queries walk one warp per query (0 = never)."""

@@ -296,6 +296,13 @@ int nbr_traverser_set_work_order(nbr_traverser t, int enabled)
     return NBR_OK;
     }
 
+int nbr_traverser_set_pair_cache(nbr_traverser t, int enabled)
+    {
+    if (!t) return fail(NBR_ERR_INVALID, "null handle");
+    t->trav.setPairCache(enabled != 0);
+    return NBR_OK;
+    }
+
 int nbr_traverser_set_warp_walk_max(nbr_traverser t, unsigned int max_queries)
     {
     if (!t) return fail(NBR_ERR_INVALID, "null handle");

@@ -249,3 +249,46 @@ def test_noncubic_offset_box(N):
     assert np.array_equal(cs, np.diff(off).astype(np.uint32))
     for r in range(0, N, max(1, N // 97)):
         assert np.array_equal(np.sort(ls[r, : cs[r]]), nbrs[off[r]:off[r + 1]])
+
+
+@pytest.mark.parametrize("rows_sorted", [True, False])
+def test_pair_cache_replays_the_count(rows_sorted):
+    # tight clusters of 20 points inside the cutoff: rows of about 20 entries (the symmetric fill),
+    # and the first queries of a cluster find more than the cache's 16 pairs themselves (they walk
+    # again); the fill with the cache, the fill without it and the whole-tree walk must agree
+    rng = np.random.default_rng(61)
+    N, L, rc = 24000, 33.0, 1.0
+    # cluster centres on a grid of spacing 3 (clusters do not meet), jittered
+    g = np.stack(np.meshgrid(np.arange(11), np.arange(11), np.arange(10), indexing="ij"), -1).reshape(-1, 3)
+    centers = (g[: N // 20] * 3.0 + 1.5 + rng.uniform(-0.2, 0.2, (N // 20, 3)))
+    P = np.mod(np.repeat(centers, 20, axis=0) + rng.normal(size=(N, 3)) * 0.12, L).astype(np.float32)
+    box = [L, L, L]
+    lbvh = nb.LBVH()
+    lbvh.build(_t(P), [0, 0, 0], box)
+    pad = nb.exact_pad(rc, 2 * L)
+    out = []
+    for mode in ("cache", "walk", "whole"):
+        trav = nb.LBVHTraverser()
+        if mode == "whole":
+            trav.set_symmetric(False)
+            trav.set_warp_walk_max(0)
+        else:
+            trav.force_symmetric()
+            trav.set_pair_cache(mode == "cache")
+        cnt = trav.traverse_self(lbvh, rc, box, pad, images="periodic", rows_sorted=rows_sorted)
+        mx = int(cnt.max().item())
+        assert 16 < mx <= 32
+        out.append(_rows(*trav.traverse_self(lbvh, rc, box, pad, images="periodic", rows_sorted=rows_sorted,
+                                             max_neigh=mx)))
+        assert np.array_equal(out[-1][0], cnt.cpu().numpy().view(np.uint32))
+    for c, lst in out[1:]:
+        assert np.array_equal(c, out[0][0])
+        assert np.array_equal(lst, out[0][1])
+    # a fill on other rows than the count's does not replay its pairs
+    trav = nb.LBVHTraverser()
+    trav.force_symmetric()
+    trav.traverse_self(lbvh, rc, box, pad, images="periodic", rows_sorted=not rows_sorted)
+    c, lst = _rows(*trav.traverse_self(lbvh, rc, box, pad, images="periodic", rows_sorted=rows_sorted,
+                                       max_neigh=int(out[0][0].max())))
+    assert np.array_equal(c, out[0][0])
+    assert np.array_equal(lst, out[0][1])

@@ -688,6 +688,18 @@ __global__ void __launch_bounds__(kHalfBlock, 6) k_traverse_half(const FastLBVHD
     unsigned int p_slot = 0, p_cap = 0, p_key = 0;
     unsigned long long p_first = 0;
     // one pair (q, j) that the query found through image `bit` (mirror: the partner's image)
+    // the query's own entry k (fill): a final id after the row's appended entries, or a key from
+    // the end of the row
+    const auto own_entry = [&](unsigned int k, unsigned int j, unsigned int bit) {
+        if (placed)
+            {
+            if (own_base + k < cap) a.list[row_first + own_base + k] = transform(tree.primitive[j]);
+            }
+        else if (k < cap)
+            {
+            a.list[row_first + (cap - 1u - k)] = (bit << kHalfKeyBits) | j;
+            }
+    };
     const auto take = [&](unsigned int j, unsigned int bit, unsigned int mirror) {
         if (OUT == kFastCount)
             {
@@ -697,14 +709,7 @@ __global__ void __launch_bounds__(kHalfBlock, 6) k_traverse_half(const FastLBVHD
             }
         else
             {
-            if (placed)
-                {
-                if (own_base + own < cap) a.list[row_first + own_base + own] = transform(tree.primitive[j]);
-                }
-            else if (own < cap)
-                {
-                a.list[row_first + (cap - 1u - own)] = (bit << kHalfKeyBits) | j;
-                }
+            own_entry(own, j, bit);
             if (j != q)
                 {
                 if (pending && p_slot < p_cap) a.list[p_first + p_slot] = p_key;
@@ -723,13 +728,45 @@ __global__ void __launch_bounds__(kHalfBlock, 6) k_traverse_half(const FastLBVHD
         const unsigned int n_cached = a.own_counted[row];
         if (n_cached <= kHalfCacheSlots)
             {
-            const unsigned int* keys = a.cache_in + (size_t)q * kHalfCacheSlots;
-            for (unsigned int k = 0; k < n_cached; ++k)
+            // four pairs at a time: their four partner atomics are in flight together, and their
+            // entries are stored once the slots are back
+            const uint4* keys = reinterpret_cast<const uint4*>(a.cache_in + (size_t)q * kHalfCacheSlots);
+            for (unsigned int k0 = 0; k0 < n_cached; k0 += 4u)
                 {
-                const unsigned int key = keys[k];
-                const unsigned int bit = key >> kHalfKeyBits;
-                take(key & kHalfKeyMask, bit, a.lattice ? 26u - bit : 0u);
+                const uint4 w = keys[k0 >> 2];
+                const unsigned int kk[4] = {w.x, w.y, w.z, w.w};
+                unsigned int slot[4];
+                unsigned int rj[4];
+#pragma unroll
+                for (unsigned int t = 0; t < 4u; ++t)
+                    {
+                    slot[t] = 0xffffffffu;
+                    rj[t] = 0u;
+                    if (k0 + t < n_cached)
+                        {
+                        const unsigned int j = kk[t] & kHalfKeyMask;
+                        own_entry(k0 + t, j, kk[t] >> kHalfKeyBits);
+                        if (j != q)
+                            {
+                            rj[t] = a.rows_sorted ? j : tree.primitive[j];
+                            slot[t] = atomicAdd(a.nneigh + rj[t], 1u);
+                            }
+                        }
+                    }
+#pragma unroll
+                for (unsigned int t = 0; t < 4u; ++t)
+                    {
+                    if (slot[t] != 0xffffffffu)
+                        {
+                        unsigned long long first = 0;
+                        unsigned int c = 0;
+                        row_layout<OUT>(a.offsets, a.caps, a.max_neigh, rj[t], first, c);
+                        const unsigned int bit = kk[t] >> kHalfKeyBits;
+                        if (slot[t] < c) a.list[first + slot[t]] = ((a.lattice ? 26u - bit : 0u) << kHalfKeyBits) | q;
+                        }
+                    }
                 }
+            own = n_cached;
             flags = 0u;
             }
         }

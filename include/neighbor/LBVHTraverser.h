@@ -158,10 +158,11 @@ class LBVHTraverser : public Tunable<unsigned int>
         void setSymmetric(bool enabled) { m_symmetric = enabled; }
         bool getSymmetric() const { return m_symmetric; }
 
-        // Work order of fills (true, default): a symmetric count records how many records each
-        // query visited, and a symmetric fill over the same tree with the same cutoff hands each
-        // block's queries to its lanes in order of those lengths; a whole-tree CSR fill orders them
-        // by row capacity.  false: sorted order.  Results do not depend on it.
+        // Work order of fills (true, default): a symmetric count without the pair cache records
+        // how many records each query visited, and a symmetric fill over the same tree with the
+        // same cutoff hands each block's queries to its lanes in order of those lengths; a
+        // whole-tree CSR fill orders them by row capacity.  false: sorted order.  Results do not
+        // depend on it.
         void setWorkOrder(bool enabled) { m_work_order = enabled; }
         bool getWorkOrder() const { return m_work_order; }
 
@@ -555,8 +556,8 @@ void LBVHTraverser::launch_half(const LaunchParameters& params, const LBVH& lbvh
         h.own_counted = m_count_own.get();
         if (m_count_cached && m_pair_cache)
             h.cache_in = m_cache.get();   // (no work order: the walks are replayed pairs)
-        else if (m_work_order)
-            h.walk_in = m_walk.get();
+        else if (m_work_order && !m_count_cached)
+            h.walk_in = m_walk.get();     // (a count with the cache records no walk lengths)
         }
     detail::check_cuda(cudaMemsetAsync(a.nneigh, 0, (size_t)N * sizeof(unsigned int), stream), "memset");
     const unsigned int grid = detail::ceil_div(N, gpu::kHalfBlock);

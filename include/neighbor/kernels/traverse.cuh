@@ -787,7 +787,7 @@ __global__ void __launch_bounds__(kHalfBlock, 6) k_traverse_half(const FastLBVHD
             while (i < n_rec)
                 {
                 const uint4 n = __ldg(tree.nodes + i);
-                if (OUT == kFastCount) ++visits;
+                if (OUT == kFastCount && !CACHE) ++visits;   // (a replayed fill needs no work order)
                 if ((int)n.w < 0)
                     {
                     const float3 x = make_float3(__uint_as_float(n.x), __uint_as_float(n.y), __uint_as_float(n.z));
@@ -817,7 +817,7 @@ __global__ void __launch_bounds__(kHalfBlock, 6) k_traverse_half(const FastLBVHD
         if (pending && p_slot < p_cap) a.list[p_first + p_slot] = p_key;
         a.own[row] = own | (placed ? kOwnPlaced : 0u);
         }
-    if (a.walk_out) a.walk_out[q] = (unsigned short)min(visits, 65535u);
+    if (!CACHE && a.walk_out) a.walk_out[q] = (unsigned short)min(visits, 65535u);
     }
 
 struct HalfOrderArgs

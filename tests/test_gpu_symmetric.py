@@ -178,6 +178,7 @@ def test_work_order_does_not_change_results(N, images):
         trav = nb.LBVHTraverser()
         trav.set_work_order(ordered)
         trav.force_symmetric()   # the symmetric kernels at every size
+        trav.set_pair_cache(False)   # the fill walks again (in the count's work order)
         cnt = trav.traverse_self(lbvh, rc, box, pad, images=imgs)   # records the walk lengths
         mx = max(1, int(cnt.max().item()))
         out.append(_rows(*trav.traverse_self(lbvh, rc, box, pad, images=imgs, max_neigh=mx)))

@@ -632,9 +632,11 @@ __device__ __forceinline__ unsigned int half_image_flags(const HalfArgs& a, cons
     }
 
 // CACHE: a count writes the pair cache (cache_out), a fill replays it (cache_in); compiled
-// separately so that the walk without it carries no test for it.
+// separately so that the walk without it carries no test for it.  Resident blocks per SM: 8 for
+// the count (32 registers; 16M points 3.57 -> 3.14 ms against 6 blocks), 6 for fills (their
+// deferred partner stores need the registers: the replaying fill at 8 blocks 2.33 -> 2.46 ms).
 template<int OUT, class TransformOpT, bool CACHE = false>
-__global__ void __launch_bounds__(kHalfBlock, 6) k_traverse_half(const FastLBVHData tree, const HalfArgs a,
+__global__ void __launch_bounds__(kHalfBlock, OUT == kFastCount ? 8 : 6) k_traverse_half(const FastLBVHData tree, const HalfArgs a,
                                                                   const TransformOpT transform)
     {
     __shared__ QuantFrame s_frame;

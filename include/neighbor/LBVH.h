@@ -20,6 +20,7 @@
 #ifndef NEIGHBOR_LBVH_H_
 #define NEIGHBOR_LBVH_H_
 
+#include <atomic>
 #include <algorithm>
 #include <cstdint>
 #include <cstring>
@@ -146,8 +147,10 @@ class LBVH : public Tunable<unsigned int>
 
         // ---- additions of this library ----
 
-        // Number of builds so far (identifies the current tree).
-        unsigned long long getBuildCount() const { return m_builds; }
+        // Identifier of the current tree: unique in the process (every build of any LBVH takes the
+        // next one), so that a traverser's results of an earlier pass are never taken for another
+        // tree's, even one built in the same memory after this object was destroyed.
+        unsigned long long getBuildId() const { return m_build_id; }
 
         // Primitives per leaf bucket of the traversal tree (1..64; rounded to a power of two).
         void setLeafSize(unsigned int leaf_size)
@@ -251,7 +254,7 @@ class LBVH : public Tunable<unsigned int>
         unsigned int m_radix_bits;
         bool m_fast_points;
         unsigned int m_epoch;
-        unsigned long long m_builds = 0;
+        unsigned long long m_build_id = 0;
         unsigned int m_block;
         unsigned int m_climb_block;
         cudaStream_t m_stream;
@@ -291,7 +294,8 @@ class LBVH : public Tunable<unsigned int>
 
         unsigned int next_epoch()
             {
-            ++m_builds;
+            static std::atomic<unsigned long long> s_next_build_id{0};
+            m_build_id = ++s_next_build_id;
             ++m_epoch;
             if (m_epoch >= (1u << 27))
                 {

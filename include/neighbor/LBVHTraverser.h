@@ -238,7 +238,8 @@ class LBVHTraverser : public Tunable<unsigned int>
             if (m_walk_lanes) return m_walk_lanes;
             return Q <= 16384u ? 32u : 16u;
             }
-        // What a symmetric count ran on; a fill with the same tag reuses its results.
+        // What a symmetric count ran on (the tree's address and process-unique build id, cutoff,
+        // images, box and rows); a fill with the same tag reuses its results.
         struct PassTag
             {
             const LBVH* tree = nullptr;
@@ -533,7 +534,7 @@ void LBVHTraverser::launch_half(const LaunchParameters& params, const LBVH& lbvh
     h.cache_out = nullptr;
     h.cache_in = nullptr;
     // what the last symmetric count ran on: this tree and build, cutoff, images, box and rows
-    const PassTag tag{&lbvh, lbvh.getBuildCount(), N, a.self_rc, a.pad, a.lattice, a.lattice_L, a.box,
+    const PassTag tag{&lbvh, lbvh.getBuildId(), N, a.self_rc, a.pad, a.lattice, a.lattice_L, a.box,
                       a.self_rows_sorted};
     if (kind == gpu::kFastCount)
         {

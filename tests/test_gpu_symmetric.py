@@ -293,3 +293,32 @@ def test_pair_cache_replays_the_count(rows_sorted):
                                        max_neigh=int(out[0][0].max())))
     assert np.array_equal(c, out[0][0])
     assert np.array_equal(lst, out[0][1])
+
+
+def test_fill_after_a_count_on_another_tree_walks():
+    # the count ran on tree A, which is then destroyed; tree B (same size, other points, possibly
+    # at A's address) is filled by the same traverser: nothing of A's count may be replayed
+    N = 20000
+    PA, L = _uniform(N, 71)
+    PB, _ = _uniform(N, 72)
+    box = [L, L, L]
+    rc = 1.3
+    pad = nb.exact_pad(rc, 2 * L)
+    trav = nb.LBVHTraverser()
+    trav.force_symmetric()
+    a = nb.LBVH()
+    a.build(_t(PA), [0, 0, 0], box)
+    trav.traverse_self(lbvh=a, rc=rc, box=box, pad=pad, images="periodic", rows_sorted=True)
+    torch.cuda.synchronize()
+    del a
+    b = nb.LBVH()
+    b.build(_t(PB), [0, 0, 0], box)
+    whole = nb.LBVHTraverser()
+    whole.set_symmetric(False)
+    whole.set_warp_walk_max(0)
+    cnt = whole.traverse_self(b, rc, box, pad, images="periodic", rows_sorted=True)
+    mx = int(cnt.max().item())
+    want = _rows(*whole.traverse_self(b, rc, box, pad, images="periodic", rows_sorted=True, max_neigh=mx))
+    got = _rows(*trav.traverse_self(b, rc, box, pad, images="periodic", rows_sorted=True, max_neigh=mx))
+    assert np.array_equal(got[0], want[0])
+    assert np.array_equal(got[1], want[1])

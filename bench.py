@@ -5,6 +5,8 @@ Workload (one "step" = one trajectory frame): 16,777,216 FP32 points uniform at 
 Gaussian moves of sigma 0.05 and wrapped; per frame a full LBVH rebuild, a count pass, the max
 count read back to size the list (the reference's two-pass pattern), and a fill pass writing a
 fixed-stride neighbor list; cutoff 1.3, 27 periodic images, exact FP32 minimum-image predicate.
+The count is a symmetric walk that keeps each query's first pairs; the fill replays them
+(--no-pair-cache: the fill walks again).
 Frames are generated on the GPU before timing (synthetic data; inputs are 201 MB per frame,
 larger than the 129 MB L2, and every step reads a new frame).
 

@@ -322,3 +322,33 @@ def test_fill_after_a_count_on_another_tree_walks():
     got = _rows(*trav.traverse_self(b, rc, box, pad, images="periodic", rows_sorted=True, max_neigh=mx))
     assert np.array_equal(got[0], want[0])
     assert np.array_equal(got[1], want[1])
+
+
+def test_pair_cache_csr_fill_equals_whole_walk():
+    # count, then a CSR fill (rows sized by the counts) that replays the count's pairs
+    N = 60000
+    P, L = _uniform(N, 81)
+    box = [L, L, L]
+    rc = 1.3
+    lbvh = nb.LBVH()
+    lbvh.build(_t(P), [0, 0, 0], box)
+    pad = nb.exact_pad(rc, 2 * L)
+    op = nb.OnePassList()
+    out = []
+    for mode in ("replay", "whole"):
+        trav = nb.LBVHTraverser()
+        if mode == "replay":
+            trav.force_symmetric()
+        else:
+            trav.set_symmetric(False)
+            trav.set_warp_walk_max(0)
+        cnt = trav.traverse_self(lbvh, rc, box, pad, images="periodic", rows_sorted=False)
+        mx = int(cnt.max().item())
+        assert mx <= 32
+        offsets, total = op.scan(cnt)
+        lst = torch.full((total + 1,), -1, dtype=torch.int32, device="cuda")
+        nn = trav.traverse_self_csr(lbvh, rc, box, pad, offsets, cnt, lst, max_capacity=mx, images="periodic",
+                                    rows_sorted=False)
+        assert torch.equal(nn, cnt)
+        out.append(lst.cpu().numpy())
+    assert np.array_equal(out[0], out[1])

@@ -175,8 +175,8 @@ class LBVHTraverser : public Tunable<unsigned int>
 
         // Routing by size (results do not depend on it).  With few queries the GPU is mostly idle
         // and the longest walks set the time.  Traversals of at most getWarpWalkMaxQueries()
-        // queries walk one warp per query, which shortens a walk about 32 times; larger ones one
-        // thread per query.  Self traversals take the symmetric walk only above
+        // queries walk one group of lanes per query (getWalkLanes()), which shortens a walk about
+        // as many times as the group has lanes; larger ones one thread per query.  Self traversals take the symmetric walk only above
         // getSymmetricMinPoints() points: below it the whole-tree walk, with no partner atomics and
         // no ordering pass, measured faster (count + fill: 32,768 points lane groups 185 us, thread
         // walk 269 us, symmetric walk 293 us; 65,536 points thread 262, groups of 8 269, symmetric

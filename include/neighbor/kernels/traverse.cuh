@@ -456,13 +456,13 @@ __global__ void k_traverse_fast(const FastLBVHData tree, const FastQueryArgs a,
 // so a record is live when no earlier live-or-not missed box of the chunk covers it (a prefix
 // maximum of the missed boxes' skip links over the lanes); live points go to the exact predicate,
 // and the accepted ones are written in record order (ballot + rank), which is the order of the
-// one-thread walk.  The next chunk starts past the chunk and past every live missed subtree.
-// Many lanes test records that a one-thread walk skips, but the walk's latency is about 32
-// times shorter, which is what a handful of long rows needs.
+// one-thread walk.  The next chunk starts past the chunk and past every missed subtree (the last
+// lane's prefix maximum).  Many lanes test records that a one-thread walk skips, but the walk's
+// latency is about 32 times shorter, which is what a handful of long rows needs.
 // ---------------------------------------------------------------------------------------------
 constexpr unsigned int kWarpWalkBlock = 256;
-// Up to this many queries, a traversal walks one warp per query: one thread per query would
-// leave most of the GPU's SMs idle.
+// Up to this many queries, a traversal walks one group of lanes per query (LBVHTraverser picks the
+// group width): one thread per query would leave most of the GPU's SMs idle.
 constexpr unsigned int kWarpWalkMaxQueries = 32768;
 // self traversals of at most this many points walk the whole tree (no symmetric walk)
 constexpr unsigned int kSymmetricMinPoints = 262144;

@@ -7,7 +7,7 @@ list row -- must be bit-identical to the whole-tree walk's, and the sets must eq
 cell list.  With the size routing off (force_symmetric), counts take the symmetric kernel at every
 size; fills with rows longer than 32 entries take the whole-tree walk (checked on clustered
 inputs); rows that overflow max_neigh keep their full count and a subset of their true neighbors.
-The whole-tree side keeps the default routing (one warp per query up to 32,768 points).
+The whole-tree side keeps the default routing (lane groups per query up to 32,768 points).
 """
 import numpy as np
 import pytest

@@ -56,3 +56,13 @@ def test_errors_do_not_cross_the_abi(lib):
     # invalid tunable is rejected before any device work (reference: Tunable.h:110-118)
     assert L.nbr_lbvh_build_points(h, ctypes.c_void_p(8), 10, lo, lo, 33, None) == 1
     assert L.nbr_lbvh_destroy(h) == 0
+
+
+def test_product_rejects_host_tensors():
+    # the product has no CPU path: a host tensor is refused before any library call
+    torch = pytest.importorskip("torch")
+    lbvh = nb.LBVH()
+    with pytest.raises(TypeError):
+        lbvh.build(torch.zeros((10, 3)), [0, 0, 0], [1, 1, 1])
+    with pytest.raises(TypeError):
+        nb.CapacityModel.targets(torch.zeros(4, dtype=torch.int32))

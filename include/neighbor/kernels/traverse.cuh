@@ -596,7 +596,8 @@ struct HalfArgs
     unsigned int max_neigh;
     const unsigned long long* offsets;
     const unsigned int* caps;
-    unsigned int* own;       // fill only: entries each row found itself
+    unsigned int* own;       // entries each row found itself (count: for a later fill; fill: for
+                             // the ordering pass, with kOwnPlaced)
     unsigned short* walk_out;       // optional: records each query visited (saturated at 65535)
     const unsigned short* walk_in;  // optional: walk lengths of an earlier pass over the same tree
     // fill only, optional: row totals and own counts of a symmetric count over the same tree and

@@ -31,10 +31,19 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+METRIC = "neighbor pairs/s (build+traverse) at 16M pts vs ref CUDA; learned vs plain"
 DEFAULT_N = 16_777_216
 DENSITY = 0.85
 RC = 1.3
 SIGMA = 0.05
+
+
+def workload_config(n, L):
+    """The `config` of both arms' lines: the workload alone (the GPU arm's tuning is reported
+    beside it)."""
+    return {"workload": f"uniform trajectory N={n} density 0.85 L={L:.2f} rc=1.3 sigma=0.05, 27 periodic "
+                        f"images, exact FP32 predicate; per step: build + count + max read + list fill",
+            "l2": f"inputs larger than L2 ({12 * n / 1e6:.0f} MB per frame, a new frame every step)"}
 
 
 def parse(argv=None):
@@ -50,7 +59,6 @@ def parse(argv=None):
     ap.add_argument("--mode", type=int, default=0, help="0 = thread per query, 1 = warp packet")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-ref-cuda", action="store_true")
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--no-clustered", action="store_true")
@@ -225,28 +233,36 @@ def make_frames(n, L, count, seed):
     return frames
 
 
-def cpu_baseline(n, L, seconds, threads=0):
-    """OpenMP cell list (oracle) on a bounded sample: all points in the grid, a prefix of
-    queries sized to take about `seconds`."""
+def cpu_frames(frames, L, threads=0, want_pairs=None):
+    """The CPU baseline (oracle/frame_list.cpp, the host port of the two-pass list): every frame
+    listed whole -- grid of all its points, a count for every point, scan, CSR list of every
+    pair -- on `threads` host threads (0 = all).  The first frame warms the buffers and is not
+    timed.  Returns the line's cpu_baseline object (plus the per-stage seconds)."""
     import numpy as np
     import oracle as O
-    rng = np.random.default_rng(123)
-    P = (rng.random((n, 3)) * L).astype(np.float32)
-    box = [L, L, L]
-    q = min(n, 1 << 18)
-    t0 = time.perf_counter()
-    nn, used = O.celllist_counts(P[:q], P, RC, [0, 0, 0], box, nthreads=threads)
-    dt = time.perf_counter() - t0
-    # grow the sample to roughly `seconds` of work
-    if dt < seconds / 4 and q < n:
-        q = int(min(n, q * max(1.0, seconds / max(dt, 1e-3) * 0.8)))
+    n = len(frames[0])
+    lister = O.FrameLister(n, nthreads=threads)
+    lister.run(frames[0], [L, L, L], RC)
+    pairs, secs, stages = 0, 0.0, np.zeros(4)
+    totals = []
+    used = 1
+    for f in frames[1:]:
         t0 = time.perf_counter()
-        nn, used = O.celllist_counts(P[:q], P, RC, [0, 0, 0], box, nthreads=threads)
-        dt = time.perf_counter() - t0
-    pairs = float(nn.astype(np.float64).sum())
-    return {"value": pairs / dt, "unit": "pairs/s", "cores": int(used), "kind": "port",
-            "sample": f"OpenMP cell list (grid of all {n} points built in the timed call), "
-                      f"{q} of {n} queries, counts only, {dt:.2f} s"}
+        tot, used, st = lister.run(f, [L, L, L], RC)
+        secs += time.perf_counter() - t0
+        pairs += tot
+        totals.append(tot)
+        stages += st
+    k = len(frames) - 1
+    out = {"value": pairs / secs, "unit": "pairs/s", "cores": int(used), "kind": "port",
+           "ms_per_frame": 1e3 * secs / k,
+           "stages_ms": {name: round(1e3 * v / k, 2) for name, v in zip(("grid", "count", "scan", "fill"), stages)},
+           "sample": f"{k} whole frames of {n} points: every point queried, CSR list of all "
+                     f"{pairs / k:.4g} pairs per frame written (grid, count, scan, fill; two passes as the "
+                     f"reference's list), {secs:.2f} s on {used} host threads"}
+    if want_pairs is not None:
+        out["pairs_equal_gpu"] = bool(totals == list(want_pairs))
+    return out
 
 
 # Row capacities of the one-pass lists: at most 32 on uniform input (rows that need more overflow
@@ -612,36 +628,46 @@ def reference_cuda(n, our_ms):
 
 
 def run_reference(args):
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    """The reference arm: the reference has no CPU path, so this times its two-pass list ported to
+    the host (oracle/frame_list.cpp) on the same workload as the GPU arm -- the uniform
+    trajectory, each step one whole frame (every point queried, the CSR list of every pair
+    written) on all host threads.  Frames are generated on the host between the timed calls."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    n = args.n
-    L = (n / DENSITY) ** (1.0 / 3.0)
     import oracle as O
     O.build()
+    n = args.n
+    L = (n / DENSITY) ** (1.0 / 3.0)
     threads = os.cpu_count() or 1
-    vals = []
-    last = None
-    per = max(args.cpu_seconds / max(args.steps, 1), 2.0)
-    for i in range(args.warmup + args.steps):
-        r = cpu_baseline(n, L, per, threads)
-        if i >= args.warmup:
-            vals.append(r["value"])
-        last = r
-    vals.sort()
-    v = vals[len(vals) // 2]
-    line = {"impl": "reference", "metric": "neighbor pairs/s (build+traverse) at 16M pts",
-            "value": v, "unit": "pairs/s", "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": f"uniform points N={n} density 0.85 L={L:.2f} rc=1.3 27 images",
-                       "parallelism": "host OpenMP"},
-            "cpu_baseline": {"value": v, "unit": "pairs/s", "cores": last["cores"],
-                             "kind": "port", "sample": last["sample"]},
+    lister = O.FrameLister(n, nthreads=threads)
+    frame = O.uniform_points(n, [L, L, L], seed=1000)
+    pairs, secs, used = 0, 0.0, 1
+    stages = [0.0] * 4
+    for k in range(args.warmup + args.steps):
+        frame = O.gaussian_move(frame, [L, L, L], SIGMA, seed=2000 + k, out=frame)
+        t0 = time.perf_counter()
+        tot, used, st = lister.run(frame, [L, L, L], RC)
+        dt = time.perf_counter() - t0
+        if k >= args.warmup:
+            pairs += tot
+            secs += dt
+            stages = [a + b for a, b in zip(stages, st)]
+    v = pairs / secs
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "pairs/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": workload_config(n, L),
+            "pairs_per_step": pairs / args.steps,
+            "stages_ms": {name: round(1e3 * v_ / args.steps, 2) for name, v_ in
+                          zip(("grid", "count", "scan", "fill"), stages)},
+            "cpu_baseline": {"value": v, "unit": "pairs/s", "cores": int(used), "kind": "port",
+                             "sample": f"{args.steps} timed trajectory steps, each one whole frame of {n} points: "
+                                       f"every point queried and the CSR list of every pair written (grid, "
+                                       f"count, scan, fill) on {used} host threads"},
             "e2e": {"value": v, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "note": "the reference has no CPU path; this is the OpenMP cell-list port with the "
-                    "same FP32 predicate (median of steps)"}
+            "note": "the reference has no CPU path (it is CUDA only); this is its two-pass neighbor list "
+                    "ported to the host cores as an OpenMP cell list with the same FP32 predicate"}
     print(json.dumps(line))
     return 0
 
@@ -682,7 +708,8 @@ def run_ours(args):
                            block_size=args.block)
         if record is not None:
             record[2].record(stream)
-        mx = int(counts.max().item())
+        # the host read of the largest count (the count's device summary; one synchronisation)
+        mx, _, _ = trav.count_summary(stream)
         if mx > cap:
             raise RuntimeError(f"max neighbors {mx} exceeds the list capacity {cap}")
         if record is not None:
@@ -718,13 +745,13 @@ def run_ours(args):
     clocks = sampler.stop()
     lbvh.check_status()
     ms = t_start.elapsed_time(t_end)
-    # Pairs per frame, counted after the timed region (the workload is deterministic; a torch
-    # integer sum over 16M counts costs far more than the pipeline itself on some builds).
+    # Pairs per frame, counted after the timed region (the workload is deterministic): the
+    # count's device summary holds each frame's total.
     for k in range(args.steps):
         lbvh.build(frames[args.warmup + k], [0, 0, 0], box, block_size=args.block)
         trav.traverse_self(lbvh, RC, box, pad, images=imgs, nneigh=counts, rows_sorted=True,
                            block_size=args.block)
-        pair_counts.append(int(counts.cpu().numpy().astype(np.int64).sum()))
+        pair_counts.append(trav.count_summary(stream)[1])
     pairs_local = float(sum(pair_counts))
     value, pairs_all, ms_max = replica_throughput(pairs_local, ms, ws)
     gap_max_ms = [r[2].elapsed_time(r[3]) for r in recs]
@@ -849,7 +876,7 @@ def run_ours(args):
     achieved = alg[dom] / (stages[dom] * 1e-3) / 1e9
     step_bytes = 12.0 * n + 16.0 * n + 4.0 * n + 4.0 * pairs_step
     line = {
-        "metric": "neighbor pairs/s (build+traverse) at 16M pts",
+        "metric": METRIC,
         "value": value,
         "unit": "pairs/s",
         "n_gpus": ws,
@@ -861,12 +888,10 @@ def run_ours(args):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": f"uniform trajectory N={n} density 0.85 L={L:.2f} rc=1.3 "
-                               f"sigma=0.05, 27 images, build+count+fill per frame",
-                   "leaf_size": args.leaf, "radix_bits": args.radix_bits, "block": args.block,
-                   "traversal": "warp packet" if args.mode == 1 else "thread per query",
-                   "l2": "inputs larger than L2 (201 MB/frame, new frame every step)",
-                   "parallelism": f"replicas x{ws}"},
+        "config": workload_config(n, L),
+        "parallelism": f"replicas x{ws}",
+        "tuning": {"leaf_size": args.leaf, "radix_bits": args.radix_bits, "block": args.block,
+                   "traversal": "warp packet" if args.mode == 1 else "thread per query"},
         "stages_ms": {k: round(v, 4) for k, v in stages.items()},
         "gaps_ms": {"count_to_fill": round(mean(gap_max_ms), 4),
                     "between_steps": round(mean(gap_step_ms), 4) if gap_step_ms else None},
@@ -897,7 +922,9 @@ def run_ours(args):
     if not args.no_small:
         line["small_32k"] = small_plain(nb, args, stream)
     if not args.no_cpu:
-        line["cpu_baseline"] = cpu_baseline(n, L, args.cpu_seconds, os.cpu_count() or 1)
+        # the same frames as the timed GPU steps (host copies of the last three; the first warms)
+        line["cpu_baseline"] = cpu_frames([f.cpu().numpy() for f in frames[-3:]], L, os.cpu_count() or 1,
+                                          want_pairs=pair_counts[-2:])
     if not args.no_ref_cuda:
         line["reference_cuda"] = reference_cuda(n, line["ms_per_step"])
     print(json.dumps(line))

@@ -14,6 +14,8 @@
 #ifndef NEIGHBOR_LBVH_TRAVERSER_H_
 #define NEIGHBOR_LBVH_TRAVERSER_H_
 
+#include <algorithm>
+#include <memory>
 #include <stdexcept>
 #include <type_traits>
 
@@ -166,12 +168,44 @@ class LBVHTraverser : public Tunable<unsigned int>
         void setWorkOrder(bool enabled) { m_work_order = enabled; }
         bool getWorkOrder() const { return m_work_order; }
 
-        // Pair cache (true, default): a symmetric count also keeps the first 16 pairs each query
-        // found itself (64 bytes per point), and a symmetric fill over the same tree, cutoff,
-        // images and rows replays them instead of walking again (queries that found more walk).
+        // Pair exchange (true, default): a symmetric count also keeps, per point, the first 16
+        // pairs it found itself and the first 16 pairs other points found with it (128 bytes per
+        // point), and a fill over the same tree, cutoff, images and rows assembles every row from
+        // them without walking (rows with more re-walk the tree).  false: the fill walks again.
         // Results do not depend on it.
         void setPairCache(bool enabled) { m_pair_cache = enabled; }
         bool getPairCache() const { return m_pair_cache; }
+
+        // Summary of the last counting self traversal (traverseSelf with CountNeighborsOp), four
+        // device words: [0] the largest count, [1] rows whose pairs did not fit the pair
+        // exchange, [2..3] the total of the counts (64-bit).  Written on the traversal's stream.
+        const unsigned int* getCountSummary() const { return m_words.get(); }
+        // The same, read on the host: synchronises `stream` (the reference's two-pass pattern
+        // reads the largest count here before the fill, benchmark/lbvh_benchmark.cc:177-196).
+        void readCountSummary(cudaStream_t stream, unsigned int& max_count, unsigned long long& total,
+                              unsigned int& past_exchange)
+            {
+            if (!m_host_words)
+                {
+                void* p = nullptr;
+                detail::check_cuda(cudaMallocHost(&p, gpu::kSummaryWords * sizeof(unsigned int)), "host alloc");
+                m_host_words.reset(static_cast<unsigned int*>(p));
+                }
+            unsigned int* h = m_host_words.get();
+            if (m_words.size() < kWordCount)
+                {
+                h[0] = h[1] = h[2] = h[3] = 0u;
+                }
+            else
+                {
+                detail::check_cuda(cudaMemcpyAsync(h, m_words.get(), gpu::kSummaryWords * sizeof(unsigned int),
+                                                   cudaMemcpyDeviceToHost, stream), "copy");
+                detail::check_cuda(cudaStreamSynchronize(stream), "sync");
+                }
+            max_count = h[0];
+            past_exchange = h[1];
+            total = (unsigned long long)h[2] | ((unsigned long long)h[3] << 32);
+            }
 
         // Routing by size (results do not depend on it).  With few queries the GPU is mostly idle
         // and the longest walks set the time.  Traversals of at most getWarpWalkMaxQueries()
@@ -229,7 +263,40 @@ class LBVHTraverser : public Tunable<unsigned int>
         unsigned int m_walk_lanes = 0;
         bool m_pair_cache = true;
         bool m_count_cached = false;
-        device_array<unsigned int> m_cache;   // pair cache of the last symmetric count
+        // pair exchange of the last symmetric count: own keys and incoming keys (16 per sorted
+        // position each) and the incoming counters
+        device_array<unsigned int> m_cache;
+        device_array<unsigned int> m_in_cache;
+        device_array<unsigned int> m_in_count;
+        // [0..4) count summary, [4] rows left to re-walk after an assembly
+        static constexpr size_t kWordCount = 8;
+        device_array<unsigned int> m_words;
+        device_array<unsigned int> m_subset;
+        struct host_free { void operator()(unsigned int* p) const { if (p) cudaFreeHost(p); } };
+        std::unique_ptr<unsigned int, host_free> m_host_words;
+        int m_sms = 0;
+        unsigned int sm_count()
+            {
+            if (!m_sms)
+                {
+                int dev = 0;
+                detail::check_cuda(cudaGetDevice(&dev), "device");
+                detail::check_cuda(cudaDeviceGetAttribute(&m_sms, cudaDevAttrMultiProcessorCount, dev), "attribute");
+                }
+            return (unsigned int)m_sms;
+            }
+        // blocks of the count summary: a few per SM (each adds its rows to the words once)
+        unsigned int summary_grid(unsigned int N)
+            {
+            return std::max(1u, std::min(detail::ceil_div(N, gpu::kSummaryBlock), 4u * sm_count()));
+            }
+        // zero the summary words before a count
+        void clear_summary(cudaStream_t stream)
+            {
+            m_words.reserve(kWordCount);
+            detail::check_cuda(cudaMemsetAsync(m_words.get(), 0, gpu::kSummaryWords * sizeof(unsigned int), stream),
+                               "memset");
+            }
         // self traversal, count + fill: 4,096 points 63 us with 32 lanes (16: 85, 8: 110);
         // 16,384 points 120 us with 32 (8: 124, 4: 172); 32,768 points 185 us with 16 (8: 188,
         // 32: 195, 4: 193; one thread per query 269)
@@ -300,6 +367,16 @@ class LBVHTraverser : public Tunable<unsigned int>
         template<class OutputOpT, class TransformOpT>
         void launch_half(const LaunchParameters& params, const LBVH& lbvh, const gpu::FastQueryArgs& a,
                          const OutputOpT& out, const TransformOpT& transform);
+
+        template<class OutputOpT, class TransformOpT>
+        void launch_assemble(const LaunchParameters& params, const LBVH& lbvh, const gpu::FastQueryArgs& a,
+                             const OutputOpT& out, const TransformOpT& transform);
+
+        PassTag self_tag(const LBVH& lbvh, const gpu::FastQueryArgs& a) const
+            {
+            return PassTag{&lbvh, lbvh.getBuildId(), lbvh.getN(), a.self_rc, a.pad, a.lattice, a.lattice_L, a.box,
+                           a.self_rows_sorted};
+            }
     };
 
 namespace detail
@@ -456,18 +533,33 @@ void LBVHTraverser::traverseSelf(const LaunchParameters& params, const LBVH& lbv
     a.pad = pad;
     detail::set_output(a, out);
     const unsigned int longest = detail::max_row(out);
-    // Counts take the symmetric kernel above the size limits; fills only while every row also
-    // fits the one-thread ordering (longer rows cost more to order than the whole-tree walk costs, and that walk
-    // writes every row already in order).
-    if (detail::is_symmetric_images<TranslateOpT>::value && m_symmetric && m_mode == kThreadTraversal
-        && !m_stats && lbvh.getN() < gpu::kHalfMaxN && lbvh.getN() > m_warp_walk_max
-        && lbvh.getN() > m_symmetric_min
-        && (output_kind<OutputOpT>::value == gpu::kFastCount
-            || (longest > 0u && longest <= gpu::kHalfRowThread)
-            || (output_kind<OutputOpT>::value == gpu::kFastList && longest == 0u)))
+    constexpr int kind = output_kind<OutputOpT>::value;
+    const bool symmetric = detail::is_symmetric_images<TranslateOpT>::value && m_symmetric
+                           && m_mode == kThreadTraversal && !m_stats && lbvh.getN() < gpu::kHalfMaxN
+                           && lbvh.getN() > m_warp_walk_max && lbvh.getN() > m_symmetric_min;
+    // Counts take the symmetric kernel above the size limits.  A fill after a count that exchanged
+    // the pairs (same tree, cutoff, images and rows) assembles the rows; other fills walk
+    // symmetrically only while every row also fits the one-thread ordering (longer rows cost
+    // more to order than the whole-tree walk costs, and that walk writes every row in order).
+    if (symmetric && kind != gpu::kFastCount && m_count_cached && m_pair_cache && self_tag(lbvh, a) == m_count_tag)
+        launch_assemble(params, lbvh, a, out, transform);
+    else if (symmetric
+             && (kind == gpu::kFastCount || (longest > 0u && longest <= gpu::kHalfRowThread)
+                 || (kind == gpu::kFastList && longest == 0u)))
         launch_half(params, lbvh, a, out, transform);
     else
+        {
         launch_fast(params, lbvh, a, out, transform, lbvh.getN());
+        if (kind == gpu::kFastCount)
+            {
+            // the count's summary (largest count, total) from the counts it wrote
+            clear_summary(params.stream);
+            const unsigned int N = lbvh.getN();
+            gpu::k_count_summary<false><<<summary_grid(N), gpu::kSummaryBlock, 0, params.stream>>>(
+                N, nullptr, nullptr, nullptr, 0, a.nneigh, m_words.get(), lbvh.getStatusPointer());
+            detail::check_cuda(cudaGetLastError(), "summary launch");
+            }
+        }
     }
 
 template<class OutputOpT, class TranslateOpT, class TransformOpT>
@@ -532,45 +624,58 @@ void LBVHTraverser::launch_half(const LaunchParameters& params, const LBVH& lbvh
     h.totals = nullptr;
     h.own_counted = nullptr;
     h.cache_out = nullptr;
-    h.cache_in = nullptr;
+    h.in_cache = nullptr;
+    h.in_count = nullptr;
     // what the last symmetric count ran on: this tree and build, cutoff, images, box and rows
-    const PassTag tag{&lbvh, lbvh.getBuildId(), N, a.self_rc, a.pad, a.lattice, a.lattice_L, a.box,
-                      a.self_rows_sorted};
+    const PassTag tag = self_tag(lbvh, a);
+    const unsigned int grid = detail::ceil_div(N, gpu::kHalfBlock);
     if (kind == gpu::kFastCount)
         {
-        m_walk.reserve(N);
         m_count_own.reserve(N);
-        m_totals.reserve(N);
-        h.walk_out = m_walk.get();
         h.own = m_count_own.get();
-        if (m_pair_cache)
-            {
-            m_cache.reserve((size_t)N * gpu::kHalfCacheSlots);
-            h.cache_out = m_cache.get();
-            }
         m_count_tag = tag;
         m_count_cached = m_pair_cache;
+        clear_summary(stream);
+        if (m_pair_cache)
+            {
+            // pair exchange: own keys, incoming keys, incoming counters (by sorted position)
+            m_cache.reserve((size_t)N * gpu::kHalfCacheSlots);
+            m_in_cache.reserve((size_t)N * gpu::kHalfCacheSlots);
+            m_in_count.reserve(N);
+            h.cache_out = m_cache.get();
+            h.in_cache = m_in_cache.get();
+            h.in_count = m_in_count.get();
+            detail::check_cuda(cudaMemsetAsync(m_in_count.get(), 0, (size_t)N * sizeof(unsigned int), stream), "memset");
+            if constexpr (kind == gpu::kFastCount)
+                gpu::k_traverse_half<kind, TransformOpT, true><<<grid, gpu::kHalfBlock, 0, stream>>>(lbvh.fastData(), h,
+                                                                                                     transform);
+            gpu::k_count_summary<true><<<summary_grid(N), gpu::kSummaryBlock, 0, stream>>>(
+                N, m_count_own.get(), m_in_count.get(), lbvh.fastData().primitive, a.self_rows_sorted, a.nneigh,
+                m_words.get(), lbvh.getStatusPointer());
+            detail::check_cuda(cudaGetLastError(), "half traversal launch");
+            return;
+            }
+        // no exchange: row counters by atomics, walk lengths and row totals for a walking fill
+        m_walk.reserve(N);
+        m_totals.reserve(N);
+        h.walk_out = m_walk.get();
         }
-    else if (tag == m_count_tag)
+    else if (tag == m_count_tag && !m_count_cached)
         {
         h.totals = m_totals.get();
         h.own_counted = m_count_own.get();
-        if (m_count_cached && m_pair_cache)
-            h.cache_in = m_cache.get();   // (no work order: the walks are replayed pairs)
-        else if (m_work_order && !m_count_cached)
-            h.walk_in = m_walk.get();     // (a count with the cache records no walk lengths)
+        if (m_work_order) h.walk_in = m_walk.get();
         }
     detail::check_cuda(cudaMemsetAsync(a.nneigh, 0, (size_t)N * sizeof(unsigned int), stream), "memset");
-    const unsigned int grid = detail::ceil_div(N, gpu::kHalfBlock);
-    if (h.cache_out || h.cache_in)
-        gpu::k_traverse_half<kind, TransformOpT, true><<<grid, gpu::kHalfBlock, 0, stream>>>(lbvh.fastData(), h,
-                                                                                             transform);
-    else
-        gpu::k_traverse_half<kind, TransformOpT, false><<<grid, gpu::kHalfBlock, 0, stream>>>(lbvh.fastData(), h,
-                                                                                              transform);
+    gpu::k_traverse_half<kind, TransformOpT, false><<<grid, gpu::kHalfBlock, 0, stream>>>(lbvh.fastData(), h,
+                                                                                          transform);
     if (kind == gpu::kFastCount)
+        {
         detail::check_cuda(cudaMemcpyAsync(m_totals.get(), a.nneigh, (size_t)N * sizeof(unsigned int),
                                            cudaMemcpyDeviceToDevice, stream), "copy");
+        gpu::k_count_summary<false><<<summary_grid(N), gpu::kSummaryBlock, 0, stream>>>(
+            N, nullptr, nullptr, nullptr, 0, a.nneigh, m_words.get(), lbvh.getStatusPointer());
+        }
     if (kind != gpu::kFastCount)
         {
         gpu::HalfOrderArgs o;
@@ -586,6 +691,47 @@ void LBVHTraverser::launch_half(const LaunchParameters& params, const LBVH& lbvh
         gpu::k_half_order_rows<TransformOpT><<<detail::ceil_div(N, 256), 256, 0, stream>>>(o, transform);
         }
     detail::check_cuda(cudaGetLastError(), "half traversal launch");
+    }
+
+template<class OutputOpT, class TransformOpT>
+void LBVHTraverser::launch_assemble(const LaunchParameters& params, const LBVH& lbvh, const gpu::FastQueryArgs& a,
+                                    const OutputOpT& out, const TransformOpT& transform)
+    {
+    constexpr int kind = output_kind<OutputOpT>::value;
+    const unsigned int N = lbvh.getN();
+    cudaStream_t stream = params.stream;
+    m_words.reserve(kWordCount);
+    m_subset.reserve(N);
+    detail::check_cuda(cudaMemsetAsync(m_words.get() + gpu::kSummaryWords, 0, sizeof(unsigned int), stream), "memset");
+    gpu::AssembleArgs g;
+    g.N = N;
+    g.rows_sorted = a.self_rows_sorted;
+    g.center = a.lattice ? 13u : 0u;
+    g.own = m_count_own.get();
+    g.in_count = m_in_count.get();
+    g.own_keys = m_cache.get();
+    g.in_keys = m_in_cache.get();
+    g.primitive = lbvh.fastData().primitive;
+    g.nneigh = a.nneigh;
+    g.list = a.list;
+    g.max_neigh = a.max_neigh;
+    g.offsets = a.offsets;
+    g.caps = a.caps;
+    g.subset = m_subset.get();
+    g.subset_count = m_words.get() + gpu::kSummaryWords;
+    g.status = lbvh.getStatusPointer();
+    gpu::k_half_assemble<kind, TransformOpT><<<detail::ceil_div(N, 256), 256, 0, stream>>>(g, transform);
+    // rows whose pairs did not fit the exchange: walked whole (their count is known on the device)
+    gpu::FastQueryArgs b = a;
+    b.Q = N;
+    b.subset = m_subset.get();
+    b.stats = nullptr;
+    b.work_order = 0;
+    const unsigned int blocks = std::max(1u, std::min(detail::ceil_div(N, gpu::kSubsetBlock), 8u * sm_count()));
+    gpu::k_traverse_subset<kind, TransformOpT><<<blocks, gpu::kSubsetBlock, 0, stream>>>(
+        lbvh.fastData(), b, transform, m_words.get() + gpu::kSummaryWords);
+    detail::check_cuda(cudaGetLastError(), "assembly launch");
+    (void)out;
     }
 
 } // namespace neighbor

@@ -351,43 +351,14 @@ __device__ __forceinline__ unsigned int capacity_class(unsigned int c)
 // predicate.  Images are walked one after the other in the same loop.  When a query visits more
 // than one image, a point is found only through the image whose padded box contains it, so each
 // pair is reported once.
+// One query walked by one thread: the body of k_traverse_fast (and of the thread mode of
+// k_traverse_subset).  Writes the row's entries (list outputs) and its count.
 template<int OUT, bool STATS, class TransformOpT>
-__global__ void k_traverse_fast(const FastLBVHData tree, const FastQueryArgs a,
-                                const TransformOpT transform)
+__device__ __forceinline__ void thread_walk(const FastLBVHData& tree, const FastQueryArgs& a,
+                                            const TransformOpT& transform, const QuantFrame& f,
+                                            unsigned int n_rec, unsigned int q, unsigned int& visits,
+                                            unsigned int& tests, unsigned int& walks)
     {
-    __shared__ QuantFrame s_frame;
-    __shared__ unsigned int s_records;
-    __shared__ unsigned int s_class[kWorkClasses];
-    __shared__ unsigned int s_order[1024];
-    if (threadIdx.x == 0)
-        {
-        s_frame = *tree.frame;
-        // a failed build leaves no tree to walk
-        s_records = ld_status(tree.status) != 0u ? 0u : *tree.n_boxes + tree.N;
-        }
-    unsigned int tq = blockIdx.x * blockDim.x + threadIdx.x;
-    if (OUT == kFastCSR && a.work_order)
-        {
-        // rows with capacities of similar size (their predicted or counted lengths) share warps
-        const bool valid = tq < a.Q;
-        unsigned int cls = 0;
-        if (valid)
-            {
-            const unsigned int row = a.spheres || a.self_rows_sorted ? tq : __float_as_uint(tree.points[tq].w);
-            cls = capacity_class(a.caps[row]);
-            }
-        tq = block_work_order(tq, valid, cls, s_class, s_order);
-        if (tq == 0xffffffffu) return;
-        }
-    else
-        {
-        __syncthreads();
-        if (tq >= a.Q) return;
-        }
-    const unsigned int q = a.subset ? a.subset[tq] : tq;
-    const QuantFrame f = s_frame;
-    const unsigned int n_rec = s_records;
-
     const FastQuery Q = load_fast_query(tree, a, q);
     const float rs = approx::fadd_ru(Q.rc, a.pad);
     unsigned int flags = n_rec ? image_flags(a, f, Q.p, rs) : 0u;
@@ -399,7 +370,6 @@ __global__ void k_traverse_fast(const FastLBVHData tree, const FastQueryArgs a,
     if (OUT != kFastCount) row_layout<OUT>(a.offsets, a.caps, a.max_neigh, Q.row, row_first, cap);
 
     unsigned int count = 0;
-    unsigned int visits = 0, tests = 0, walks = 0;
     while (flags)
         {
         const int bit = __ffs(flags) - 1;
@@ -447,6 +417,50 @@ __global__ void k_traverse_fast(const FastLBVHData tree, const FastQueryArgs a,
             walk(std::false_type());
         }
     a.nneigh[Q.row] = count;
+    }
+
+// One thread per query, stackless: a box record is tested against the query's box (hit: the next
+// record, miss: the skip link); a point record inside the query's padded box goes to the exact
+// predicate.  Images are walked one after the other in the same loop.  When a query visits more
+// than one image, a point is found only through the image whose padded box contains it, so each
+// pair is reported once.
+template<int OUT, bool STATS, class TransformOpT>
+__global__ void k_traverse_fast(const FastLBVHData tree, const FastQueryArgs a,
+                                const TransformOpT transform)
+    {
+    __shared__ QuantFrame s_frame;
+    __shared__ unsigned int s_records;
+    __shared__ unsigned int s_class[kWorkClasses];
+    __shared__ unsigned int s_order[1024];
+    if (threadIdx.x == 0)
+        {
+        s_frame = *tree.frame;
+        // a failed build leaves no tree to walk
+        s_records = ld_status(tree.status) != 0u ? 0u : *tree.n_boxes + tree.N;
+        }
+    unsigned int tq = blockIdx.x * blockDim.x + threadIdx.x;
+    if (OUT == kFastCSR && a.work_order)
+        {
+        // rows with capacities of similar size (their predicted or counted lengths) share warps
+        const bool valid = tq < a.Q;
+        unsigned int cls = 0;
+        if (valid)
+            {
+            const unsigned int row = a.spheres || a.self_rows_sorted ? tq : __float_as_uint(tree.points[tq].w);
+            cls = capacity_class(a.caps[row]);
+            }
+        tq = block_work_order(tq, valid, cls, s_class, s_order);
+        if (tq == 0xffffffffu) return;
+        }
+    else
+        {
+        __syncthreads();
+        if (tq >= a.Q) return;
+        }
+    const unsigned int q = a.subset ? a.subset[tq] : tq;
+    const QuantFrame f = s_frame;
+    unsigned int visits = 0, tests = 0, walks = 0;
+    thread_walk<OUT, STATS>(tree, a, transform, f, s_records, q, visits, tests, walks);
     if (STATS) add_stats(a.stats, visits, tests, walks);
     }
 
@@ -470,29 +484,14 @@ constexpr unsigned int kSymmetricMinPoints = 262144;
 // G < 32: the same walk by groups of G lanes, 32 / G queries per warp (chunks of G records).  A
 // group's shuffles and ballots name only its own lanes, so the groups of a warp may be at
 // different records or images.
-template<int OUT, class TransformOpT, int G = 32>
-__global__ void __launch_bounds__(kWarpWalkBlock) k_traverse_warp(const FastLBVHData tree, const FastQueryArgs a,
-                                                                  const TransformOpT transform)
+// One query walked by a group of G lanes: the body of k_traverse_warp (and of the group mode of
+// k_traverse_subset).  Every lane of the group calls it with the same q; lane 0 writes the count.
+template<int OUT, class TransformOpT, int G>
+__device__ __forceinline__ void group_walk(const FastLBVHData& tree, const FastQueryArgs& a,
+                                           const TransformOpT& transform, const QuantFrame& f,
+                                           unsigned int n_rec, unsigned int q, unsigned int lane,
+                                           unsigned int gmask, unsigned int lt)
     {
-    static_assert(G == 4 || G == 8 || G == 16 || G == 32, "lane groups of 4, 8, 16 or 32");
-    __shared__ QuantFrame s_frame;
-    __shared__ unsigned int s_records;
-    if (threadIdx.x == 0)
-        {
-        s_frame = *tree.frame;
-        s_records = ld_status(tree.status) != 0u ? 0u : *tree.n_boxes + tree.N;
-        }
-    __syncthreads();
-    const unsigned int lane = threadIdx.x & (unsigned int)(G - 1);   // lane within the group
-    const unsigned int gmask = G == 32 ? 0xffffffffu
-                                       : (((1u << (G & 31)) - 1u) << ((threadIdx.x & 31u) & ~(unsigned int)(G - 1)));
-    const unsigned int tq = (blockIdx.x * blockDim.x + threadIdx.x) / (unsigned int)G;
-    if (tq >= a.Q) return;   // whole groups
-    const unsigned int q = a.subset ? a.subset[tq] : tq;
-    const QuantFrame f = s_frame;
-    const unsigned int n_rec = s_records;
-    const unsigned int lt = lanemask_lt() & gmask;
-
     const FastQuery Q = load_fast_query(tree, a, q);
     const float rs = approx::fadd_ru(Q.rc, a.pad);
     unsigned int flags = n_rec ? image_flags(a, f, Q.p, rs) : 0u;
@@ -502,7 +501,7 @@ __global__ void __launch_bounds__(kWarpWalkBlock) k_traverse_warp(const FastLBVH
     unsigned int cap = 0;
     if (OUT != kFastCount) row_layout<OUT>(a.offsets, a.caps, a.max_neigh, Q.row, row_first, cap);
 
-    unsigned int count = 0;   // warp-uniform
+    unsigned int count = 0;   // group-uniform
     while (flags)
         {
         const int bit = __ffs(flags) - 1;
@@ -553,6 +552,75 @@ __global__ void __launch_bounds__(kWarpWalkBlock) k_traverse_warp(const FastLBVH
     if (lane == 0u) a.nneigh[Q.row] = count;
     }
 
+// G < 32: the same walk by groups of G lanes, 32 / G queries per warp (chunks of G records).  A
+// group's shuffles and ballots name only its own lanes, so the groups of a warp may be at
+// different records or images.
+template<int OUT, class TransformOpT, int G = 32>
+__global__ void __launch_bounds__(kWarpWalkBlock) k_traverse_warp(const FastLBVHData tree, const FastQueryArgs a,
+                                                                  const TransformOpT transform)
+    {
+    static_assert(G == 4 || G == 8 || G == 16 || G == 32, "lane groups of 4, 8, 16 or 32");
+    __shared__ QuantFrame s_frame;
+    __shared__ unsigned int s_records;
+    if (threadIdx.x == 0)
+        {
+        s_frame = *tree.frame;
+        s_records = ld_status(tree.status) != 0u ? 0u : *tree.n_boxes + tree.N;
+        }
+    __syncthreads();
+    const unsigned int lane = threadIdx.x & (unsigned int)(G - 1);   // lane within the group
+    const unsigned int gmask = G == 32 ? 0xffffffffu
+                                       : (((1u << (G & 31)) - 1u) << ((threadIdx.x & 31u) & ~(unsigned int)(G - 1)));
+    const unsigned int tq = (blockIdx.x * blockDim.x + threadIdx.x) / (unsigned int)G;
+    if (tq >= a.Q) return;   // whole groups
+    const unsigned int q = a.subset ? a.subset[tq] : tq;
+    const QuantFrame f = s_frame;
+    group_walk<OUT, TransformOpT, G>(tree, a, transform, f, s_records, q, lane, gmask, lanemask_lt() & gmask);
+    }
+
+// Rows re-walked whole, their sorted positions in subset[0 .. *subset_count) (a count known only
+// on the device, e.g. the rows an assembly pass could not finish).  A persistent grid: with at
+// most kSubsetGroupMax rows each row gets a warp (a few long walks set the time, and 32 lanes
+// shorten each about 32 times); with more, each row gets one thread (the total work sets it).
+constexpr unsigned int kSubsetBlock = 256;
+constexpr unsigned int kSubsetGroupMax = 32768;
+
+template<int OUT, class TransformOpT>
+__global__ void __launch_bounds__(kSubsetBlock) k_traverse_subset(const FastLBVHData tree, const FastQueryArgs a,
+                                                                  const TransformOpT transform,
+                                                                  const unsigned int* __restrict__ subset_count)
+    {
+    __shared__ QuantFrame s_frame;
+    __shared__ unsigned int s_records;
+    __shared__ unsigned int s_n;
+    if (threadIdx.x == 0)
+        {
+        s_frame = *tree.frame;
+        s_records = ld_status(tree.status) != 0u ? 0u : *tree.n_boxes + tree.N;
+        s_n = min(*subset_count, a.Q);
+        }
+    __syncthreads();
+    const unsigned int n = s_n;
+    const unsigned int n_rec = s_records;
+    if (n == 0u || n_rec == 0u) return;
+    const QuantFrame f = s_frame;
+    const unsigned int gid = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned int threads = gridDim.x * blockDim.x;
+    if (n <= kSubsetGroupMax)
+        {
+        const unsigned int lane = threadIdx.x & 31u;
+        const unsigned int lt = lanemask_lt();
+        for (unsigned int t = gid >> 5; t < n; t += threads >> 5)
+            group_walk<OUT, TransformOpT, 32>(tree, a, transform, f, n_rec, a.subset[t], lane, 0xffffffffu, lt);
+        }
+    else
+        {
+        unsigned int visits = 0, tests = 0, walks = 0;
+        for (unsigned int t = gid; t < n; t += threads)
+            thread_walk<OUT, false>(tree, a, transform, f, n_rec, a.subset[t], visits, tests, walks);
+        }
+    }
+
 // ---------------------------------------------------------------------------------------------
 // Symmetric (half) self traversal.  When the queries are the tree's own points with one cutoff
 // and the image set is symmetric (the self image, or the 27-image lattice), the FP32
@@ -563,19 +631,29 @@ __global__ void __launch_bounds__(kWarpWalkBlock) k_traverse_warp(const FastLBVH
 // every record after it is still either visited or excluded by a box it was tested against.
 // A pair (s, j) then counts for both rows.
 //
-// Count: rows start at zero; the partner's row gets an atomic increment, the query's own total
-// one atomic add at the end.
-// Fill: each entry is first written as a key image << 27 | sorted position.  The query writes
-// the entries it found itself from the end of its row backwards (already in ascending key order)
-// and records how many in own[]; entries found for a row by other queries are appended from the
-// front through an atomic cursor (nneigh, zero on entry).  k_half_order_rows then sorts each row
-// by key and maps keys to transform(primitive) ids, which gives every row the order of the
-// reference's rope traversal (images in ascending order, partners in ascending sorted position
-// within an image), independent of the order of the atomics.  The image through which a partner
-// finds the query is the mirror image (26 - image on the lattice).  A row with more entries than
-// its capacity (max_neigh, or its own capacity in a CSR list) keeps that many of them (which
-// ones is unspecified) and its full count.  Capacities are at most kHalfRowThread, so that one
-// thread orders a row; longer rows are filled by the whole-tree walk, which writes them in order.
+// Two ways to turn the pairs into list rows:
+//
+// Pair exchange (the count keeps the pairs; default).  The count writes, per query, the first
+// kHalfCacheSlots keys (image << 27 | sorted position) it found itself, in the order found (own
+// keys: ascending), and deposits each pair in the partner's incoming slots: the slot is the old
+// value of an atomic increment of the partner's incoming counter, the key the query's position
+// with the mirror image (the image through which the partner finds the query; 26 - image on the
+// lattice).  k_count_summary then writes each row's count (own + incoming), the largest count and
+// the pair total.  A fill over the same tree, cutoff, images and rows walks nothing:
+// k_half_assemble sorts each row's incoming keys, merges them with its own keys and writes the
+// row, in the order of the reference's rope traversal (images ascending, sorted positions
+// ascending within an image).  A row whose own or incoming keys did not fit the slots is
+// re-walked whole (k_traverse_subset).
+//
+// Key ordering pass (when the count did not keep the pairs).  Each entry is first written as a
+// key.  The query writes the entries it found itself from the end of its row backwards (already
+// in ascending key order) and records how many in own[]; entries found for a row by other queries
+// are appended from the front through an atomic cursor (nneigh, zero on entry).
+// k_half_order_rows then sorts each row by key and maps keys to transform(primitive) ids.  A row
+// with more entries than its capacity (max_neigh, or its own capacity in a CSR list) keeps that
+// many of them (which ones is unspecified) and its full count.  Capacities are at most
+// kHalfRowThread, so that one thread orders a row; longer rows are filled by the whole-tree walk,
+// which writes them in order.
 // ---------------------------------------------------------------------------------------------
 constexpr unsigned int kHalfKeyBits = 27;
 constexpr unsigned int kHalfKeyMask = (1u << kHalfKeyBits) - 1u;
@@ -605,12 +683,12 @@ struct HalfArgs
     // final ids straight after the row's appended entries
     const unsigned int* totals;
     const unsigned int* own_counted;
-    // Pair cache: a count writes the first kHalfCacheSlots keys (image << 27 | sorted position)
-    // each query found itself, in the order found (cache_out); a fill over the same tree and rows
-    // replays them instead of walking for every query that found at most that many (cache_in,
-    // with own_counted)
+    // Pair exchange (count only, CACHE): own keys (kHalfCacheSlots per sorted position, in the
+    // order found), incoming keys at the slots in_count hands out (in_count zero on entry); own[]
+    // is then indexed by sorted position
     unsigned int* cache_out;
-    const unsigned int* cache_in;
+    unsigned int* in_cache;
+    unsigned int* in_count;
     };
 
 constexpr unsigned int kHalfCacheSlots = 16;
@@ -632,14 +710,15 @@ __device__ __forceinline__ unsigned int half_image_flags(const HalfArgs& a, cons
     return hit ? 1u : 0u;
     }
 
-// CACHE: a count writes the pair cache (cache_out), a fill replays it (cache_in); compiled
-// separately so that the walk without it carries no test for it.  Resident blocks per SM: 8 for
-// the count (32 registers; 16M points 3.57 -> 3.14 ms against 6 blocks), 6 for fills (their
-// deferred partner stores need the registers: the replaying fill at 8 blocks 2.33 -> 2.46 ms).
+// CACHE (counts only): the pair exchange -- own keys, incoming keys and counters by sorted
+// position; compiled separately so that the walk without it carries no test for it.  Resident
+// blocks per SM: 8 for counts (16M points 3.57 -> 3.14 ms against 6 blocks), 6 for fills (their
+// deferred partner stores need the registers).
 template<int OUT, class TransformOpT, bool CACHE = false>
 __global__ void __launch_bounds__(kHalfBlock, OUT == kFastCount ? 8 : 6) k_traverse_half(const FastLBVHData tree, const HalfArgs a,
                                                                   const TransformOpT transform)
     {
+    static_assert(!CACHE || OUT == kFastCount, "the pair exchange is a count's");
     __shared__ QuantFrame s_frame;
     __shared__ unsigned int s_records;
     __shared__ unsigned int s_class[kWorkClasses];
@@ -690,6 +769,13 @@ __global__ void __launch_bounds__(kHalfBlock, OUT == kFastCount ? 8 : 6) k_trave
     bool pending = false;
     unsigned int p_slot = 0, p_cap = 0, p_key = 0;
     unsigned long long p_first = 0;
+    // the exchange count's pending deposit: partner (mirror image << 27 | position) and its slot
+    // (no slot: 0xffffffff)
+    unsigned int x_jm = 0u, x_slot = 0xffffffffu;
+    const auto deposit = [&]() {
+        if (x_slot < kHalfCacheSlots)
+            a.in_cache[(size_t)(x_jm & kHalfKeyMask) * kHalfCacheSlots + x_slot] = (x_jm & ~kHalfKeyMask) | q;
+    };
     // one pair (q, j) that the query found through image `bit` (mirror: the partner's image)
     // the query's own entry k (fill): a final id after the row's appended entries, or a key from
     // the end of the row
@@ -706,9 +792,21 @@ __global__ void __launch_bounds__(kHalfBlock, OUT == kFastCount ? 8 : 6) k_trave
     const auto take = [&](unsigned int j, unsigned int bit, unsigned int mirror) {
         if (OUT == kFastCount)
             {
-            if (j != q) atomicAdd(a.nneigh + (a.rows_sorted ? j : tree.primitive[j]), 1u);
-            if (CACHE && own < kHalfCacheSlots)
-                a.cache_out[(size_t)q * kHalfCacheSlots + own] = (bit << kHalfKeyBits) | j;
+            if (CACHE)
+                {
+                if (own < kHalfCacheSlots) a.cache_out[(size_t)q * kHalfCacheSlots + own] = (bit << kHalfKeyBits) | j;
+                if (j != q)
+                    {
+                    // the previous partner's key goes to its slot now that the slot is known
+                    deposit();
+                    x_slot = atomicAdd(a.in_count + j, 1u);
+                    x_jm = (mirror << kHalfKeyBits) | j;
+                    }
+                }
+            else if (j != q)
+                {
+                atomicAdd(a.nneigh + (a.rows_sorted ? j : tree.primitive[j]), 1u);
+                }
             }
         else
             {
@@ -725,54 +823,6 @@ __global__ void __launch_bounds__(kHalfBlock, OUT == kFastCount ? 8 : 6) k_trave
             }
         ++own;
     };
-    if (CACHE && OUT != kFastCount)
-        {
-        // the count's pairs of this query, replayed in the order it found them
-        const unsigned int n_cached = a.own_counted[row];
-        if (n_cached <= kHalfCacheSlots)
-            {
-            // four pairs at a time: their four partner atomics are in flight together, and their
-            // entries are stored once the slots are back
-            const uint4* keys = reinterpret_cast<const uint4*>(a.cache_in + (size_t)q * kHalfCacheSlots);
-            for (unsigned int k0 = 0; k0 < n_cached; k0 += 4u)
-                {
-                const uint4 w = keys[k0 >> 2];
-                const unsigned int kk[4] = {w.x, w.y, w.z, w.w};
-                unsigned int slot[4];
-                unsigned int rj[4];
-#pragma unroll
-                for (unsigned int t = 0; t < 4u; ++t)
-                    {
-                    slot[t] = 0xffffffffu;
-                    rj[t] = 0u;
-                    if (k0 + t < n_cached)
-                        {
-                        const unsigned int j = kk[t] & kHalfKeyMask;
-                        own_entry(k0 + t, j, kk[t] >> kHalfKeyBits);
-                        if (j != q)
-                            {
-                            rj[t] = a.rows_sorted ? j : tree.primitive[j];
-                            slot[t] = atomicAdd(a.nneigh + rj[t], 1u);
-                            }
-                        }
-                    }
-#pragma unroll
-                for (unsigned int t = 0; t < 4u; ++t)
-                    {
-                    if (slot[t] != 0xffffffffu)
-                        {
-                        unsigned long long first = 0;
-                        unsigned int c = 0;
-                        row_layout<OUT>(a.offsets, a.caps, a.max_neigh, rj[t], first, c);
-                        const unsigned int bit = kk[t] >> kHalfKeyBits;
-                        if (slot[t] < c) a.list[first + slot[t]] = ((a.lattice ? 26u - bit : 0u) << kHalfKeyBits) | q;
-                        }
-                    }
-                }
-            own = n_cached;
-            flags = 0u;
-            }
-        }
     while (flags)
         {
         const int bit = __ffs(flags) - 1;
@@ -790,7 +840,7 @@ __global__ void __launch_bounds__(kHalfBlock, OUT == kFastCount ? 8 : 6) k_trave
             while (i < n_rec)
                 {
                 const uint4 n = __ldg(tree.nodes + i);
-                if (OUT == kFastCount && !CACHE) ++visits;   // (a replayed fill needs no work order)
+                if (OUT == kFastCount && !CACHE) ++visits;   // (an exchanged count's fill walks nothing)
                 if ((int)n.w < 0)
                     {
                     const float3 x = make_float3(__uint_as_float(n.x), __uint_as_float(n.y), __uint_as_float(n.z));
@@ -810,7 +860,12 @@ __global__ void __launch_bounds__(kHalfBlock, OUT == kFastCount ? 8 : 6) k_trave
         else
             walk(std::false_type());
         }
-    if (OUT == kFastCount)
+    if (OUT == kFastCount && CACHE)
+        {
+        deposit();
+        a.own[q] = own;
+        }
+    else if (OUT == kFastCount)
         {
         if (own) atomicAdd(a.nneigh + row, own);
         if (a.own) a.own[row] = own;
@@ -821,6 +876,247 @@ __global__ void __launch_bounds__(kHalfBlock, OUT == kFastCount ? 8 : 6) k_trave
         a.own[row] = own | (placed ? kOwnPlaced : 0u);
         }
     if (!CACHE && a.walk_out) a.walk_out[q] = (unsigned short)min(visits, 65535u);
+    }
+
+// Summary of a count, in four device words: [0] the largest row count, [1] rows whose own or
+// incoming keys did not fit the pair exchange's slots, [2..3] the pair total (64-bit, ordered
+// pairs, self included).  The words are zero on entry.
+//   EXCHANGE: the rows of a pair-exchange count: nneigh[row(s)] = own[s] + in_count[s].
+//   otherwise: the counts already in nneigh[0..N) (any count route).
+constexpr unsigned int kSummaryWords = 4;
+constexpr unsigned int kSummaryBlock = 256;
+
+template<bool EXCHANGE>
+__global__ void __launch_bounds__(kSummaryBlock) k_count_summary(unsigned int N, const unsigned int* __restrict__ own,
+                                                                 const unsigned int* __restrict__ in_count,
+                                                                 const unsigned int* __restrict__ primitive,
+                                                                 int rows_sorted, unsigned int* nneigh,
+                                                                 unsigned int* words, const unsigned int* status)
+    {
+    // a grid of a few blocks per SM strides over the rows; one atomic per word and block (the
+    // words are shared by the whole grid: an atomic per warp measured 0.7 ms at 16M rows)
+    __shared__ unsigned int s_max[kSummaryBlock / 32], s_past[kSummaryBlock / 32];
+    __shared__ unsigned long long s_sum[kSummaryBlock / 32];
+    const bool failed = status != nullptr && ld_status(status) != 0u;
+    unsigned int mx = 0, past = 0;
+    unsigned long long sum = 0;
+    for (unsigned int s = blockIdx.x * blockDim.x + threadIdx.x; s < N; s += gridDim.x * blockDim.x)
+        {
+        if (failed)
+            {
+            if (EXCHANGE) nneigh[s] = 0u;   // a failed build has no pairs
+            continue;
+            }
+        unsigned int total;
+        if (EXCHANGE)
+            {
+            const unsigned int o = own[s], i = in_count[s];
+            total = o + i;
+            nneigh[rows_sorted ? s : primitive[s]] = total;
+            past += (o > kHalfCacheSlots || i > kHalfCacheSlots) ? 1u : 0u;
+            }
+        else
+            {
+            total = nneigh[s];
+            }
+        mx = max(mx, total);
+        sum += total;
+        }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        {
+        mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        past += __shfl_xor_sync(0xffffffffu, past, o);
+        sum += __shfl_xor_sync(0xffffffffu, sum, o);
+        }
+    const unsigned int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31u) == 0u)
+        {
+        s_max[w] = mx;
+        s_past[w] = past;
+        s_sum[w] = sum;
+        }
+    __syncthreads();
+    if (threadIdx.x == 0)
+        {
+        for (unsigned int k = 1; k < kSummaryBlock / 32; ++k)
+            {
+            mx = max(mx, s_max[k]);
+            past += s_past[k];
+            sum += s_sum[k];
+            }
+        if (mx) atomicMax(words + 0, mx);
+        if (past) atomicAdd(words + 1, past);
+        if (sum) atomicAdd(reinterpret_cast<unsigned long long*>(words + 2), sum);
+        }
+    }
+
+// ---------------------------------------------------------------------------------------------
+// Assembly of list rows from a pair-exchange count (no walk, no atomics on rows).  One thread per
+// sorted position s: its own keys (ascending: found in pre-order from its own record) and its
+// incoming keys (in the order the partners' atomics arrived) go to registers, the incoming keys
+// are sorted with a sorting network, and the row is written in key order (image, then sorted
+// position) as transform(primitive) ids -- the order of the reference's rope traversal.  When
+// every key has the query's own image (`center`), each incoming key (a partner before s) sorts
+// before each own key (s and partners after it), so the row is the sorted incoming keys followed
+// by the own keys; otherwise the two sorted halves are merged (bitonic).  The first min(count,
+// capacity) entries are written, which is what the reference's NeighborListOp keeps of a row that
+// overflows.  Rows whose keys did not fit the slots are appended to subset[] for a whole walk.
+// ---------------------------------------------------------------------------------------------
+struct AssembleArgs
+    {
+    unsigned int N;
+    int rows_sorted;
+    unsigned int center;                 // image field of pairs through the query's own image
+    const unsigned int* own;             // own keys found, by sorted position
+    const unsigned int* in_count;        // incoming keys deposited, by sorted position
+    const unsigned int* own_keys;        // kHalfCacheSlots per sorted position
+    const unsigned int* in_keys;         // kHalfCacheSlots per sorted position
+    const unsigned int* primitive;
+    unsigned int* nneigh;
+    unsigned int* list;
+    unsigned int max_neigh;              // stride of a fixed-stride list
+    const unsigned long long* offsets;   // CSR rows (kFastCSR)
+    const unsigned int* caps;
+    unsigned int* subset;                // rows to re-walk (sorted positions)
+    unsigned int* subset_count;          // zero on entry
+    const unsigned int* status;
+    };
+
+// Compare-exchange of two registers into ascending (UP) or descending order.
+template<bool UP>
+__device__ __forceinline__ void cas(unsigned int& x, unsigned int& y)
+    {
+    const unsigned int lo = min(x, y), hi = max(x, y);
+    x = UP ? lo : hi;
+    y = UP ? hi : lo;
+    }
+
+// Bitonic sort of v[B .. B+M) into ascending order (M a power of two; indices resolve at compile
+// time, so the keys stay in registers).
+template<int M, int B, int K>
+__device__ __forceinline__ void bitonic_sort(unsigned int (&v)[K])
+    {
+#pragma unroll
+    for (int k = 2; k <= M; k <<= 1)
+#pragma unroll
+        for (int j = k >> 1; j > 0; j >>= 1)
+#pragma unroll
+            for (int i = 0; i < M; ++i)
+                {
+                const int l = i ^ j;
+                if (l > i)
+                    {
+                    if ((i & k) == 0)
+                        cas<true>(v[B + i], v[B + l]);
+                    else
+                        cas<false>(v[B + i], v[B + l]);
+                    }
+                }
+    }
+
+template<int OUT, class TransformOpT>
+__global__ void __launch_bounds__(256) k_half_assemble(const AssembleArgs a, const TransformOpT transform)
+    {
+    constexpr int S = (int)kHalfCacheSlots;
+    static_assert(S == 16, "16 own and 16 incoming slots");
+    const unsigned int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= a.N) return;
+    if (ld_status(a.status) != 0u)
+        {
+        a.nneigh[s] = 0u;   // a failed build has no pairs
+        return;
+        }
+    const unsigned int o = a.own[s], ni = a.in_count[s];
+    const unsigned int total = o + ni;
+    const unsigned int row = a.rows_sorted ? s : a.primitive[s];
+    a.nneigh[row] = total;
+    if (o > kHalfCacheSlots || ni > kHalfCacheSlots)
+        {
+        a.subset[atomicAdd(a.subset_count, 1u)] = s;
+        return;
+        }
+    unsigned long long first = 0;
+    unsigned int cap = 0;
+    row_layout<OUT>(a.offsets, a.caps, a.max_neigh, row, first, cap);
+    // v[0..16): own keys, v[16..32): incoming keys; unused slots hold 0xffffffff, above every key
+    unsigned int v[2 * S];
+    const uint4* ok = reinterpret_cast<const uint4*>(a.own_keys + (size_t)s * S);
+    const uint4* ik = reinterpret_cast<const uint4*>(a.in_keys + (size_t)s * S);
+#pragma unroll
+    for (int w = 0; w < S / 4; ++w)
+        {
+        const uint4 x = 4u * w < o ? ok[w] : make_uint4(~0u, ~0u, ~0u, ~0u);
+        const uint4 y = 4u * w < ni ? ik[w] : make_uint4(~0u, ~0u, ~0u, ~0u);
+        v[4 * w + 0] = x.x;
+        v[4 * w + 1] = x.y;
+        v[4 * w + 2] = x.z;
+        v[4 * w + 3] = x.w;
+        v[S + 4 * w + 0] = y.x;
+        v[S + 4 * w + 1] = y.y;
+        v[S + 4 * w + 2] = y.z;
+        v[S + 4 * w + 3] = y.w;
+        }
+    bool single = true;
+#pragma unroll
+    for (int k = 0; k < S; ++k)
+        {
+        if ((unsigned int)k >= o) v[k] = ~0u;
+        else single = single && (v[k] >> kHalfKeyBits) == a.center;
+        if ((unsigned int)k >= ni) v[S + k] = ~0u;
+        else single = single && (v[S + k] >> kHalfKeyBits) == a.center;
+        }
+    if (ni > 1u)
+        {
+        if (ni <= 4u)
+            bitonic_sort<4, S>(v);
+        else if (ni <= 8u)
+            bitonic_sort<8, S>(v);
+        else
+            bitonic_sort<16, S>(v);
+        }
+    unsigned int* out = a.list + first;
+    // ids are gathered before any entry is stored, so that the gathers are in flight together
+    // (a store to the list could otherwise alias the next gather)
+    if (single)
+        {
+#pragma unroll
+        for (int k = 0; k < S; ++k)
+            {
+            if ((unsigned int)k < ni) v[S + k] = transform(__ldg(a.primitive + (v[S + k] & kHalfKeyMask)));
+            if ((unsigned int)k < o) v[k] = transform(__ldg(a.primitive + (v[k] & kHalfKeyMask)));
+            }
+#pragma unroll
+        for (int k = 0; k < S; ++k)
+            if ((unsigned int)k < ni && (unsigned int)k < cap) out[k] = v[S + k];
+#pragma unroll
+        for (int k = 0; k < S; ++k)
+            if ((unsigned int)k < o && ni + k < cap) out[ni + k] = v[k];
+        return;
+        }
+    // own ascending then incoming descending is a bitonic sequence: merge it (reversing the
+    // incoming half is a renaming of registers)
+#pragma unroll
+    for (int k = 0; k < S / 2; ++k)
+        {
+        const unsigned int t = v[S + k];
+        v[S + k] = v[2 * S - 1 - k];
+        v[2 * S - 1 - k] = t;
+        }
+#pragma unroll
+    for (int j = S; j > 0; j >>= 1)
+#pragma unroll
+        for (int i = 0; i < 2 * S; ++i)
+            {
+            const int l = i ^ j;
+            if (l > i) cas<true>(v[i], v[l]);
+            }
+#pragma unroll
+    for (int k = 0; k < 2 * S; ++k)
+        if ((unsigned int)k < total) v[k] = transform(__ldg(a.primitive + (v[k] & kHalfKeyMask)));
+#pragma unroll
+    for (int k = 0; k < 2 * S; ++k)
+        if ((unsigned int)k < total && (unsigned int)k < cap) out[k] = v[k];
     }
 
 struct HalfOrderArgs

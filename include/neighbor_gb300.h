@@ -130,10 +130,26 @@ int nbr_traverser_set_symmetric(nbr_traverser t, int enabled);
  * or in sorted order (0).  Results are the same either way. */
 int nbr_traverser_set_work_order(nbr_traverser t, int enabled);
 
-/* Addition: a symmetric count keeps the first 16 pairs each query found itself (64 bytes per
- * point) and a symmetric fill over the same tree, cutoff, images and rows replays them instead of
- * walking again (1, default), or every fill walks (0).  Results are the same either way. */
+/* Addition: pair exchange -- a symmetric count keeps, per point, the first 16 pairs it found
+ * itself and the first 16 pairs other points found with it (128 bytes per point), and a fill over
+ * the same tree, cutoff, images and rows assembles the rows from them without walking (1,
+ * default; rows with more pairs walk), or every fill walks (0).  Results are the same either
+ * way. */
 int nbr_traverser_set_pair_cache(nbr_traverser t, int enabled);
+
+/* Addition: summary of the last counting self traversal (nbr_traverse_self with list == NULL) on
+ * this traverser: the largest count, the total of the counts (ordered pairs, self included) and
+ * the rows whose pairs did not fit the pair exchange.  Synchronises `stream`: it is the host read
+ * of the largest count between the count and the list pass (the reference's benchmark reads its
+ * counts on the host after the traversal, benchmark/lbvh_benchmark.cc:233-237); any pointer may
+ * be NULL. */
+int nbr_traverser_count_summary(nbr_traverser t, unsigned int* max_count, unsigned long long* total,
+                                unsigned int* past_exchange, void* stream);
+/* Addition: device address of the same four 32-bit words ([0] largest count, [1] rows past the
+ * exchange, [2..3] the 64-bit total, low word first), written in stream order by each counting
+ * self traversal, for callers that copy them without a synchronisation.  NULL before the first
+ * count. */
+int nbr_traverser_count_summary_device(nbr_traverser t, const unsigned int** words);
 
 /* Addition, routing by size: traversals of at most max_queries queries (self traversals included)
  * walk one warp per query, larger ones one thread per query (default 32,768; 0 = never).  Self

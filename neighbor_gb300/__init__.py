@@ -106,6 +106,9 @@ def _declare(L):
     sig("nbr_traverser_set_symmetric_min_points", [_P, ctypes.c_uint])
     sig("nbr_traverser_set_walk_lanes", [_P, ctypes.c_uint])
     sig("nbr_traverser_get_data", [_P, _PP, _PP, _PP, _PP])
+    sig("nbr_traverser_count_summary", [_P, ctypes.POINTER(_U), ctypes.POINTER(ctypes.c_ulonglong),
+                                        ctypes.POINTER(_U), _P])
+    sig("nbr_traverser_count_summary_device", [_P, _PP])
     sig("nbr_traverse", [_P, _P, _I, _P, _U, _P, _P, _F, _P, _U, _P, _P, _P, _U, _U, _P])
     sig("nbr_traverse_self", [_P, _P, _F, _P, _F, _P, _U, _P, _P, _P, _U, _I, _U, _P])
     sig("nbr_exact_pad", [_F, _F], _F)
@@ -166,7 +169,8 @@ EXPORTED = ["nbr_last_error", "nbr_version", "nbr_lbvh_create", "nbr_lbvh_destro
             "nbr_debug_inject_alloc_failures",
             "nbr_traverser_set_work_order", "nbr_traverser_set_warp_walk_max",
             "nbr_traverser_set_symmetric_min_points", "nbr_traverser_set_walk_lanes",
-            "nbr_traverser_set_pair_cache",
+            "nbr_traverser_set_pair_cache", "nbr_traverser_count_summary",
+            "nbr_traverser_count_summary_device",
             "nbr_traverser_get_data", "nbr_traverse", "nbr_traverse_self", "nbr_exact_pad",
             "nbr_debug_wait_timeout", "nbr_morton_sort_noalloc", "nbr_traverse_self_csr",
             "nbr_traverse_self_subset_csr",
@@ -475,8 +479,25 @@ class LBVHTraverser:
         _check(self._L.nbr_traverser_set_work_order(self._h, 1 if enabled else 0))
 
     def set_pair_cache(self, enabled: bool):
-        """A symmetric count keeps each query's first 16 pairs for the next fill (True, default)."""
+        """Pair exchange: a symmetric count keeps each point's pairs so that the next fill
+        assembles the rows without walking (True, default)."""
         _check(self._L.nbr_traverser_set_pair_cache(self._h, 1 if enabled else 0))
+
+    def count_summary(self, stream=None):
+        """(largest count, total of the counts, rows past the pair exchange) of the last counting
+        self traversal; synchronises the stream."""
+        mx, past = ctypes.c_uint(), ctypes.c_uint()
+        tot = ctypes.c_ulonglong()
+        _check(self._L.nbr_traverser_count_summary(self._h, ctypes.byref(mx), ctypes.byref(tot),
+                                                   ctypes.byref(past), _stream_ptr(stream)))
+        return mx.value, tot.value, past.value
+
+    def count_summary_device(self):
+        """Device address of the summary words ([0] max, [1] rows past the exchange, [2..3]
+        64-bit total), or 0 before the first count."""
+        p = ctypes.c_void_p()
+        _check(self._L.nbr_traverser_count_summary_device(self._h, ctypes.byref(p)))
+        return p.value or 0
 
     def set_warp_walk_max(self, max_queries: int):
         """Traversals of at most max_queries queries walk one warp per query (0 = never)."""

@@ -303,6 +303,27 @@ int nbr_traverser_set_pair_cache(nbr_traverser t, int enabled)
     return NBR_OK;
     }
 
+int nbr_traverser_count_summary(nbr_traverser t, unsigned int* max_count, unsigned long long* total,
+                                unsigned int* past_exchange, void* stream)
+    {
+    if (!t) return fail(NBR_ERR_INVALID, "null handle");
+    return guarded([&] {
+        unsigned int mx = 0, past = 0;
+        unsigned long long tot = 0;
+        t->trav.readCountSummary(as_stream(stream), mx, tot, past);
+        if (max_count) *max_count = mx;
+        if (total) *total = tot;
+        if (past_exchange) *past_exchange = past;
+    });
+    }
+
+int nbr_traverser_count_summary_device(nbr_traverser t, const unsigned int** words)
+    {
+    if (!t || !words) return fail(NBR_ERR_INVALID, "null argument");
+    *words = t->trav.getCountSummary();
+    return NBR_OK;
+    }
+
 int nbr_traverser_set_warp_walk_max(nbr_traverser t, unsigned int max_queries)
     {
     if (!t) return fail(NBR_ERR_INVALID, "null handle");

@@ -18,7 +18,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "liboracle.so")
-SOURCES = [os.path.join(HERE, "oracle.cpp")]
+SOURCES = [os.path.join(HERE, "oracle.cpp"), os.path.join(HERE, "frame_list.cpp")]
 
 SENTINEL = 0x7FFFFFFF
 INSERT_POINT, INSERT_SPHERE = 0, 1
@@ -34,10 +34,20 @@ def build(force: bool = False) -> str:
     newest = max(os.path.getmtime(s) for s in SOURCES + [os.path.join(HERE, "oracle.h")])
     if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= newest:
         return LIB_PATH
-    tmp = LIB_PATH + f".tmp{os.getpid()}"
-    cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-frounding-math",
-           "-ffp-contract=off", "-o", tmp] + SOURCES
-    subprocess.run(cmd, check=True)
+    tag = f".tmp{os.getpid()}"
+    tmp = LIB_PATH + tag
+    # oracle.cpp switches the rounding mode (-frounding-math); frame_list.cpp, the timed CPU
+    # baseline, rounds to nearest only and is optimised fully.  Neither fuses a*b+c.
+    objs = [os.path.join(BUILD_DIR, "oracle.o" + tag), os.path.join(BUILD_DIR, "frame_list.o" + tag)]
+    procs = [subprocess.Popen(["g++", "-O2", "-std=c++17", "-fPIC", "-fopenmp", "-frounding-math",
+                               "-ffp-contract=off", "-c", "-o", objs[0], SOURCES[0]]),
+             subprocess.Popen(["g++", "-O3", "-std=c++17", "-fPIC", "-fopenmp", "-ffp-contract=off",
+                               "-fno-trapping-math", "-c", "-o", objs[1], SOURCES[1]])]
+    if any(p.wait() != 0 for p in procs):
+        raise subprocess.CalledProcessError(1, "g++ (oracle)")
+    subprocess.run(["g++", "-shared", "-fopenmp", "-o", tmp] + objs, check=True)
+    for o in objs:
+        os.remove(o)
     os.replace(tmp, LIB_PATH)
     return LIB_PATH
 
@@ -91,6 +101,10 @@ def _declare(L):
     L.orc_celllist.restype = ctypes.c_int
     L.orc_celllist_csr.argtypes = [_P, _P, _f, _u32, _P, _u32, _P, _P, _P, _P, ctypes.c_int]
     L.orc_celllist_csr.restype = ctypes.c_int
+    L.orc_frame_list.argtypes = [_P, _u32, _P, _P, _f, ctypes.c_int, _P, _P, _P, ctypes.c_uint64, _P, _P, _P]
+    L.orc_frame_list.restype = ctypes.c_int
+    L.orc_uniform_points.argtypes = [_P, _u32, _P, _P, ctypes.c_uint64]
+    L.orc_gaussian_move.argtypes = [_P, _P, _u32, _P, _P, _f, ctypes.c_uint64]
     L.orc_pair_distance_minus_rc_f64.argtypes = [_P, _P, _f, _P]
     L.orc_pair_distance_minus_rc_f64.restype = ctypes.c_double
     L.orc_fast_nodes.argtypes = [_u32, _u32, _P, _P, _P, _P, _P, _P, _P, _P]
@@ -298,3 +312,50 @@ def cap_forward_backward(params, features, targets, batch, offset, stride, mode=
     lib().orc_cap_forward_backward(_ptr(P), _ptr(F), _ptr(T), len(T), batch, offset, stride, mode,
                                    _ptr(grad), _ptr(loss), _ptr(y))
     return grad, float(loss[0]), y
+
+
+class FrameLister:
+    """Whole-frame self neighbor list on the host cores (frame_list.cpp): the benchmark's CPU
+    baseline.  Keeps its output buffers between frames, so that a timed call allocates nothing
+    of the list's size."""
+
+    def __init__(self, n, nthreads=0, slots_per_point=16):
+        self.n = int(n)
+        self.nthreads = int(nthreads)
+        self.counts = np.empty(self.n, np.uint32)
+        self.offsets = np.empty(self.n + 1, np.uint64)
+        self.order = np.empty(self.n, np.uint32)
+        self.list = np.empty(max(1, self.n * slots_per_point), np.uint32)
+
+    def run(self, points, L, rc, lo=(0.0, 0.0, 0.0)):
+        """List the frame; returns (total pairs, threads used, seconds of grid/count/scan/fill).
+        Rows are in grid order (self.order[k] is the point of row k)."""
+        p = _f32(points, (-1, 3))
+        assert len(p) == self.n
+        total = ctypes.c_uint64()
+        secs = np.zeros(4, np.float64)
+        used = lib().orc_frame_list(_ptr(p), self.n, _ptr(_f32(lo)), _ptr(_f32(L)), float(rc), self.nthreads,
+                                    _ptr(self.counts), _ptr(self.offsets), _ptr(self.list), len(self.list),
+                                    _ptr(self.order), ctypes.byref(total), _ptr(secs))
+        if used < 0:   # more pairs than the buffer holds: grow it and list again
+            self.list = np.empty(int(total.value * 1.25) + 1, np.uint32)
+            used = lib().orc_frame_list(_ptr(p), self.n, _ptr(_f32(lo)), _ptr(_f32(L)), float(rc), self.nthreads,
+                                        _ptr(self.counts), _ptr(self.offsets), _ptr(self.list), len(self.list),
+                                        _ptr(self.order), ctypes.byref(total), _ptr(secs))
+        return int(total.value), int(used), secs
+
+
+def uniform_points(n, L, seed, lo=(0.0, 0.0, 0.0)):
+    """n points uniform in [lo, lo+L) (host, counter-based generator)."""
+    out = np.empty((int(n), 3), np.float32)
+    lib().orc_uniform_points(_ptr(out), int(n), _ptr(_f32(lo)), _ptr(_f32(L)), int(seed))
+    return out
+
+
+def gaussian_move(points, L, sigma, seed, lo=(0.0, 0.0, 0.0), out=None):
+    """Every point moved by an i.i.d. Gaussian of `sigma` per axis and wrapped into [lo, lo+L)."""
+    p = _f32(points, (-1, 3))
+    if out is None:
+        out = np.empty_like(p)
+    lib().orc_gaussian_move(_ptr(p), _ptr(out), len(p), _ptr(_f32(lo)), _ptr(_f32(L)), float(sigma), int(seed))
+    return out

@@ -118,6 +118,21 @@ int orc_celllist_csr(const float* qpos, const float* qr, float rc, uint32_t Q,
                      const float box_L[3], const uint64_t* offsets, uint32_t* nbrs,
                      int nthreads);
 
+/* ---- Whole-frame host neighbor list (frame_list.cpp; the benchmark's CPU baseline) ----
+ * Self list of all N points in the periodic box [lo, lo+L): grid build, count pass, exclusive
+ * scan, fill pass, every stage on the host threads.  Rows in grid order: counts[N],
+ * offsets[N+1] (uint64), list[total] original indices (list_cap entries available),
+ * order[N] (optional) the point of each row.  seconds[4] (optional): grid, count, scan, fill.
+ * Returns the number of threads used, or -1 when total > list_cap (counts and offsets valid). */
+int orc_frame_list(const float* pts, uint32_t N, const float lo[3], const float L[3], float rc,
+                   int nthreads, uint32_t* counts, uint64_t* offsets, uint32_t* list,
+                   uint64_t list_cap, uint32_t* order, uint64_t* total, double* seconds);
+/* Host trajectory frames: uniform points in [lo, lo+L) and i.i.d. Gaussian moves (sigma) with
+ * wrap, from a counter-based generator (independent of the thread count). */
+void orc_uniform_points(float* out, uint32_t N, const float lo[3], const float L[3], uint64_t seed);
+void orc_gaussian_move(const float* in, float* out, uint32_t N, const float lo[3], const float L[3],
+                       float sigma, uint64_t seed);
+
 /* FP64 check of a pair: returns the signed difference |r| - rc in double precision with a
  * minimum image computed in double. */
 double orc_pair_distance_minus_rc_f64(const float* pi, const float* pj, float rc,

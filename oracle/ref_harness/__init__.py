@@ -72,10 +72,11 @@ def run_bench(n, steps=5, warmup=2, rc=1.3, timeout=600):
     return json.loads(r.stdout.strip().splitlines()[-1])
 
 
-def run_dump(points, lo, hi, rc, box, timeout=300):
+def run_dump(points, lo, hi, rc, box, timeout=300, exact_only=False):
     """The reference's tree arrays, compressed nodes, counts (stock and exact query, 27 periodic
     images of `box`, queries = the points in input order) and the exact query's neighbor list
-    (stride = the largest count) for the given points."""
+    (stride = the largest count) for the given points.  exact_only: skip the stock query's
+    counts and lists."""
     P = np.ascontiguousarray(points, np.float32).reshape(-1, 3)
     n = len(P)
     with tempfile.TemporaryDirectory() as d:
@@ -84,6 +85,8 @@ def run_dump(points, lo, hi, rc, box, timeout=300):
         prefix = os.path.join(d, "ref")
         args = [DRIVER, "dump", src, str(n), *[repr(float(x)) for x in lo], *[repr(float(x)) for x in hi],
                 repr(float(rc)), *[repr(float(x)) for x in box], prefix]
+        if exact_only:
+            args.append("exact_only")
         r = subprocess.run(args, capture_output=True, text=True, timeout=timeout)
         if r.returncode != 0:
             raise RuntimeError(f"reference driver failed ({r.returncode}): {r.stderr.strip()[-400:]}")

@@ -370,7 +370,7 @@ int run_bench(const Kernels& K, unsigned int n, int steps, int warmup, float rc)
     }
 
 int run_dump(const Kernels& K, const char* in_path, unsigned int n, float3 slo, float3 shi, float rc, float3 box,
-             const char* out_prefix)
+             const char* out_prefix, bool exact_only)
     {
     std::vector<float3> hp(n);
     FILE* f = fopen(in_path, "rb");
@@ -401,6 +401,7 @@ int run_dump(const Kernels& K, const char* in_path, unsigned int n, float3 slo, 
     for (unsigned int i = 0; i < n; ++i) hs[i] = make_float4(hp[i].x, hp[i].y, hp[i].z, rc);
     check(cudaMemcpy(sph, hs.data(), (size_t)n * 16, cudaMemcpyHostToDevice), "copy");
     ImageListOp im{img, 27};
+    if (!exact_only)
         {
         SphereQueryOp q{sph, n};
         CountNeighborsOp out{c_stock};
@@ -460,11 +461,11 @@ int run_dump(const Kernels& K, const char* in_path, unsigned int n, float3 slo, 
     dump("lo", T.lo, nodes * 12);
     dump("hi", T.hi, nodes * 12);
     dump("data", T.data, nodes * 16);
-    dump("count_stock", c_stock, (size_t)n * 4);
+    if (!exact_only) dump("count_stock", c_stock, (size_t)n * 4);
     dump("count_exact", c_exact, (size_t)n * 4);
     dump("count_list", c_list, (size_t)n * 4);
     dump("list_exact", list, (size_t)n * list_stride * 4);
-    dump("list_stock", list_s, (size_t)n * stock_stride * 4);
+    if (!exact_only) dump("list_stock", list_s, (size_t)n * stock_stride * 4);
     printf("{\"dumped\": %u, \"list_stride\": %u}\n", n, list_stride);
     return 0;
     }
@@ -485,7 +486,8 @@ int main(int argc, char** argv)
                         make_float3((float)atof(argv[4]), (float)atof(argv[5]), (float)atof(argv[6])),
                         make_float3((float)atof(argv[7]), (float)atof(argv[8]), (float)atof(argv[9])),
                         (float)atof(argv[10]),
-                        make_float3((float)atof(argv[11]), (float)atof(argv[12]), (float)atof(argv[13])), argv[14]);
+                        make_float3((float)atof(argv[11]), (float)atof(argv[12]), (float)atof(argv[13])), argv[14],
+                        argc >= 16 && std::string(argv[15]) == "exact_only");
     fprintf(stderr, "bad arguments\n");
     return 1;
     }

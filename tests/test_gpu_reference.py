@@ -93,16 +93,19 @@ def test_library_matches_reference_kernels(name, P, L, rc):
                            images="periodic", max_neigh=mx)
     got = lst.cpu().numpy().view(np.uint32)
     assert np.array_equal(np.where(valid, got, 0), np.where(valid, ref_list, 0))
-    # self traversals: whole-tree walk with one thread per query, symmetric walk, one warp per query
-    for route in ("thread", "symmetric", "warp"):
+    # self traversals: whole-tree walk with one thread per query, symmetric walk (a fill on its
+    # own), symmetric count + fill assembled from its pair exchange, one warp per query
+    for route in ("thread", "symmetric", "exchange", "warp"):
         st = nb.LBVHTraverser()
         if route == "thread":
             st.set_symmetric(False)
             st.set_warp_walk_max(0)
-        elif route == "symmetric":
+        elif route in ("symmetric", "exchange"):
             st.force_symmetric()
         else:
             st.set_warp_walk_max(len(P))
+        if route == "exchange":
+            st.traverse_self(lbvh, rc, box, pad, images="periodic", rows_sorted=False)
         nn, lst = st.traverse_self(lbvh, rc, box, pad, images="periodic", max_neigh=mx, rows_sorted=False)
         assert np.array_equal(nn.cpu().numpy().view(np.uint32), ref["count_exact"]), route
         got = lst.cpu().numpy().view(np.uint32)

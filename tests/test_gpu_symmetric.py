@@ -5,9 +5,12 @@ writes it to both rows; the rows are then ordered by (image, sorted position), t
 whole-tree walk (and of the reference's rope traversal).  So the full outputs -- counts and every
 list row -- must be bit-identical to the whole-tree walk's, and the sets must equal the oracle's
 cell list.  With the size routing off (force_symmetric), counts take the symmetric kernel at every
-size; fills with rows longer than 32 entries take the whole-tree walk (checked on clustered
-inputs); rows that overflow max_neigh keep their full count and a subset of their true neighbors.
-The whole-tree side keeps the default routing (lane groups per query up to 32,768 points).
+size.  A fill after a count on the same traverser assembles the rows from the count's pair
+exchange (rows whose pairs did not fit it are walked again, one warp per row for up to 32,768
+such rows, one thread per row above); a fill without such a count walks symmetrically while rows
+fit 32 entries and takes the whole-tree walk beyond.  Rows that overflow max_neigh keep their full
+count and a subset of their true neighbors.  The whole-tree side keeps the default routing (lane
+groups per query up to 32,768 points).
 """
 import numpy as np
 import pytest
@@ -253,10 +256,10 @@ def test_noncubic_offset_box(N):
 
 
 @pytest.mark.parametrize("rows_sorted", [True, False])
-def test_pair_cache_replays_the_count(rows_sorted):
-    # tight clusters of 20 points inside the cutoff: rows of about 20 entries (the symmetric fill),
-    # and the first queries of a cluster find more than the cache's 16 pairs themselves (they walk
-    # again); the fill with the cache, the fill without it and the whole-tree walk must agree
+def test_pair_exchange_assembles_the_count(rows_sorted):
+    # tight clusters of 20 points inside the cutoff: rows of about 20 entries; the first points of
+    # a cluster find more than 16 pairs themselves and the last ones receive more than 16 (both
+    # are walked again); the assembled fill, the walking fill and the whole-tree walk must agree
     rng = np.random.default_rng(61)
     N, L, rc = 24000, 33.0, 1.0
     # cluster centres on a grid of spacing 3 (clusters do not meet), jittered
@@ -285,7 +288,7 @@ def test_pair_cache_replays_the_count(rows_sorted):
     for c, lst in out[1:]:
         assert np.array_equal(c, out[0][0])
         assert np.array_equal(lst, out[0][1])
-    # a fill on other rows than the count's does not replay its pairs
+    # a fill on other rows than the count's does not assemble from its pairs
     trav = nb.LBVHTraverser()
     trav.force_symmetric()
     trav.traverse_self(lbvh, rc, box, pad, images="periodic", rows_sorted=not rows_sorted)
@@ -297,7 +300,7 @@ def test_pair_cache_replays_the_count(rows_sorted):
 
 def test_fill_after_a_count_on_another_tree_walks():
     # the count ran on tree A, which is then destroyed; tree B (same size, other points, possibly
-    # at A's address) is filled by the same traverser: nothing of A's count may be replayed
+    # at A's address) is filled by the same traverser: nothing of A's count may be reused
     N = 20000
     PA, L = _uniform(N, 71)
     PB, _ = _uniform(N, 72)
@@ -325,7 +328,7 @@ def test_fill_after_a_count_on_another_tree_walks():
 
 
 def test_pair_cache_csr_fill_equals_whole_walk():
-    # count, then a CSR fill (rows sized by the counts) that replays the count's pairs
+    # count, then a CSR fill (rows sized by the counts) assembled from the count's pairs
     N = 60000
     P, L = _uniform(N, 81)
     box = [L, L, L]
@@ -335,9 +338,9 @@ def test_pair_cache_csr_fill_equals_whole_walk():
     pad = nb.exact_pad(rc, 2 * L)
     op = nb.OnePassList()
     out = []
-    for mode in ("replay", "whole"):
+    for mode in ("assembled", "whole"):
         trav = nb.LBVHTraverser()
-        if mode == "replay":
+        if mode == "assembled":
             trav.force_symmetric()
         else:
             trav.set_symmetric(False)
@@ -352,3 +355,72 @@ def test_pair_cache_csr_fill_equals_whole_walk():
         assert torch.equal(nn, cnt)
         out.append(lst.cpu().numpy())
     assert np.array_equal(out[0], out[1])
+
+
+@pytest.mark.parametrize("per,N", [(30, 24000), (40, 80000)])
+def test_rows_past_the_exchange_are_walked(per, N):
+    # tight clusters of `per` points inside the cutoff: most rows hold more pairs than the
+    # exchange keeps.  24,000 such rows are walked one warp per row, 80,000 one thread per row;
+    # rows in both cases equal the whole-tree walk, for a fixed-stride list and a CSR list.
+    rng = np.random.default_rng(per)
+    n_cl = N // per
+    side = int(np.ceil(n_cl ** (1.0 / 3.0)))
+    L = side * 3.0
+    g = np.stack(np.meshgrid(np.arange(side), np.arange(side), np.arange(side), indexing="ij"), -1).reshape(-1, 3)
+    centers = g[:n_cl] * 3.0 + 1.5
+    P = np.mod(np.repeat(centers, per, axis=0) + rng.normal(size=(N, 3)) * 0.1, L).astype(np.float32)
+    rc = 1.0
+    box = [L, L, L]
+    lbvh = nb.LBVH()
+    lbvh.build(_t(P), [0, 0, 0], box)
+    pad = nb.exact_pad(rc, 2 * L)
+    trav = nb.LBVHTraverser()
+    trav.force_symmetric()
+    cnt = trav.traverse_self(lbvh, rc, box, pad, images="periodic", rows_sorted=True)
+    mx, total, past = trav.count_summary()
+    c = cnt.cpu().numpy().view(np.uint32)
+    assert mx == int(c.max()) and total == int(c.astype(np.int64).sum())
+    assert past > (20000 if N == 24000 else 60000)
+    whole = nb.LBVHTraverser()
+    whole.set_symmetric(False)
+    whole.set_warp_walk_max(0)
+    want = _rows(*whole.traverse_self(lbvh, rc, box, pad, images="periodic", rows_sorted=True, max_neigh=mx))
+    got = _rows(*trav.traverse_self(lbvh, rc, box, pad, images="periodic", rows_sorted=True, max_neigh=mx))
+    assert np.array_equal(got[0], want[0])
+    assert np.array_equal(got[1], want[1])
+    op = nb.OnePassList()
+    offsets, tot = op.scan(cnt)
+    lst = torch.full((tot + 1,), -1, dtype=torch.int32, device="cuda")
+    nn = trav.traverse_self_csr(lbvh, rc, box, pad, offsets, cnt, lst, max_capacity=mx, images="periodic",
+                                rows_sorted=True)
+    assert torch.equal(nn, cnt)
+    flat = lst[:tot].cpu().numpy().view(np.uint32)
+    off = offsets.cpu().numpy()
+    for r in range(0, N, 97):
+        assert np.array_equal(flat[off[r]:off[r] + c[r]], want[1][r, : c[r]])
+
+
+@pytest.mark.parametrize("symmetric", [True, False])
+def test_count_summary(symmetric):
+    # the largest count and the total on the device equal the counts' own, on either route
+    N = 50000
+    P, L = _uniform(N, 91)
+    box = [L, L, L]
+    rc = 1.3
+    lbvh = nb.LBVH()
+    lbvh.build(_t(P), [0, 0, 0], box)
+    pad = nb.exact_pad(rc, 2 * L)
+    trav = nb.LBVHTraverser()
+    if symmetric:
+        trav.force_symmetric()
+    else:
+        trav.set_symmetric(False)
+        trav.set_warp_walk_max(0)
+    for rows_sorted in (True, False):
+        cnt = trav.traverse_self(lbvh, rc, box, pad, images="periodic", rows_sorted=rows_sorted)
+        mx, total, past = trav.count_summary()
+        c = cnt.cpu().numpy().view(np.uint32)
+        assert mx == int(c.max())
+        assert total == int(c.astype(np.int64).sum())
+        assert 0 <= past < N // 100
+        assert trav.count_summary_device() != 0

@@ -64,15 +64,14 @@ def test_reference_arm_runs_on_rank_zero_only(monkeypatch, capsys):
 
 
 def test_reference_arm_json_line(monkeypatch, capsys):
-    # the reference arm runs the oracle's cell list on the host cores: its JSON line carries the
-    # contract's keys (one rank)
+    # the reference arm lists whole trajectory frames on the host cores: its JSON line carries
+    # the contract's keys (one rank), and the GPU arm's metric and config
     import json
     sys.path.insert(0, ROOT)
     import bench
     monkeypatch.delenv("WORLD_SIZE", raising=False)
     monkeypatch.delenv("RANK", raising=False)
-    args = bench.parse(["--impl", "reference", "--steps", "2", "--warmup", "1", "--n", "32768",
-                        "--cpu-seconds", "0.2"])
+    args = bench.parse(["--impl", "reference", "--steps", "2", "--warmup", "1", "--n", "32768"])
     assert bench.run_reference(args) == 0
     line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
     assert line["impl"] == "reference"
@@ -81,3 +80,9 @@ def test_reference_arm_json_line(monkeypatch, capsys):
     assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
     assert line["e2e"] == {"value": line["value"], "unit": "pairs/s", "h2d_bytes_per_step": 0,
                            "d2h_bytes_per_step": 0}
+    L = (32768 / 0.85) ** (1.0 / 3.0)
+    assert line["metric"] == bench.METRIC
+    assert line["config"] == bench.workload_config(32768, L)
+    assert line["ms_per_step"] > 0
+    # every point of every frame is listed: about 8.8 ordered pairs per point at this density
+    assert 8.0 * 32768 < line["pairs_per_step"] < 9.7 * 32768

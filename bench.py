@@ -57,6 +57,8 @@ def parse(argv=None):
     ap.add_argument("--radix-bits", type=int, default=8)
     ap.add_argument("--block", type=int, default=256)
     ap.add_argument("--mode", type=int, default=0, help="0 = thread per query, 1 = warp packet")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="keep --leaf/--radix-bits/--climb instead of the autotuner's choice")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-ref-cuda", action="store_true")
@@ -384,8 +386,8 @@ def clustered_c3(nb, args, stream, n=4_000_000, rc=1.0, steps=5, warmup=2):
         lbvh.build(p, [0, 0, 0], box, block_size=args.block)
         trav.traverse_self(lbvh, rc, box, pad, images="periodic", nneigh=counts, rows_sorted=True,
                            block_size=args.block)
-        mx = int(counts.max().item())
-        offsets, total = op_plain.scan(counts)
+        mx, total, _ = trav.count_summary(stream)   # the host read of the two-pass pattern
+        offsets, _ = op_plain.scan(counts, read_total=False)
         if store.get("cap", 0) < total:
             store["list"] = torch.empty(total + 1, dtype=torch.int32, device="cuda")
             store["cap"] = total
@@ -404,6 +406,9 @@ def clustered_c3(nb, args, stream, n=4_000_000, rc=1.0, steps=5, warmup=2):
     cnt = counts.clone()
     exact = bool(torch.equal(op.result(n)["nneigh"].view(torch.int32), cnt))
     pairs = float(sum(totals)) / len(totals)
+    ref = None
+    if not args.no_ref_cuda:
+        ref = reference_frames([f.cpu().numpy() for f in frames], rc, L, steps, warmup)
     return {"workload": f"clustered N={n} (70% in 2000 blobs, sigma log-U[0.5,3]) density 0.85 "
                         f"L={L:.2f} rc={rc}, 27 images",
             "plain_ms_per_step": ms_plain, "learned_ms_per_step": ms_learned,
@@ -416,7 +421,25 @@ def clustered_c3(nb, args, stream, n=4_000_000, rc=1.0, steps=5, warmup=2):
             "margins": [round(v, 3) for v in model.margins], "train_s": round(train_s, 2),
             "train_loss": loss, "plain": "count + exclusive scan + exact CSR fill",
             "learned": "capacity network (overlapping the build after its sort) + one CSR fill + exact "
-                       "re-run of overflowed rows"}
+                       "re-run of overflowed rows",
+            "reference_cuda": ref,
+            "plain_vs_reference_cuda": (ref["step_ms"] / ms_plain) if ref and "step_ms" in ref else None}
+
+
+def reference_frames(frames, rc, L, steps, warmup):
+    """The reference's own kernels on the given frames (the plain two-pass step, queries in sorted
+    order, stride list), every block size; None-safe summary."""
+    try:
+        from oracle import ref_harness
+        if not (ref_harness.build_if_available() and ref_harness.available()):
+            return {"unavailable": "reference kernels not built here"}
+        r = ref_harness.run_frames(frames, rc, L, steps, warmup)
+    except Exception as e:  # measurement aid only: never fails the bench
+        return {"unavailable": f"{type(e).__name__}: {e}"[:200]}
+    best, sweep = best_block(r)
+    return {"step_ms": best["step_ms"], "block": best["block"], "pairs_per_step": r["pairs_per_step"],
+            "stages_ms": {k: best[k] for k in ("build_ms", "setup_ms", "count_ms", "fill_ms")},
+            "sweep_ms": sweep, "step": "build, setup, count, max read, fill (stride list) on the same frames"}
 
 
 def batched_ensemble(nb, args, stream, S=4096, rc=1.3, steps=5, max_neigh=48, seed=77):
@@ -507,14 +530,14 @@ def polydisperse_step(nb, trees, trav, species, L, skin=0.4, diam=(1.0, 10.0), l
             pad = nb.exact_pad(R, 2 * L)
             if i == j:
                 cnt = trav.traverse_self(trees[j], R, box, pad, images="periodic", rows_sorted=False)
-                mx = int(cnt.max().item())
+                mx = trav.count_summary()[0]
                 cnt, lst = trav.traverse_self(trees[j], R, box, pad, images="periodic", rows_sorted=False,
                                               max_neigh=max(mx, 1), nneigh=cnt)
             else:
                 sph = torch.cat([qp, torch.full((qp.shape[0], 1), R, device="cuda")], 1)
                 cnt = trav.traverse(trees[j], sph, query=nb.QUERY_EXACT, points=tp, box=box, pad=pad,
                                     images="periodic")
-                mx = int(cnt.max().item())
+                mx = trav.count_summary()[0]
                 cnt, lst = trav.traverse(trees[j], sph, query=nb.QUERY_EXACT, points=tp, box=box, pad=pad,
                                          images="periodic", max_neigh=max(mx, 1), nneigh=cnt)
             out[(i, j)] = (cnt, lst, R)
@@ -550,7 +573,23 @@ def polydisperse_c2(nb, args, stream, steps=5, warmup=2):
         want, _ = O.celllist_counts(qp[sel], tp, R, [0, 0, 0], [L, L, L])
         checked = checked and bool(np.array_equal(c[sel], want))
     total = float(sum(int(cnt.cpu().numpy().view(np.uint32).astype(np.int64).sum()) for cnt, _, _ in out.values()))
-    return {"workload": f"polydisperse: {n_small} spheres d=1 + {n_large} spheres d=10, volume fraction 0.10 each, "
+    ref = None
+    if not args.no_ref_cuda:
+        try:
+            from oracle import ref_harness
+            if ref_harness.build_if_available() and ref_harness.available():
+                r = ref_harness.run_poly([f[0].cpu().numpy() for f in frames], [f[1].cpu().numpy() for f in frames],
+                                         L, steps, warmup)
+                best, sweep = best_block(r)
+                ref = {"step_ms": best["step_ms"], "block": best["block"], "pairs_per_step": r["pairs_per_step"],
+                       "sweep_ms": sweep}
+            else:
+                ref = {"unavailable": "reference kernels not built here"}
+        except Exception as e:  # measurement aid only: never fails the bench
+            ref = {"unavailable": f"{type(e).__name__}: {e}"[:200]}
+    return {"reference_cuda": ref,
+            "vs_reference_cuda": (ref["step_ms"] / ms) if ref and "step_ms" in ref else None,
+            "workload": f"polydisperse: {n_small} spheres d=1 + {n_large} spheres d=10, volume fraction 0.10 each, "
                         f"L={L:.2f}, cutoff (d_i+d_j)/2+0.4, 27 images, 2 trees x 4 traversals",
             "ms_per_step": ms, "value": total / (ms * 1e-3), "unit": "pairs/s", "pairs_per_step": total,
             "pairs": pairs, "check_vs_oracle": checked,
@@ -580,7 +619,7 @@ def small_plain(nb, args, stream, n=32_768, steps=200, warmup=20):
         lbvh.build(p, [0, 0, 0], box, block_size=args.block)
         trav.traverse_self(lbvh, RC, box, pad, images="periodic", nneigh=counts, rows_sorted=True,
                            block_size=args.block)
-        mx = int(counts.max().item())
+        mx = trav.count_summary(stream)[0]
         trav.traverse_self(lbvh, RC, box, pad, images="periodic", max_neigh=mx, nneigh=counts,
                            neigh_list=lst, rows_sorted=True, block_size=args.block)
         e1.record(stream)
@@ -608,23 +647,34 @@ def small_plain(nb, args, stream, n=32_768, steps=200, warmup=20):
     return out
 
 
-def reference_cuda(n, our_ms):
+def best_block(result):
+    """The block size with the fewest milliseconds per step of a reference-harness sweep, and the
+    sweep in compact form."""
+    best = min(result["results"], key=lambda x: x["step_ms"])
+    sweep = {str(r["block"]): round(r["step_ms"], 4) for r in result["results"]}
+    return best, sweep
+
+
+def reference_cuda(n, our_ms, steps=20, warmup=3):
     """The reference's own CUDA kernels on the same GPU and workload (oracle/ref_harness): the
-    plain two-pass step (build, setup, count, max, fill) with the best block size of 32..512."""
+    plain two-pass step (build, setup, count, max, fill) on a uniform trajectory of the same
+    size, every block size of 32..1024 (the reference's tunable range) with `steps` timed steps
+    each; the best block size is the reference's number."""
     try:
         from oracle import ref_harness
         if not (ref_harness.build_if_available() and ref_harness.available()):
             return {"unavailable": "reference kernels not built here"}
-        r = ref_harness.run_bench(n, steps=5, warmup=2, rc=RC)
+        r = ref_harness.run_bench(n, steps=steps, warmup=warmup, rc=RC)
     except Exception as e:  # measurement aid only: never fails the bench
         return {"unavailable": f"{type(e).__name__}: {e}"[:200]}
-    best = min(r["results"], key=lambda x: x["step_ms"])
-    return {"step_ms": best["step_ms"], "block": best["block"],
+    best, sweep = best_block(r)
+    return {"step_ms": best["step_ms"], "step_ms_median": best["step_ms_median"], "block": best["block"],
             "stages_ms": {k: best[k] for k in ("build_ms", "setup_ms", "count_ms", "fill_ms")},
-            "value": best["pairs_per_step"] / (best["step_ms"] * 1e-3), "unit": "pairs/s",
-            "our_speedup": best["step_ms"] / our_ms, "all_blocks": r["results"],
-            "note": "reference kernels compiled from its headers, launched in its build/setup/"
-                    "traverse order with CUB SortPairs; exact query op; queries in sorted order"}
+            "value": r["pairs_per_step"] / (best["step_ms"] * 1e-3), "unit": "pairs/s",
+            "our_speedup": best["step_ms"] / our_ms, "steps_per_block": steps, "sweep_ms": sweep,
+            "note": "reference kernels compiled from its headers, launched in its build/setup/traverse order "
+                    "with CUB SortPairs; exact query op; queries in sorted order; its own trajectory frames "
+                    "(same size, density, sigma)"}
 
 
 def run_reference(args):
@@ -695,6 +745,14 @@ def run_ours(args):
     counts = torch.empty(n, dtype=torch.int32, device="cuda")
     cap = 64
     lst = torch.empty(n * cap, dtype=torch.int32, device="cuda")
+    tuned = None
+    if not args.no_tune:
+        # leaf size, sort digit width and climb block from the autotuner, timed on the first
+        # warm-up frame (outside the timed region); the same lists whatever it picks
+        t0 = time.perf_counter()
+        tuned = nb.tune_self(lbvh, trav, frames[0], [0, 0, 0], box, RC, box, pad, reps=3)
+        tuned["tune_s"] = round(time.perf_counter() - t0, 2)
+        args.leaf, args.radix_bits, args.climb = tuned["leaf_size"], tuned["radix_bits"], tuned["climb_block"]
 
     ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
 
@@ -772,92 +830,17 @@ def run_ours(args):
         got = counts.cpu().numpy().view(np.uint32)[sel]
         check = bool(np.array_equal(got, want))
 
+    # every row of the last frame's list against the reference's own kernels (row hashes)
+    check_ref = None
+    if rank == 0 and not args.no_ref_cuda:
+        check_ref = check_list_vs_reference(frames[-1], lbvh, lst, counts, step_max[-1], L)
+
     # e2e through the C ABI with host buffers: every step copies its frame from pinned host memory
     # and its counts and list back to pinned host memory.  Two sets of buffers: the copies of step
     # k's results run on a second stream while step k + 1 computes.
     e2e = None
     if not args.no_e2e:
-        host_in = [f.cpu().pin_memory() for f in frames[-2:]]
-        pairs_of = []                        # pairs of the two frames (counted outside the timing)
-        for f in frames[-2:]:
-            lbvh.build(f, [0, 0, 0], box, block_size=args.block)
-            trav.traverse_self(lbvh, RC, box, pad, images=imgs, nneigh=counts, rows_sorted=True,
-                               block_size=args.block)
-            pairs_of.append(int(counts.cpu().numpy().astype(np.int64).sum()))
-        dev_in = [torch.empty((n, 3), dtype=torch.float32, device="cuda") for _ in range(2)]
-        cnt_b = [counts, torch.empty(n, dtype=torch.int32, device="cuda")]
-        lst_b = [lst, torch.empty(n * cap, dtype=torch.int32, device="cuda")]
-        host_counts = [torch.empty(n, dtype=torch.int32).pin_memory() for _ in range(2)]
-        host_list = [torch.empty(n * cap, dtype=torch.int32).pin_memory() for _ in range(2)]
-        copy_stream = torch.cuda.Stream()   # results to the host
-        load_stream = torch.cuda.Stream()   # inputs to the device
-        done = [torch.cuda.Event() for _ in range(2)]
-        computed = [torch.cuda.Event() for _ in range(2)]
-        loaded = [torch.cuda.Event() for _ in range(2)]
-        started = torch.cuda.Event()
-
-        rows_b = [torch.empty(n, dtype=torch.int32, device="cuda") for _ in range(2)]
-        scan_op = nb.OnePassList()
-
-        def e2e_step(b, p):
-            # the plain two-pass step with the list in CSR form (count, scan, fill), so that only
-            # the valid entries travel to the host
-            lbvh.build(p, [0, 0, 0], box, block_size=args.block)
-            trav.traverse_self(lbvh, RC, box, pad, images=imgs, nneigh=cnt_b[b], rows_sorted=True,
-                               block_size=args.block)
-            mx = int(cnt_b[b].max().item())
-            offsets, total = scan_op.scan(cnt_b[b])
-            if total > n * cap:
-                raise RuntimeError(f"{total} pairs exceed the list buffer")
-            trav.traverse_self_csr(lbvh, RC, box, pad, offsets, cnt_b[b], lst_b[b], max_capacity=mx,
-                                   images=imgs, nneigh=rows_b[b], block_size=args.block)
-            return total
-
-        e_steps = max(4, min(args.steps, 10))
-        h2d = d2h = 0
-        e_pairs = 0
-        torch.cuda.synchronize()
-        e0, e1 = ev(), ev()
-        e0.record(stream)
-        started.record(stream)
-
-        def load(k):
-            # step k's frame into input buffer k % 2, once step k - 2 (its last user) has computed
-            bb = k % 2
-            with torch.cuda.stream(load_stream):
-                load_stream.wait_event(started if k < 2 else computed[bb])
-                dev_in[bb].copy_(host_in[k % 2], non_blocking=True)
-                loaded[bb].record(load_stream)
-
-        load(0)
-        for k in range(e_steps):
-            b = k % 2
-            if k + 1 < e_steps:
-                load(k + 1)                  # the next frame travels while this step computes
-            stream.wait_event(loaded[b])
-            if k >= 2:
-                stream.wait_event(done[b])   # buffers b are free once step k-2's results are home
-            total = e2e_step(b, dev_in[b])
-            computed[b].record(stream)
-            with torch.cuda.stream(copy_stream):
-                copy_stream.wait_event(computed[b])
-                host_counts[b].copy_(rows_b[b], non_blocking=True)
-                host_list[b][:total].copy_(lst_b[b][:total], non_blocking=True)
-                done[b].record(copy_stream)
-            h2d += n * 12
-            d2h += n * 4 + total * 4
-            e_pairs += pairs_of[k % 2]
-        stream.wait_event(done[(e_steps - 1) % 2])
-        stream.wait_event(done[e_steps % 2])
-        e1.record(stream)
-        torch.cuda.synchronize()
-        ems = e0.elapsed_time(e1)
-        assert int(host_counts[(e_steps - 1) % 2].numpy().astype(np.int64).sum()) == pairs_of[(e_steps - 1) % 2]
-        e2e = {"value": sum_over_ranks(e_pairs, ws) / (max_over_ranks(ems, ws) / 1e3),
-               "unit": "pairs/s", "h2d_bytes_per_step": h2d // e_steps,
-               "d2h_bytes_per_step": d2h // e_steps, "steps": e_steps,
-               "overlap": "step k+1's frame copied in and step k's results copied out while steps compute",
-               "list": "CSR (counts + the valid entries), filled by the same two passes"}
+        e2e = e2e_section(nb, args, frames, lbvh, trav, counts, lst, cap, L, stream, ws)
 
     if rank != 0:
         return 0
@@ -870,9 +853,11 @@ def run_ours(args):
     alg = {"build": 12.0 * n, "count": 20.0 * n, "fill": 20.0 * n + 4.0 * pairs_step}
     dom = max(stages, key=stages.get)
     passes = (30 + args.radix_bits - 1) // args.radix_bits
+    # per step: histogram, digit offsets, one onesweep per pass, climb, climb across blocks, scan,
+    # emit (build); symmetric count and its summary; assembly and the re-walk of rows past the
+    # pair exchange (fill)
     build_launches = 2 + passes + 1 + (1 if n > args.climb else 0) + 2
-    launches_per_step = [build_launches + 1 + (2 if 0 < m <= 32 and args.mode == 0 else 1)
-                         for m in step_max]
+    launches_per_step = build_launches + 2 + 2
     achieved = alg[dom] / (stages[dom] * 1e-3) / 1e9
     step_bytes = 12.0 * n + 16.0 * n + 4.0 * n + 4.0 * pairs_step
     line = {
@@ -890,8 +875,9 @@ def run_ours(args):
         "data": "synthetic",
         "config": workload_config(n, L),
         "parallelism": f"replicas x{ws}",
-        "tuning": {"leaf_size": args.leaf, "radix_bits": args.radix_bits, "block": args.block,
-                   "traversal": "warp packet" if args.mode == 1 else "thread per query"},
+        "tuning": {"leaf_size": args.leaf, "radix_bits": args.radix_bits, "climb_block": args.climb,
+                   "block": args.block, "traversal": "warp packet" if args.mode == 1 else "thread per query",
+                   "autotuner": tuned if tuned is not None else "off (--no-tune)"},
         "stages_ms": {k: round(v, 4) for k, v in stages.items()},
         "gaps_ms": {"count_to_fill": round(mean(gap_max_ms), 4),
                     "between_steps": round(mean(gap_step_ms), 4) if gap_step_ms else None},
@@ -899,16 +885,15 @@ def run_ours(args):
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
                      "traffic": stage_traffic(dom, n),
-                     # what bounds the traversal instead: instruction issue (ncu, 8M capture)
+                     # what bounds the traversal instead: instruction issue (ncu capture)
                      "issue_active_pct": stage_profile(dom).get("issue_active_pct"),
                      "lanes_active": stage_profile(dom).get("lanes_active_per_warp_instruction"),
                      "step_achieved": step_bytes / (ms_max / args.steps * 1e-3) / 1e9},
-        # per step: histogram, digit offsets, one onesweep per pass, climb, climb across blocks,
-        # scan, emit (build) + count traversal + fill traversal (+ row ordering for rows <= 32)
-        "gpu_launches": sum(launches_per_step),
+        "gpu_launches": launches_per_step * args.steps,
         "clocks": clocks,
         "e2e": e2e,
         "check_vs_oracle": check,
+        "check_vs_reference": check_ref,
     }
     if not args.no_learned:
         line["learned"] = learned_uniform(nb, n, L, frames, args.warmup, line["ms_per_step"], pairs_step,
@@ -927,8 +912,170 @@ def run_ours(args):
                                           want_pairs=pair_counts[-2:])
     if not args.no_ref_cuda:
         line["reference_cuda"] = reference_cuda(n, line["ms_per_step"])
+    line["summary"] = summary(line)
     print(json.dumps(line))
     return 0
+
+
+def summary(line):
+    """The headline figures of every section, last in the line (a truncated log keeps its end)."""
+    def get(d, *keys):
+        for k in keys:
+            if not isinstance(d, dict) or k not in d:
+                return None
+            d = d[k]
+        return round(d, 4) if isinstance(d, float) else d
+    return {"ms_per_step": get(line, "ms_per_step"),
+            "e2e_vs_value": (round(line["e2e"]["value"] / line["value"], 4) if line.get("e2e") else None),
+            "vs_reference_cuda": get(line, "reference_cuda", "our_speedup"),
+            "reference_cuda_ms": get(line, "reference_cuda", "step_ms"),
+            "check_vs_reference": get(line, "check_vs_reference", "rows_equal"),
+            "cpu_pairs_per_s": get(line, "cpu_baseline", "value"),
+            "learned_vs_plain_16m": get(line, "learned", "vs_plain"),
+            "clustered_learned_vs_plain": get(line, "clustered_4m", "learned_vs_plain"),
+            "clustered_vs_reference_cuda": get(line, "clustered_4m", "plain_vs_reference_cuda"),
+            "polydisperse_ms": get(line, "polydisperse_1m", "ms_per_step"),
+            "polydisperse_vs_reference_cuda": get(line, "polydisperse_1m", "vs_reference_cuda"),
+            "batched_vs_sequential": get(line, "batched_4096", "batched_vs_sequential"),
+            "small_32k_vs_reference_cuda": get(line, "small_32k", "speedup_vs_reference")}
+
+
+def row_hashes(nb_list, counts, mx):
+    """Row hashes of a fixed-stride list (the reference harness's k_row_hash), on the GPU:
+    sum over k < count of (entry_k + 1) * C_k plus count * C_COUNT, exact in int64."""
+    import torch
+    from oracle import ref_harness
+    n = counts.shape[0]
+    coef = torch.tensor(ref_harness.hash_coefficients(mx).astype("int64"), device="cuda")
+    c = counts.long()
+    out = torch.empty(n, dtype=torch.int64, device="cuda")
+    rows = nb_list[: n * mx].view(n, mx)
+    step = 1 << 22
+    for a in range(0, n, step):
+        b = min(n, a + step)
+        valid = torch.arange(mx, device="cuda")[None, :] < c[a:b, None]
+        e = (rows[a:b].long() + 1) * coef[None, :]
+        out[a:b] = torch.where(valid, e, torch.zeros_like(e)).sum(1) + c[a:b] * ref_harness.HASH_COUNT
+    return out
+
+
+def check_list_vs_reference(frame, lbvh, lst, counts, mx, L):
+    """Every row of the last timed frame's list (rows by sorted position, stride mx) against the
+    list the reference's own kernels write for the same points (rows by point): counts and row
+    hashes equal, row for row."""
+    import numpy as np
+    try:
+        from oracle import ref_harness
+        if not (ref_harness.build_if_available() and ref_harness.available()):
+            return {"unavailable": "reference kernels not built here"}
+        if mx > 64:
+            return {"unavailable": f"rows of {mx} entries (the hash is exact up to 64)"}
+        ref_count, ref_hash, ref_mx = ref_harness.run_hash(frame.cpu().numpy(), RC, L)
+        prim = lbvh.primitives().cpu().numpy().view(np.uint32)
+        ours = row_hashes(lst, counts, mx).cpu().numpy().view(np.uint64)
+        c = counts.cpu().numpy().view(np.uint32)
+        bad = int(np.count_nonzero((ours != ref_hash[prim]) | (c != ref_count[prim])))
+        return {"rows": int(len(c)), "rows_equal": bad == 0, "rows_differing": bad, "max_count": int(mx),
+                "reference_max_count": ref_mx,
+                "how": "per-row hash (order-sensitive) and count of every row of the last timed frame against "
+                       "the reference kernels' exact list of the same points"}
+    except Exception as e:  # measurement aid only: never fails the bench
+        return {"unavailable": f"{type(e).__name__}: {e}"[:200]}
+
+
+def e2e_section(nb, args, frames, lbvh, trav, counts, lst, cap, L, stream, ws):
+    """The plain step through the C ABI with host buffers: each step's frame is copied in from
+    pinned host memory and its counts and CSR list go back to pinned host memory.  The only host
+    wait per step is the count summary (largest count and total), as in the device-timed step;
+    the scan into CSR offsets is enqueued without a read, and the copies run on their own
+    streams, overlapping the next step."""
+    import numpy as np
+    import torch
+    n = args.n
+    box = [L, L, L]
+    pad = nb.exact_pad(RC, 2 * L)
+    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+    e_steps = max(4, min(args.steps, 10))
+    host_in = [f.cpu().pin_memory() for f in frames[-2:]]
+    dev_in = [torch.empty((n, 3), dtype=torch.float32, device="cuda") for _ in range(2)]
+    cnt_b = [counts, torch.empty(n, dtype=torch.int32, device="cuda")]
+    lst_b = [lst, torch.empty(n * cap, dtype=torch.int32, device="cuda")]
+    off_b = [torch.empty(n, dtype=torch.int64, device="cuda") for _ in range(2)]
+    rows_b = [torch.empty(n, dtype=torch.int32, device="cuda") for _ in range(2)]
+    host_counts = [torch.empty(n, dtype=torch.int32).pin_memory() for _ in range(2)]
+    host_list = [torch.empty(n * cap, dtype=torch.int32).pin_memory() for _ in range(2)]
+    copy_stream = torch.cuda.Stream()   # results to the host
+    load_stream = torch.cuda.Stream()   # inputs to the device
+    done = [torch.cuda.Event() for _ in range(2)]
+    computed = [torch.cuda.Event() for _ in range(2)]
+    loaded = [torch.cuda.Event() for _ in range(2)]
+    started = torch.cuda.Event()
+    scan_op = nb.OnePassList()
+
+    def e2e_step(b, p):
+        # the plain two-pass step with the list in CSR form (count, scan, fill), so that only
+        # the valid entries travel to the host
+        lbvh.build(p, [0, 0, 0], box, block_size=args.block)
+        trav.traverse_self(lbvh, RC, box, pad, images="periodic", nneigh=cnt_b[b], rows_sorted=True,
+                           block_size=args.block)
+        mx, total, _ = trav.count_summary(stream)          # the step's one host read
+        if total > n * cap:
+            raise RuntimeError(f"{total} pairs exceed the list buffer")
+        scan_op.scan(cnt_b[b], out=off_b[b], read_total=False)
+        trav.traverse_self_csr(lbvh, RC, box, pad, off_b[b], cnt_b[b], lst_b[b], max_capacity=mx,
+                               images="periodic", nneigh=rows_b[b], block_size=args.block)
+        return total
+
+    def load(k):
+        # step k's frame into input buffer k % 2, once step k - 2 (its last user) has computed
+        bb = k % 2
+        with torch.cuda.stream(load_stream):
+            load_stream.wait_event(started if k < 2 else computed[bb])
+            dev_in[bb].copy_(host_in[k % 2], non_blocking=True)
+            loaded[bb].record(load_stream)
+
+    def run():
+        h2d = d2h = pairs = 0
+        torch.cuda.synchronize()
+        e0, e1 = ev(), ev()
+        e0.record(stream)
+        started.record(stream)
+        load(0)
+        totals = []
+        for k in range(e_steps):
+            b = k % 2
+            if k + 1 < e_steps:
+                load(k + 1)                  # the next frame travels while this step computes
+            stream.wait_event(loaded[b])
+            if k >= 2:
+                stream.wait_event(done[b])   # buffers b are free once step k-2's results are home
+            total = e2e_step(b, dev_in[b])
+            totals.append(total)
+            computed[b].record(stream)
+            with torch.cuda.stream(copy_stream):
+                copy_stream.wait_event(computed[b])
+                host_counts[b].copy_(rows_b[b], non_blocking=True)
+                host_list[b][:total].copy_(lst_b[b][:total], non_blocking=True)
+                done[b].record(copy_stream)
+            h2d += n * 12
+            d2h += n * 4 + total * 4
+            pairs += total
+        stream.wait_event(done[(e_steps - 1) % 2])
+        stream.wait_event(done[e_steps % 2])
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1), h2d, d2h, pairs, totals
+
+    run()   # warm: buffers, pinned pages, streams
+    ems, h2d, d2h, e_pairs, totals = run()
+    assert int(host_counts[(e_steps - 1) % 2].numpy().astype(np.int64).sum()) == totals[-1]
+    return {"value": sum_over_ranks(e_pairs, ws) / (max_over_ranks(ems, ws) / 1e3),
+            "unit": "pairs/s", "h2d_bytes_per_step": h2d // e_steps,
+            "d2h_bytes_per_step": d2h // e_steps, "steps": e_steps,
+            "ms_per_step": ems / e_steps,
+            "overlap": "step k+1's frame copied in and step k's results copied out while steps compute",
+            "host_waits_per_step": 1,
+            "list": "CSR (counts + the valid entries), filled by the same two passes"}
 
 
 def main():

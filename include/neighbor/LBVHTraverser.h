@@ -176,9 +176,10 @@ class LBVHTraverser : public Tunable<unsigned int>
         void setPairCache(bool enabled) { m_pair_cache = enabled; }
         bool getPairCache() const { return m_pair_cache; }
 
-        // Summary of the last counting self traversal (traverseSelf with CountNeighborsOp), four
-        // device words: [0] the largest count, [1] rows whose pairs did not fit the pair
-        // exchange, [2..3] the total of the counts (64-bit).  Written on the traversal's stream.
+        // Summary of the last counting traversal (traverse or traverseSelf with
+        // CountNeighborsOp), four device words: [0] the largest count, [1] rows whose pairs did
+        // not fit the pair exchange (symmetric self counts), [2..3] the total of the counts
+        // (64-bit).  Written on the traversal's stream.
         const unsigned int* getCountSummary() const { return m_words.get(); }
         // The same, read on the host: synchronises `stream` (the reference's two-pass pattern
         // reads the largest count here before the fill, benchmark/lbvh_benchmark.cc:177-196).
@@ -289,6 +290,14 @@ class LBVHTraverser : public Tunable<unsigned int>
         unsigned int summary_grid(unsigned int N)
             {
             return std::max(1u, std::min(detail::ceil_div(N, gpu::kSummaryBlock), 4u * sm_count()));
+            }
+        // the summary (largest count, total) of counts already written to nneigh[0..Q)
+        void summarize_counts(cudaStream_t stream, unsigned int* nneigh, unsigned int Q, const unsigned int* status)
+            {
+            clear_summary(stream);
+            gpu::k_count_summary<false><<<summary_grid(Q), gpu::kSummaryBlock, 0, stream>>>(
+                Q, nullptr, nullptr, nullptr, 0, nneigh, m_words.get(), status);
+            detail::check_cuda(cudaGetLastError(), "summary launch");
             }
         // zero the summary words before a count
         void clear_summary(cudaStream_t stream)
@@ -493,6 +502,8 @@ void LBVHTraverser::traverse(const LaunchParameters& params, const LBVH& lbvh, c
             a.box = query.box;
             a.pad = query.pad;
             launch_fast(params, lbvh, a, out, transform, query.size());
+            if constexpr (std::is_same<OutputOpT, CountNeighborsOp>::value)
+                summarize_counts(params.stream, out.nneigh, query.size(), lbvh.getStatusPointer());
             return;
             }
         }
@@ -503,6 +514,8 @@ void LBVHTraverser::traverse(const LaunchParameters& params, const LBVH& lbvh, c
         <<<detail::ceil_div(query.size(), bs), bs, 0, params.stream>>>(out, data(), query, images,
                                                                         lbvh.getStatusPointer());
     detail::check_cuda(cudaGetLastError(), "traversal launch");
+    if constexpr (std::is_same<OutputOpT, CountNeighborsOp>::value)
+        summarize_counts(params.stream, out.nneigh, query.size(), lbvh.getStatusPointer());
     }
 
 template<class OutputOpT, class TranslateOpT, class TransformOpT>
@@ -550,15 +563,7 @@ void LBVHTraverser::traverseSelf(const LaunchParameters& params, const LBVH& lbv
     else
         {
         launch_fast(params, lbvh, a, out, transform, lbvh.getN());
-        if (kind == gpu::kFastCount)
-            {
-            // the count's summary (largest count, total) from the counts it wrote
-            clear_summary(params.stream);
-            const unsigned int N = lbvh.getN();
-            gpu::k_count_summary<false><<<summary_grid(N), gpu::kSummaryBlock, 0, params.stream>>>(
-                N, nullptr, nullptr, nullptr, 0, a.nneigh, m_words.get(), lbvh.getStatusPointer());
-            detail::check_cuda(cudaGetLastError(), "summary launch");
-            }
+        if (kind == gpu::kFastCount) summarize_counts(params.stream, a.nneigh, lbvh.getN(), lbvh.getStatusPointer());
         }
     }
 

@@ -581,7 +581,9 @@ __global__ void __launch_bounds__(kWarpWalkBlock) k_traverse_warp(const FastLBVH
 // Rows re-walked whole, their sorted positions in subset[0 .. *subset_count) (a count known only
 // on the device, e.g. the rows an assembly pass could not finish).  A persistent grid: with at
 // most kSubsetGroupMax rows each row gets a warp (a few long walks set the time, and 32 lanes
-// shorten each about 32 times); with more, each row gets one thread (the total work sets it).
+// shorten each about 32 times); with more, each row gets one thread (the total work sets it), and
+// each block hands its rows to its lanes in order of their counts (nneigh, already written), so
+// that a warp's lanes walk about as long as each other.
 constexpr unsigned int kSubsetBlock = 256;
 constexpr unsigned int kSubsetGroupMax = 32768;
 
@@ -593,6 +595,8 @@ __global__ void __launch_bounds__(kSubsetBlock) k_traverse_subset(const FastLBVH
     __shared__ QuantFrame s_frame;
     __shared__ unsigned int s_records;
     __shared__ unsigned int s_n;
+    __shared__ unsigned int s_class[kWorkClasses];
+    __shared__ unsigned int s_order[kSubsetBlock];
     if (threadIdx.x == 0)
         {
         s_frame = *tree.frame;
@@ -616,8 +620,23 @@ __global__ void __launch_bounds__(kSubsetBlock) k_traverse_subset(const FastLBVH
     else
         {
         unsigned int visits = 0, tests = 0, walks = 0;
-        for (unsigned int t = gid; t < n; t += threads)
-            thread_walk<OUT, false>(tree, a, transform, f, n_rec, a.subset[t], visits, tests, walks);
+        // block-uniform trip count: every thread of the block reaches block_work_order's barriers
+        for (unsigned int b0 = blockIdx.x * blockDim.x; b0 < n; b0 += threads)
+            {
+            const unsigned int item = b0 + threadIdx.x;
+            const bool valid = item < n;
+            unsigned int cls = 0;
+            if (valid)
+                {
+                const unsigned int q = a.subset[item];
+                const unsigned int row = a.self_rows_sorted ? q : __float_as_uint(tree.points[q].w);
+                cls = capacity_class(a.nneigh[row]);
+                }
+            const unsigned int t = block_work_order(item, valid, cls, s_class, s_order);
+            if (t != 0xffffffffu)
+                thread_walk<OUT, false>(tree, a, transform, f, n_rec, a.subset[t], visits, tests, walks);
+            __syncthreads();   // s_order is rewritten by the next round
+            }
         }
     }
 

@@ -12,5 +12,6 @@
 
 #include "LBVH.h"
 #include "LBVHTraverser.h"
+#include "SelfListTuner.h"
 
 #endif // NEIGHBOR_NEIGHBOR_H_

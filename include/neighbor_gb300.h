@@ -137,9 +137,9 @@ int nbr_traverser_set_work_order(nbr_traverser t, int enabled);
  * way. */
 int nbr_traverser_set_pair_cache(nbr_traverser t, int enabled);
 
-/* Addition: summary of the last counting self traversal (nbr_traverse_self with list == NULL) on
- * this traverser: the largest count, the total of the counts (ordered pairs, self included) and
- * the rows whose pairs did not fit the pair exchange.  Synchronises `stream`: it is the host read
+/* Addition: summary of the last counting traversal (nbr_traverse or nbr_traverse_self with
+ * list == NULL) on this traverser: the largest count, the total of the counts (ordered pairs,
+ * self included) and the rows whose pairs did not fit the pair exchange (symmetric self counts).  Synchronises `stream`: it is the host read
  * of the largest count between the count and the list pass (the reference's benchmark reads its
  * counts on the host after the traversal, benchmark/lbvh_benchmark.cc:233-237); any pointer may
  * be NULL. */
@@ -189,6 +189,21 @@ int nbr_traverse_self(nbr_traverser t, nbr_lbvh h, float rc, const float box[3],
                       unsigned int* nneigh, unsigned int* list, unsigned int max_neigh,
                       int rows_sorted, unsigned int block_size, void* stream);
 
+/* Addition (no counterpart in the reference, whose Tunable only lists valid block sizes,
+ * include/neighbor/Tunable.h:28-118): autotune the self neighbor list of `points` -- time the
+ * step build + count + host read of the largest count + fill for every leaf size (1, 2, 4, 8),
+ * sort digit width (8, 10) and climb block (256, 512), `reps` timed steps each, and apply the
+ * fastest to h (nbr_lbvh_set_leaf_size / _radix_bits / _climb_block).  The choice is cached per
+ * (N rounded up to a power of two, rc, number density of lo..hi in quarter octaves); a cached
+ * class is applied without timing (*ms = 0).  periodic: the 27 images of box, else the self
+ * image.  Synchronises `stream`; results never depend on the configuration. */
+int nbr_tune_self(nbr_lbvh h, nbr_traverser t, const float* points, unsigned int N, const float lo[3],
+                  const float hi[3], float rc, const float box[3], float pad, int periodic, unsigned int reps,
+                  void* stream, unsigned int* leaf_size, unsigned int* radix_bits, unsigned int* climb_block,
+                  float* ms);
+/* Forget every configuration nbr_tune_self has cached (process-wide). */
+int nbr_tune_self_clear(void);
+
 /* Test hook for failure detection (no counterpart in the reference): runs the chained scan
  * used by the build with its first tile never published, so the look-back of the next tile must
  * give up after its bounded wait (about a second) instead of hanging.  Writes the resulting
@@ -216,6 +231,21 @@ int nbr_debug_inject_alloc_failures(unsigned int count);
 int nbr_morton_sort_noalloc(const float* points, unsigned int N, const float lo[3],
                             const float hi[3], unsigned int* codes_out, unsigned int* order_out,
                             void* stream);
+
+/* No counterpart in the reference.  Status of the last nbr_morton_sort_noalloc call on the current
+ * device: copies the fixed array's status word to the host on `stream` (after that call's work)
+ * and synchronises `stream`; allocates nothing.  Returns NBR_ERR_DEVICE_WAIT (status_out != 0)
+ * when a bounded look-back wait of that call gave up: its outputs are then not valid.  points,
+ * codes_out and order_out of a sort must be memory of the current device (NBR_ERR_INVALID
+ * otherwise). */
+int nbr_morton_sort_noalloc_status(unsigned int* status_out, void* stream);
+
+/* Test hook for the status above (no counterpart in the reference): the same sort with its first
+ * tile never run, so that the next tile's look-back gives up after its bounded wait; the status
+ * then reports it.  N must exceed one sort tile (4096 points). */
+int nbr_debug_noalloc_wait_timeout(const float* points, unsigned int N, const float lo[3],
+                                   const float hi[3], unsigned int* codes_out, unsigned int* order_out,
+                                   void* stream);
 
 /* Addition (double-precision inputs, e.g. HOOMD-blue built with Scalar = double): LBVH::build
  * with PointInsertOpF64 -- each point's box is the point rounded outward to FP32
@@ -333,7 +363,8 @@ int nbr_onepass_build_learned(nbr_onepass op, nbr_capmodel m, nbr_traverser t, n
 /* The list of the last build: entries, row offsets (uint64[N]), capacities, counts, total slots. */
 int nbr_onepass_get(nbr_onepass op, const unsigned int** list, const unsigned long long** offsets,
                     const unsigned int** caps, const unsigned int** nneigh, unsigned long long* total);
-/* Exclusive scan of n counts into uint64 offsets; *total = their sum (synchronises). */
+/* Exclusive scan of n counts into uint64 offsets; *total = their sum (synchronises), or with
+ * total == NULL the scan is only enqueued on `stream`. */
 int nbr_onepass_scan(nbr_onepass op, const unsigned int* counts, unsigned int n,
                      unsigned long long* offsets, unsigned long long* total, void* stream);
 

@@ -109,6 +109,9 @@ def _declare(L):
     sig("nbr_traverser_count_summary", [_P, ctypes.POINTER(_U), ctypes.POINTER(ctypes.c_ulonglong),
                                         ctypes.POINTER(_U), _P])
     sig("nbr_traverser_count_summary_device", [_P, _PP])
+    sig("nbr_tune_self", [_P, _P, _P, _U, _P, _P, _F, _P, _F, _I, _U, _P, ctypes.POINTER(_U),
+                          ctypes.POINTER(_U), ctypes.POINTER(_U), ctypes.POINTER(_F)])
+    sig("nbr_tune_self_clear", [])
     sig("nbr_traverse", [_P, _P, _I, _P, _U, _P, _P, _F, _P, _U, _P, _P, _P, _U, _U, _P])
     sig("nbr_traverse_self", [_P, _P, _F, _P, _F, _P, _U, _P, _P, _P, _U, _I, _U, _P])
     sig("nbr_exact_pad", [_F, _F], _F)
@@ -116,6 +119,8 @@ def _declare(L):
     sig("nbr_traverse_f64", [_P, _P, _P, _U, _P, _P, _F, _P, _U, _P, _P, _P, _U, _U, _P])
     sig("nbr_debug_wait_timeout", [ctypes.POINTER(_U), _P])
     sig("nbr_morton_sort_noalloc", [_P, _U, _P, _P, _P, _P, _P])
+    sig("nbr_morton_sort_noalloc_status", [ctypes.POINTER(_U), _P])
+    sig("nbr_debug_noalloc_wait_timeout", [_P, _U, _P, _P, _P, _P, _P])
     _ULL = ctypes.c_ulonglong
     sig("nbr_traverse_self_csr", [_P, _P, _F, _P, _F, _P, _U, _P, _P, _P, _P, _P, _U, _I, _U, _P])
     sig("nbr_traverse_self_subset_csr", [_P, _P, _F, _P, _F, _P, _U, _P, _P, _U, _P, _P, _P, _P, _I, _P])
@@ -170,9 +175,10 @@ EXPORTED = ["nbr_last_error", "nbr_version", "nbr_lbvh_create", "nbr_lbvh_destro
             "nbr_traverser_set_work_order", "nbr_traverser_set_warp_walk_max",
             "nbr_traverser_set_symmetric_min_points", "nbr_traverser_set_walk_lanes",
             "nbr_traverser_set_pair_cache", "nbr_traverser_count_summary",
-            "nbr_traverser_count_summary_device",
+            "nbr_traverser_count_summary_device", "nbr_tune_self", "nbr_tune_self_clear",
             "nbr_traverser_get_data", "nbr_traverse", "nbr_traverse_self", "nbr_exact_pad",
-            "nbr_debug_wait_timeout", "nbr_morton_sort_noalloc", "nbr_traverse_self_csr",
+            "nbr_debug_wait_timeout", "nbr_morton_sort_noalloc", "nbr_morton_sort_noalloc_status",
+            "nbr_debug_noalloc_wait_timeout", "nbr_traverse_self_csr",
             "nbr_traverse_self_subset_csr",
             "nbr_capmodel_create", "nbr_capmodel_destroy", "nbr_capmodel_get_params",
             "nbr_capmodel_set_params", "nbr_capmodel_set_margin", "nbr_capmodel_get_margin",
@@ -267,10 +273,7 @@ def debug_wait_timeout(stream=None) -> int:
     return st.value
 
 
-def morton_sort_noalloc(points, lo, hi, codes_out, order_out, stream=None):
-    """Morton codes of the points and their stable order, without any device allocation by the
-    library: all working memory is its fixed device array (at most NOALLOC_MAX_POINTS points).
-    codes_out / order_out: preallocated CUDA int32 tensors of N elements."""
+def _noalloc_args(points, codes_out, order_out):
     torch = _torch()
     p = _dev(points, torch.float32, 3)
     n = p.shape[0]
@@ -278,8 +281,61 @@ def morton_sort_noalloc(points, lo, hi, codes_out, order_out, stream=None):
         if not (isinstance(t, torch.Tensor) and t.is_cuda and t.is_contiguous() and t.numel() >= n
                 and t.element_size() == 4):
             raise TypeError("outputs must be contiguous 4-byte CUDA tensors of N elements")
-    _check(load().nbr_morton_sort_noalloc(_ptr(p), n, _f3(lo), _f3(hi), _ptr(codes_out),
-                                          _ptr(order_out), _stream_ptr(stream)))
+        if t.device != p.device:
+            raise ValueError("points and outputs must be on one device")
+    return p, n
+
+
+def morton_sort_noalloc(points, lo, hi, codes_out, order_out, stream=None):
+    """Morton codes of the points and their stable order, without any device allocation by the
+    library: all working memory is its fixed device array (at most NOALLOC_MAX_POINTS points).
+    codes_out / order_out: preallocated CUDA int32 tensors of N elements on the points' device
+    (the call runs there).  A look-back wait that gave up is reported by morton_sort_noalloc_status."""
+    torch = _torch()
+    p, n = _noalloc_args(points, codes_out, order_out)
+    with torch.cuda.device(p.device):
+        _check(load().nbr_morton_sort_noalloc(_ptr(p), n, _f3(lo), _f3(hi), _ptr(codes_out),
+                                              _ptr(order_out), _stream_ptr(stream)))
+
+
+def morton_sort_noalloc_status(stream=None, device=None) -> int:
+    """Status word of the last morton_sort_noalloc call on `device` (synchronises the stream);
+    raises NeighborError (bounded device wait gave up) when it is set."""
+    torch = _torch()
+    st = ctypes.c_uint()
+    with torch.cuda.device(device if device is not None else torch.cuda.current_device()):
+        _check(load().nbr_morton_sort_noalloc_status(ctypes.byref(st), _stream_ptr(stream)))
+    return st.value
+
+
+def debug_noalloc_wait_timeout(points, lo, hi, codes_out, order_out, stream=None):
+    """Test hook: the allocation-free sort with its first tile never run (the next look-back gives
+    up); morton_sort_noalloc_status then reports it."""
+    torch = _torch()
+    p, n = _noalloc_args(points, codes_out, order_out)
+    with torch.cuda.device(p.device):
+        _check(load().nbr_debug_noalloc_wait_timeout(_ptr(p), n, _f3(lo), _f3(hi), _ptr(codes_out),
+                                                     _ptr(order_out), _stream_ptr(stream)))
+
+
+def tune_self(lbvh, trav, points, lo, hi, rc: float, box, pad: float, periodic: bool = True, reps: int = 3,
+              stream=None):
+    """Autotune the self neighbor list of `points` (leaf size, sort digit width, climb block) by
+    timing the whole two-pass step on them; applies the fastest to `lbvh` and returns it as a
+    dict (ms = 0 when the workload's class was cached)."""
+    torch = _torch()
+    p = _dev(points, torch.float32, 3)
+    leaf, bits, climb = ctypes.c_uint(), ctypes.c_uint(), ctypes.c_uint()
+    ms = ctypes.c_float()
+    _check(load().nbr_tune_self(lbvh.handle, trav._h, _ptr(p), p.shape[0], _f3(lo), _f3(hi), float(rc), _f3(box),
+                                float(pad), 1 if periodic else 0, int(reps), _stream_ptr(stream), ctypes.byref(leaf),
+                                ctypes.byref(bits), ctypes.byref(climb), ctypes.byref(ms)))
+    return {"leaf_size": leaf.value, "radix_bits": bits.value, "climb_block": climb.value, "ms": ms.value}
+
+
+def tune_self_clear():
+    """Forget every configuration tune_self has cached."""
+    _check(load().nbr_tune_self_clear())
 
 
 def inject_alloc_failures(count: int):
@@ -855,15 +911,17 @@ class OnePassList:
                     nneigh=_view(nn.value, (N,), "<u4", torch.int32),
                     total=total.value)
 
-    def scan(self, counts, stream=None):
-        """Exclusive scan of int32 counts into int64 offsets; returns (offsets, total)."""
+    def scan(self, counts, stream=None, out=None, read_total: bool = True):
+        """Exclusive scan of int32 counts into int64 offsets; returns (offsets, total).  With
+        read_total False the scan is only enqueued (no synchronisation) and total is None."""
         torch = _torch()
         c = _dev(counts, torch.int32)
-        out = torch.empty(c.shape[0], dtype=torch.int64, device="cuda")
+        if out is None:
+            out = torch.empty(c.shape[0], dtype=torch.int64, device="cuda")
         total = ctypes.c_ulonglong()
-        _check(self._L.nbr_onepass_scan(self._h, _ptr(c), c.shape[0], _ptr(out), ctypes.byref(total),
-                                        _stream_ptr(stream)))
-        return out, total.value
+        _check(self._L.nbr_onepass_scan(self._h, _ptr(c), c.shape[0], _ptr(out),
+                                        ctypes.byref(total) if read_total else None, _stream_ptr(stream)))
+        return out, (total.value if read_total else None)
 
 
 class BatchedList:

@@ -453,6 +453,31 @@ int nbr_traverse_f64(nbr_traverser t, nbr_lbvh h, const double* spheres, unsigne
     });
     }
 
+int nbr_tune_self(nbr_lbvh h, nbr_traverser t, const float* points, unsigned int N, const float lo[3],
+                  const float hi[3], float rc, const float box[3], float pad, int periodic, unsigned int reps,
+                  void* stream, unsigned int* leaf_size, unsigned int* radix_bits, unsigned int* climb_block,
+                  float* ms)
+    {
+    if (!h || !t || !lo || !hi || !box || (N > 0 && !points)) return fail(NBR_ERR_INVALID, "null argument");
+    if (N == 0) return fail(NBR_ERR_INVALID, "nothing to tune: N = 0");
+    return guarded([&] {
+        neighbor::SelfListTuner tuner;
+        const neighbor::SelfListConfig c =
+            tuner.tune(h->lbvh, t->trav, reinterpret_cast<const float3*>(points), N, f3(lo), f3(hi), rc, f3(box), pad,
+                       periodic != 0, reps, as_stream(stream));
+        if (leaf_size) *leaf_size = c.leaf_size;
+        if (radix_bits) *radix_bits = c.radix_bits;
+        if (climb_block) *climb_block = c.climb_block;
+        if (ms) *ms = c.ms;
+    });
+    }
+
+int nbr_tune_self_clear(void)
+    {
+    neighbor::SelfListTuner::clearCache();
+    return NBR_OK;
+    }
+
 int nbr_debug_inject_alloc_failures(unsigned int count)
     {
     neighbor::detail::injected_alloc_failures().store(count);

@@ -312,7 +312,8 @@ int nbr_onepass_scan(nbr_onepass op, const unsigned int* counts, unsigned int n,
     {
     if (!op || (n > 0 && (!counts || !offsets))) return fail(NBR_ERR_INVALID, "null argument");
     return guarded([&] {
-        const unsigned long long t = n ? op->list.scan(counts, n, offsets, as_stream(stream)) : 0ull;
+        // without a total to return, the scan is only enqueued (no synchronisation)
+        const unsigned long long t = n ? op->list.scan(counts, n, offsets, as_stream(stream), total != nullptr) : 0ull;
         if (total) *total = t;
     });
     }

@@ -21,7 +21,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(os.path.dirname(HERE), "_ref")
 CUBIN = os.path.join(OUT, "ref_kernels.cubin")
 DRIVER = os.path.join(OUT, "ref_driver")
-REFERENCE_INCLUDE = "/root/reference/include"  # the reference sources, where they exist
+# The reference's headers, where its sources exist (the build machine; never the GPU machine, which
+# uses the cubin built there).  NEIGHBOR_REFERENCE_INCLUDE points the recipe elsewhere.
+REFERENCE_INCLUDE = os.environ.get("NEIGHBOR_REFERENCE_INCLUDE", "/root/reference/include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -62,21 +64,75 @@ def available() -> bool:
     return os.path.exists(CUBIN) and os.path.exists(DRIVER)
 
 
-def run_bench(n, steps=5, warmup=2, rc=1.3, timeout=600):
-    """Time the reference's plain two-pass step (build, setup, count, max, fill) on uniform
-    trajectory frames for block sizes 32..512; returns the driver's JSON."""
-    r = subprocess.run([DRIVER, "bench", str(n), str(steps), str(warmup), str(rc)],
-                       capture_output=True, text=True, timeout=timeout)
+def _run(args, timeout):
+    r = subprocess.run([DRIVER, *[str(a) for a in args]], capture_output=True, text=True, timeout=timeout)
     if r.returncode != 0:
         raise RuntimeError(f"reference driver failed ({r.returncode}): {r.stderr.strip()[-400:]}")
     return json.loads(r.stdout.strip().splitlines()[-1])
 
 
-def run_dump(points, lo, hi, rc, box, timeout=300, exact_only=False):
+def run_bench(n, steps=20, warmup=3, rc=1.3, timeout=900):
+    """Time the reference's plain two-pass step (build, setup, count, max, fill) on uniform
+    trajectory frames for every block size 32..1024 (step 32); returns the driver's JSON."""
+    return _run(["bench", n, steps, warmup, rc], timeout)
+
+
+def _write_frames(path, frames):
+    with open(path, "wb") as f:
+        for fr in frames:
+            np.ascontiguousarray(fr, np.float32).reshape(-1, 3).tofile(f)
+
+
+def run_frames(frames, rc, L, steps, warmup, timeout=900):
+    """The same plain step on the given frames (a list of [n, 3] float32 arrays, cycled), queries
+    in the tree's sorted order, 27 images of the cube of side L, every block size."""
+    n = len(frames[0])
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "frames.f32")
+        _write_frames(path, frames)
+        return _run(["frames", path, n, len(frames), repr(float(rc)), repr(float(L)), steps, warmup], timeout)
+
+
+def run_poly(small_frames, large_frames, L, steps, warmup, timeout=900):
+    """Two-tree polydisperse step (diameters 1 and 10, cutoff (di+dj)/2 + 0.4, 27 images) on the
+    given frames of each species, every block size."""
+    with tempfile.TemporaryDirectory() as d:
+        sp, lp = os.path.join(d, "small.f32"), os.path.join(d, "large.f32")
+        _write_frames(sp, small_frames)
+        _write_frames(lp, large_frames)
+        return _run(["poly", sp, len(small_frames[0]), lp, len(large_frames[0]), len(small_frames),
+                     repr(float(L)), steps, warmup], timeout)
+
+
+# Row hash of a neighbor list (the driver's k_row_hash): sum over k < count of (entry_k + 1) * C_k
+# plus count * C_COUNT, exact in 64-bit integers for rows of up to 64 entries.
+HASH_COUNT = 0x2545F491
+
+
+def hash_coefficients(m):
+    k = np.arange(m, dtype=np.uint64)
+    return ((((k + 1) * np.uint64(2654435761)) % np.uint64(1 << 32)) & np.uint64(0x7FFFFFFF)) | np.uint64(1)
+
+
+def run_hash(points, rc, L, timeout=900):
+    """Counts and row hashes of the reference's exact neighbor list of the points (queries in
+    input order, 27 images of the cube of side L)."""
+    P = np.ascontiguousarray(points, np.float32).reshape(-1, 3)
+    n = len(P)
+    with tempfile.TemporaryDirectory() as d:
+        src = os.path.join(d, "points.f32")
+        P.tofile(src)
+        prefix = os.path.join(d, "ref")
+        info = _run(["hash", src, n, repr(float(rc)), repr(float(L)), prefix], timeout)
+        return (np.fromfile(prefix + ".count", np.uint32), np.fromfile(prefix + ".hash", np.uint64),
+                int(info["max_count"]))
+
+
+def run_dump(points, lo, hi, rc, box, timeout=300, exact_only=False, sphere_radius=None):
     """The reference's tree arrays, compressed nodes, counts (stock and exact query, 27 periodic
     images of `box`, queries = the points in input order) and the exact query's neighbor list
     (stride = the largest count) for the given points.  exact_only: skip the stock query's
-    counts and lists."""
+    counts and lists; sphere_radius: build with SphereInsertOp of that radius."""
     P = np.ascontiguousarray(points, np.float32).reshape(-1, 3)
     n = len(P)
     with tempfile.TemporaryDirectory() as d:
@@ -87,6 +143,8 @@ def run_dump(points, lo, hi, rc, box, timeout=300, exact_only=False):
                 repr(float(rc)), *[repr(float(x)) for x in box], prefix]
         if exact_only:
             args.append("exact_only")
+        elif sphere_radius is not None:
+            args += ["sphere", repr(float(sphere_radius))]
         r = subprocess.run(args, capture_output=True, text=True, timeout=timeout)
         if r.returncode != 0:
             raise RuntimeError(f"reference driver failed ({r.returncode}): {r.stderr.strip()[-400:]}")

@@ -8,8 +8,15 @@
 // (include/neighbor/LBVHTraverser.h:378-390,481-510) and traverse (:414-450).  The sort is CUB's,
 // called exactly as the reference calls it (include/neighbor/kernels/LBVH.cuh:421-443).
 //
-//   ref_driver bench N steps warmup rc          time the plain two-pass step on uniform frames
-//   ref_driver dump  in.f32 N lo3 hi3 rc L3 out  write the reference's outputs for given points
+//   ref_driver bench N steps warmup rc               time the plain two-pass step on uniform
+//                                                    trajectory frames, every block size 32..1024
+//   ref_driver frames in.f32 N F rc L steps warmup   the same step on F given frames (cycled)
+//   ref_driver poly s.f32 Ns l.f32 Nl F L steps warmup   two-tree polydisperse step (diameters 1
+//                                                    and 10, cutoff (di+dj)/2 + 0.4) on F frames
+//   ref_driver dump  in.f32 N lo3 hi3 rc L3 out [exact_only | sphere r]
+//                                                    write the reference's outputs for given
+//                                                    points (sphere r: a SphereInsertOp tree)
+//   ref_driver hash  in.f32 N rc L out               counts and per-row hashes of the exact list
 //
 // Kernel parameters are passed as byte images of the reference's structs; the layouts below are
 // asserted here and, against the reference's own definitions, in ref_kernels.cu.
@@ -30,6 +37,7 @@
 namespace
 {
 struct PointInsertOp { const float3* points; unsigned int N; };
+struct SphereInsertOp { const float3* points; float r; unsigned int N; };
 struct LBVHData { int* parent; int* left; int* right; unsigned int* primitive; float3* lo; float3* hi; int root; };
 struct LBVHCompressedData { int root; int4* data; float3* lo; float3* hi; float3* bins; };
 struct CountNeighborsOp { unsigned int* nneigh; };
@@ -40,6 +48,8 @@ struct NullTransformOp {};
 struct RefExactQueryOp { const float4* spheres; unsigned int N; const float3* points; float3 box; float pad; };
 
 static_assert(sizeof(PointInsertOp) == 16 && offsetof(PointInsertOp, N) == 8, "layout");
+static_assert(sizeof(SphereInsertOp) == 16 && offsetof(SphereInsertOp, r) == 8 && offsetof(SphereInsertOp, N) == 12,
+              "layout");
 static_assert(sizeof(LBVHData) == 56 && offsetof(LBVHData, root) == 48, "layout");
 static_assert(sizeof(LBVHCompressedData) == 40 && offsetof(LBVHCompressedData, data) == 8, "layout");
 static_assert(sizeof(CountNeighborsOp) == 8, "layout");
@@ -62,6 +72,7 @@ void checkd(CUresult e, const char* what)
 struct Kernels
     {
     CUfunction gen_codes = nullptr, gen_tree = nullptr, bubble = nullptr, one = nullptr, compress = nullptr;
+    CUfunction gen_codes_sph = nullptr, bubble_sph = nullptr, one_sph = nullptr;
     CUfunction count_stock = nullptr, count_exact = nullptr, list_exact = nullptr, list_stock = nullptr;
     };
 
@@ -83,10 +94,11 @@ Kernels load_kernels(const char* cubin)
         CUfunction f;
         checkd(cuModuleGetFunction(&f, mod, name), "get function");
         auto has = [&](const char* x) { return s.find(x) != std::string::npos; };
-        if (has("lbvh_gen_codes")) k.gen_codes = f;
+        const bool sph = has("SphereInsertOp");
+        if (has("lbvh_gen_codes")) (sph ? k.gen_codes_sph : k.gen_codes) = f;
         else if (has("lbvh_gen_tree")) k.gen_tree = f;
-        else if (has("lbvh_bubble_aabbs")) k.bubble = f;
-        else if (has("lbvh_one_primitive")) k.one = f;
+        else if (has("lbvh_bubble_aabbs")) (sph ? k.bubble_sph : k.bubble) = f;
+        else if (has("lbvh_one_primitive")) (sph ? k.one_sph : k.one) = f;
         else if (has("lbvh_compress_ropes")) k.compress = f;
         else if (has("lbvh_traverse_ropes") && has("CountNeighborsOp") && has("SphereQueryOp")) k.count_stock = f;
         else if (has("lbvh_traverse_ropes") && has("CountNeighborsOp") && has("RefExactQueryOp")) k.count_exact = f;
@@ -94,7 +106,7 @@ Kernels load_kernels(const char* cubin)
         else if (has("lbvh_traverse_ropes") && has("NeighborListOp") && has("SphereQueryOp")) k.list_stock = f;
         }
     if (!k.gen_codes || !k.gen_tree || !k.bubble || !k.one || !k.compress || !k.count_stock || !k.count_exact || !k.list_exact
-        || !k.list_stock)
+        || !k.list_stock || !k.gen_codes_sph || !k.bubble_sph || !k.one_sph)
         { fprintf(stderr, "reference kernels missing from %s\n", cubin); exit(3); }
     return k;
     }
@@ -160,22 +172,27 @@ struct RefTree
         return t;
         }
 
-    // LBVH::build (include/neighbor/LBVH.h:242-318)
-    void build(const Kernels& K, const float3* pts, float3 slo, float3 shi, unsigned int bs, cudaStream_t s)
+    // LBVH::build (include/neighbor/LBVH.h:242-318) with PointInsertOp, or SphereInsertOp of
+    // radius r when r >= 0
+    void build(const Kernels& K, const float3* pts, float3 slo, float3 shi, unsigned int bs, cudaStream_t s,
+               float r = -1.f)
         {
         PointInsertOp ins{pts, N};
+        SphereInsertOp sins{pts, r, N};
+        const bool sphere = r >= 0.f;
+        void* insp = sphere ? (void*)&sins : (void*)&ins;
         sel_codes = sel_idx = 0;
         if (N == 1)
             {
             LBVHData t = tree_data();
-            void* a[] = {&t, &ins};
-            checkd(cuLaunchKernel(K.one, 1, 1, 1, 1, 1, 1, 0, (CUstream)s, a, nullptr), "launch");
+            void* a[] = {&t, insp};
+            checkd(cuLaunchKernel(sphere ? K.one_sph : K.one, 1, 1, 1, 1, 1, 1, 0, (CUstream)s, a, nullptr), "launch");
             return;
             }
         unsigned int n = N;
             {
-            void* a[] = {&codes[0], &idx[0], &ins, &slo, &shi, &n};
-            launch(K.gen_codes, n, bs, s, a);
+            void* a[] = {&codes[0], &idx[0], insp, &slo, &shi, &n};
+            launch(sphere ? K.gen_codes_sph : K.gen_codes, n, bs, s, a);
             }
         cub::DoubleBuffer<unsigned int> k(codes[0], codes[1]), v(idx[0], idx[1]);
         check(cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, k, v, (int)n, 0, 30, s), "sort");
@@ -189,8 +206,8 @@ struct RefTree
             }
         check(cudaMemsetAsync(locks, 0, (size_t)(n - 1) * 4, s), "memset");
             {
-            void* a[] = {&t, &ins, &locks, &n};
-            launch(K.bubble, n, bs, s, a);
+            void* a[] = {&t, insp, &locks, &n};
+            launch(sphere ? K.bubble_sph : K.bubble, n, bs, s, a);
             }
         }
 
@@ -242,12 +259,12 @@ __global__ void k_move(const float3* in, float3* out, unsigned int n, float L, f
     }
 
 // Query spheres in the tree's sorted order (the reference benchmark's query order,
-// benchmark/lbvh_benchmark.cc:177-184).
+// benchmark/lbvh_benchmark.cc:177-184), or in input order when prim is null.
 __global__ void k_spheres(const float3* p, const unsigned int* prim, float4* sph, unsigned int n, float rc)
     {
     const unsigned int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const float3 x = p[prim[i]];
+    const float3 x = p[prim ? prim[i] : i];
     sph[i] = make_float4(x.x, x.y, x.z, rc);
     }
 
@@ -267,82 +284,138 @@ void images27(float3 L, std::vector<float3>& img)
                 img.push_back(make_float3(L.x * (float)ix, L.y * (float)iy, L.z * (float)iz));
     }
 
-int run_bench(const Kernels& K, unsigned int n, int steps, int warmup, float rc)
+// Block sizes the reference's tunables accept (LBVH.h:225, LBVHTraverser.h:358: 32..1024 by 32).
+std::vector<unsigned int> all_blocks()
     {
-    const float L = std::cbrt(n / 0.85f);
-    const float3 box = make_float3(L, L, L);
-    cudaStream_t s;
-    check(cudaStreamCreate(&s), "stream");
-    std::vector<float3*> frames(steps + warmup);
-    float3* base;
-    check(cudaMalloc(&base, (size_t)n * 12), "alloc");
-    k_uniform<<<(n + 255) / 256, 256, 0, s>>>(base, n, L, 1234u);
-    const float3* prev = base;
-    for (size_t f = 0; f < frames.size(); ++f)
+    std::vector<unsigned int> b;
+    for (unsigned int bs = 32; bs <= 1024; bs += 32) b.push_back(bs);
+    return b;
+    }
+
+// Buffers of one plain two-pass list: query spheres, counts, list, CUB max.
+struct TwoPass
+    {
+    unsigned int n = 0, cap = 0;
+    float4* sph = nullptr;
+    unsigned int *nn = nullptr, *list = nullptr, *dmax = nullptr;
+    void* rtmp = nullptr;
+    size_t rtmp_bytes = 0;
+    void allocate(unsigned int q, unsigned int list_cap)
         {
-        check(cudaMalloc(&frames[f], (size_t)n * 12), "alloc");
-        k_move<<<(n + 255) / 256, 256, 0, s>>>(prev, frames[f], n, L, 0.05f, 77u + (unsigned)f);
-        prev = frames[f];
+        n = q;
+        cap = list_cap;
+        check(cudaMalloc(&sph, (size_t)std::max(q, 1u) * 16), "alloc");
+        check(cudaMalloc(&nn, (size_t)std::max(q, 1u) * 4), "alloc");
+        check(cudaMalloc(&dmax, 4), "alloc");
+        check(cudaMalloc(&list, (size_t)std::max(q, 1u) * cap * 4), "alloc");
+        check(cub::DeviceReduce::Max(nullptr, rtmp_bytes, nn, dmax, (int)std::max(q, 1u)), "reduce size");
+        check(cudaMalloc(&rtmp, rtmp_bytes), "alloc");
         }
+    };
+
+// The reference's two-pass list for one set of queries (benchmark/lbvh_benchmark.cc's traversal
+// with CountNeighborsOp, the host read of the largest count, then NeighborListOp of that stride;
+// include/neighbor/OutputOps.h:28-176): count, CUB max, host read, fill.  Returns the largest
+// count.
+unsigned int two_pass(const Kernels& K, const LBVHCompressedData& c, const RefExactQueryOp& q, const ImageListOp& im,
+                      TwoPass& b, unsigned int bs, cudaStream_t s, cudaEvent_t after_count = nullptr)
+    {
+    if (q.N == 0) return 0;
+        {
+        CountNeighborsOp out{b.nn};
+        void* a[] = {&out, (void*)&c, (void*)&q, (void*)&im};
+        launch(K.count_exact, q.N, bs, s, a);
+        }
+    if (after_count) check(cudaEventRecord(after_count, s), "rec");
+    check(cub::DeviceReduce::Max(b.rtmp, b.rtmp_bytes, b.nn, b.dmax, (int)q.N, s), "reduce");
+    unsigned int mx = 0;
+    check(cudaMemcpyAsync(&mx, b.dmax, 4, cudaMemcpyDeviceToHost, s), "copy");
+    check(cudaStreamSynchronize(s), "sync");
+    if (mx > b.cap)
+        {
+        // a longer row than any before: the list buffer grows (in the warm-up steps of a sweep)
+        check(cudaFree(b.list), "free");
+        b.cap = mx + mx / 4u;
+        check(cudaMalloc(&b.list, (size_t)b.n * b.cap * 4), "alloc");
+        }
+        {
+        NeighborListOp out{b.list, b.nn, std::max(mx, 1u)};
+        void* a[] = {&out, (void*)&c, (void*)&q, (void*)&im};
+        launch(K.list_exact, q.N, bs, s, a);
+        }
+    return mx;
+    }
+
+unsigned long long sum_counts(const unsigned int* d, unsigned int n)
+    {
+    std::vector<unsigned int> h(n);
+    check(cudaMemcpy(h.data(), d, (size_t)n * 4, cudaMemcpyDeviceToHost), "copy");
+    unsigned long long t = 0;
+    for (unsigned int x : h) t += x;
+    return t;
+    }
+
+float* read_points(const char* path, size_t count)
+    {
+    std::vector<float> h(count * 3);
+    FILE* f = fopen(path, "rb");
+    if (!f || fread(h.data(), 12, count, f) != count) { fprintf(stderr, "cannot read %s\n", path); exit(5); }
+    fclose(f);
+    float* d;
+    check(cudaMalloc(&d, std::max<size_t>(count, 1) * 12), "alloc");
+    check(cudaMemcpy(d, h.data(), count * 12, cudaMemcpyHostToDevice), "copy");
+    return d;
+    }
+
+float3* image_list(float L)
+    {
     std::vector<float3> himg;
-    images27(box, himg);
+    images27(make_float3(L, L, L), himg);
     float3* img;
     check(cudaMalloc(&img, 27 * 12), "alloc");
     check(cudaMemcpy(img, himg.data(), 27 * 12, cudaMemcpyHostToDevice), "copy");
+    return img;
+    }
+
+// Plain two-pass step of one point tree queried by its own points in sorted order (the reference
+// benchmark's query order, benchmark/lbvh_benchmark.cc:177-184) on frames[it % F], timed per
+// block size over `steps` steps after `warmup`.  Prints one JSON object.
+int sweep_self(const Kernels& K, const std::vector<const float3*>& frames, unsigned int n, float rc, float L, int steps,
+               int warmup, const char* label)
+    {
+    const float3 box = make_float3(L, L, L);
+    cudaStream_t s;
+    check(cudaStreamCreate(&s), "stream");
+    float3* img = image_list(L);
     RefTree T;
     T.allocate(n);
-    float4* sph;
-    unsigned int *nn, *list, *dmax;
-    check(cudaMalloc(&sph, (size_t)n * 16), "alloc");
-    check(cudaMalloc(&nn, (size_t)n * 4), "alloc");
-    check(cudaMalloc(&dmax, 4), "alloc");
-    const unsigned int cap = 64;
-    check(cudaMalloc(&list, (size_t)n * cap * 4), "alloc");
-    void* rtmp = nullptr;
-    size_t rtmp_bytes = 0;
-    check(cub::DeviceReduce::Max(nullptr, rtmp_bytes, nn, dmax, (int)n), "reduce size");
-    check(cudaMalloc(&rtmp, rtmp_bytes), "alloc");
+    TwoPass b;
+    b.allocate(n, 96);
     const float pad = exact_pad(rc, 2 * L);
     check(cudaStreamSynchronize(s), "sync");
-
-    printf("{\"impl\": \"reference-cuda\", \"n\": %u, \"rc\": %g, \"steps\": %d, \"results\": [", n, rc, steps);
-    const unsigned int blocks[] = {32, 64, 128, 256, 512};
+    printf("{\"impl\": \"reference-cuda\", \"workload\": \"%s\", \"n\": %u, \"rc\": %g, \"steps\": %d, \"warmup\": %d, "
+           "\"results\": [", label, n, rc, steps, warmup);
     bool first = true;
-    for (unsigned int bs : blocks)
+    double pairs_sum = 0;
+    for (unsigned int bs : all_blocks())
         {
         cudaEvent_t ev[6];
         for (auto& e : ev) check(cudaEventCreate(&e), "event");
-        double t_build = 0, t_setup = 0, t_count = 0, t_fill = 0, t_total = 0, pairs = 0;
+        std::vector<double> step_ms;
+        double t_build = 0, t_setup = 0, t_count = 0, t_fill = 0;
         for (int it = 0; it < warmup + steps; ++it)
             {
             const bool timed = it >= warmup;
-            const float3* P = frames[it];
+            const float3* P = frames[it % frames.size()];
             check(cudaEventRecord(ev[0], s), "rec");
             T.build(K, P, make_float3(0, 0, 0), box, bs, s);
-            k_spheres<<<(n + 255) / 256, 256, 0, s>>>(P, T.idx[T.sel_idx], sph, n, rc);
+            k_spheres<<<(n + 255) / 256, 256, 0, s>>>(P, T.idx[T.sel_idx], b.sph, n, rc);
             check(cudaEventRecord(ev[1], s), "rec");
             LBVHCompressedData c = T.compress(K, bs, s);
             check(cudaEventRecord(ev[2], s), "rec");
-            RefExactQueryOp q{sph, n, P, box, pad};
-            // the exact op refines against the points indexed by primitive id: the input order
+            RefExactQueryOp q{b.sph, n, P, box, pad};
             ImageListOp im{img, 27};
-                {
-                CountNeighborsOp out{nn};
-                void* a[] = {&out, &c, &q, &im};
-                launch(K.count_exact, n, bs, s, a);
-                }
-            check(cudaEventRecord(ev[3], s), "rec");
-            check(cub::DeviceReduce::Max(rtmp, rtmp_bytes, nn, dmax, (int)n, s), "reduce");
-            unsigned int mx = 0;
-            check(cudaMemcpyAsync(&mx, dmax, 4, cudaMemcpyDeviceToHost, s), "copy");
-            check(cudaStreamSynchronize(s), "sync");
-            if (mx > cap) { fprintf(stderr, "max neighbors %u exceeds %u\n", mx, cap); return 4; }
-            check(cudaEventRecord(ev[4], s), "rec");
-                {
-                NeighborListOp out{list, nn, mx};
-                void* a[] = {&out, &c, &q, &im};
-                launch(K.list_exact, n, bs, s, a);
-                }
+            two_pass(K, c, q, im, b, bs, s, ev[3]);
             check(cudaEventRecord(ev[5], s), "rec");
             check(cudaStreamSynchronize(s), "sync");
             if (timed)
@@ -351,26 +424,194 @@ int run_bench(const Kernels& K, unsigned int n, int steps, int warmup, float rc)
                 cudaEventElapsedTime(&ms, ev[0], ev[1]); t_build += ms;
                 cudaEventElapsedTime(&ms, ev[1], ev[2]); t_setup += ms;
                 cudaEventElapsedTime(&ms, ev[2], ev[3]); t_count += ms;
-                cudaEventElapsedTime(&ms, ev[4], ev[5]); t_fill += ms;
-                cudaEventElapsedTime(&ms, ev[0], ev[5]); t_total += ms;
-                std::vector<unsigned int> h(n);
-                check(cudaMemcpy(h.data(), nn, (size_t)n * 4, cudaMemcpyDeviceToHost), "copy");
-                for (unsigned int x : h) pairs += x;
+                cudaEventElapsedTime(&ms, ev[3], ev[5]); t_fill += ms;
+                cudaEventElapsedTime(&ms, ev[0], ev[5]); step_ms.push_back(ms);
+                // pairs of every timed frame, counted with the first block size (the same frames
+                // for every block size)
+                if (first) pairs_sum += (double)sum_counts(b.nn, n);
                 }
             }
-        printf("%s{\"block\": %u, \"build_ms\": %.4f, \"spheres_and_build_ms\": %.4f, \"setup_ms\": %.4f, \"count_ms\": %.4f, "
-               "\"fill_ms\": %.4f, \"step_ms\": %.4f, \"pairs_per_step\": %.1f}",
-               first ? "" : ", ", bs, t_build / steps, t_build / steps, t_setup / steps, t_count / steps, t_fill / steps,
-               t_total / steps, pairs / steps);
+        double mean = 0;
+        for (double v : step_ms) mean += v;
+        mean /= step_ms.size();
+        std::vector<double> sorted = step_ms;
+        std::sort(sorted.begin(), sorted.end());
+        printf("%s{\"block\": %u, \"build_ms\": %.4f, \"setup_ms\": %.4f, \"count_ms\": %.4f, \"fill_ms\": %.4f, "
+               "\"step_ms\": %.4f, \"step_ms_median\": %.4f}",
+               first ? "" : ", ", bs, t_build / steps, t_setup / steps, t_count / steps, t_fill / steps, mean,
+               sorted[sorted.size() / 2]);
         first = false;
         for (auto& e : ev) cudaEventDestroy(e);
         }
-    printf("]}\n");
+    printf("], \"pairs_per_step\": %.1f}\n", pairs_sum / steps);
+    return 0;
+    }
+
+int run_bench(const Kernels& K, unsigned int n, int steps, int warmup, float rc)
+    {
+    const float L = std::cbrt(n / 0.85f);
+    std::vector<const float3*> frames;
+    float3* base;
+    check(cudaMalloc(&base, (size_t)n * 12), "alloc");
+    k_uniform<<<(n + 255) / 256, 256>>>(base, n, L, 1234u);
+    const float3* prev = base;
+    for (int f = 0; f < steps + warmup; ++f)
+        {
+        float3* p;
+        check(cudaMalloc(&p, (size_t)n * 12), "alloc");
+        k_move<<<(n + 255) / 256, 256>>>(prev, p, n, L, 0.05f, 77u + (unsigned)f);
+        frames.push_back(p);
+        prev = p;
+        }
+    check(cudaDeviceSynchronize(), "sync");
+    return sweep_self(K, frames, n, rc, L, steps, warmup, "uniform trajectory (sigma 0.05)");
+    }
+
+int run_frames(const Kernels& K, const char* path, unsigned int n, int F, float rc, float L, int steps, int warmup)
+    {
+    float* all = read_points(path, (size_t)n * F);
+    std::vector<const float3*> frames;
+    for (int f = 0; f < F; ++f) frames.push_back(reinterpret_cast<const float3*>(all) + (size_t)f * n);
+    return sweep_self(K, frames, n, rc, L, steps, warmup, "given frames");
+    }
+
+// Polydisperse step: a tree per species (PointInsertOp), every (query species, tree) pair listed
+// with cutoff (d_i + d_j)/2 + 0.4: self pairs query the tree's points in sorted order, cross pairs
+// the other species' points in input order.
+int run_poly(const Kernels& K, const char* spath, unsigned int ns, const char* lpath, unsigned int nl, int F, float L,
+             int steps, int warmup)
+    {
+    float* sp = read_points(spath, (size_t)ns * F);
+    float* lp = read_points(lpath, (size_t)nl * F);
+    const float3 box = make_float3(L, L, L);
+    const float diam[2] = {1.0f, 10.0f};
+    const unsigned int cnt[2] = {ns, nl};
+    cudaStream_t s;
+    check(cudaStreamCreate(&s), "stream");
+    float3* img = image_list(L);
+    RefTree T[2];
+    T[0].allocate(ns);
+    T[1].allocate(nl);
+    TwoPass b[2][2];
+    for (int i = 0; i < 2; ++i)
+        for (int j = 0; j < 2; ++j) b[i][j].allocate(cnt[i], (i == 0 && j == 0) ? 64u : 4096u);
+    printf("{\"impl\": \"reference-cuda\", \"workload\": \"polydisperse\", \"n_small\": %u, \"n_large\": %u, "
+           "\"steps\": %d, \"warmup\": %d, \"results\": [", ns, nl, steps, warmup);
+    bool first = true;
+    double pairs = 0;
+    for (unsigned int bs : all_blocks())
+        {
+        cudaEvent_t e0, e1;
+        check(cudaEventCreate(&e0), "event");
+        check(cudaEventCreate(&e1), "event");
+        std::vector<double> step_ms;
+        for (int it = 0; it < warmup + steps; ++it)
+            {
+            const int f = it % F;
+            const float3* P[2] = {reinterpret_cast<const float3*>(sp) + (size_t)f * ns,
+                                  reinterpret_cast<const float3*>(lp) + (size_t)f * nl};
+            check(cudaEventRecord(e0, s), "rec");
+            LBVHCompressedData c[2];
+            for (int j = 0; j < 2; ++j)
+                {
+                T[j].build(K, P[j], make_float3(0, 0, 0), box, bs, s);
+                c[j] = T[j].compress(K, bs, s);
+                }
+            double step_pairs = 0;
+            for (int i = 0; i < 2; ++i)
+                for (int j = 0; j < 2; ++j)
+                    {
+                    const float R = 0.5f * (diam[i] + diam[j]) + 0.4f;
+                    if (i == j)
+                        k_spheres<<<(cnt[i] + 255) / 256, 256, 0, s>>>(P[j], T[j].idx[T[j].sel_idx], b[i][j].sph, cnt[i], R);
+                    else
+                        k_spheres<<<(cnt[i] + 255) / 256, 256, 0, s>>>(P[i], nullptr, b[i][j].sph, cnt[i], R);
+                    RefExactQueryOp q{b[i][j].sph, cnt[i], P[j], box, exact_pad(R, 2 * L)};
+                    ImageListOp im{img, 27};
+                    two_pass(K, c[j], q, im, b[i][j], bs, s);
+                    }
+            check(cudaEventRecord(e1, s), "rec");
+            check(cudaStreamSynchronize(s), "sync");
+            if (it >= warmup)
+                {
+                float ms;
+                cudaEventElapsedTime(&ms, e0, e1);
+                step_ms.push_back(ms);
+                if (first)
+                    for (int i = 0; i < 2; ++i)
+                        for (int j = 0; j < 2; ++j) step_pairs += (double)sum_counts(b[i][j].nn, cnt[i]);
+                pairs += step_pairs;
+                }
+            }
+        double mean = 0;
+        for (double v : step_ms) mean += v;
+        mean /= step_ms.size();
+        std::sort(step_ms.begin(), step_ms.end());
+        printf("%s{\"block\": %u, \"step_ms\": %.4f, \"step_ms_median\": %.4f}", first ? "" : ", ", bs, mean,
+               step_ms[step_ms.size() / 2]);
+        first = false;
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        }
+    printf("], \"pairs_per_step\": %.1f}\n", pairs / steps);
+    return 0;
+    }
+
+// Row hash of a neighbor list, sum over k < count of (entry_k + 1) * C_k plus count * C_count, in
+// 64-bit integers (no overflow for rows of up to 64 entries): C_k = ((k + 1) * 2654435761 mod 2^32)
+// with the top bit cleared and the low bit set; C_count = 0x2545F491.
+__global__ void k_row_hash(const unsigned int* list, const unsigned int* nn, unsigned int stride, unsigned int n,
+                           unsigned long long* out)
+    {
+    const unsigned int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const unsigned int c = nn[i];
+    unsigned long long h = (unsigned long long)c * 0x2545F491ull;
+    for (unsigned int k = 0; k < c && k < stride; ++k)
+        {
+        const unsigned long long ck = (((k + 1u) * 2654435761u) & 0x7fffffffu) | 1u;
+        h += (unsigned long long)(list[(size_t)i * stride + k] + 1u) * ck;
+        }
+    out[i] = h;
+    }
+
+// Counts and row hashes of the exact neighbor list of the given points (queries in input order,
+// 27 images of the cube of side L), for comparing a large list with the library's row by row.
+int run_hash(const Kernels& K, const char* path, unsigned int n, float rc, float L, const char* out_prefix)
+    {
+    float* P = read_points(path, n);
+    const float3 box = make_float3(L, L, L);
+    RefTree T;
+    T.allocate(n);
+    T.build(K, reinterpret_cast<const float3*>(P), make_float3(0, 0, 0), box, 128, 0);
+    LBVHCompressedData c = T.compress(K, 128, 0);
+    float3* img = image_list(L);
+    TwoPass b;
+    b.allocate(n, 64);
+    k_spheres<<<(n + 255) / 256, 256>>>(reinterpret_cast<const float3*>(P), nullptr, b.sph, n, rc);
+    RefExactQueryOp q{b.sph, n, reinterpret_cast<const float3*>(P), box, exact_pad(rc, 2 * L)};
+    ImageListOp im{img, 27};
+    const unsigned int mx = two_pass(K, c, q, im, b, 128, 0);
+    unsigned long long* h;
+    check(cudaMalloc(&h, (size_t)n * 8), "alloc");
+    k_row_hash<<<(n + 255) / 256, 256>>>(b.list, b.nn, std::max(mx, 1u), n, h);
+    check(cudaDeviceSynchronize(), "sync");
+    auto dump = [&](const char* name, const void* ptr, size_t bytes) {
+        std::string fn = std::string(out_prefix) + "." + name;
+        std::vector<char> buf(bytes);
+        check(cudaMemcpy(buf.data(), ptr, bytes, cudaMemcpyDefault), "copy");
+        FILE* o = fopen(fn.c_str(), "wb");
+        fwrite(buf.data(), 1, bytes, o);
+        fclose(o);
+    };
+    dump("count", b.nn, (size_t)n * 4);
+    dump("hash", h, (size_t)n * 8);
+    printf("{\"hashed\": %u, \"max_count\": %u}\n", n, mx);
     return 0;
     }
 
 int run_dump(const Kernels& K, const char* in_path, unsigned int n, float3 slo, float3 shi, float rc, float3 box,
-             const char* out_prefix, bool exact_only)
+             const char* out_prefix, bool exact_only, float sphere_r)
     {
     std::vector<float3> hp(n);
     FILE* f = fopen(in_path, "rb");
@@ -383,7 +624,7 @@ int run_dump(const Kernels& K, const char* in_path, unsigned int n, float3 slo, 
     T.allocate(n);
     unsigned int list_stride = 0, stock_stride = 0;
     unsigned int *list_s = nullptr, *c_list_s = nullptr;
-    T.build(K, P, slo, shi, 32, 0);
+    T.build(K, P, slo, shi, 32, 0, sphere_r);
     LBVHCompressedData c = T.compress(K, 32, 0);
     std::vector<float3> himg;
     images27(box, himg);
@@ -481,13 +722,22 @@ int main(int argc, char** argv)
     const std::string mode = argv[1];
     if (mode == "bench" && argc >= 6)
         return run_bench(K, (unsigned int)atol(argv[2]), atoi(argv[3]), atoi(argv[4]), (float)atof(argv[5]));
+    if (mode == "frames" && argc >= 9)
+        return run_frames(K, argv[2], (unsigned int)atol(argv[3]), atoi(argv[4]), (float)atof(argv[5]),
+                          (float)atof(argv[6]), atoi(argv[7]), atoi(argv[8]));
+    if (mode == "poly" && argc >= 10)
+        return run_poly(K, argv[2], (unsigned int)atol(argv[3]), argv[4], (unsigned int)atol(argv[5]), atoi(argv[6]),
+                        (float)atof(argv[7]), atoi(argv[8]), atoi(argv[9]));
+    if (mode == "hash" && argc >= 7)
+        return run_hash(K, argv[2], (unsigned int)atol(argv[3]), (float)atof(argv[4]), (float)atof(argv[5]), argv[6]);
     if (mode == "dump" && argc >= 15)
         return run_dump(K, argv[2], (unsigned int)atol(argv[3]),
                         make_float3((float)atof(argv[4]), (float)atof(argv[5]), (float)atof(argv[6])),
                         make_float3((float)atof(argv[7]), (float)atof(argv[8]), (float)atof(argv[9])),
                         (float)atof(argv[10]),
                         make_float3((float)atof(argv[11]), (float)atof(argv[12]), (float)atof(argv[13])), argv[14],
-                        argc >= 16 && std::string(argv[15]) == "exact_only");
+                        argc >= 16 && std::string(argv[15]) == "exact_only",
+                        (argc >= 17 && std::string(argv[15]) == "sphere") ? (float)atof(argv[16]) : -1.f);
     fprintf(stderr, "bad arguments\n");
     return 1;
     }

@@ -53,6 +53,8 @@ struct RefExactQueryOp
 
 // Kernel-parameter layouts the driver mirrors (ref_driver.cu asserts the same numbers).
 static_assert(sizeof(neighbor::PointInsertOp) == 16 && offsetof(neighbor::PointInsertOp, N) == 8, "PointInsertOp layout");
+static_assert(sizeof(neighbor::SphereInsertOp) == 16 && offsetof(neighbor::SphereInsertOp, r) == 8
+              && offsetof(neighbor::SphereInsertOp, N) == 12, "SphereInsertOp layout");
 static_assert(sizeof(neighbor::LBVHData) == 56 && offsetof(neighbor::LBVHData, root) == 48, "LBVHData layout");
 static_assert(sizeof(neighbor::ConstLBVHData) == 56 && offsetof(neighbor::ConstLBVHData, root) == 48, "ConstLBVHData layout");
 static_assert(sizeof(neighbor::LBVHCompressedData) == 40 && offsetof(neighbor::LBVHCompressedData, data) == 8, "LBVHCompressedData layout");
@@ -75,6 +77,11 @@ template __global__ void lbvh_gen_codes<PointInsertOp>(unsigned int*, unsigned i
 template __global__ void lbvh_bubble_aabbs<PointInsertOp>(const LBVHData, const PointInsertOp, unsigned int*,
                                                           const unsigned int);
 template __global__ void lbvh_one_primitive<PointInsertOp>(const LBVHData, const PointInsertOp);
+template __global__ void lbvh_gen_codes<SphereInsertOp>(unsigned int*, unsigned int*, const SphereInsertOp, const float3,
+                                                        const float3, const unsigned int);
+template __global__ void lbvh_bubble_aabbs<SphereInsertOp>(const LBVHData, const SphereInsertOp, unsigned int*,
+                                                           const unsigned int);
+template __global__ void lbvh_one_primitive<SphereInsertOp>(const LBVHData, const SphereInsertOp);
 template __global__ void lbvh_compress_ropes<NullTransformOp>(const LBVHCompressedData, const NullTransformOp,
                                                               const ConstLBVHData, const unsigned int, const unsigned int);
 template __global__ void lbvh_traverse_ropes<CountNeighborsOp, SphereQueryOp, ImageListOp<float3>>(

@@ -119,8 +119,22 @@ def test_validate_superset_and_exact(kats):
     assert int(w) == fx["weighted_checksum"]
 
 
+def fp32_disagreement_bound(pi, pj, rc, L):
+    """Largest |r - rc| at which the FP32 minimum-image predicate may decide a pair differently
+    from FP64: 1 ulp(rc), plus, for every axis on which the pair wraps, half an ulp of the FP32
+    difference pj - pi that is rounded before the wrap subtracts L (about L)."""
+    rc = np.float32(rc)
+    d = np.abs(np.asarray(pj, np.float32) - np.asarray(pi, np.float32))
+    Lf = np.asarray(L, np.float32)
+    wraps = (Lf > 0) & (d >= np.float32(0.5) * Lf)
+    extra = np.sqrt(np.sum(np.where(wraps, (0.5 * np.spacing(np.maximum(d, 1e-30).astype(np.float32))) ** 2, 0.0),
+                           axis=-1))
+    return float(np.spacing(rc)) + extra
+
+
 def test_fp64_disagreements_within_one_ulp():
-    # Pairs where FP32 and FP64 decide differently must lie within ~1 ulp of rc.
+    # Pairs where FP32 and FP64 decide differently must lie within 1 ulp of rc (plus the rounding
+    # of a wrapped difference for pairs across the periodic boundary).
     rng = np.random.default_rng(7)
     L = np.float32(12.0)
     P = (rng.random((3000, 3)) * L).astype(np.float32)
@@ -133,5 +147,61 @@ def test_fp64_disagreements_within_one_ulp():
             d = O.pair_distance_minus_rc_f64(P[i], P[j], rc, [L, L, L])
             if (d <= 0) != (j in s):
                 n_flag += 1
-                assert abs(d) < 4 * np.spacing(rc), (i, j, d)
+                assert abs(d) < fp32_disagreement_bound(P[i], P[j], rc, [L, L, L]), (i, j, d)
     assert n_flag < 5
+
+
+def test_fp32_predicate_disagrees_with_fp64_only_within_one_ulp():
+    # Adversarial pairs: distances within 3 ulp of rc in random directions, coordinates up to
+    # 270 (the benchmark's box).  The FP32 predicate's operation order (d = pj - pi, squares,
+    # ((dx*dx + dy*dy) + dz*dz) <= rc*rc, all rounded to nearest) must agree with the exact
+    # FP64 distance on every pair farther than 1 ulp(rc) from the cutoff.
+    rng = np.random.default_rng(17)
+    rc = np.float32(1.3)
+    rc2 = np.float32(rc * rc)
+    ulp = np.float64(np.spacing(rc))
+    n_dis = 0
+    for L in (12.0, 270.25):
+        pi = (rng.random((400000, 3)) * L).astype(np.float32)
+        u = rng.normal(size=pi.shape)
+        u /= np.linalg.norm(u, axis=1, keepdims=True)
+        r = np.float64(rc) + rng.uniform(-3, 3, len(pi)) * ulp
+        pj = (pi.astype(np.float64) + u * r[:, None]).astype(np.float32)
+        d = pj - pi
+        f32 = ((d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1]) + d[:, 2] * d[:, 2]) <= rc2
+        rd = np.sqrt(((pj.astype(np.float64) - pi.astype(np.float64)) ** 2).sum(1))
+        dis = f32 != (rd <= np.float64(rc))
+        n_dis += int(dis.sum())
+        assert np.all(np.abs(rd[dis] - np.float64(rc)) < ulp)
+    assert n_dis > 1000   # the pairs do reach the cutoff's rounding
+
+
+@pytest.mark.parametrize("L", [12.0, 33.78, 270.25])
+def test_wrapped_pairs_disagree_within_the_wrap_bound(L):
+    # Pairs across the periodic boundary: the FP32 difference pj - pi (up to about L) is rounded
+    # before the wrap, so FP32 and FP64 (with the same FP32 box length) may differ by up to half
+    # an ulp of it per wrapped axis on top of 1 ulp(rc) -- and no further.
+    rng = np.random.default_rng(int(L * 100))
+    rc = np.float32(1.3)
+    rc2 = np.float32(rc * rc)
+    Lf = np.float32(L)
+    h = np.float32(0.5) * Lf
+    n = 300000
+    pi = (rng.random((n, 3)) * L).astype(np.float32)
+    pi[:, 0] = (rng.random(n) * 1.3).astype(np.float32)   # next to the x = 0 face
+    u = rng.normal(size=(n, 3))
+    u[:, 0] = -np.abs(u[:, 0]) - 0.3                     # partners across it
+    u /= np.linalg.norm(u, axis=1, keepdims=True)
+    r = np.float64(rc) + rng.uniform(-300, 300, n) * np.spacing(rc)
+    pj = np.mod(pi.astype(np.float64) + u * r[:, None], np.float64(Lf)).astype(np.float32)
+    pj = np.where(pj >= Lf, np.float32(0), pj)
+    d = pj - pi
+    d = np.where(d >= h, d - Lf, np.where(d < -h, d + Lf, d))
+    f32 = ((d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1]) + d[:, 2] * d[:, 2]) <= rc2
+    dd = pj.astype(np.float64) - pi.astype(np.float64)
+    dd -= np.float64(Lf) * np.round(dd / np.float64(Lf))
+    rd = np.sqrt((dd * dd).sum(1))
+    dis = f32 != (rd <= np.float64(rc))
+    assert dis.sum() > 100
+    bound = fp32_disagreement_bound(pi[dis], pj[dis], rc, [L, L, L])
+    assert np.all(np.abs(rd[dis] - np.float64(rc)) < bound)

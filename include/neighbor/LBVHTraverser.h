@@ -178,8 +178,9 @@ class LBVHTraverser : public Tunable<unsigned int>
 
         // Summary of the last counting traversal (traverse or traverseSelf with
         // CountNeighborsOp), four device words: [0] the largest count, [1] rows whose pairs did
-        // not fit the pair exchange (symmetric self counts), [2..3] the total of the counts
-        // (64-bit).  Written on the traversal's stream.
+        // not fit the pair exchange (exchanging self counts) or, for other counts, rows of more
+        // than 32 entries (which no exchange could hold), [2..3] the total of the counts (64-bit).
+        // Written on the traversal's stream.
         const unsigned int* getCountSummary() const { return m_words.get(); }
         // The same, read on the host: synchronises `stream` (the reference's two-pass pattern
         // reads the largest count here before the fill, benchmark/lbvh_benchmark.cc:177-196).
@@ -206,6 +207,18 @@ class LBVHTraverser : public Tunable<unsigned int>
             max_count = h[0];
             past_exchange = h[1];
             total = (unsigned long long)h[2] | ((unsigned long long)h[3] << 32);
+            // a self count's summary read on the host also steers the following fill and the
+            // next counts (results never depend on it): with more than a quarter of the rows past
+            // the exchange, the exchange costs more than it saves
+            if (m_summary_self && m_words.size() >= kWordCount)
+                {
+                // an exchanging count measures its rows past the exchange (dense above a quarter of
+                // the rows); another counts only rows longer than 32, a lower bound (dense above
+                // an eighth, so that the choice does not flip back and forth between frames)
+                m_summary_read = true;
+                const unsigned long long n = m_summary_n, p = past_exchange;
+                m_dense = m_summary_exchange ? p * 4ull > n : p * 8ull > n;
+                }
             }
 
         // Routing by size (results do not depend on it).  With few queries the GPU is mostly idle
@@ -264,12 +277,21 @@ class LBVHTraverser : public Tunable<unsigned int>
         unsigned int m_walk_lanes = 0;
         bool m_pair_cache = true;
         bool m_count_cached = false;
+        // the summary words come from a self count (m_summary_self); its summary was read on the
+        // host (m_summary_read); that summary found more than a quarter of the rows past the
+        // exchange, or too long for it (m_dense)
+        bool m_summary_self = false;
+        bool m_summary_read = false;
+        bool m_dense = false;
+        bool m_summary_exchange = false;   // the summary's count used the exchange
+        unsigned int m_summary_n = 0;      // rows of the summary's count
         // pair exchange of the last symmetric count: own keys and incoming keys (16 per sorted
         // position each) and the incoming counters
         device_array<unsigned int> m_cache;
         device_array<unsigned int> m_in_cache;
         device_array<unsigned int> m_in_count;
-        // [0..4) count summary, [4] rows left to re-walk after an assembly
+        device_array<unsigned char> m_lost;   // rows counted without a deposited key
+        // [0..4) count summary, [4] rows left to re-walk after an assembly, [5] the re-walk's ticket
         static constexpr size_t kWordCount = 8;
         device_array<unsigned int> m_words;
         device_array<unsigned int> m_subset;
@@ -296,7 +318,7 @@ class LBVHTraverser : public Tunable<unsigned int>
             {
             clear_summary(stream);
             gpu::k_count_summary<false><<<summary_grid(Q), gpu::kSummaryBlock, 0, stream>>>(
-                Q, nullptr, nullptr, nullptr, 0, nneigh, m_words.get(), status);
+                Q, nullptr, nullptr, nullptr, nullptr, 0, nneigh, m_words.get(), status);
             detail::check_cuda(cudaGetLastError(), "summary launch");
             }
         // zero the summary words before a count
@@ -503,7 +525,10 @@ void LBVHTraverser::traverse(const LaunchParameters& params, const LBVH& lbvh, c
             a.pad = query.pad;
             launch_fast(params, lbvh, a, out, transform, query.size());
             if constexpr (std::is_same<OutputOpT, CountNeighborsOp>::value)
+                {
                 summarize_counts(params.stream, out.nneigh, query.size(), lbvh.getStatusPointer());
+                m_summary_self = false;
+                }
             return;
             }
         }
@@ -515,7 +540,10 @@ void LBVHTraverser::traverse(const LaunchParameters& params, const LBVH& lbvh, c
                                                                         lbvh.getStatusPointer());
     detail::check_cuda(cudaGetLastError(), "traversal launch");
     if constexpr (std::is_same<OutputOpT, CountNeighborsOp>::value)
+        {
         summarize_counts(params.stream, out.nneigh, query.size(), lbvh.getStatusPointer());
+        m_summary_self = false;
+        }
     }
 
 template<class OutputOpT, class TranslateOpT, class TransformOpT>
@@ -554,7 +582,10 @@ void LBVHTraverser::traverseSelf(const LaunchParameters& params, const LBVH& lbv
     // the pairs (same tree, cutoff, images and rows) assembles the rows; other fills walk
     // symmetrically only while every row also fits the one-thread ordering (longer rows cost
     // more to order than the whole-tree walk costs, and that walk writes every row in order).
-    if (symmetric && kind != gpu::kFastCount && m_count_cached && m_pair_cache && self_tag(lbvh, a) == m_count_tag)
+    // (a fill after an exchanging count whose summary showed most work past the exchange walks
+    // the whole tree: the assembly would re-walk those rows anyway, in a less coherent order)
+    if (symmetric && kind != gpu::kFastCount && m_count_cached && m_pair_cache && self_tag(lbvh, a) == m_count_tag
+        && !(m_summary_read && m_dense))
         launch_assemble(params, lbvh, a, out, transform);
     else if (symmetric
              && (kind == gpu::kFastCount || (longest > 0u && longest <= gpu::kHalfRowThread)
@@ -563,7 +594,14 @@ void LBVHTraverser::traverseSelf(const LaunchParameters& params, const LBVH& lbv
     else
         {
         launch_fast(params, lbvh, a, out, transform, lbvh.getN());
-        if (kind == gpu::kFastCount) summarize_counts(params.stream, a.nneigh, lbvh.getN(), lbvh.getStatusPointer());
+        if (kind == gpu::kFastCount)
+            {
+            summarize_counts(params.stream, a.nneigh, lbvh.getN(), lbvh.getStatusPointer());
+            m_summary_self = true;
+            m_summary_read = false;
+            m_summary_exchange = false;
+            m_summary_n = lbvh.getN();
+            }
         }
     }
 
@@ -631,6 +669,7 @@ void LBVHTraverser::launch_half(const LaunchParameters& params, const LBVH& lbvh
     h.cache_out = nullptr;
     h.in_cache = nullptr;
     h.in_count = nullptr;
+    h.in_lost = nullptr;
     // what the last symmetric count ran on: this tree and build, cutoff, images, box and rows
     const PassTag tag = self_tag(lbvh, a);
     const unsigned int grid = detail::ceil_div(N, gpu::kHalfBlock);
@@ -639,23 +678,31 @@ void LBVHTraverser::launch_half(const LaunchParameters& params, const LBVH& lbvh
         m_count_own.reserve(N);
         h.own = m_count_own.get();
         m_count_tag = tag;
-        m_count_cached = m_pair_cache;
+        // the exchange unless the last read summary of a self count found a dense workload
+        m_count_cached = m_pair_cache && !m_dense;
+        m_summary_self = true;
+        m_summary_read = false;
+        m_summary_exchange = m_count_cached;
+        m_summary_n = N;
         clear_summary(stream);
-        if (m_pair_cache)
+        if (m_count_cached)
             {
             // pair exchange: own keys, incoming keys, incoming counters (by sorted position)
             m_cache.reserve((size_t)N * gpu::kHalfCacheSlots);
             m_in_cache.reserve((size_t)N * gpu::kHalfCacheSlots);
             m_in_count.reserve(N);
+            m_lost.reserve(N);
             h.cache_out = m_cache.get();
             h.in_cache = m_in_cache.get();
             h.in_count = m_in_count.get();
+            h.in_lost = m_lost.get();
             detail::check_cuda(cudaMemsetAsync(m_in_count.get(), 0, (size_t)N * sizeof(unsigned int), stream), "memset");
+            detail::check_cuda(cudaMemsetAsync(m_lost.get(), 0, N, stream), "memset");
             if constexpr (kind == gpu::kFastCount)
                 gpu::k_traverse_half<kind, TransformOpT, true><<<grid, gpu::kHalfBlock, 0, stream>>>(lbvh.fastData(), h,
                                                                                                      transform);
             gpu::k_count_summary<true><<<summary_grid(N), gpu::kSummaryBlock, 0, stream>>>(
-                N, m_count_own.get(), m_in_count.get(), lbvh.fastData().primitive, a.self_rows_sorted, a.nneigh,
+                N, m_count_own.get(), m_in_count.get(), m_lost.get(), lbvh.fastData().primitive, a.self_rows_sorted, a.nneigh,
                 m_words.get(), lbvh.getStatusPointer());
             detail::check_cuda(cudaGetLastError(), "half traversal launch");
             return;
@@ -679,7 +726,7 @@ void LBVHTraverser::launch_half(const LaunchParameters& params, const LBVH& lbvh
         detail::check_cuda(cudaMemcpyAsync(m_totals.get(), a.nneigh, (size_t)N * sizeof(unsigned int),
                                            cudaMemcpyDeviceToDevice, stream), "copy");
         gpu::k_count_summary<false><<<summary_grid(N), gpu::kSummaryBlock, 0, stream>>>(
-            N, nullptr, nullptr, nullptr, 0, a.nneigh, m_words.get(), lbvh.getStatusPointer());
+            N, nullptr, nullptr, nullptr, nullptr, 0, a.nneigh, m_words.get(), lbvh.getStatusPointer());
         }
     if (kind != gpu::kFastCount)
         {
@@ -707,13 +754,16 @@ void LBVHTraverser::launch_assemble(const LaunchParameters& params, const LBVH& 
     cudaStream_t stream = params.stream;
     m_words.reserve(kWordCount);
     m_subset.reserve(N);
-    detail::check_cuda(cudaMemsetAsync(m_words.get() + gpu::kSummaryWords, 0, sizeof(unsigned int), stream), "memset");
+    // the re-walk list's length and the re-walk's ticket start at zero
+    detail::check_cuda(cudaMemsetAsync(m_words.get() + gpu::kSummaryWords, 0, 2 * sizeof(unsigned int), stream),
+                       "memset");
     gpu::AssembleArgs g;
     g.N = N;
     g.rows_sorted = a.self_rows_sorted;
     g.center = a.lattice ? 13u : 0u;
     g.own = m_count_own.get();
     g.in_count = m_in_count.get();
+    g.lost = m_lost.get();
     g.own_keys = m_cache.get();
     g.in_keys = m_in_cache.get();
     g.primitive = lbvh.fastData().primitive;
@@ -733,8 +783,13 @@ void LBVHTraverser::launch_assemble(const LaunchParameters& params, const LBVH& 
     b.stats = nullptr;
     b.work_order = 0;
     const unsigned int blocks = std::max(1u, std::min(detail::ceil_div(N, gpu::kSubsetBlock), 8u * sm_count()));
+    gpu::SubsetScan scan;
+    scan.own = m_count_own.get();
+    scan.in_count = m_in_count.get();
+    scan.lost = m_lost.get();
+    scan.ticket = m_words.get() + gpu::kSummaryWords + 1;
     gpu::k_traverse_subset<kind, TransformOpT><<<blocks, gpu::kSubsetBlock, 0, stream>>>(
-        lbvh.fastData(), b, transform, m_words.get() + gpu::kSummaryWords);
+        lbvh.fastData(), b, transform, m_words.get() + gpu::kSummaryWords, scan);
     detail::check_cuda(cudaGetLastError(), "assembly launch");
     (void)out;
     }

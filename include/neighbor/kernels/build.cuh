@@ -770,17 +770,24 @@ __global__ void __launch_bounds__(T) k_climb(const InsertOpT insert, const Climb
     if (s < end) A.counts[s] = s_count[t];
 
     // the climb continues across blocks (k_climb_global) from the splits of this block that only
-    // one child reached and from the nodes whose parent split is on the block's edge
-    if (t + 1u < end - base && s_arrive[t] == 1u)
+    // one child reached and from the nodes whose parent split is on the block's edge; the block's
+    // items take one range of the list (one global atomic per block; their order does not matter)
+    const bool half = t + 1u < end - base && s_arrive[t] == 1u;
+    const unsigned int mine = (half ? 1u : 0u) + (boundary ? 1u : 0u);
+    __shared__ unsigned int s_items, s_items_base;
+    if (t == 0) s_items = 0u;
+    __syncthreads();
+    const unsigned int local = mine ? atomicAdd(&s_items, mine) : 0u;
+    __syncthreads();
+    if (t == 0) s_items_base = s_items ? atomicAdd(A.n_items, s_items) : 0u;
+    __syncthreads();
+    unsigned int k = s_items_base + local;
+    if (half)
         {
-        const unsigned int k = atomicAdd(A.n_items, 1u);
         if (k < A.item_capacity) A.items[k] = make_uint2(s_idb[2 * t + s_side[t]].x, base + t);
+        ++k;
         }
-    if (boundary)
-        {
-        const unsigned int k = atomicAdd(A.n_items, 1u);
-        if (k < A.item_capacity) A.items[k] = make_uint2(X.id, gp);
-        }
+    if (boundary && k < A.item_capacity) A.items[k] = make_uint2(X.id, gp);
     }
 
 // Second stage of the climb: one thread per pending node, arrival words in global memory.

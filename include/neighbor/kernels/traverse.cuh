@@ -578,68 +578,6 @@ __global__ void __launch_bounds__(kWarpWalkBlock) k_traverse_warp(const FastLBVH
     group_walk<OUT, TransformOpT, G>(tree, a, transform, f, s_records, q, lane, gmask, lanemask_lt() & gmask);
     }
 
-// Rows re-walked whole, their sorted positions in subset[0 .. *subset_count) (a count known only
-// on the device, e.g. the rows an assembly pass could not finish).  A persistent grid: with at
-// most kSubsetGroupMax rows each row gets a warp (a few long walks set the time, and 32 lanes
-// shorten each about 32 times); with more, each row gets one thread (the total work sets it), and
-// each block hands its rows to its lanes in order of their counts (nneigh, already written), so
-// that a warp's lanes walk about as long as each other.
-constexpr unsigned int kSubsetBlock = 256;
-constexpr unsigned int kSubsetGroupMax = 32768;
-
-template<int OUT, class TransformOpT>
-__global__ void __launch_bounds__(kSubsetBlock) k_traverse_subset(const FastLBVHData tree, const FastQueryArgs a,
-                                                                  const TransformOpT transform,
-                                                                  const unsigned int* __restrict__ subset_count)
-    {
-    __shared__ QuantFrame s_frame;
-    __shared__ unsigned int s_records;
-    __shared__ unsigned int s_n;
-    __shared__ unsigned int s_class[kWorkClasses];
-    __shared__ unsigned int s_order[kSubsetBlock];
-    if (threadIdx.x == 0)
-        {
-        s_frame = *tree.frame;
-        s_records = ld_status(tree.status) != 0u ? 0u : *tree.n_boxes + tree.N;
-        s_n = min(*subset_count, a.Q);
-        }
-    __syncthreads();
-    const unsigned int n = s_n;
-    const unsigned int n_rec = s_records;
-    if (n == 0u || n_rec == 0u) return;
-    const QuantFrame f = s_frame;
-    const unsigned int gid = blockIdx.x * blockDim.x + threadIdx.x;
-    const unsigned int threads = gridDim.x * blockDim.x;
-    if (n <= kSubsetGroupMax)
-        {
-        const unsigned int lane = threadIdx.x & 31u;
-        const unsigned int lt = lanemask_lt();
-        for (unsigned int t = gid >> 5; t < n; t += threads >> 5)
-            group_walk<OUT, TransformOpT, 32>(tree, a, transform, f, n_rec, a.subset[t], lane, 0xffffffffu, lt);
-        }
-    else
-        {
-        unsigned int visits = 0, tests = 0, walks = 0;
-        // block-uniform trip count: every thread of the block reaches block_work_order's barriers
-        for (unsigned int b0 = blockIdx.x * blockDim.x; b0 < n; b0 += threads)
-            {
-            const unsigned int item = b0 + threadIdx.x;
-            const bool valid = item < n;
-            unsigned int cls = 0;
-            if (valid)
-                {
-                const unsigned int q = a.subset[item];
-                const unsigned int row = a.self_rows_sorted ? q : __float_as_uint(tree.points[q].w);
-                cls = capacity_class(a.nneigh[row]);
-                }
-            const unsigned int t = block_work_order(item, valid, cls, s_class, s_order);
-            if (t != 0xffffffffu)
-                thread_walk<OUT, false>(tree, a, transform, f, n_rec, a.subset[t], visits, tests, walks);
-            __syncthreads();   // s_order is rewritten by the next round
-            }
-        }
-    }
-
 // ---------------------------------------------------------------------------------------------
 // Symmetric (half) self traversal.  When the queries are the tree's own points with one cutoff
 // and the image set is symmetric (the self image, or the 27-image lattice), the FP32
@@ -708,6 +646,8 @@ struct HalfArgs
     unsigned int* cache_out;
     unsigned int* in_cache;
     unsigned int* in_count;
+    // rows a partner counted without depositing its key (zero on entry): past the exchange
+    unsigned char* in_lost;
     };
 
 constexpr unsigned int kHalfCacheSlots = 16;
@@ -816,10 +756,22 @@ __global__ void __launch_bounds__(kHalfBlock, OUT == kFastCount ? 8 : 6) k_trave
                 if (own < kHalfCacheSlots) a.cache_out[(size_t)q * kHalfCacheSlots + own] = (bit << kHalfKeyBits) | j;
                 if (j != q)
                     {
-                    // the previous partner's key goes to its slot now that the slot is known
-                    deposit();
-                    x_slot = atomicAdd(a.in_count + j, 1u);
-                    x_jm = (mirror << kHalfKeyBits) | j;
+                    if (own < kHalfCacheSlots)
+                        {
+                        // the previous partner's key goes to its slot now that the slot is known
+                        deposit();
+                        x_slot = atomicAdd(a.in_count + j, 1u);
+                        x_jm = (mirror << kHalfKeyBits) | j;
+                        }
+                    else
+                        {
+                        // A query with more pairs than its own slots lies in a dense region, where
+                        // the partners' slots fill up too (and their counters are contended): the
+                        // partner is counted without waiting for a slot and its row is marked for
+                        // the fill's re-walk.
+                        atomicAdd(a.in_count + j, 1u);
+                        a.in_lost[j] = 1u;
+                        }
                     }
                 }
             else if (j != q)
@@ -897,9 +849,17 @@ __global__ void __launch_bounds__(kHalfBlock, OUT == kFastCount ? 8 : 6) k_trave
     if (!CACHE && a.walk_out) a.walk_out[q] = (unsigned short)min(visits, 65535u);
     }
 
+// A row is past the pair exchange -- its row is walked again by the fill -- when its own or its
+// incoming keys did not fit their slots, or when a partner counted it without depositing a key.
+__device__ __forceinline__ bool past_exchange(unsigned int own, unsigned int in, unsigned char lost)
+    {
+    return own > kHalfCacheSlots || in > kHalfCacheSlots || lost != 0u;
+    }
+
 // Summary of a count, in four device words: [0] the largest row count, [1] rows whose own or
-// incoming keys did not fit the pair exchange's slots, [2..3] the pair total (64-bit, ordered
-// pairs, self included).  The words are zero on entry.
+// incoming keys did not fit the pair exchange's slots (EXCHANGE) or rows longer than both slot
+// sets together (otherwise), [2..3] the pair total (64-bit, ordered pairs, self included).  The
+// words are zero on entry.
 //   EXCHANGE: the rows of a pair-exchange count: nneigh[row(s)] = own[s] + in_count[s].
 //   otherwise: the counts already in nneigh[0..N) (any count route).
 constexpr unsigned int kSummaryWords = 4;
@@ -908,6 +868,7 @@ constexpr unsigned int kSummaryBlock = 256;
 template<bool EXCHANGE>
 __global__ void __launch_bounds__(kSummaryBlock) k_count_summary(unsigned int N, const unsigned int* __restrict__ own,
                                                                  const unsigned int* __restrict__ in_count,
+                                                                 const unsigned char* __restrict__ lost,
                                                                  const unsigned int* __restrict__ primitive,
                                                                  int rows_sorted, unsigned int* nneigh,
                                                                  unsigned int* words, const unsigned int* status)
@@ -932,11 +893,12 @@ __global__ void __launch_bounds__(kSummaryBlock) k_count_summary(unsigned int N,
             const unsigned int o = own[s], i = in_count[s];
             total = o + i;
             nneigh[rows_sorted ? s : primitive[s]] = total;
-            past += (o > kHalfCacheSlots || i > kHalfCacheSlots) ? 1u : 0u;
+            past += past_exchange(o, i, lost[s]) ? 1u : 0u;
             }
         else
             {
             total = nneigh[s];
+            past += total > 2u * kHalfCacheSlots ? 1u : 0u;   // too long for any exchange
             }
         mx = max(mx, total);
         sum += total;
@@ -970,6 +932,79 @@ __global__ void __launch_bounds__(kSummaryBlock) k_count_summary(unsigned int N,
         }
     }
 
+// Rows re-walked whole after an assembly (the rows past the pair exchange; their number is known
+// only on the device, *subset_count).  A persistent grid.  With at most kSubsetGroupMax rows, the
+// rows listed in subset[] each get a warp (a few long walks set the time, and 32 lanes shorten
+// each about 32 times).  With more, the grid scans all rows in sorted order in chunks of a block
+// (handed out by a ticket) and gives each row past the exchange one thread, in order of the
+// rows' counts within the block: neighboring queries keep walking neighboring records, and a
+// warp's lanes walk about as long as each other (the total work sets the time).
+constexpr unsigned int kSubsetBlock = 256;
+constexpr unsigned int kSubsetGroupMax = 32768;
+
+// What tells the scan which rows are past the exchange.
+struct SubsetScan
+    {
+    const unsigned int* own;        // own keys found, by sorted position
+    const unsigned int* in_count;   // incoming keys counted, by sorted position
+    const unsigned char* lost;      // rows counted without a deposited key
+    unsigned int* ticket;           // zero on entry
+    };
+
+template<int OUT, class TransformOpT>
+__global__ void __launch_bounds__(kSubsetBlock) k_traverse_subset(const FastLBVHData tree, const FastQueryArgs a,
+                                                                  const TransformOpT transform,
+                                                                  const unsigned int* __restrict__ subset_count,
+                                                                  const SubsetScan scan)
+    {
+    __shared__ QuantFrame s_frame;
+    __shared__ unsigned int s_records;
+    __shared__ unsigned int s_n;
+    __shared__ unsigned int s_chunk;
+    __shared__ unsigned int s_class[kWorkClasses];
+    __shared__ unsigned int s_order[kSubsetBlock];
+    if (threadIdx.x == 0)
+        {
+        s_frame = *tree.frame;
+        s_records = ld_status(tree.status) != 0u ? 0u : *tree.n_boxes + tree.N;
+        s_n = *subset_count;
+        }
+    __syncthreads();
+    const unsigned int n = s_n;
+    const unsigned int n_rec = s_records;
+    if (n == 0u || n_rec == 0u) return;
+    const QuantFrame f = s_frame;
+    if (n <= kSubsetGroupMax)
+        {
+        const unsigned int gid = blockIdx.x * blockDim.x + threadIdx.x;
+        const unsigned int lane = threadIdx.x & 31u;
+        const unsigned int lt = lanemask_lt();
+        for (unsigned int t = gid >> 5; t < n; t += (gridDim.x * blockDim.x) >> 5)
+            group_walk<OUT, TransformOpT, 32>(tree, a, transform, f, n_rec, a.subset[t], lane, 0xffffffffu, lt);
+        return;
+        }
+    unsigned int visits = 0, tests = 0, walks = 0;
+    const unsigned int N = tree.N;
+    while (true)
+        {
+        if (threadIdx.x == 0) s_chunk = atomicAdd(scan.ticket, 1u);
+        __syncthreads();
+        const unsigned int b0 = s_chunk * blockDim.x;
+        if (b0 >= N) break;   // block-uniform
+        const unsigned int item = b0 + threadIdx.x;
+        const bool valid = item < N && past_exchange(scan.own[item], scan.in_count[item], scan.lost[item]);
+        unsigned int cls = 0;
+        if (valid)
+            {
+            const unsigned int row = a.self_rows_sorted ? item : __float_as_uint(tree.points[item].w);
+            cls = capacity_class(a.nneigh[row]);
+            }
+        const unsigned int t = block_work_order(item, valid, cls, s_class, s_order);
+        if (t != 0xffffffffu) thread_walk<OUT, false>(tree, a, transform, f, n_rec, t, visits, tests, walks);
+        __syncthreads();   // s_chunk and s_order are rewritten by the next round
+        }
+    }
+
 // ---------------------------------------------------------------------------------------------
 // Assembly of list rows from a pair-exchange count (no walk, no atomics on rows).  One thread per
 // sorted position s: its own keys (ascending: found in pre-order from its own record) and its
@@ -989,6 +1024,7 @@ struct AssembleArgs
     unsigned int center;                 // image field of pairs through the query's own image
     const unsigned int* own;             // own keys found, by sorted position
     const unsigned int* in_count;        // incoming keys deposited, by sorted position
+    const unsigned char* lost;           // rows counted without a deposited key
     const unsigned int* own_keys;        // kHalfCacheSlots per sorted position
     const unsigned int* in_keys;         // kHalfCacheSlots per sorted position
     const unsigned int* primitive;
@@ -1050,9 +1086,19 @@ __global__ void __launch_bounds__(256) k_half_assemble(const AssembleArgs a, con
     const unsigned int total = o + ni;
     const unsigned int row = a.rows_sorted ? s : a.primitive[s];
     a.nneigh[row] = total;
-    if (o > kHalfCacheSlots || ni > kHalfCacheSlots)
+    const bool past = past_exchange(o, ni, a.lost[s]);
+    // rows past the exchange join the re-walk list (one atomic per warp); past kSubsetGroupMax
+    // rows the re-walk scans all rows instead and the list is not needed
+    const unsigned int active = __activemask();
+    const unsigned int ballot = __ballot_sync(active, past);
+    if (past)
         {
-        a.subset[atomicAdd(a.subset_count, 1u)] = s;
+        const unsigned int leader = __ffs(ballot) - 1u;
+        unsigned int base = 0u;
+        if ((threadIdx.x & 31u) == leader) base = atomicAdd(a.subset_count, __popc(ballot));
+        base = __shfl_sync(ballot, base, leader);
+        const unsigned int k = base + __popc(ballot & lanemask_lt());
+        if (k < kSubsetGroupMax) a.subset[k] = s;
         return;
         }
     unsigned long long first = 0;

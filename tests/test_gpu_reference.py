@@ -110,3 +110,34 @@ def test_library_matches_reference_kernels(name, P, L, rc):
         assert np.array_equal(nn.cpu().numpy().view(np.uint32), ref["count_exact"]), route
         got = lst.cpu().numpy().view(np.uint32)
         assert np.array_equal(np.where(valid, got, 0), np.where(valid, ref_list, 0)), route
+
+
+@pytest.mark.parametrize("radius", [0.25, 1.5])
+def test_sphere_tree_matches_reference_kernels(radius):
+    # SphereInsertOp (include/neighbor/InsertOps.h:57-96): the tree of spheres of one radius --
+    # codes of the box centres, primitive order, hierarchy and the FP32 boxes -- and the
+    # reference-layout nodes equal the reference kernels' own sphere tree bit for bit, as do the
+    # stock query's counts over it
+    rng = np.random.default_rng(int(radius * 100))
+    L = 20.0
+    P = (rng.random((12000, 3)) * L).astype(np.float32)
+    box = [L, L, L]
+    ref = ref_harness.run_dump(P, [0, 0, 0], box, 1.0, box, sphere_radius=radius)
+    lbvh = nb.LBVH()
+    lbvh.build(_t(P), [0, 0, 0], box, radius=radius)
+    lbvh.check_status()
+    a = lbvh.arrays()
+    assert np.array_equal(lbvh.codes().cpu().numpy().view(np.uint32), ref["codes"])
+    assert np.array_equal(a["primitive"].cpu().numpy().view(np.uint32), ref["primitive"])
+    assert np.array_equal(a["parent"].cpu().numpy(), ref["parent"])
+    assert np.array_equal(a["left"].cpu().numpy(), ref["left"])
+    assert np.array_equal(a["right"].cpu().numpy(), ref["right"])
+    assert np.array_equal(a["lo"].cpu().numpy(), ref["lo"])
+    assert np.array_equal(a["hi"].cpu().numpy(), ref["hi"])
+    trav = nb.LBVHTraverser()
+    trav.setup(lbvh)
+    torch.cuda.synchronize()
+    assert np.array_equal(trav.get_data(lbvh)["data"].cpu().numpy(), ref["data"])
+    sph = _t(np.concatenate([P, np.full((len(P), 1), 1.0, np.float32)], 1))
+    stock = trav.traverse(lbvh, sph, images=nb.images27(box)).cpu().numpy().view(np.uint32)
+    assert np.array_equal(stock, ref["count_stock"])

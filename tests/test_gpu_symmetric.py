@@ -377,10 +377,10 @@ def test_rows_past_the_exchange_are_walked(per, N):
     trav = nb.LBVHTraverser()
     trav.force_symmetric()
     cnt = trav.traverse_self(lbvh, rc, box, pad, images="periodic", rows_sorted=True)
-    mx, total, past = trav.count_summary()
+    # (the largest count from the counts themselves: a summary read on the host would steer these
+    # dense fills to the whole-tree walk, and this test is about the assembly and its re-walk)
     c = cnt.cpu().numpy().view(np.uint32)
-    assert mx == int(c.max()) and total == int(c.astype(np.int64).sum())
-    assert past > (20000 if N == 24000 else 60000)
+    mx = int(c.max())
     whole = nb.LBVHTraverser()
     whole.set_symmetric(False)
     whole.set_warp_walk_max(0)
@@ -398,6 +398,23 @@ def test_rows_past_the_exchange_are_walked(per, N):
     off = offsets.cpu().numpy()
     for r in range(0, N, 97):
         assert np.array_equal(flat[off[r]:off[r] + c[r]], want[1][r, : c[r]])
+    mx2, total, past = trav.count_summary()
+    assert mx2 == mx and total == int(c.astype(np.int64).sum())
+    assert past > (20000 if N == 24000 else 60000)
+    # With the summary read, the fill walks the whole tree and the next counts skip the exchange
+    # (too many rows past it); a count without the exchange reports rows longer than 32, and the
+    # lists stay the same through every step of that sequence.
+    got = _rows(*trav.traverse_self(lbvh, rc, box, pad, images="periodic", rows_sorted=True, max_neigh=mx))
+    assert np.array_equal(got[0], want[0]) and np.array_equal(got[1], want[1])
+    for k in range(2):
+        cnt2 = trav.traverse_self(lbvh, rc, box, pad, images="periodic", rows_sorted=True)
+        assert torch.equal(cnt2, cnt)
+        m3, t3, rows_past = trav.count_summary()
+        assert m3 == mx and t3 == total
+        if k == 0:   # the count after the dense summary: no exchange, rows longer than 32 reported
+            assert rows_past == int(np.count_nonzero(c > 32))
+        got = _rows(*trav.traverse_self(lbvh, rc, box, pad, images="periodic", rows_sorted=True, max_neigh=mx))
+        assert np.array_equal(got[0], want[0]) and np.array_equal(got[1], want[1])
 
 
 @pytest.mark.parametrize("symmetric", [True, False])

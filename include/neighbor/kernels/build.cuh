@@ -430,12 +430,28 @@ static __global__ void __launch_bounds__(kScanBlock) k_scan_exclusive(const unsi
     const unsigned int base = tile * kScanTile + tid * kScanItems;
     unsigned int v[kScanItems];
     unsigned int sum = 0;
-#pragma unroll
-    for (int k = 0; k < kScanItems; ++k)
+    static_assert(kScanItems % 4 == 0, "16-byte loads");
+    if (base + kScanItems <= n)
         {
-        v[k] = (base + k < n) ? in[base + k] : 0u;
-        sum += v[k];
+        // a whole thread's items in range: 16-byte loads (base is a multiple of 16 words)
+        const uint4* in4 = reinterpret_cast<const uint4*>(in + base);
+#pragma unroll
+        for (int k = 0; k < kScanItems / 4; ++k)
+            {
+            const uint4 w = in4[k];
+            v[4 * k] = w.x;
+            v[4 * k + 1] = w.y;
+            v[4 * k + 2] = w.z;
+            v[4 * k + 3] = w.w;
+            }
         }
+    else
+        {
+#pragma unroll
+        for (int k = 0; k < kScanItems; ++k) v[k] = (base + k < n) ? in[base + k] : 0u;
+        }
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) sum += v[k];
     unsigned int incl = sum;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1)
@@ -473,12 +489,35 @@ static __global__ void __launch_bounds__(kScanBlock) k_scan_exclusive(const unsi
         }
     __syncthreads();
     unsigned int run = s_excl + s_warp[warp] + incl - sum;
-#pragma unroll
-    for (int k = 0; k < kScanItems; ++k)
+    if (base + kScanItems <= n)
         {
-        if (base + k <= n) out[base + k] = run;
-        if (base + k == n && total_out) *total_out = run;
-        run += v[k];
+        // every output of the thread lies before out[n] (the total, written by the thread whose
+        // items start at n): 16-byte stores
+        uint4* out4 = reinterpret_cast<uint4*>(out + base);
+#pragma unroll
+        for (int k = 0; k < kScanItems / 4; ++k)
+            {
+            uint4 w;
+            w.x = run;
+            run += v[4 * k];
+            w.y = run;
+            run += v[4 * k + 1];
+            w.z = run;
+            run += v[4 * k + 2];
+            w.w = run;
+            run += v[4 * k + 3];
+            out4[k] = w;
+            }
+        }
+    else
+        {
+#pragma unroll
+        for (int k = 0; k < kScanItems; ++k)
+            {
+            if (base + k <= n) out[base + k] = run;
+            if (base + k == n && total_out) *total_out = run;
+            run += v[k];
+            }
         }
     }
 

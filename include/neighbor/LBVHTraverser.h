@@ -308,10 +308,11 @@ class LBVHTraverser : public Tunable<unsigned int>
                 }
             return (unsigned int)m_sms;
             }
-        // blocks of the count summary: a few per SM (each adds its rows to the words once)
+        // blocks of the count summary: enough per SM to keep its loads in flight, each adding its
+        // rows to the words once (16M rows: 4 blocks per SM 0.111 ms)
         unsigned int summary_grid(unsigned int N)
             {
-            return std::max(1u, std::min(detail::ceil_div(N, gpu::kSummaryBlock), 4u * sm_count()));
+            return std::max(1u, std::min(detail::ceil_div(N, gpu::kSummaryBlock), 16u * sm_count()));
             }
         // the summary (largest count, total) of counts already written to nneigh[0..Q)
         void summarize_counts(cudaStream_t stream, unsigned int* nneigh, unsigned int Q, const unsigned int* status)

@@ -317,6 +317,32 @@ def time_steps(fn, frames, warmup, stream):
     return e0.elapsed_time(e1) / max(1, len(frames) - warmup), outs
 
 
+def time_predict(nb, model, lbvh, box, rc, n, stream, reps=10):
+    """CUDA-event time of one capacity prediction (occupancy grid + fused features and network)
+    on the current tree with each inference kernel: mma.sync warp tiles and tcgen05 128-query
+    tiles with Tensor Memory accumulators.  The inputs (codes, points: 20 B per point) exceed L2."""
+    import torch
+    caps = torch.empty(n, dtype=torch.int32, device="cuda")
+    keep = model.infer_kernel
+    out = {}
+    for name, k in (("warp_tiles_mma_sync", nb.CAP_INFER_WARP_TILES),
+                    ("tensor_memory_tcgen05", nb.CAP_INFER_TENSOR_MEMORY)):
+        model.infer_kernel = k
+        for _ in range(3):
+            model.predict(lbvh, [0, 0, 0], box, rc, caps=caps, stream=stream)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            model.predict(lbvh, [0, 0, 0], box, rc, caps=caps, stream=stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        out[name] = round(e0.elapsed_time(e1) / reps, 4)
+    model.infer_kernel = keep
+    out["status"] = model.status()
+    out["kernel_in_step"] = "tensor_memory_tcgen05" if keep == nb.CAP_INFER_TENSOR_MEMORY else "warp_tiles_mma_sync"
+    return out
+
+
 def learned_uniform(nb, n, L, frames, warmup, plain_ms, pairs_step, args, stream):
     """The learned one-pass form of the same trajectory step: build, capacity prediction,
     one traversal into a CSR list, exact re-run of the rows that overflowed."""
@@ -342,7 +368,9 @@ def learned_uniform(nb, n, L, frames, warmup, plain_ms, pairs_step, args, stream
     cnt = trav.traverse_self(lbvh, RC, box, pad, images="periodic", rows_sorted=True)
     exact = bool(torch.equal(res["nneigh"].view(torch.int32), cnt))
     ovf = [s["overflow_rows"] for s in stats]
+    predict_ms = time_predict(nb, model, lbvh, box, RC, n, stream)
     return {"ms_per_step": ms, "value": pairs_step / (ms * 1e-3), "unit": "pairs/s",
+            "predict_ms": predict_ms,
             "vs_plain": plain_ms / ms, "slots_per_point": stats[-1]["slots"] / n,
             "overflow_rows_mean": sum(ovf) / len(ovf), "counts_equal_plain": exact,
             "margin": model.margin, "margins": [round(v, 3) for v in model.margins], "cap_max": UNIFORM_CAP_MAX, "train_s": round(train_s, 2),
@@ -932,6 +960,8 @@ def summary(line):
             "check_vs_reference": get(line, "check_vs_reference", "rows_equal"),
             "cpu_pairs_per_s": get(line, "cpu_baseline", "value"),
             "learned_vs_plain_16m": get(line, "learned", "vs_plain"),
+            "predict_ms_mma_sync": get(line, "learned", "predict_ms", "warp_tiles_mma_sync"),
+            "predict_ms_tcgen05": get(line, "learned", "predict_ms", "tensor_memory_tcgen05"),
             "clustered_learned_vs_plain": get(line, "clustered_4m", "learned_vs_plain"),
             "clustered_vs_reference_cuda": get(line, "clustered_4m", "plain_vs_reference_cuda"),
             "polydisperse_ms": get(line, "polydisperse_1m", "ms_per_step"),

@@ -34,9 +34,11 @@ class CapacityModel
         static constexpr int kParams = gpu::kCapParams;
         static constexpr int kFeatures = gpu::kCapIn;
 
-        explicit CapacityModel(unsigned long long seed = 1) : m_step(0)
+        explicit CapacityModel(unsigned long long seed = 1) : m_step(0), m_infer(InferKernel::WarpTiles)
             {
             setMargin(0.f);
+            m_status.reserve(1);
+            detail::check_cuda(cudaMemset(m_status.get(), 0, sizeof(unsigned int)), "memset");
             m_p.reserve(kParams);
             m_m.reserve(kParams);
             m_v.reserve(kParams);
@@ -167,14 +169,64 @@ class CapacityModel
             a.rows_sorted = rows_sorted ? 1 : 0;
             a.y_out = y;
             a.cap_out = caps;
-            const unsigned int tiles = detail::ceil_div(N, 32);
+            a.status = m_status.get();
             int dev = 0, sms = 152;
             detail::check_cuda(cudaGetDevice(&dev), "device");
             detail::check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "attribute");
-            // persistent: two blocks per SM (the kernel's register budget) walk all tiles
-            const unsigned int grid = std::min(detail::ceil_div(tiles, gpu::kCapInferWarps), (unsigned int)sms * 2u);
-            gpu::k_cap_infer<<<grid, gpu::kCapInferWarps * 32, 0, stream>>>(a);
+            if (m_infer == InferKernel::TensorMemory)
+                {
+                static bool attr = false;
+                if (!attr)
+                    {
+                    detail::check_cuda(cudaFuncSetAttribute(gpu::k_cap_infer_tc,
+                                                            cudaFuncAttributePreferredSharedMemoryCarveout,
+                                                            (int)cudaSharedmemCarveoutMaxShared),
+                                       "inference attribute");
+                    attr = true;
+                    }
+                // persistent: kCapTcMinBlocks blocks of 128 queries per SM walk all tiles
+                const unsigned int tiles = detail::ceil_div(N, (unsigned int)gpu::kCapTcRows);
+                const unsigned int grid = std::min(tiles, (unsigned int)sms * (unsigned int)gpu::kCapTcMinBlocks);
+                gpu::k_cap_infer_tc<<<grid, gpu::kCapTcRows, 0, stream>>>(a);
+                }
+            else
+                {
+                // persistent: two blocks per SM (the kernel's register budget) walk all tiles
+                const unsigned int tiles = detail::ceil_div(N, 32);
+                const unsigned int grid =
+                    std::min(detail::ceil_div(tiles, gpu::kCapInferWarps), (unsigned int)sms * 2u);
+                gpu::k_cap_infer<<<grid, gpu::kCapInferWarps * 32, 0, stream>>>(a);
+                }
             detail::check_cuda(cudaGetLastError(), "capacity inference launch");
+            }
+
+    public:
+        // The inference kernel: warp tiles of mma.sync m16n8k16 (k_cap_infer) or 128-query tiles
+        // on tcgen05 with Tensor Memory accumulators (k_cap_infer_tc).  Both give the same
+        // capacities up to FP32 summation order.
+        enum class InferKernel : int
+            {
+            WarpTiles = 0,
+            TensorMemory = 1,
+            };
+        void setInferKernel(InferKernel k) { m_infer = k; }
+        InferKernel getInferKernel() const { return m_infer; }
+
+        // Device status word of the inference (gpu::kStatusTensorWait: a tensor-core wait gave up
+        // and that prediction is incomplete).  Reads it and clears it; synchronises the device.
+        unsigned int takeStatus()
+            {
+            unsigned int v = 0;
+            detail::check_cuda(cudaMemcpy(&v, m_status.get(), sizeof(v), cudaMemcpyDeviceToHost), "copy");
+            detail::check_cuda(cudaMemset(m_status.get(), 0, sizeof(v)), "memset");
+            return v;
+            }
+        // Throws if a wait of the inference gave up.
+        void checkStatus()
+            {
+            const unsigned int v = takeStatus();
+            if (v & gpu::kStatusTensorWait)
+                throw std::runtime_error("capacity inference: a wait for a tensor-core MMA gave up (output incomplete)");
             }
 
     public:
@@ -348,7 +400,9 @@ class CapacityModel
         device_array<float> m_loss;
         device_array<__nv_bfloat16> m_w;
         device_array<unsigned int> m_occ;
+        device_array<unsigned int> m_status;
         unsigned int m_step;
+        InferKernel m_infer;
         float m_margins[gpu::kCapMarginBins];
 
         static void append(std::vector<unsigned char>& b, const void* p, size_t n)

@@ -24,6 +24,8 @@
 //                        hidden layers are BF16 mma.sync m16n8k16 tiles with FP32 accumulators (a
 //                        layer's accumulator fragments are the next layer's A fragments) and the
 //                        output layer is folded into the second layer's accumulators
+//   k_cap_infer_tc       the same on the fifth-generation tensor cores: 128-query tiles, tcgen05.mma
+//                        from shared-memory operands into Tensor Memory, tcgen05.ld epilogues
 //   k_cap_train_step     forward + backward of a mini-batch on CUDA cores (one thread per sample,
 //                        block tiles in shared memory), gradients summed in FP32
 //   k_cap_adam           Adam update of the FP32 master weights and their BF16 copies
@@ -33,6 +35,7 @@
 #include <cuda_bf16.h>
 
 #include "common.cuh"
+#include "tcgen05.cuh"
 
 namespace neighbor
 {
@@ -239,6 +242,7 @@ struct CapInferArgs
     int rows_sorted;                // row of sorted position s: s or primitive id
     float* y_out;                   // optional: network output per row
     unsigned int* cap_out;          // capacity per row
+    unsigned int* status;           // device status word (k_cap_infer_tc: kStatusTensorWait)
     };
 
 __device__ __forceinline__ unsigned int pack_bf16x2(float lo, float hi)
@@ -278,6 +282,85 @@ __device__ __forceinline__ unsigned int cap_row(const CapInferArgs& a, unsigned 
     {
     if (a.rows_sorted) return s;
     return a.points ? __float_as_uint(a.points[s].w) : a.primitive[s];
+    }
+
+// Features of a warp's 32 sorted points s (one per lane) as cap_features() gives them, gathered
+// once per distinct coarse cell: sorted points of one cell are consecutive, so the 32 points lie in
+// m (typically a few) cells, and the warp's lanes share the 27 m occupancy lookups.  Writes the BF16
+// feature row of each distinct cell to cell[k * STRIDE ..] (features 0..26, 30, 31; `part` is
+// scratch of 32 x 9 words) and returns, per lane, the row k of its cell and its two point-specific
+// words: word 13 = (feature 26 of its cell, x fraction), word 14 = (y, z fractions).
+template<int STRIDE>
+__device__ __forceinline__ void cap_warp_features(const CapInferArgs& a, const float* s_log, unsigned int s,
+                                                  unsigned int lane, unsigned int* part, unsigned short* cell,
+                                                  unsigned int& ci_out, uint2& pt_out)
+    {
+    const unsigned int sh = a.frame.shift;
+    const int G = 1024 >> sh;
+    const unsigned int lane_le = lanemask_lt() | (1u << lane);
+    // lane nb < 27 gathers neighbor cell nb = 9(dx+1) + 3(dy+1) + (dz+1) of every distinct cell
+    const unsigned int nb_x = lane / 9u, nb_y = 3u + (lane / 3u) % 3u, nb_z = 6u + lane % 3u;
+    const unsigned int c = a.codes[s] >> (3u * sh);
+    const float3 pos = cap_position(a, s);   // loaded early: used after the occupancy gather
+    const unsigned int c_prev = __shfl_up_sync(0xffffffffu, c, 1);
+    const unsigned int heads = __ballot_sync(0xffffffffu, lane == 0u || c != c_prev);
+    const unsigned int m = __popc(heads);
+    const unsigned int ci = __popc(heads & lane_le) - 1u;
+    const int cx = (int)compact1by2(c >> 2);
+    const int cy = (int)compact1by2(c >> 1);
+    const int cz = (int)compact1by2(c);
+    ci_out = ci;
+    if ((heads >> lane) & 1u)
+        {
+        unsigned int p[3], v[3];
+        cap_axis(cx, G, a.frame.periodic, p, v);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) part[ci * 9 + d] = v[d] ? p[d] : 0xffffffffu;
+        cap_axis(cy, G, a.frame.periodic, p, v);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) part[ci * 9 + 3 + d] = v[d] ? p[d] : 0xffffffffu;
+        cap_axis(cz, G, a.frame.periodic, p, v);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) part[ci * 9 + 6 + d] = v[d] ? p[d] : 0xffffffffu;
+        }
+    __syncwarp();
+    // one distinct cell per step: lanes 0..26 its 27 occupancies (a spread part of 0xffffffff,
+    // outside an open grid, makes the index >= 2^30), lane 30 the log of their sum (a warp
+    // reduction), lane 31 the constant; the loads of four cells are issued before their sums
+    for (unsigned int k0 = 0; k0 < m; k0 += 4u)
+        {
+        unsigned int o[4];
+#pragma unroll
+        for (unsigned int j = 0; j < 4u; ++j)
+            {
+            const unsigned int* pk = part + (k0 + j) * 9u;
+            o[j] = 0u;
+            if (lane < 27u && k0 + j < m)
+                {
+                const unsigned int idx = (pk[nb_x] << 2) | (pk[nb_y] << 1) | pk[nb_z];
+                if (idx < (1u << 30)) o[j] = __ldg(a.occ + idx);
+                }
+            }
+#pragma unroll
+        for (unsigned int j = 0; j < 4u; ++j)
+            {
+            const unsigned int k = k0 + j;
+            if (k >= m) break;   // uniform over the warp
+            const unsigned int sum = __reduce_add_sync(0xffffffffu, o[j]);
+            const float f = lane < 27u ? cap_log1p(s_log, o[j]) : (lane == 31u ? 1.f : cap_log1p(s_log, sum));
+            if (lane < 27u || lane >= 30u)
+                cell[k * STRIDE + lane] = __bfloat16_as_ushort(__float2bfloat16_rn(f));
+            }
+        }
+    __syncwarp();
+    {
+    // the point's own words: 13 = (feature 26 of its cell, x fraction), 14 = (y, z fractions)
+    float fr3[3];
+    cap_frac(a.frame, pos, cx, cy, cz, fr3);
+    const unsigned int f26 = cell[ci * STRIDE + 26];
+    pt_out = make_uint2(f26 | ((unsigned int)__bfloat16_as_ushort(__float2bfloat16_rn(fr3[0])) << 16),
+                        pack_bf16x2(fr3[1], fr3[2]));
+    }
     }
 
 constexpr int kCapInferWarps = 8;
@@ -335,85 +418,21 @@ __global__ void __launch_bounds__(kCapInferWarps * 32, kCapInferMinBlocks) k_cap
     const unsigned int warp = threadIdx.x >> 5;
     const unsigned int g = lane >> 2;   // groupID
     const unsigned int t = lane & 3u;   // thread in group
-    // lane nb < 27 gathers neighbor cell nb = 9(dx+1) + 3(dy+1) + (dz+1) of every distinct cell
-    const unsigned int nb_x = lane / 9u, nb_y = 3u + (lane / 3u) % 3u, nb_z = 6u + lane % 3u;
     unsigned int* part = s_part[warp];
     unsigned short* cell = s_cell[warp];
     unsigned int* cidx = s_ci[warp];
     uint2* pt = s_pt[warp];
-    const unsigned int sh = a.frame.shift;
-    const int G = 1024 >> sh;
-    const unsigned int lane_le = lanemask_lt() | (1u << lane);
     const unsigned int n_tiles = (a.N + 31u) / 32u;
     for (unsigned int tile = blockIdx.x * kCapInferWarps + warp; tile < n_tiles; tile += gridDim.x * kCapInferWarps)
         {
         const unsigned int base = tile * 32u;
-        // Features as cap_features() gives them, gathered once per distinct coarse cell: sorted
-        // points of one cell are consecutive, so a warp's 32 points lie in m (typically a few)
-        // cells, and the warp's lanes share the 27 m occupancy lookups.  Lanes past the end
-        // repeat the last point (their outputs are not written).
+        // lanes past the end repeat the last point (their outputs are not written)
         const unsigned int s = base + min(lane, a.N - 1u - base);
-        const unsigned int c = a.codes[s] >> (3u * sh);
-        const float3 pos = cap_position(a, s);   // loaded early: used after the occupancy gather
-        const unsigned int c_prev = __shfl_up_sync(0xffffffffu, c, 1);
-        const unsigned int heads = __ballot_sync(0xffffffffu, lane == 0u || c != c_prev);
-        const unsigned int m = __popc(heads);
-        const unsigned int ci = __popc(heads & lane_le) - 1u;
-        const int cx = (int)compact1by2(c >> 2);
-        const int cy = (int)compact1by2(c >> 1);
-        const int cz = (int)compact1by2(c);
+        unsigned int ci;
+        uint2 ptw;
+        cap_warp_features<kCapCellStride>(a, s_log, s, lane, part, cell, ci, ptw);
         cidx[lane] = ci;
-        if ((heads >> lane) & 1u)
-            {
-            unsigned int p[3], v[3];
-            cap_axis(cx, G, a.frame.periodic, p, v);
-#pragma unroll
-            for (int d = 0; d < 3; ++d) part[ci * 9 + d] = v[d] ? p[d] : 0xffffffffu;
-            cap_axis(cy, G, a.frame.periodic, p, v);
-#pragma unroll
-            for (int d = 0; d < 3; ++d) part[ci * 9 + 3 + d] = v[d] ? p[d] : 0xffffffffu;
-            cap_axis(cz, G, a.frame.periodic, p, v);
-#pragma unroll
-            for (int d = 0; d < 3; ++d) part[ci * 9 + 6 + d] = v[d] ? p[d] : 0xffffffffu;
-            }
-        __syncwarp();
-        // one distinct cell per step: lanes 0..26 its 27 occupancies (a spread part of 0xffffffff,
-        // outside an open grid, makes the index >= 2^30), lane 30 the log of their sum (a warp
-        // reduction), lane 31 the constant; the loads of four cells are issued before their sums
-        for (unsigned int k0 = 0; k0 < m; k0 += 4u)
-            {
-            unsigned int o[4];
-#pragma unroll
-            for (unsigned int j = 0; j < 4u; ++j)
-                {
-                const unsigned int* pk = part + (k0 + j) * 9u;
-                o[j] = 0u;
-                if (lane < 27u && k0 + j < m)
-                    {
-                    const unsigned int idx = (pk[nb_x] << 2) | (pk[nb_y] << 1) | pk[nb_z];
-                    if (idx < (1u << 30)) o[j] = __ldg(a.occ + idx);
-                    }
-                }
-#pragma unroll
-            for (unsigned int j = 0; j < 4u; ++j)
-                {
-                const unsigned int k = k0 + j;
-                if (k >= m) break;   // uniform over the warp
-                const unsigned int sum = __reduce_add_sync(0xffffffffu, o[j]);
-                const float f = lane < 27u ? cap_log1p(s_log, o[j]) : (lane == 31u ? 1.f : cap_log1p(s_log, sum));
-                if (lane < 27u || lane >= 30u)
-                    cell[k * kCapCellStride + lane] = __bfloat16_as_ushort(__float2bfloat16_rn(f));
-                }
-            }
-        __syncwarp();
-        {
-        // the point's own words: 13 = (feature 26 of its cell, x fraction), 14 = (y, z fractions)
-        float fr3[3];
-        cap_frac(a.frame, pos, cx, cy, cz, fr3);
-        const unsigned int f26 = cell[ci * kCapCellStride + 26];
-        pt[lane] = make_uint2(f26 | ((unsigned int)__bfloat16_as_ushort(__float2bfloat16_rn(fr3[0])) << 16),
-                              pack_bf16x2(fr3[1], fr3[2]));
-        }
+        pt[lane] = ptw;
         __syncwarp();
         // The two m16 tiles (rows g, g + 8 and g + 16, g + 24 of this lane) go through the layers
         // kCapInferTiles at a time: every B fragment read from shared memory feeds that many MMAs.
@@ -531,6 +550,199 @@ __global__ void __launch_bounds__(kCapInferWarps * 32, kCapInferMinBlocks) k_cap
         }
         __syncwarp();
         }
+    }
+
+// ---------------------------------------------------------------------------------------------
+// Inference on the fifth-generation tensor cores (tcgen05).  A block of four warps takes 128
+// consecutive queries per step -- the M of one MMA.  Each warp gathers the features of its 32
+// queries as k_cap_infer does, and each lane writes its query's BF16 feature row into the A tile
+// of layer 1 (shared memory, K-major core matrices).  One thread issues H1 = X W1^T as two
+// tcgen05.mma (M 128, N 64, K 16) into 64 Tensor Memory columns; their completion arrives on an
+// mbarrier.  Each warp reads its 32 TMEM lanes (lane = query, a row per thread) with tcgen05.ld,
+// adds b1, applies the ReLU, rounds to BF16 and writes the A tile of layer 2; H2 = H1 W2^T (four
+// MMAs into the same columns) follows, and the output layer is a per-thread FP32 dot product of
+// relu(H2 + b2) with w3.  The rounding points are those of k_cap_infer: BF16 inputs, weights and
+// first hidden layer, FP32 accumulation and biases.  Accumulators start at zero and the bias is
+// added after the MMA (k_cap_infer starts them at the bias): outputs agree to FP32 summation
+// order.  Every mbarrier wait is bounded: one that gives up sets kStatusTensorWait, waits once
+// more (bounded) for the MMA in flight, frees the block's Tensor Memory and ends the block.
+// ---------------------------------------------------------------------------------------------
+constexpr int kCapTcWarps = 4;
+constexpr int kCapTcRows = kCapTcWarps * 32;   // 128 queries = the MMA's M = the TMEM lanes
+constexpr unsigned int kCapTcCols = 64;        // TMEM columns: H1, then H2 (N = 64)
+// ~39 KB of shared memory per block: five blocks per SM (20 warps, 320 of the 512 TMEM columns)
+constexpr int kCapTcMinBlocks = 5;
+// BF16 values per gathered cell row: 80 bytes, so that a row is read as five 16-byte words
+constexpr int kCapTcCellStride = 40;
+constexpr unsigned int kCapTcWaitLimit = 1u << 22;
+
+__global__ void __launch_bounds__(kCapTcRows, kCapTcMinBlocks) k_cap_infer_tc(const CapInferArgs a)
+    {
+    // A of layer 1: 128 rows x 32 BF16 (K-major core matrices, SBO 512)
+    __shared__ __align__(1024) unsigned char s_x[kCapTcRows * kCapIn * 2];
+    // A of layer 2: 128 rows x 64 BF16 (SBO 1024).  Warp w's rows are bytes [4096 w, 4096 w + 4096),
+    // which also hold its gather scratch (cell parts, cell rows) while its features are formed.
+    __shared__ __align__(1024) unsigned char s_h[kCapTcRows * kCapHidden * 2];
+    // B operands: W1 (64 x 32) and W2 (64 x 64), rows = output units, K-major like A
+    __shared__ __align__(1024) unsigned char s_w1[kCapHidden * kCapIn * 2];
+    __shared__ __align__(1024) unsigned char s_w2[kCapHidden * kCapHidden * 2];
+    __shared__ float s_b1[kCapHidden];
+    __shared__ float s_b2[kCapHidden];
+    __shared__ float s_w3[kCapHidden];
+    __shared__ float s_log[kCapLogTable];
+    __shared__ __align__(8) unsigned long long s_bar;
+    __shared__ unsigned int s_tmem;
+
+    const unsigned int lane = threadIdx.x & 31u;
+    const unsigned int warp = threadIdx.x >> 5;
+    // 16-byte chunk (n, kg) of a weight matrix = W[n][8 kg .. 8 kg + 7]
+    const uint4* wsrc = reinterpret_cast<const uint4*>(a.w);
+    for (unsigned int i = threadIdx.x; i < (unsigned int)(kCapHidden * kCapIn / 8); i += blockDim.x)
+        *reinterpret_cast<uint4*>(s_w1 + tc::kmajor_offset(i / (kCapIn / 8), (i % (kCapIn / 8)) * 8u, kCapIn)) =
+            wsrc[kCapBfW1 / 8 + i];
+    for (unsigned int i = threadIdx.x; i < (unsigned int)(kCapHidden * kCapHidden / 8); i += blockDim.x)
+        *reinterpret_cast<uint4*>(s_w2 + tc::kmajor_offset(i / (kCapHidden / 8), (i % (kCapHidden / 8)) * 8u,
+                                                           kCapHidden)) = wsrc[kCapBfW2 / 8 + i];
+    for (unsigned int i = threadIdx.x; i < (unsigned int)kCapHidden; i += blockDim.x)
+        {
+        s_b1[i] = a.p[kCapOffB1 + i];
+        s_b2[i] = a.p[kCapOffB2 + i];
+        s_w3[i] = __bfloat162float(a.w[kCapBfW3 + i]);
+        }
+    cap_fill_log_table(s_log);
+    if (warp == 0) tc::tmem_alloc(&s_tmem, kCapTcCols);
+    if (threadIdx.x == 0) tc::mbar_init(&s_bar, 1u);
+    tc::fence_proxy_async();   // the weights are read by the tensor core
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const unsigned int tmem = s_tmem;
+    const unsigned int t_rows = tmem + ((warp * 32u) << 16);   // this warp's 32 TMEM lanes
+    const float b3 = a.p[kCapOffB3];
+    unsigned int* part = reinterpret_cast<unsigned int*>(s_h + warp * 4096u);
+    unsigned short* cell = reinterpret_cast<unsigned short*>(s_h + warp * 4096u + 32u * 9u * 4u);
+    const unsigned int r = warp * 32u + lane;   // the thread's row of the tile
+    constexpr unsigned int idesc = tc::idesc_bf16_f32(kCapTcRows, kCapHidden);
+    const unsigned int x_addr = tc::smem_addr(s_x);
+    const unsigned int h_addr = tc::smem_addr(s_h);
+    const unsigned int w1_addr = tc::smem_addr(s_w1);
+    const unsigned int w2_addr = tc::smem_addr(s_w2);
+    unsigned int phase = 0u;
+    bool failed = false;
+    const unsigned int n_tiles = (a.N + (unsigned int)kCapTcRows - 1u) / (unsigned int)kCapTcRows;
+    for (unsigned int tile = blockIdx.x; tile < n_tiles; tile += gridDim.x)
+        {
+        // rows past the end repeat the last query (their outputs are not written)
+        const unsigned int q = tile * (unsigned int)kCapTcRows + r;
+        unsigned int ci;
+        uint2 ptw;
+        cap_warp_features<kCapTcCellStride>(a, s_log, min(q, a.N - 1u), lane, part, cell, ci, ptw);
+        {
+        // the query's feature row: its cell's row with words 13 and 14 its own
+        const uint4* src = reinterpret_cast<const uint4*>(cell + ci * kCapTcCellStride);
+        const uint4 v0 = src[0], v1 = src[1], v2 = src[2];
+        uint4 v3 = src[3];
+        v3.y = ptw.x;
+        v3.z = ptw.y;
+        *reinterpret_cast<uint4*>(s_x + tc::kmajor_offset(r, 0u, kCapIn)) = v0;
+        *reinterpret_cast<uint4*>(s_x + tc::kmajor_offset(r, 8u, kCapIn)) = v1;
+        *reinterpret_cast<uint4*>(s_x + tc::kmajor_offset(r, 16u, kCapIn)) = v2;
+        *reinterpret_cast<uint4*>(s_x + tc::kmajor_offset(r, 24u, kCapIn)) = v3;
+        }
+        tc::fence_proxy_async();
+        __syncthreads();
+        if (threadIdx.x == 0)
+            {
+            tc::fence_after_sync();
+#pragma unroll
+            for (unsigned int k = 0; k < (unsigned int)kCapIn / 16u; ++k)
+                tc::mma_bf16(tmem, tc::smem_desc(x_addr + k * 256u, 128u, kCapIn * 16u),
+                             tc::smem_desc(w1_addr + k * 256u, 128u, kCapIn * 16u), idesc, k > 0u);
+            tc::mma_commit(&s_bar);
+            }
+        bool ok = tc::mbar_wait_bounded(&s_bar, phase, kCapTcWaitLimit);
+        if (__syncthreads_or(!ok))
+            {
+            failed = true;
+            break;
+            }
+        phase ^= 1u;
+        tc::fence_after_sync();
+        {
+        // H1 = relu(acc + b1) rounded to BF16 -> the thread's row of the A tile of layer 2
+        unsigned int v[4][16];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) tc::ld_32x32b_x16(t_rows + 16u * c, v[c]);
+#pragma unroll
+        for (int c = 0; c < 4; ++c) tc::wait_ld(v[c]);
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+#pragma unroll
+            for (int h = 0; h < 2; ++h)
+                {
+                const int n0 = 16 * c + 8 * h;
+                unsigned int o[4];
+#pragma unroll
+                for (int j = 0; j < 4; ++j)
+                    o[j] = pack_relu_bf16x2(__uint_as_float(v[c][8 * h + 2 * j]) + s_b1[n0 + 2 * j],
+                                            __uint_as_float(v[c][8 * h + 2 * j + 1]) + s_b1[n0 + 2 * j + 1]);
+                *reinterpret_cast<uint4*>(s_h + tc::kmajor_offset(r, (unsigned int)n0, kCapHidden)) =
+                    make_uint4(o[0], o[1], o[2], o[3]);
+                }
+        }
+        tc::fence_proxy_async();
+        tc::fence_before_sync();
+        __syncthreads();
+        if (threadIdx.x == 0)
+            {
+            tc::fence_after_sync();
+#pragma unroll
+            for (unsigned int k = 0; k < (unsigned int)kCapHidden / 16u; ++k)
+                tc::mma_bf16(tmem, tc::smem_desc(h_addr + k * 256u, 128u, kCapHidden * 16u),
+                             tc::smem_desc(w2_addr + k * 256u, 128u, kCapHidden * 16u), idesc, k > 0u);
+            tc::mma_commit(&s_bar);
+            }
+        ok = tc::mbar_wait_bounded(&s_bar, phase, kCapTcWaitLimit);
+        if (__syncthreads_or(!ok))
+            {
+            failed = true;
+            break;
+            }
+        phase ^= 1u;
+        tc::fence_after_sync();
+        float z = 0.f;
+        {
+        unsigned int v[4][16];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) tc::ld_32x32b_x16(t_rows + 16u * c, v[c]);
+#pragma unroll
+        for (int c = 0; c < 4; ++c) tc::wait_ld(v[c]);
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+#pragma unroll
+            for (int j = 0; j < 16; ++j)
+                z = fmaf(fmaxf(__uint_as_float(v[c][j]) + s_b2[16 * c + j], 0.f), s_w3[16 * c + j], z);
+        }
+        // the next tile's MMA (after the next barrier) overwrites the columns just read
+        tc::fence_before_sync();
+        if (q < a.N)
+            {
+            const float y = cap_softplus(z + b3);
+            const unsigned int row = cap_row(a, q);
+            if (a.y_out) a.y_out[row] = y;
+            a.cap_out[row] = cap_from_output(y, a.margins[cap_margin_bin(y)], a.cap_max);
+            }
+        }
+    if (failed)
+        {
+        if (threadIdx.x == 0 && a.status) atomicOr(a.status, kStatusTensorWait);
+        // the MMA may still be in flight: give it one more bounded wait before its columns go
+        tc::mbar_wait_bounded(&s_bar, phase, kCapTcWaitLimit);
+        }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if (warp == 0) tc::tmem_dealloc(tmem, kCapTcCols);
     }
 
 // ---------------------------------------------------------------------------------------------

@@ -21,6 +21,7 @@ enum StatusBits : unsigned int
     kStatusOk = 0u,
     kStatusSortLookback = 1u,
     kStatusScanLookback = 2u,
+    kStatusTensorWait = 4u,   // a wait for a tensor-core MMA gave up
     };
 
 // Upper bound on polls of one look-back word (each poll sleeps ~64 ns after the first few), so a

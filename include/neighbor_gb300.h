@@ -312,6 +312,17 @@ int nbr_capmodel_get_margin(nbr_capmodel m, float* margin);
 int nbr_capmodel_set_margins(nbr_capmodel m, const float* margins);
 int nbr_capmodel_get_margins(nbr_capmodel m, float* margins);
 
+/* Inference kernel (no counterpart in the reference): NBR_CAP_INFER_WARP_TILES = warp tiles of
+ * mma.sync m16n8k16 (k_cap_infer), NBR_CAP_INFER_TENSOR_MEMORY = 128-query tiles on tcgen05 with
+ * Tensor Memory accumulators (k_cap_infer_tc).  Capacities agree up to FP32 summation order.
+ * nbr_capmodel_status reads and clears the device status word of the inference (bit 4 = a
+ * bounded wait for a tensor-core MMA gave up; that prediction is incomplete); synchronises. */
+#define NBR_CAP_INFER_WARP_TILES 0
+#define NBR_CAP_INFER_TENSOR_MEMORY 1
+int nbr_capmodel_set_infer_kernel(nbr_capmodel m, int kernel);
+int nbr_capmodel_get_infer_kernel(nbr_capmodel m, int* kernel);
+int nbr_capmodel_status(nbr_capmodel m, unsigned int* status);
+
 /* Weights file of a trained model: "NBRCAPMD", version 1, its shapes, the FP32 parameters and
  * margin table, and an FNV-1a hash; load returns NBR_ERR_INVALID for a file whose magic,
  * version, shapes, size or hash differ. */

@@ -134,6 +134,9 @@ def _declare(L):
     sig("nbr_capmodel_save", [_P, ctypes.c_char_p])
     sig("nbr_capmodel_load", [_P, ctypes.c_char_p])
     sig("nbr_capmodel_get_margins", [_P, _P])
+    sig("nbr_capmodel_set_infer_kernel", [_P, _I])
+    sig("nbr_capmodel_get_infer_kernel", [_P, ctypes.POINTER(_I)])
+    sig("nbr_capmodel_status", [_P, ctypes.POINTER(_U)])
     sig("nbr_capmodel_level", [_F, _P, _P, ctypes.POINTER(_U)])
     sig("nbr_capmodel_features", [_P, _P, _P, _P, _F, _I, _P, _P])
     sig("nbr_capmodel_predict", [_P, _P, _P, _P, _F, _I, _I, _U, _P, _P, _P])
@@ -183,7 +186,8 @@ EXPORTED = ["nbr_last_error", "nbr_version", "nbr_lbvh_create", "nbr_lbvh_destro
             "nbr_capmodel_create", "nbr_capmodel_destroy", "nbr_capmodel_get_params",
             "nbr_capmodel_set_params", "nbr_capmodel_set_margin", "nbr_capmodel_get_margin",
             "nbr_capmodel_set_margins", "nbr_capmodel_get_margins", "nbr_capmodel_save",
-            "nbr_capmodel_load",
+            "nbr_capmodel_load", "nbr_capmodel_set_infer_kernel", "nbr_capmodel_get_infer_kernel",
+            "nbr_capmodel_status",
             "nbr_capmodel_level", "nbr_capmodel_features", "nbr_capmodel_predict",
             "nbr_capmodel_targets", "nbr_capmodel_gradient", "nbr_capmodel_train",
             "nbr_onepass_create", "nbr_onepass_destroy", "nbr_onepass_capacity",
@@ -198,6 +202,8 @@ BATCH_MAX_N = 16384
 CAP_PARAMS = 6337
 CAP_FEATURES = 32
 CAP_MARGIN_BINS = 16
+CAP_INFER_WARP_TILES = 0      # mma.sync m16n8k16 warp tiles (k_cap_infer)
+CAP_INFER_TENSOR_MEMORY = 1   # tcgen05 128-query tiles, Tensor Memory accumulators (k_cap_infer_tc)
 
 NOALLOC_MAX_POINTS = 1 << 20
 
@@ -763,6 +769,23 @@ class CapacityModel:
     def margins(self, table):
         t = (ctypes.c_float * CAP_MARGIN_BINS)(*[float(v) for v in table])
         _check(self._L.nbr_capmodel_set_margins(self._h, ctypes.cast(t, ctypes.c_void_p)))
+
+    @property
+    def infer_kernel(self) -> int:
+        """CAP_INFER_WARP_TILES or CAP_INFER_TENSOR_MEMORY: the kernel predict() runs."""
+        v = ctypes.c_int()
+        _check(self._L.nbr_capmodel_get_infer_kernel(self._h, ctypes.byref(v)))
+        return v.value
+
+    @infer_kernel.setter
+    def infer_kernel(self, kernel: int):
+        _check(self._L.nbr_capmodel_set_infer_kernel(self._h, int(kernel)))
+
+    def status(self) -> int:
+        """Device status word of the inference, read and cleared (4 = a tensor-core wait gave up)."""
+        v = ctypes.c_uint()
+        _check(self._L.nbr_capmodel_status(self._h, ctypes.byref(v)))
+        return v.value
 
     def save(self, path: str):
         """Write the weights file (parameters, margin table, shapes, hash)."""

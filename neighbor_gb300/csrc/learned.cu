@@ -158,6 +158,28 @@ int nbr_capmodel_get_margins(nbr_capmodel m, float* margins)
     return NBR_OK;
     }
 
+int nbr_capmodel_set_infer_kernel(nbr_capmodel m, int kernel)
+    {
+    if (!m) return fail(NBR_ERR_INVALID, "null handle");
+    if (kernel != NBR_CAP_INFER_WARP_TILES && kernel != NBR_CAP_INFER_TENSOR_MEMORY)
+        return fail(NBR_ERR_INVALID, "unknown inference kernel");
+    m->model.setInferKernel(static_cast<neighbor::CapacityModel::InferKernel>(kernel));
+    return NBR_OK;
+    }
+
+int nbr_capmodel_get_infer_kernel(nbr_capmodel m, int* kernel)
+    {
+    if (!m || !kernel) return fail(NBR_ERR_INVALID, "null argument");
+    *kernel = static_cast<int>(m->model.getInferKernel());
+    return NBR_OK;
+    }
+
+int nbr_capmodel_status(nbr_capmodel m, unsigned int* status)
+    {
+    if (!m || !status) return fail(NBR_ERR_INVALID, "null argument");
+    return guarded([&] { *status = m->model.takeStatus(); });
+    }
+
 int nbr_capmodel_save(nbr_capmodel m, const char* path)
     {
     if (!m || !path) return fail(NBR_ERR_INVALID, "null argument");

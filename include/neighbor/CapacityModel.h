@@ -34,7 +34,7 @@ class CapacityModel
         static constexpr int kParams = gpu::kCapParams;
         static constexpr int kFeatures = gpu::kCapIn;
 
-        explicit CapacityModel(unsigned long long seed = 1) : m_step(0), m_infer(InferKernel::WarpTiles)
+        explicit CapacityModel(unsigned long long seed = 1) : m_step(0), m_infer(InferKernel::TensorMemory)
             {
             setMargin(0.f);
             m_status.reserve(1);

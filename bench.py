@@ -66,6 +66,7 @@ def parse(argv=None):
     ap.add_argument("--no-clustered", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-polydisperse", action="store_true")
+    ap.add_argument("--no-f64", action="store_true", help="skip the double-precision section")
     ap.add_argument("--no-small", action="store_true")
     ap.add_argument("--train-steps", type=int, default=4000)
     ap.add_argument("--climb", type=int, default=512)
@@ -572,6 +573,88 @@ def polydisperse_step(nb, trees, trav, species, L, skin=0.4, diam=(1.0, 10.0), l
     return out
 
 
+def double_precision(nb, args, stream, n=16_777_216, rc=RC, steps=5, warmup=2, n_frames=3):
+    """Double-precision positions (HOOMD-blue's Scalar = double): the plain two-pass step on a
+    uniform trajectory of n points (density 0.85, sigma 0.05, frames cycled) with PointInsertOpF64
+    and ExactSphereQueryOpF64 -- build, queries in the tree's sorted order, count, host read of the
+    largest count, fill -- on the double walk (k_traverse_fast_f64).  Beside it: the same step on
+    the library's reference-layout walk of the same op, and the reference's own kernels running it
+    with the harness's double insert and exact query ops on the same frames.  Checks: the last
+    frame's counts and row hashes against the reference-layout walk, its pair total against the
+    reference kernels'."""
+    import numpy as np
+    import torch
+    # the box length is a float (the reference driver reads it as one): both sides wrap by it
+    L = float(np.float32((n / DENSITY) ** (1.0 / 3.0)))
+    box = [L, L, L]
+    pad = nb.exact_pad(rc, 2 * L)
+    g = torch.Generator(device="cuda")
+    g.manual_seed(5151)
+    base = [torch.rand((n, 3), dtype=torch.float64, device="cuda", generator=g) * L]
+    for _ in range(n_frames - 1):
+        step_ = torch.randn((n, 3), dtype=torch.float64, device="cuda", generator=g) * SIGMA
+        base.append(torch.remainder(base[-1] + step_, L))
+    frames = [base[k % n_frames] for k in range(warmup + steps)]
+    lbvh = nb.LBVH(leaf_size=args.leaf, radix_bits=args.radix_bits, climb_block=args.climb)
+    sph = torch.empty((n, 4), dtype=torch.float64, device="cuda")
+    sph[:, 3] = rc
+    counts = torch.empty(n, dtype=torch.int32, device="cuda")
+    store = {"flat": torch.empty(n * 32, dtype=torch.int32, device="cuda")}
+
+    def make_step(trav):
+        def step(P):
+            lbvh.build_f64(P, [0, 0, 0], box, block_size=args.block)
+            sph[:, :3] = P[lbvh.primitives().long()]
+            trav.traverse_f64(lbvh, sph, P, box, pad, images="periodic", nneigh=counts, block_size=args.block)
+            mx, total, _ = trav.count_summary(stream)   # the host read of the two-pass pattern
+            if store["flat"].numel() < n * mx:
+                store["flat"] = torch.empty(n * mx, dtype=torch.int32, device="cuda")
+            lst = store["flat"][: n * max(mx, 1)].view(n, max(mx, 1))
+            trav.traverse_f64(lbvh, sph, P, box, pad, images="periodic", max_neigh=max(mx, 1), nneigh=counts,
+                              neigh_list=lst, block_size=args.block)
+            return total, mx
+        return step
+
+    fast = nb.LBVHTraverser()
+    ms_fast, outs = time_steps(make_step(fast), frames, warmup, stream)
+    total_last, mx_last = outs[-1]
+    c_fast = counts.clone()
+    h_fast = row_hashes(store["flat"], c_fast, max(mx_last, 1)) if mx_last <= 64 else None
+    ref_layout = nb.LBVHTraverser()
+    ref_layout.set_fast_path(False)
+    ms_ref_layout, outs_r = time_steps(make_step(ref_layout), frames, warmup, stream)
+    c_ref = counts.clone()
+    h_ref = row_hashes(store["flat"], c_ref, max(outs_r[-1][1], 1)) if outs_r[-1][1] <= 64 else None
+    rows_equal = bool(torch.equal(c_fast, c_ref)) and h_fast is not None and h_ref is not None \
+        and bool(torch.equal(h_fast, h_ref))
+    pairs = float(sum(o[0] for o in outs)) / len(outs)
+    ref = None
+    if not args.no_ref_cuda:
+        try:
+            from oracle import ref_harness
+            if ref_harness.build_if_available() and ref_harness.available():
+                r = ref_harness.run_frames64([b.cpu().numpy() for b in base], rc, L, steps, warmup)
+                best, sweep = best_block(r)
+                ref = {"step_ms": best["step_ms"], "block": best["block"],
+                       "stages_ms": {k: best[k] for k in ("build_ms", "setup_ms", "count_ms", "fill_ms")},
+                       "pairs_last_frame": r["pairs_last_frame"], "sweep_ms": sweep,
+                       "step": "build, setup, count, max read, fill (stride list) on the same double frames"}
+            else:
+                ref = {"unavailable": "reference kernels not built here"}
+        except Exception as e:  # measurement aid only: never fails the bench
+            ref = {"unavailable": f"{type(e).__name__}: {e}"[:200]}
+    out = {"workload": f"uniform trajectory N={n} in float64, density 0.85 L={L:.2f} rc={rc} sigma={SIGMA}, "
+                       f"{n_frames} frames cycled, 27 images; build + count + max read + fill",
+           "ms_per_step": ms_fast, "value": pairs / (ms_fast * 1e-3), "unit": "pairs/s", "pairs_per_step": pairs,
+           "reference_layout_walk_ms": ms_ref_layout,
+           "rows_equal_reference_layout_walk": rows_equal,
+           "reference_cuda": ref}
+    if ref and "step_ms" in ref:
+        out["vs_reference_cuda"] = ref["step_ms"] / ms_fast
+        out["pairs_last_frame_equal_reference"] = float(total_last) == float(ref["pairs_last_frame"])
+    return out
+
+
 def polydisperse_c2(nb, args, stream, steps=5, warmup=2):
     """Polydisperse colloid mixture: 999,001 spheres of diameter 1 and 999 of diameter 10, each
     species at volume fraction 0.10, uniform in a periodic cube (L = 173.59); one tree per
@@ -930,6 +1013,8 @@ def run_ours(args):
         line["clustered_4m"] = clustered_c3(nb, args, stream)
     if not args.no_polydisperse:
         line["polydisperse_1m"] = polydisperse_c2(nb, args, stream)
+    if not args.no_f64:
+        line["double_16m"] = double_precision(nb, args, stream, n=n)
     if not args.no_batched:
         line["batched_4096"] = batched_ensemble(nb, args, stream)
     if not args.no_small:
@@ -964,6 +1049,8 @@ def summary(line):
             "predict_ms_tcgen05": get(line, "learned", "predict_ms", "tensor_memory_tcgen05"),
             "clustered_learned_vs_plain": get(line, "clustered_4m", "learned_vs_plain"),
             "clustered_vs_reference_cuda": get(line, "clustered_4m", "plain_vs_reference_cuda"),
+            "double_16m_ms": get(line, "double_16m", "ms_per_step"),
+            "double_16m_vs_reference_cuda": get(line, "double_16m", "vs_reference_cuda"),
             "polydisperse_ms": get(line, "polydisperse_1m", "ms_per_step"),
             "polydisperse_vs_reference_cuda": get(line, "polydisperse_1m", "vs_reference_cuda"),
             "batched_vs_sequential": get(line, "batched_4096", "batched_vs_sequential"),

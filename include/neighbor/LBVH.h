@@ -26,6 +26,7 @@
 #include <cstring>
 #include <stdexcept>
 #include <string>
+#include <type_traits>
 
 #include <cuda_runtime.h>
 
@@ -68,7 +69,7 @@ class LBVH : public Tunable<unsigned int>
     public:
         LBVH()
             : Tunable<unsigned int>(32, 1024, 32), m_root(LBVHSentinel), m_N(0), m_N_internal(0),
-              m_N_nodes(0), m_capacity(0), m_leaf_size(4), m_radix_bits(8), m_fast_points(false),
+              m_N_nodes(0), m_capacity(0), m_leaf_size(4), m_radix_bits(8), m_fast_points(false), m_fast_f64(false),
               m_epoch(0), m_block(256), m_climb_block(512), m_stream(0), m_ref_valid(true),
               m_sorted_event(nullptr)
             {}
@@ -181,6 +182,9 @@ class LBVH : public Tunable<unsigned int>
 
         // True when the last build used a point insert op, so fastData() holds point positions.
         bool hasFastData() const { return m_fast_points && m_N > 0; }
+        // True when the last build used PointInsertOpF64: fastData()'s point records hold each
+        // double point rounded down to FP32 (its leaf box's lower corner), for the double walk.
+        bool hasFastF64Data() const { return m_fast_f64 && m_N > 0; }
 
         FastLBVHData fastData() const
             {
@@ -253,6 +257,7 @@ class LBVH : public Tunable<unsigned int>
         unsigned int m_leaf_size;
         unsigned int m_radix_bits;
         bool m_fast_points;
+        bool m_fast_f64;
         unsigned int m_epoch;
         unsigned long long m_build_id = 0;
         unsigned int m_block;
@@ -490,6 +495,7 @@ void LBVH::build(const LaunchParameters& params, const InsertOpT& insert, const 
     const detail::TraceRange trace_range("neighbor::LBVH::build");
     setup(params, insert);
     m_fast_points = is_point_insert<InsertOpT>::value;
+    m_fast_f64 = std::is_same<InsertOpT, PointInsertOpF64>::value;
     m_ref_valid = true;
     if (m_N == 0) return;
     checkParameter(params);

@@ -8,7 +8,8 @@
 //
 // Routing.  An ExactSphereQueryOp with CountNeighborsOp or NeighborListOp on a tree built from
 // points runs the fast kernel over the LBVH's 16-bit pre-order nodes (no compression step; the
-// transform is applied to the reported ids).  Any other combination of ops -- including the
+// transform is applied to the reported ids); an ExactSphereQueryOpF64 on a tree of
+// PointInsertOpF64 runs the same walk with the double predicate (k_traverse_fast_f64).  Any other combination of ops -- including the
 // stock SphereQueryOp, whose superset result depends on the node format -- runs the
 // reference-layout rope kernel, so it returns exactly what the reference returns.
 #ifndef NEIGHBOR_LBVH_TRAVERSER_H_
@@ -525,6 +526,54 @@ void LBVHTraverser::traverse(const LaunchParameters& params, const LBVH& lbvh, c
             a.box = query.box;
             a.pad = query.pad;
             launch_fast(params, lbvh, a, out, transform, query.size());
+            if constexpr (std::is_same<OutputOpT, CountNeighborsOp>::value)
+                {
+                summarize_counts(params.stream, out.nneigh, query.size(), lbvh.getStatusPointer());
+                m_summary_self = false;
+                }
+            return;
+            }
+        }
+
+    if constexpr (std::is_same<QueryOpT, ExactSphereQueryOpF64>::value && output_kind<OutputOpT>::value != 0
+                  && detail::is_float3_images<TranslateOpT>::value)
+        {
+        if (m_fast_enabled && lbvh.hasFastF64Data())
+            {
+            gpu::FastQueryArgsF64 a;
+            a.spheres = query.spheres;
+            a.Q = query.size();
+            a.points = query.points;
+            a.box = query.box;
+            a.pad = query.pad;
+            a.images = detail::image_pointer(images);
+            a.n_images = images.size();
+            a.lattice = detail::image_lattice(images);
+            a.lattice_L = detail::lattice_box(images, make_float3((float)query.box.x, (float)query.box.y,
+                                                                  (float)query.box.z));
+            a.nneigh = out.nneigh;
+            if constexpr (std::is_same<OutputOpT, NeighborListOp>::value)
+                {
+                a.list = out.neigh_list;
+                a.max_neigh = out.max_neigh;
+                }
+            else if constexpr (std::is_same<OutputOpT, CSRNeighborListOp>::value)
+                {
+                a.list = out.neigh_list;
+                a.max_neigh = out.max_capacity;
+                a.offsets = out.offsets;
+                a.caps = out.capacity;
+                }
+            else
+                {
+                a.list = nullptr;
+                a.max_neigh = 0;
+                }
+            constexpr int kind = output_kind<OutputOpT>::value;
+            const unsigned int bs = params.tunable;
+            gpu::k_traverse_fast_f64<kind, TransformOpT><<<detail::ceil_div(query.size(), bs), bs, 0, params.stream>>>(
+                lbvh.fastData(), a, transform);
+            detail::check_cuda(cudaGetLastError(), "double traversal launch");
             if constexpr (std::is_same<OutputOpT, CountNeighborsOp>::value)
                 {
                 summarize_counts(params.stream, out.nneigh, query.size(), lbvh.getStatusPointer());

@@ -465,6 +465,177 @@ __global__ void k_traverse_fast(const FastLBVHData tree, const FastQueryArgs a,
     }
 
 // ---------------------------------------------------------------------------------------------
+// Double-precision queries (ExactSphereQueryOpF64 on a tree of PointInsertOpF64): the walk of
+// k_traverse_fast over the same records, with every pair decided as the double predicate decides
+// it and double arithmetic only where FP32 cannot decide.
+//
+// Records.  A point record holds the leaf box's lower corner, the double point rounded down to
+// FP32.  The query box of an image is the double box (centre + image, radius cutoff + pad, the
+// op's own rounding) rounded outward to FP32.  A point inside the double box has its rounded-down
+// corner inside the FP32 box (the corner is the largest float not above the point, and both box
+// faces are floats on the right side of the point), so the record test never drops a pair.  Image
+// boxes are separated by box lengths above 2 (cutoff + pad), so each pair is found through one
+// image.  Images are chosen in FP32 with a margin (a superset: an extra image finds nothing).
+//
+// Pairs.  d = minimum image of (record - query) in FP32 differs from the double d of the exact
+// predicate by at most 4 ulp(M) per component, M bounding every coordinate and box length: the
+// query rounded to nearest (1/2 ulp), the record rounded down (1 ulp), the difference and the wrap
+// each rounded (1/2 ulp(2M) = 1 ulp(M) each), the box length rounded (1/2 ulp).  A wrap that
+// FP32 and double decide differently leaves |d| near L/2 > cutoff in both.  So |d|_FP32 and |d|
+// differ by less than 7 ulp(M), and the squares and sums of FP32 add a relative 3 2^-24.  With
+// eps = 16 ulp(M) + 8 2^-24 rc + 2 ulp(rc): |d|^2_FP32 below (rc - eps)^2 is a pair for the double
+// predicate, above (rc + eps)^2 is not, and only the band between takes exact_pair_f64 on the
+// double positions (read through the reported id, as the op's refine() reads them).
+// Rows hold the same entries in the same order as the reference-layout walk of the same op: both
+// visit the images in bit order and the points of a subtree in sorted order.
+// ---------------------------------------------------------------------------------------------
+struct FastQueryArgsF64
+    {
+    const double4_16a* spheres;  // (x, y, z, cutoff) per query
+    unsigned int Q;
+    const double3* points;       // double positions, indexed by the reported id
+    double3 box;                 // periodic lengths for the minimum image (0 = open)
+    float pad;
+    const float3* images;        // image list; NULL => self image only, or the lattice below
+    unsigned int n_images;
+    int lattice;
+    float3 lattice_L;
+    unsigned int* nneigh;
+    unsigned int* list;
+    unsigned int max_neigh;
+    const unsigned long long* offsets = nullptr;  // kFastCSR
+    const unsigned int* caps = nullptr;           // kFastCSR
+    };
+
+__device__ __forceinline__ float3 image_vector_f64(const FastQueryArgsF64& a, int i)
+    {
+    if (a.lattice) return PeriodicImagesOp(a.lattice_L).get((unsigned int)i);
+    return a.images ? a.images[i] : make_float3(0.f, 0.f, 0.f);
+    }
+
+// ulp of a non-negative finite float (the spacing of floats at x's binade; 0 below the normals).
+__device__ __forceinline__ float ulp_of(float x)
+    {
+    return __int_as_float(__float_as_int(x) & 0x7f800000) * 1.1920929e-7f;   // 2^e * 2^-23
+    }
+
+__device__ __forceinline__ float wrap_f32(float d, float L)
+    {
+    if (L > 0.f)
+        {
+        const float h = __fmul_rn(0.5f, L);
+        if (d >= h)
+            d = __fsub_rn(d, L);
+        else if (d < -h)
+            d = __fadd_rn(d, L);
+        }
+    return d;
+    }
+
+template<int OUT, class TransformOpT>
+__global__ void k_traverse_fast_f64(const FastLBVHData tree, const FastQueryArgsF64 a, const TransformOpT transform)
+    {
+    __shared__ QuantFrame s_frame;
+    __shared__ unsigned int s_records;
+    if (threadIdx.x == 0)
+        {
+        s_frame = *tree.frame;
+        s_records = ld_status(tree.status) != 0u ? 0u : *tree.n_boxes + tree.N;
+        }
+    __syncthreads();
+    const unsigned int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= a.Q) return;
+    const QuantFrame f = s_frame;
+    const unsigned int n_rec = s_records;
+    const double4_16a s = a.spheres[q];
+    const double3 P = make_double3(s.x, s.y, s.z);
+    const double rs = __dadd_ru(s.w, (double)a.pad);
+    const float3 Pf = make_float3(__double2float_rn(P.x), __double2float_rn(P.y), __double2float_rn(P.z));
+    const float3 Lf = make_float3(__double2float_rn(a.box.x), __double2float_rn(a.box.y), __double2float_rn(a.box.z));
+    // M bounds every coordinate of the query, the scene and the box lengths (and the images)
+    float M = fmaxf(fmaxf(fabsf(Pf.x), fabsf(Pf.y)), fabsf(Pf.z));
+    M = fmaxf(M, fmaxf(fmaxf(fabsf(f.lo.x), fabsf(f.lo.y)), fabsf(f.lo.z)));
+    M = fmaxf(M, fmaxf(fmaxf(fabsf(f.hi.x), fabsf(f.hi.y)), fabsf(f.hi.z)));
+    M = fmaxf(M, fmaxf(fmaxf(Lf.x, Lf.y), Lf.z));
+    const float rcf = __double2float_ru(s.w);
+    const float eps = 16.f * ulp_of(fmaxf(M, 1.17549435e-38f)) + 4.7683716e-7f * rcf + 2.f * ulp_of(rcf);
+    const float lo_r = approx::fsub_rd(__double2float_rd(s.w), eps);
+    const float in2 = lo_r > 0.f ? approx::fmul_rd(lo_r, lo_r) : -1.f;   // below: a pair
+    const float hi_r = approx::fadd_ru(rcf, eps);
+    const float out2 = approx::fmul_ru(hi_r, hi_r);                        // above: not a pair
+    // images whose box may meet the scene, in FP32 with a margin for the query's rounding
+    const float rsf = approx::fadd_ru(__double2float_ru(rs), 2.f * ulp_of(fmaxf(M, 1.17549435e-38f)));
+    unsigned int flags = 0u;
+    if (n_rec)
+        {
+        if (a.lattice)
+            flags = lattice_flags(a.lattice_L, f, Pf, rsf);
+        else
+            {
+            const unsigned int nimg = a.images ? min(a.n_images, 32u) : 1u;
+            for (unsigned int k = 0; k < nimg; ++k)
+                {
+                const float3 t = image_vector_f64(a, (int)k);
+                const float3 c = make_float3(__fadd_rn(Pf.x, t.x), __fadd_rn(Pf.y, t.y), __fadd_rn(Pf.z, t.z));
+                const float3 lo = make_float3(approx::fsub_rd(c.x, rsf), approx::fsub_rd(c.y, rsf), approx::fsub_rd(c.z, rsf));
+                const float3 hi = make_float3(approx::fadd_ru(c.x, rsf), approx::fadd_ru(c.y, rsf), approx::fadd_ru(c.z, rsf));
+                if (lo.x <= f.hi.x && hi.x >= f.lo.x && lo.y <= f.hi.y && hi.y >= f.lo.y && lo.z <= f.hi.z
+                    && hi.z >= f.lo.z)
+                    flags |= 1u << k;
+                }
+            }
+        }
+    unsigned long long row_first = 0;
+    unsigned int cap = 0;
+    if (OUT != kFastCount) row_layout<OUT>(a.offsets, a.caps, a.max_neigh, q, row_first, cap);
+    unsigned int count = 0;
+    while (flags)
+        {
+        const int bit = __ffs(flags) - 1;
+        flags &= flags - 1u;
+        const float3 t = image_vector_f64(a, bit);
+        const double3 c = make_double3(__dadd_rn(P.x, (double)t.x), __dadd_rn(P.y, (double)t.y),
+                                       __dadd_rn(P.z, (double)t.z));
+        const float3 qlo = make_float3(__double2float_rd(__dsub_rd(c.x, rs)), __double2float_rd(__dsub_rd(c.y, rs)),
+                                       __double2float_rd(__dsub_rd(c.z, rs)));
+        const float3 qhi = make_float3(__double2float_ru(__dadd_ru(c.x, rs)), __double2float_ru(__dadd_ru(c.y, rs)),
+                                       __double2float_ru(__dadd_ru(c.z, rs)));
+        const uint3 qb = pack_query_box(f, qlo, qhi);
+        unsigned int i = 0;
+        while (i < n_rec)
+            {
+            const uint4 n = __ldg(tree.nodes + i);
+            if ((int)n.w < 0)
+                {
+                const float3 x = make_float3(__uint_as_float(n.x), __uint_as_float(n.y), __uint_as_float(n.z));
+                if (point_in_box(x, qlo, qhi))
+                    {
+                    const float dx = wrap_f32(__fsub_rn(x.x, Pf.x), Lf.x);
+                    const float dy = wrap_f32(__fsub_rn(x.y, Pf.y), Lf.y);
+                    const float dz = wrap_f32(__fsub_rn(x.z, Pf.z), Lf.z);
+                    const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+                    if (d2 <= out2)
+                        {
+                        const unsigned int id = transform(tree.primitive[n.w & ~kLeafFlag]);
+                        if (d2 < in2 || exact_pair_f64(P, a.points[id], s.w, a.box))
+                            {
+                            if (OUT != kFastCount && count < cap) a.list[row_first + count] = id;
+                            ++count;
+                            }
+                        }
+                    }
+                ++i;
+                }
+            else
+                {
+                i = node_overlaps(n, qb) ? i + 1u : max(n.w, i + 1u);
+                }
+            }
+        }
+    a.nneigh[q] = count;
+    }
+
+// ---------------------------------------------------------------------------------------------
 // One warp per query (long rows, few queries).  The warp takes the records in chunks of 32 in
 // pre-order: lane k tests record i + k.  A box that misses covers the records up to its skip link,
 // so a record is live when no earlier live-or-not missed box of the chunk covers it (a prefix

@@ -93,6 +93,19 @@ def run_frames(frames, rc, L, steps, warmup, timeout=900):
         return _run(["frames", path, n, len(frames), repr(float(rc)), repr(float(L)), steps, warmup], timeout)
 
 
+def run_frames64(frames, rc, L, steps, warmup, timeout=900):
+    """The plain step on the given double-precision frames ([n, 3] float64 arrays, cycled) with the
+    harness's double insert op and double exact query op through the reference's kernels, every
+    block size; adds the pair total of the last timed frame."""
+    n = len(frames[0])
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "frames.f64")
+        with open(path, "wb") as f:
+            for fr in frames:
+                np.ascontiguousarray(fr, np.float64).reshape(-1, 3).tofile(f)
+        return _run(["frames64", path, n, len(frames), repr(float(rc)), repr(float(L)), steps, warmup], timeout)
+
+
 def run_poly(small_frames, large_frames, L, steps, warmup, timeout=900):
     """Two-tree polydisperse step (diameters 1 and 10, cutoff (di+dj)/2 + 0.4, 27 images) on the
     given frames of each species, every block size."""

@@ -17,6 +17,9 @@
 //                                                    write the reference's outputs for given
 //                                                    points (sphere r: a SphereInsertOp tree)
 //   ref_driver hash  in.f32 N rc L out               counts and per-row hashes of the exact list
+//   ref_driver frames64 in.f64 N F rc L steps warmup the plain two-pass step on F given double
+//                                                    frames (the harness's double insert and
+//                                                    exact query ops), every block size
 //
 // Kernel parameters are passed as byte images of the reference's structs; the layouts below are
 // asserted here and, against the reference's own definitions, in ref_kernels.cu.
@@ -46,6 +49,9 @@ struct ImageListOp { const float3* images; unsigned int N; };
 struct SphereQueryOp { const float4* spheres; unsigned int N; };
 struct NullTransformOp {};
 struct RefExactQueryOp { const float4* spheres; unsigned int N; const float3* points; float3 box; float pad; };
+struct RefPointInsertOpF64 { const double3* points; unsigned int N; };
+struct __align__(16) RefSphereF64 { double x, y, z, w; };
+struct RefExactQueryOpF64 { const RefSphereF64* spheres; unsigned int N; const double3* points; double3 box; float pad; };
 
 static_assert(sizeof(PointInsertOp) == 16 && offsetof(PointInsertOp, N) == 8, "layout");
 static_assert(sizeof(SphereInsertOp) == 16 && offsetof(SphereInsertOp, r) == 8 && offsetof(SphereInsertOp, N) == 12,
@@ -59,6 +65,10 @@ static_assert(sizeof(SphereQueryOp) == 16, "layout");
 static_assert(sizeof(NullTransformOp) == 1, "layout");
 static_assert(sizeof(RefExactQueryOp) == 40 && offsetof(RefExactQueryOp, points) == 16
               && offsetof(RefExactQueryOp, box) == 24 && offsetof(RefExactQueryOp, pad) == 36, "layout");
+static_assert(sizeof(RefPointInsertOpF64) == 16 && offsetof(RefPointInsertOpF64, N) == 8, "layout");
+static_assert(sizeof(RefExactQueryOpF64) == 56 && offsetof(RefExactQueryOpF64, N) == 8
+              && offsetof(RefExactQueryOpF64, points) == 16 && offsetof(RefExactQueryOpF64, box) == 24
+              && offsetof(RefExactQueryOpF64, pad) == 48, "layout");
 
 void check(cudaError_t e, const char* what)
     {
@@ -74,6 +84,7 @@ struct Kernels
     CUfunction gen_codes = nullptr, gen_tree = nullptr, bubble = nullptr, one = nullptr, compress = nullptr;
     CUfunction gen_codes_sph = nullptr, bubble_sph = nullptr, one_sph = nullptr;
     CUfunction count_stock = nullptr, count_exact = nullptr, list_exact = nullptr, list_stock = nullptr;
+    CUfunction gen_codes_f64 = nullptr, bubble_f64 = nullptr, one_f64 = nullptr, count_f64 = nullptr, list_f64 = nullptr;
     };
 
 Kernels load_kernels(const char* cubin)
@@ -95,6 +106,19 @@ Kernels load_kernels(const char* cubin)
         checkd(cuModuleGetFunction(&f, mod, name), "get function");
         auto has = [&](const char* x) { return s.find(x) != std::string::npos; };
         const bool sph = has("SphereInsertOp");
+        if (has("RefPointInsertOpF64"))
+            {
+            if (has("lbvh_gen_codes")) k.gen_codes_f64 = f;
+            else if (has("lbvh_bubble_aabbs")) k.bubble_f64 = f;
+            else if (has("lbvh_one_primitive")) k.one_f64 = f;
+            continue;
+            }
+        if (has("RefExactQueryOpF64"))
+            {
+            if (has("CountNeighborsOp")) k.count_f64 = f;
+            else if (has("NeighborListOp")) k.list_f64 = f;
+            continue;
+            }
         if (has("lbvh_gen_codes")) (sph ? k.gen_codes_sph : k.gen_codes) = f;
         else if (has("lbvh_gen_tree")) k.gen_tree = f;
         else if (has("lbvh_bubble_aabbs")) (sph ? k.bubble_sph : k.bubble) = f;
@@ -106,7 +130,8 @@ Kernels load_kernels(const char* cubin)
         else if (has("lbvh_traverse_ropes") && has("NeighborListOp") && has("SphereQueryOp")) k.list_stock = f;
         }
     if (!k.gen_codes || !k.gen_tree || !k.bubble || !k.one || !k.compress || !k.count_stock || !k.count_exact || !k.list_exact
-        || !k.list_stock || !k.gen_codes_sph || !k.bubble_sph || !k.one_sph)
+        || !k.list_stock || !k.gen_codes_sph || !k.bubble_sph || !k.one_sph || !k.gen_codes_f64 || !k.bubble_f64
+        || !k.one_f64 || !k.count_f64 || !k.list_f64)
         { fprintf(stderr, "reference kernels missing from %s\n", cubin); exit(3); }
     return k;
     }
@@ -179,20 +204,34 @@ struct RefTree
         {
         PointInsertOp ins{pts, N};
         SphereInsertOp sins{pts, r, N};
-        const bool sphere = r >= 0.f;
-        void* insp = sphere ? (void*)&sins : (void*)&ins;
+        if (r >= 0.f)
+            build_with(K, K.gen_codes_sph, K.bubble_sph, K.one_sph, &sins, slo, shi, bs, s);
+        else
+            build_with(K, K.gen_codes, K.bubble, K.one, &ins, slo, shi, bs, s);
+        }
+
+    // the same with the harness's double-precision point insert op
+    void build_f64(const Kernels& K, const double3* pts, float3 slo, float3 shi, unsigned int bs, cudaStream_t s)
+        {
+        RefPointInsertOpF64 ins{pts, N};
+        build_with(K, K.gen_codes_f64, K.bubble_f64, K.one_f64, &ins, slo, shi, bs, s);
+        }
+
+    void build_with(const Kernels& K, CUfunction gen_codes, CUfunction bubble, CUfunction one, void* insp, float3 slo,
+                    float3 shi, unsigned int bs, cudaStream_t s)
+        {
         sel_codes = sel_idx = 0;
         if (N == 1)
             {
             LBVHData t = tree_data();
             void* a[] = {&t, insp};
-            checkd(cuLaunchKernel(sphere ? K.one_sph : K.one, 1, 1, 1, 1, 1, 1, 0, (CUstream)s, a, nullptr), "launch");
+            checkd(cuLaunchKernel(one, 1, 1, 1, 1, 1, 1, 0, (CUstream)s, a, nullptr), "launch");
             return;
             }
         unsigned int n = N;
             {
             void* a[] = {&codes[0], &idx[0], insp, &slo, &shi, &n};
-            launch(sphere ? K.gen_codes_sph : K.gen_codes, n, bs, s, a);
+            launch(gen_codes, n, bs, s, a);
             }
         cub::DoubleBuffer<unsigned int> k(codes[0], codes[1]), v(idx[0], idx[1]);
         check(cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, k, v, (int)n, 0, 30, s), "sort");
@@ -207,7 +246,7 @@ struct RefTree
         check(cudaMemsetAsync(locks, 0, (size_t)(n - 1) * 4, s), "memset");
             {
             void* a[] = {&t, insp, &locks, &n};
-            launch(sphere ? K.bubble_sph : K.bubble, n, bs, s, a);
+            launch(bubble, n, bs, s, a);
             }
         }
 
@@ -317,17 +356,34 @@ struct TwoPass
 // with CountNeighborsOp, the host read of the largest count, then NeighborListOp of that stride;
 // include/neighbor/OutputOps.h:28-176): count, CUB max, host read, fill.  Returns the largest
 // count.
+unsigned int two_pass_with(CUfunction count, CUfunction list, const LBVHCompressedData& c, const void* q, unsigned int Q,
+                           const ImageListOp& im, TwoPass& b, unsigned int bs, cudaStream_t s, cudaEvent_t after_count);
+
 unsigned int two_pass(const Kernels& K, const LBVHCompressedData& c, const RefExactQueryOp& q, const ImageListOp& im,
                       TwoPass& b, unsigned int bs, cudaStream_t s, cudaEvent_t after_count = nullptr)
     {
-    if (q.N == 0) return 0;
+    return two_pass_with(K.count_exact, K.list_exact, c, &q, q.N, im, b, bs, s, after_count);
+    }
+
+// the same with the harness's double-precision exact query op
+unsigned int two_pass_f64(const Kernels& K, const LBVHCompressedData& c, const RefExactQueryOpF64& q,
+                          const ImageListOp& im, TwoPass& b, unsigned int bs, cudaStream_t s,
+                          cudaEvent_t after_count = nullptr)
+    {
+    return two_pass_with(K.count_f64, K.list_f64, c, &q, q.N, im, b, bs, s, after_count);
+    }
+
+unsigned int two_pass_with(CUfunction count, CUfunction list, const LBVHCompressedData& c, const void* q, unsigned int Q,
+                           const ImageListOp& im, TwoPass& b, unsigned int bs, cudaStream_t s, cudaEvent_t after_count)
+    {
+    if (Q == 0) return 0;
         {
         CountNeighborsOp out{b.nn};
-        void* a[] = {&out, (void*)&c, (void*)&q, (void*)&im};
-        launch(K.count_exact, q.N, bs, s, a);
+        void* a[] = {&out, (void*)&c, (void*)q, (void*)&im};
+        launch(count, Q, bs, s, a);
         }
     if (after_count) check(cudaEventRecord(after_count, s), "rec");
-    check(cub::DeviceReduce::Max(b.rtmp, b.rtmp_bytes, b.nn, b.dmax, (int)q.N, s), "reduce");
+    check(cub::DeviceReduce::Max(b.rtmp, b.rtmp_bytes, b.nn, b.dmax, (int)Q, s), "reduce");
     unsigned int mx = 0;
     check(cudaMemcpyAsync(&mx, b.dmax, 4, cudaMemcpyDeviceToHost, s), "copy");
     check(cudaStreamSynchronize(s), "sync");
@@ -340,8 +396,8 @@ unsigned int two_pass(const Kernels& K, const LBVHCompressedData& c, const RefEx
         }
         {
         NeighborListOp out{b.list, b.nn, std::max(mx, 1u)};
-        void* a[] = {&out, (void*)&c, (void*)&q, (void*)&im};
-        launch(K.list_exact, q.N, bs, s, a);
+        void* a[] = {&out, (void*)&c, (void*)q, (void*)&im};
+        launch(list, Q, bs, s, a);
         }
     return mx;
     }
@@ -473,6 +529,106 @@ int run_frames(const Kernels& K, const char* path, unsigned int n, int F, float 
     std::vector<const float3*> frames;
     for (int f = 0; f < F; ++f) frames.push_back(reinterpret_cast<const float3*>(all) + (size_t)f * n);
     return sweep_self(K, frames, n, rc, L, steps, warmup, "given frames");
+    }
+
+// Query spheres in double precision, in the tree's sorted order.
+__global__ void k_spheres_f64(const double3* p, const unsigned int* prim, RefSphereF64* sph, unsigned int n, double rc)
+    {
+    const unsigned int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double3 x = p[prim[i]];
+    RefSphereF64 q;
+    q.x = x.x;
+    q.y = x.y;
+    q.z = x.z;
+    q.w = rc;
+    sph[i] = q;
+    }
+
+double* read_points_f64(const char* path, size_t count)
+    {
+    std::vector<double> h(count * 3);
+    FILE* f = fopen(path, "rb");
+    if (!f || fread(h.data(), 24, count, f) != count) { fprintf(stderr, "cannot read %s\n", path); exit(5); }
+    fclose(f);
+    double* d;
+    check(cudaMalloc(&d, std::max<size_t>(count, 1) * 24), "alloc");
+    check(cudaMemcpy(d, h.data(), count * 24, cudaMemcpyHostToDevice), "copy");
+    return d;
+    }
+
+// The plain two-pass step on double-precision frames (cycled): build with the double insert op,
+// setup, count, max, fill with the double exact query (queries in sorted order, 27 images of the
+// cube of side L), every block size; as sweep_self, plus the pair total of the last timed frame.
+int run_frames64(const Kernels& K, const char* path, unsigned int n, int F, double rc, float L, int steps, int warmup)
+    {
+    double* all = read_points_f64(path, (size_t)n * F);
+    const double3 box = make_double3(L, L, L);
+    cudaStream_t s;
+    check(cudaStreamCreate(&s), "stream");
+    float3* img = image_list(L);
+    RefTree T;
+    T.allocate(n);
+    TwoPass b;
+    b.allocate(n, 96);
+    RefSphereF64* sph;
+    check(cudaMalloc(&sph, (size_t)std::max(n, 1u) * sizeof(RefSphereF64)), "alloc");
+    const float pad = exact_pad((float)rc, 2 * L);
+    check(cudaStreamSynchronize(s), "sync");
+    printf("{\"impl\": \"reference-cuda\", \"workload\": \"given double frames\", \"n\": %u, \"rc\": %g, \"steps\": %d, "
+           "\"warmup\": %d, \"results\": [", n, rc, steps, warmup);
+    bool first = true;
+    double pairs_sum = 0, pairs_last = 0;
+    for (unsigned int bs : all_blocks())
+        {
+        cudaEvent_t ev[6];
+        for (auto& e : ev) check(cudaEventCreate(&e), "event");
+        std::vector<double> step_ms;
+        double t_build = 0, t_setup = 0, t_count = 0, t_fill = 0;
+        for (int it = 0; it < warmup + steps; ++it)
+            {
+            const bool timed = it >= warmup;
+            const double3* P = reinterpret_cast<const double3*>(all) + (size_t)(it % F) * n;
+            check(cudaEventRecord(ev[0], s), "rec");
+            T.build_f64(K, P, make_float3(0, 0, 0), make_float3(L, L, L), bs, s);
+            k_spheres_f64<<<(n + 255) / 256, 256, 0, s>>>(P, T.idx[T.sel_idx], sph, n, rc);
+            check(cudaEventRecord(ev[1], s), "rec");
+            LBVHCompressedData c = T.compress(K, bs, s);
+            check(cudaEventRecord(ev[2], s), "rec");
+            RefExactQueryOpF64 q{sph, n, P, box, pad};
+            ImageListOp im{img, 27};
+            two_pass_f64(K, c, q, im, b, bs, s, ev[3]);
+            check(cudaEventRecord(ev[5], s), "rec");
+            check(cudaStreamSynchronize(s), "sync");
+            if (timed)
+                {
+                float ms;
+                cudaEventElapsedTime(&ms, ev[0], ev[1]); t_build += ms;
+                cudaEventElapsedTime(&ms, ev[1], ev[2]); t_setup += ms;
+                cudaEventElapsedTime(&ms, ev[2], ev[3]); t_count += ms;
+                cudaEventElapsedTime(&ms, ev[3], ev[5]); t_fill += ms;
+                cudaEventElapsedTime(&ms, ev[0], ev[5]); step_ms.push_back(ms);
+                if (first)
+                    {
+                    pairs_last = (double)sum_counts(b.nn, n);
+                    pairs_sum += pairs_last;
+                    }
+                }
+            }
+        double mean = 0;
+        for (double v : step_ms) mean += v;
+        mean /= step_ms.size();
+        std::vector<double> sorted = step_ms;
+        std::sort(sorted.begin(), sorted.end());
+        printf("%s{\"block\": %u, \"build_ms\": %.4f, \"setup_ms\": %.4f, \"count_ms\": %.4f, \"fill_ms\": %.4f, "
+               "\"step_ms\": %.4f, \"step_ms_median\": %.4f}",
+               first ? "" : ", ", bs, t_build / steps, t_setup / steps, t_count / steps, t_fill / steps, mean,
+               sorted[sorted.size() / 2]);
+        first = false;
+        for (auto& e : ev) cudaEventDestroy(e);
+        }
+    printf("], \"pairs_per_step\": %.1f, \"pairs_last_frame\": %.1f}\n", pairs_sum / steps, pairs_last);
+    return 0;
     }
 
 // Polydisperse step: a tree per species (PointInsertOp), every (query species, tree) pair listed
@@ -728,6 +884,9 @@ int main(int argc, char** argv)
     if (mode == "poly" && argc >= 10)
         return run_poly(K, argv[2], (unsigned int)atol(argv[3]), argv[4], (unsigned int)atol(argv[5]), atoi(argv[6]),
                         (float)atof(argv[7]), atoi(argv[8]), atoi(argv[9]));
+    if (mode == "frames64" && argc >= 9)
+        return run_frames64(K, argv[2], (unsigned int)atol(argv[3]), atoi(argv[4]), atof(argv[5]), (float)atof(argv[6]),
+                            atoi(argv[7]), atoi(argv[8]));
     if (mode == "hash" && argc >= 7)
         return run_hash(K, argv[2], (unsigned int)atol(argv[3]), (float)atof(argv[4]), (float)atof(argv[5]), argv[6]);
     if (mode == "dump" && argc >= 15)

@@ -2,7 +2,8 @@
 // LBVH.cuh and LBVHTraverser.cuh), compiled from its headers where they lie into a cubin for the
 // reference harness (TEST / MEASUREMENT INFRASTRUCTURE ONLY; see ref_driver.cu).  Nothing of the
 // reference is copied here: this unit only instantiates its templates with the ops the harness
-// runs, and defines one plugin query op through the reference's public operator interface.
+// runs, and defines plugin ops through the reference's public operator interface (an FP32 exact
+// sphere query, and a double-precision point insert op and exact sphere query).
 #include <cstddef>
 
 #include <neighbor/neighbor.h>
@@ -51,6 +52,71 @@ struct RefExactQueryOp
     __host__ __device__ __forceinline__ unsigned int size() const { return N; }
     };
 
+// Double-precision points (HOOMD-blue's Scalar = double positions, as in the reference's own
+// benchmark ops, benchmark/lbvh_benchmark.cuh:25-92) through the reference's InsertOp interface:
+// each leaf box is the point rounded outward by the reference's BoundingBox(double3, double3).
+struct RefPointInsertOpF64
+    {
+    const double3* points;
+    unsigned int N;
+
+    __device__ __forceinline__ neighbor::BoundingBox get(const unsigned int idx) const
+        {
+        const double3 p = points[idx];
+        return neighbor::BoundingBox(p, p);
+        }
+    __host__ __device__ __forceinline__ unsigned int size() const { return N; }
+    };
+
+struct __align__(16) RefSphereF64
+    {
+    double x, y, z, w;
+    };
+
+// Exact sphere query on double positions: volume = the reference's BoundingSphere(double3,
+// double) of the imaged centre with radius cutoff + pad; refine() = the double minimum-image
+// predicate with the operation order pinned (the library's exact_pair_f64).
+struct RefExactQueryOpF64
+    {
+    const RefSphereF64* spheres;
+    unsigned int N;
+    const double3* points;
+    double3 box;
+    float pad;
+
+    typedef RefSphereF64 ThreadData;
+    typedef neighbor::BoundingSphere Volume;
+
+    __device__ __forceinline__ ThreadData setup(const unsigned int idx) const { return spheres[idx]; }
+    __device__ __forceinline__ Volume get(const ThreadData& q, const float3& image) const
+        {
+        const double3 t = make_double3(__dadd_rn(q.x, (double)image.x), __dadd_rn(q.y, (double)image.y),
+                                       __dadd_rn(q.z, (double)image.z));
+        return neighbor::BoundingSphere(t, __dadd_ru(q.w, (double)pad));
+        }
+    __device__ __forceinline__ bool overlap(const Volume& v, const neighbor::BoundingBox& b) const { return v.overlap(b); }
+    __device__ __forceinline__ static double wrap(double d, double L)
+        {
+        if (L > 0.0)
+            {
+            const double h = __dmul_rn(0.5, L);
+            if (d >= h) d = __dsub_rn(d, L);
+            else if (d < -h) d = __dadd_rn(d, L);
+            }
+        return d;
+        }
+    __device__ __forceinline__ bool refine(const ThreadData& q, const int primitive) const
+        {
+        const double3 p = points[primitive];
+        const double dx = wrap(__dsub_rn(p.x, q.x), box.x);
+        const double dy = wrap(__dsub_rn(p.y, q.y), box.y);
+        const double dz = wrap(__dsub_rn(p.z, q.z), box.z);
+        const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+        return d2 <= __dmul_rn(q.w, q.w);
+        }
+    __host__ __device__ __forceinline__ unsigned int size() const { return N; }
+    };
+
 // Kernel-parameter layouts the driver mirrors (ref_driver.cu asserts the same numbers).
 static_assert(sizeof(neighbor::PointInsertOp) == 16 && offsetof(neighbor::PointInsertOp, N) == 8, "PointInsertOp layout");
 static_assert(sizeof(neighbor::SphereInsertOp) == 16 && offsetof(neighbor::SphereInsertOp, r) == 8
@@ -65,6 +131,10 @@ static_assert(sizeof(neighbor::SphereQueryOp) == 16, "SphereQueryOp layout");
 static_assert(sizeof(neighbor::NullTransformOp) == 1, "NullTransformOp layout");
 static_assert(sizeof(RefExactQueryOp) == 40 && offsetof(RefExactQueryOp, points) == 16 && offsetof(RefExactQueryOp, box) == 24
               && offsetof(RefExactQueryOp, pad) == 36, "RefExactQueryOp layout");
+static_assert(sizeof(RefPointInsertOpF64) == 16 && offsetof(RefPointInsertOpF64, N) == 8, "RefPointInsertOpF64 layout");
+static_assert(sizeof(RefExactQueryOpF64) == 56 && offsetof(RefExactQueryOpF64, N) == 8
+              && offsetof(RefExactQueryOpF64, points) == 16 && offsetof(RefExactQueryOpF64, box) == 24
+              && offsetof(RefExactQueryOpF64, pad) == 48, "RefExactQueryOpF64 layout");
 
 namespace neighbor
 {
@@ -82,6 +152,15 @@ template __global__ void lbvh_gen_codes<SphereInsertOp>(unsigned int*, unsigned 
 template __global__ void lbvh_bubble_aabbs<SphereInsertOp>(const LBVHData, const SphereInsertOp, unsigned int*,
                                                            const unsigned int);
 template __global__ void lbvh_one_primitive<SphereInsertOp>(const LBVHData, const SphereInsertOp);
+template __global__ void lbvh_gen_codes<RefPointInsertOpF64>(unsigned int*, unsigned int*, const RefPointInsertOpF64,
+                                                             const float3, const float3, const unsigned int);
+template __global__ void lbvh_bubble_aabbs<RefPointInsertOpF64>(const LBVHData, const RefPointInsertOpF64, unsigned int*,
+                                                                const unsigned int);
+template __global__ void lbvh_one_primitive<RefPointInsertOpF64>(const LBVHData, const RefPointInsertOpF64);
+template __global__ void lbvh_traverse_ropes<CountNeighborsOp, RefExactQueryOpF64, ImageListOp<float3>>(
+    const CountNeighborsOp, const LBVHCompressedData, const RefExactQueryOpF64, const ImageListOp<float3>);
+template __global__ void lbvh_traverse_ropes<NeighborListOp, RefExactQueryOpF64, ImageListOp<float3>>(
+    const NeighborListOp, const LBVHCompressedData, const RefExactQueryOpF64, const ImageListOp<float3>);
 template __global__ void lbvh_compress_ropes<NullTransformOp>(const LBVHCompressedData, const NullTransformOp,
                                                               const ConstLBVHData, const unsigned int, const unsigned int);
 template __global__ void lbvh_traverse_ropes<CountNeighborsOp, SphereQueryOp, ImageListOp<float3>>(

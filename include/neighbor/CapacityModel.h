@@ -38,6 +38,7 @@ class CapacityModel
             {
             setMargin(0.f);
             m_status.reserve(1);
+            m_tiles.reserve(1);
             detail::check_cuda(cudaMemset(m_status.get(), 0, sizeof(unsigned int)), "memset");
             m_p.reserve(kParams);
             m_m.reserve(kParams);
@@ -170,6 +171,7 @@ class CapacityModel
             a.y_out = y;
             a.cap_out = caps;
             a.status = m_status.get();
+            a.tile_counter = nullptr;
             int dev = 0, sms = 152;
             detail::check_cuda(cudaGetDevice(&dev), "device");
             detail::check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "attribute");
@@ -184,9 +186,12 @@ class CapacityModel
                                        "inference attribute");
                     attr = true;
                     }
-                // persistent: kCapTcMinBlocks blocks of 128 queries per SM walk all tiles
+                // persistent: kCapTcMinBlocks blocks of 128 queries per SM take the tiles from a
+                // ticket counter
                 const unsigned int tiles = detail::ceil_div(N, (unsigned int)gpu::kCapTcRows);
                 const unsigned int grid = std::min(tiles, (unsigned int)sms * (unsigned int)gpu::kCapTcMinBlocks);
+                detail::check_cuda(cudaMemsetAsync(m_tiles.get(), 0, sizeof(unsigned int), stream), "memset");
+                a.tile_counter = m_tiles.get();
                 gpu::k_cap_infer_tc<<<grid, gpu::kCapTcRows, 0, stream>>>(a);
                 }
             else
@@ -401,6 +406,7 @@ class CapacityModel
         device_array<__nv_bfloat16> m_w;
         device_array<unsigned int> m_occ;
         device_array<unsigned int> m_status;
+        device_array<unsigned int> m_tiles;
         unsigned int m_step;
         InferKernel m_infer;
         float m_margins[gpu::kCapMarginBins];

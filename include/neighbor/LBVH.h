@@ -237,7 +237,7 @@ class LBVH : public Tunable<unsigned int>
     private:
         // tile shape of the onesweep sort: threads per block, keys per thread
         static constexpr int kSortBlock = 256;
-        static constexpr int kSortItems = 8;
+        static constexpr int kSortItems = 16;
         // layout of the small scratch buffer (uint32 words)
         static constexpr size_t kSmallHist = 0;            // 4 passes x 1024
         static constexpr size_t kSmallOffsets = 4096;      // 4 passes x 1024

@@ -227,8 +227,11 @@ class OnePassNeighborList
             }
 
         // The learned one-pass step in one call: build the tree of `points`, predict every row's
-        // capacity with `model`, fill the list.  The prediction needs only the sort's output, so it
-        // runs on a second stream from LBVH::sortedEvent() on, alongside the rest of the build.
+        // capacity with `model`, fill the list.  The prediction needs only the sort's output: the
+        // warp-tile kernel runs on a second stream from LBVH::sortedEvent() on, alongside the rest
+        // of the build; the tcgen05 kernel runs after the build on the caller's stream (16M
+        // points: 9.01 ms per step there against 9.48 ms beside the build, where its blocks hold
+        // back the climb's; the warp-tile kernel 9.07 beside, 9.10 after).
         template<class TransformOpT = NullTransformOp>
         Stats buildLearned(const LBVHTraverser::LaunchParameters& params, LBVH& lbvh, LBVHTraverser& trav,
                            CapacityModel& model, const float3* points, unsigned int N, const float3& lo,
@@ -244,6 +247,13 @@ class OnePassNeighborList
                 {
                 const unsigned int one = 1u;
                 detail::check_cuda(cudaMemcpy(caps, &one, sizeof(one), cudaMemcpyHostToDevice), "copy");
+                return build(params, lbvh, trav, rc, box, pad, periodic, rows_sorted, cap_max, transform);
+                }
+            if (model.getInferKernel() == CapacityModel::InferKernel::TensorMemory)
+                {
+                model.predictSorted(lbvh.getCodes().get(), lbvh.getPrimitives().get(), points, N,
+                                    CapacityModel::frame(lo, hi, rc, periodic), rows_sorted, cap_max, caps, nullptr,
+                                    stream);
                 return build(params, lbvh, trav, rc, box, pad, periodic, rows_sorted, cap_max, transform);
                 }
             if (!m_side)

@@ -191,7 +191,7 @@ struct OnesweepConfig
     };
 
 template<class InsertOpT, int RB, int BLOCK, int ITEMS, bool FIRST>
-__global__ void __launch_bounds__(BLOCK, ITEMS <= 8 ? 4 : 2) k_onesweep(const InsertOpT insert, float3 scene_lo,
+__global__ void __launch_bounds__(BLOCK, ITEMS <= 8 ? 6 : 4) k_onesweep(const InsertOpT insert, float3 scene_lo,
                                                     float3 scene_ext,
                                                     const unsigned int* __restrict__ keys_in,
                                                     const unsigned int* __restrict__ vals_in,

@@ -243,6 +243,7 @@ struct CapInferArgs
     float* y_out;                   // optional: network output per row
     unsigned int* cap_out;          // capacity per row
     unsigned int* status;           // device status word (k_cap_infer_tc: kStatusTensorWait)
+    unsigned int* tile_counter;     // k_cap_infer_tc: zero on entry; blocks take tiles from it
     };
 
 __device__ __forceinline__ unsigned int pack_bf16x2(float lo, float hi)
@@ -592,6 +593,7 @@ __global__ void __launch_bounds__(kCapTcRows, kCapTcMinBlocks) k_cap_infer_tc(co
     __shared__ float s_log[kCapLogTable];
     __shared__ __align__(8) unsigned long long s_bar;
     __shared__ unsigned int s_tmem;
+    __shared__ unsigned int s_tile;
 
     const unsigned int lane = threadIdx.x & 31u;
     const unsigned int warp = threadIdx.x >> 5;
@@ -630,8 +632,16 @@ __global__ void __launch_bounds__(kCapTcRows, kCapTcMinBlocks) k_cap_infer_tc(co
     unsigned int phase = 0u;
     bool failed = false;
     const unsigned int n_tiles = (a.N + (unsigned int)kCapTcRows - 1u) / (unsigned int)kCapTcRows;
-    for (unsigned int tile = blockIdx.x; tile < n_tiles; tile += gridDim.x)
+    // Each block takes its first tile by its index and the next ones from a ticket counter, so that
+    // blocks that start late (the kernel may share the GPU with a build still running) take fewer.
+    for (unsigned int it = 0;; ++it)
         {
+        if (threadIdx.x == 0)
+            s_tile = it == 0 ? blockIdx.x
+                             : (a.tile_counter ? gridDim.x + atomicAdd(a.tile_counter, 1u) : blockIdx.x + it * gridDim.x);
+        __syncthreads();
+        const unsigned int tile = s_tile;
+        if (tile >= n_tiles) break;
         // rows past the end repeat the last query (their outputs are not written)
         const unsigned int q = tile * (unsigned int)kCapTcRows + r;
         unsigned int ci;

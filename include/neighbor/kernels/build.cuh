@@ -19,7 +19,10 @@
 #define NEIGHBOR_KERNELS_BUILD_CUH_
 
 #include <cfloat>
+#include <cstdint>
+#include <type_traits>
 
+#include "../InsertOps.h"
 #include "common.cuh"
 
 namespace neighbor
@@ -112,9 +115,8 @@ __global__ void __launch_bounds__(256) k_codes_histogram(const InsertOpT insert,
     float3 bmin = make_float3(FLT_MAX, FLT_MAX, FLT_MAX);
     float3 bmax = make_float3(-FLT_MAX, -FLT_MAX, -FLT_MAX);
     const unsigned int stride = gridDim.x * blockDim.x;
-    for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += stride)
-        {
-        const BoundingBox b = insert.get(i);
+    // one primitive's box: bounds, code, histograms
+    const auto one = [&](const BoundingBox& b) -> unsigned int {
         bmin.x = fminf(bmin.x, b.lo.x);
         bmin.y = fminf(bmin.y, b.lo.y);
         bmin.z = fminf(bmin.z, b.lo.z);
@@ -122,9 +124,41 @@ __global__ void __launch_bounds__(256) k_codes_histogram(const InsertOpT insert,
         bmax.y = fmaxf(bmax.y, b.hi.y);
         bmax.z = fmaxf(bmax.z, b.hi.z);
         const unsigned int code = morton_code(b, scene_lo, scene_ext);
-        if (codes_out) codes_out[i] = code;
 #pragma unroll
         for (int p = 0; p < P; ++p) atomicAdd(&s_hist[p * R + ((code >> (p * RB)) & (R - 1))], 1u);
+        return code;
+    };
+    unsigned int first_scalar = 0u;
+    if constexpr (std::is_same<InsertOpT, PointInsertOp>::value)
+        {
+        // Points: each thread reads four consecutive float3 as three aligned float4 (48 bytes)
+        // and writes their four codes as one uint4, when the arrays are 16-byte aligned; the
+        // last N % 4 points take the loop below.
+        const bool aligned = ((reinterpret_cast<uintptr_t>(insert.points) | reinterpret_cast<uintptr_t>(codes_out)) & 15u) == 0u;
+        if (aligned)
+            {
+            const unsigned int groups = N / 4u;
+            const float4* p4 = reinterpret_cast<const float4*>(insert.points);
+            for (unsigned int g = blockIdx.x * blockDim.x + threadIdx.x; g < groups; g += stride)
+                {
+                const float4 a = __ldg(p4 + 3u * g);
+                const float4 b = __ldg(p4 + 3u * g + 1u);
+                const float4 c = __ldg(p4 + 3u * g + 2u);
+                const float3 q[4] = {make_float3(a.x, a.y, a.z), make_float3(a.w, b.x, b.y),
+                                     make_float3(b.z, b.w, c.x), make_float3(c.y, c.z, c.w)};
+                unsigned int code[4];
+#pragma unroll
+                for (int k = 0; k < 4; ++k) code[k] = one(BoundingBox(q[k], q[k]));
+                if (codes_out)
+                    reinterpret_cast<uint4*>(codes_out)[g] = make_uint4(code[0], code[1], code[2], code[3]);
+                }
+            first_scalar = groups * 4u;
+            }
+        }
+    for (unsigned int i = first_scalar + blockIdx.x * blockDim.x + threadIdx.x; i < N; i += stride)
+        {
+        const unsigned int code = one(insert.get(i));
+        if (codes_out) codes_out[i] = code;
         }
     float vals[6] = {bmin.x, bmin.y, bmin.z, bmax.x, bmax.y, bmax.z};
 #pragma unroll

@@ -1051,7 +1051,28 @@ __global__ void __launch_bounds__(kSummaryBlock) k_count_summary(unsigned int N,
     const bool failed = status != nullptr && ld_status(status) != 0u;
     unsigned int mx = 0, past = 0;
     unsigned long long sum = 0;
-    for (unsigned int s = blockIdx.x * blockDim.x + threadIdx.x; s < N; s += gridDim.x * blockDim.x)
+    unsigned int first_scalar = 0u;
+    if (EXCHANGE && !failed && rows_sorted
+        && ((reinterpret_cast<uintptr_t>(own) | reinterpret_cast<uintptr_t>(in_count) | reinterpret_cast<uintptr_t>(nneigh)) & 15u) == 0u
+        && (reinterpret_cast<uintptr_t>(lost) & 3u) == 0u)
+        {
+        // rows in sorted order: four per thread, as 16-byte loads and one 16-byte store
+        const unsigned int groups = N / 4u;
+        for (unsigned int g = blockIdx.x * blockDim.x + threadIdx.x; g < groups; g += gridDim.x * blockDim.x)
+            {
+            const uint4 o = reinterpret_cast<const uint4*>(own)[g];
+            const uint4 i = reinterpret_cast<const uint4*>(in_count)[g];
+            const uchar4 l = reinterpret_cast<const uchar4*>(lost)[g];
+            const uint4 t = make_uint4(o.x + i.x, o.y + i.y, o.z + i.z, o.w + i.w);
+            reinterpret_cast<uint4*>(nneigh)[g] = t;
+            past += (past_exchange(o.x, i.x, l.x) ? 1u : 0u) + (past_exchange(o.y, i.y, l.y) ? 1u : 0u)
+                    + (past_exchange(o.z, i.z, l.z) ? 1u : 0u) + (past_exchange(o.w, i.w, l.w) ? 1u : 0u);
+            mx = max(max(mx, max(t.x, t.y)), max(t.z, t.w));
+            sum += (unsigned long long)t.x + t.y + t.z + t.w;
+            }
+        first_scalar = groups * 4u;
+        }
+    for (unsigned int s = first_scalar + blockIdx.x * blockDim.x + threadIdx.x; s < N; s += gridDim.x * blockDim.x)
         {
         if (failed)
             {

@@ -427,9 +427,10 @@ static __global__ void k_gen_hierarchy(const unsigned int* __restrict__ codes, u
 
 // ---------------------------------------------------------------------------------------------
 // Chained exclusive scan: out[i] = sum(in[0..i)), out[n] = total, *total_out = total.
-// 256 threads x 16 items per tile; tiles taken in launch order; look-back on one status word.
+// 512 threads x 16 items per tile (16M counts: 2.054 -> 2.043 ms whole build against 256 x 16);
+// tiles taken in launch order; look-back on one status word.
 // ---------------------------------------------------------------------------------------------
-constexpr int kScanBlock = 256;
+constexpr int kScanBlock = 512;
 constexpr int kScanItems = 16;
 constexpr int kScanTile = kScanBlock * kScanItems;
 

@@ -626,10 +626,12 @@ class LBVHTraverser:
         return nneigh, lst
 
     def traverse_f64(self, lbvh: LBVH, spheres, points, box, pad: float, images=None, map=None,
-                     max_neigh: Optional[int] = None, nneigh=None, neigh_list=None, block_size: int = 32,
+                     max_neigh: Optional[int] = None, nneigh=None, neigh_list=None, block_size: int = 256,
                      stream=None):
         """Exact sphere queries on double positions (ExactSphereQueryOpF64): spheres float64 [Q, 4],
-        points float64 [N, 3], box the periodic lengths (0 = open), images as traverse()."""
+        points float64 [N, 3], box the periodic lengths (0 = open), images as traverse().  On a
+        tree of double points this is the double fast walk, one thread per query in blocks of
+        block_size."""
         torch = _torch()
         sph = _dev(spheres, torch.float64, 4)
         pts = _dev(points, torch.float64, 3)

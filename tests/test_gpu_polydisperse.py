@@ -27,8 +27,10 @@ def test_two_species_lists_match_cell_list():
     L = float(((n_small * np.pi / 6.0 + n_large * np.pi / 6.0 * 1000.0) / 0.2) ** (1.0 / 3.0))
     species = bench.polydisperse_frame(n_small, n_large, L, 5)
     trees = [nb.LBVH(), nb.LBVH()]
-    trav = nb.LBVHTraverser()
-    out = bench.polydisperse_step(nb, trees, trav, species, L)
+    travs = [nb.LBVHTraverser() for _ in range(4)]
+    streams = [torch.cuda.Stream() for _ in range(4)]
+    out = bench.polydisperse_step(nb, trees, travs, species, L, streams=streams)
+    torch.cuda.synchronize()
     for (i, j), (cnt, lst, R) in out.items():
         qp = species[i].cpu().numpy()
         tp = species[j].cpu().numpy()

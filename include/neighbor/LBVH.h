@@ -238,6 +238,10 @@ class LBVH : public Tunable<unsigned int>
         // tile shape of the onesweep sort: threads per block, keys per thread
         static constexpr int kSortBlock = 256;
         static constexpr int kSortItems = 16;
+        // below kSortSmallN keys the passes take tiles of kSortItemsSmall keys per thread: more
+        // tiles, so that a small sort spreads over more SMs
+        static constexpr int kSortItemsSmall = 4;
+        static constexpr unsigned int kSortSmallN = 1u << 20;
         // layout of the small scratch buffer (uint32 words)
         static constexpr size_t kSmallHist = 0;            // 4 passes x 1024
         static constexpr size_t kSmallOffsets = 4096;      // 4 passes x 1024
@@ -315,7 +319,7 @@ class LBVH : public Tunable<unsigned int>
             return m_epoch;
             }
 
-        template<class InsertOpT, int RB>
+        template<class InsertOpT, int RB, int ITEMS>
         void sort_codes(const InsertOpT& insert, const float3& lo, const float3& ext,
                         cudaStream_t stream, unsigned int epoch);
     };
@@ -385,7 +389,9 @@ inline void LBVH::allocate(unsigned int N)
     m_payload.reserve(N);
     // one status word per (tile, digit, pass), enough for the widest configuration (4 passes x 256
     // digits, or 3 passes x 1024 digits) of the sort's tiles
-    const size_t tiles = detail::ceil_div((size_t)N, (size_t)kSortBlock * kSortItems);
+    // the most tiles any size up to this capacity sorts in: small tiles below kSortSmallN keys
+    const size_t tiles = std::max(detail::ceil_div((size_t)std::min(N, kSortSmallN - 1u), (size_t)kSortBlock * kSortItemsSmall),
+                                  detail::ceil_div((size_t)N, (size_t)kSortBlock * kSortItems));
     const size_t need = tiles * 4 * 1024;
     if (m_sort_status.size() < need)
         {
@@ -401,14 +407,13 @@ inline void LBVH::allocate(unsigned int N)
     m_capacity = N;
     }
 
-template<class InsertOpT, int RB>
+template<class InsertOpT, int RB, int ITEMS>
 void LBVH::sort_codes(const InsertOpT& insert, const float3& lo, const float3& ext,
                       cudaStream_t stream, unsigned int epoch)
     {
     constexpr int R = gpu::RadixConfig<RB>::kRadix;
     constexpr int P = gpu::RadixConfig<RB>::kPasses;
     constexpr int BLOCK = kSortBlock;
-    constexpr int ITEMS = kSortItems;
     typedef gpu::OnesweepConfig<RB, BLOCK, ITEMS> Cfg;
     const unsigned int N = m_N;
     unsigned int* small = m_small.get();
@@ -519,9 +524,19 @@ void LBVH::build(const LaunchParameters& params, const InsertOpT& insert, const 
         gpu::k_single_init<<<1, 32, 0, stream>>>(m_indexes.current().get(), m_parent.get(), m_live.get());
         }
     else if (m_radix_bits == 10)
-        sort_codes<InsertOpT, 10>(insert, lo, ext, stream, epoch);
+        {
+        if (N < kSortSmallN)
+            sort_codes<InsertOpT, 10, kSortItemsSmall>(insert, lo, ext, stream, epoch);
+        else
+            sort_codes<InsertOpT, 10, kSortItems>(insert, lo, ext, stream, epoch);
+        }
     else
-        sort_codes<InsertOpT, 8>(insert, lo, ext, stream, epoch);
+        {
+        if (N < kSortSmallN)
+            sort_codes<InsertOpT, 8, kSortItemsSmall>(insert, lo, ext, stream, epoch);
+        else
+            sort_codes<InsertOpT, 8, kSortItems>(insert, lo, ext, stream, epoch);
+        }
     if (!m_sorted_event)
         detail::check_cuda(cudaEventCreateWithFlags(&m_sorted_event, cudaEventDisableTiming), "event create");
     detail::check_cuda(cudaEventRecord(m_sorted_event, stream), "event record");

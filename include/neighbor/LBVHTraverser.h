@@ -223,14 +223,14 @@ class LBVHTraverser : public Tunable<unsigned int>
             }
 
         // Routing by size (results do not depend on it).  With few queries the GPU is mostly idle
-        // and the longest walks set the time.  Traversals of at most getWarpWalkMaxQueries()
-        // queries walk one group of lanes per query (getWalkLanes()), which shortens a walk about
-        // as many times as the group has lanes; larger ones one thread per query.  Self traversals take the symmetric walk only above
-        // getSymmetricMinPoints() points: below it the whole-tree walk, with no partner atomics and
-        // no ordering pass, measured faster (count + fill: 32,768 points lane groups 185 us, thread
-        // walk 269 us, symmetric walk 293 us; 65,536 points thread 262, groups of 8 269, symmetric
-        // 310 us; 262,144 points thread 338, symmetric 349 us; 1,048,576 points 867 / 720 us).
-        // 0 turns a limit off.
+        // and the longest walks set the time.  Self traversals of more than
+        // getSymmetricMinPoints() points take the symmetric walk with the pair exchange; other
+        // traversals of at most getWarpWalkMaxQueries() queries walk one group of lanes per query
+        // (getWalkLanes()), which shortens a walk about as many times as the group has lanes, and
+        // larger ones one thread per query.  Build + count + max + fill, median of 30 steps:
+        // 16,384 points lane groups 248 us, symmetric 294; 32,768 points 319 / 304; 65,536
+        // points 429 / 341; 262,144 points 558 / 427 (thread walk 556); 524,288 points thread 773,
+        // symmetric 548.  0 turns a limit off.
         void setWarpWalkMaxQueries(unsigned int q) { m_warp_walk_max = q; }
         unsigned int getWarpWalkMaxQueries() const { return m_warp_walk_max; }
         void setSymmetricMinPoints(unsigned int n) { m_symmetric_min = n; }
@@ -627,7 +627,7 @@ void LBVHTraverser::traverseSelf(const LaunchParameters& params, const LBVH& lbv
     constexpr int kind = output_kind<OutputOpT>::value;
     const bool symmetric = detail::is_symmetric_images<TranslateOpT>::value && m_symmetric
                            && m_mode == kThreadTraversal && !m_stats && lbvh.getN() < gpu::kHalfMaxN
-                           && lbvh.getN() > m_warp_walk_max && lbvh.getN() > m_symmetric_min;
+                           && lbvh.getN() > m_symmetric_min;
     // Counts take the symmetric kernel above the size limits.  A fill after a count that exchanged
     // the pairs (same tree, cutoff, images and rows) assembles the rows; other fills walk
     // symmetrically only while every row also fits the one-thread ordering (longer rows cost

@@ -649,8 +649,9 @@ constexpr unsigned int kWarpWalkBlock = 256;
 // Up to this many queries, a traversal walks one group of lanes per query (LBVHTraverser picks the
 // group width): one thread per query would leave most of the GPU's SMs idle.
 constexpr unsigned int kWarpWalkMaxQueries = 32768;
-// self traversals of at most this many points walk the whole tree (no symmetric walk)
-constexpr unsigned int kSymmetricMinPoints = 262144;
+// self traversals of at most this many points walk the whole tree (no symmetric walk); above it
+// the symmetric walk with the pair exchange, whatever the lane-group limit
+constexpr unsigned int kSymmetricMinPoints = 16384;
 
 // G < 32: the same walk by groups of G lanes, 32 / G queries per warp (chunks of G records).  A
 // group's shuffles and ballots name only its own lanes, so the groups of a warp may be at

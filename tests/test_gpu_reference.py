@@ -103,6 +103,7 @@ def test_library_matches_reference_kernels(name, P, L, rc):
         elif route in ("symmetric", "exchange"):
             st.force_symmetric()
         else:
+            st.set_symmetric(False)
             st.set_warp_walk_max(len(P))
         if route == "exchange":
             st.traverse_self(lbvh, rc, box, pad, images="periodic", rows_sorted=False)

@@ -49,6 +49,7 @@ def _traverser(route, N):
     elif route == "symmetric":
         trav.force_symmetric()
     else:
+        trav.set_symmetric(False)
         trav.set_warp_walk_max(max(N, 1))
         trav.set_walk_lanes(int(route[1:]))
     return trav

@@ -827,7 +827,7 @@ constexpr unsigned int kHalfCacheSlots = 16;
 // own[] flag of a row whose own entries were written as final ids after its appended entries
 constexpr unsigned int kOwnPlaced = 0x80000000u;
 
-constexpr unsigned int kHalfBlock = 256;
+constexpr unsigned int kHalfBlock = 128;
 
 // Images (bits of the 27-image lattice, or bit 0 for the self image) whose padded query box
 // meets the root box.
@@ -842,11 +842,12 @@ __device__ __forceinline__ unsigned int half_image_flags(const HalfArgs& a, cons
     }
 
 // CACHE (counts only): the pair exchange -- own keys, incoming keys and counters by sorted
-// position; compiled separately so that the walk without it carries no test for it.  Resident
-// blocks per SM: 8 for counts (16M points 3.57 -> 3.14 ms against 6 blocks), 6 for fills (their
+// position; compiled separately so that the walk without it carries no test for it.  Blocks of
+// 128 queries (16M points: count 3.40 -> 3.35 ms against 256, 3.54 with 512); resident threads
+// per SM: 2,048 for counts (3.57 -> 3.14 ms against 1,536), 1,536 for fills (their
 // deferred partner stores need the registers).
 template<int OUT, class TransformOpT, bool CACHE = false>
-__global__ void __launch_bounds__(kHalfBlock, OUT == kFastCount ? 8 : 6) k_traverse_half(const FastLBVHData tree, const HalfArgs a,
+__global__ void __launch_bounds__(kHalfBlock, OUT == kFastCount ? 16 : 12) k_traverse_half(const FastLBVHData tree, const HalfArgs a,
                                                                   const TransformOpT transform)
     {
     static_assert(!CACHE || OUT == kFastCount, "the pair exchange is a count's");

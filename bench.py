@@ -598,10 +598,12 @@ def double_precision(nb, args, stream, n=16_777_216, rc=RC, steps=5, warmup=2, n
     """Double-precision positions (HOOMD-blue's Scalar = double): the plain two-pass step on a
     uniform trajectory of n points (density 0.85, sigma 0.05, frames cycled) with PointInsertOpF64
     and ExactSphereQueryOpF64 -- build, queries in the tree's sorted order, count, host read of the
-    largest count, fill -- on the double walk (k_traverse_fast_f64).  Beside it: the same step on
-    the library's reference-layout walk of the same op, and the reference's own kernels running it
-    with the harness's double insert and exact query ops on the same frames.  Checks: the last
-    frame's counts and row hashes against the reference-layout walk, its pair total against the
+    largest count, fill -- as double self queries (traverse_self_f64: the symmetric double walk
+    with the pair exchange, the fill assembled from it).  Beside it: the same step with the queries
+    given as spheres (traverse_f64: the whole-tree double walk, count and fill), on the library's
+    reference-layout walk of the same op, and on the reference's own kernels with the harness's
+    double insert and exact query ops on the same frames.  Checks: the last frame's counts and row
+    hashes against the whole-tree walk and the reference-layout walk, its pair total against the
     reference kernels'."""
     import numpy as np
     import torch
@@ -636,11 +638,27 @@ def double_precision(nb, args, stream, n=16_777_216, rc=RC, steps=5, warmup=2, n
             return total, mx
         return step
 
-    fast = nb.LBVHTraverser()
-    ms_fast, outs = time_steps(make_step(fast), frames, warmup, stream)
+    def self_step(P):
+        lbvh.build_f64(P, [0, 0, 0], box, block_size=args.block)
+        trav_self.traverse_self_f64(lbvh, P, rc, box, pad, images="periodic", nneigh=counts, rows_sorted=True,
+                                    block_size=args.block)
+        mx, total, _ = trav_self.count_summary(stream)   # the host read of the two-pass pattern
+        if store["flat"].numel() < n * mx:
+            store["flat"] = torch.empty(n * mx, dtype=torch.int32, device="cuda")
+        lst = store["flat"][: n * max(mx, 1)].view(n, max(mx, 1))
+        trav_self.traverse_self_f64(lbvh, P, rc, box, pad, images="periodic", max_neigh=max(mx, 1), nneigh=counts,
+                                    neigh_list=lst, rows_sorted=True, block_size=args.block)
+        return total, mx
+
+    trav_self = nb.LBVHTraverser()
+    ms_fast, outs = time_steps(self_step, frames, warmup, stream)
     total_last, mx_last = outs[-1]
     c_fast = counts.clone()
     h_fast = row_hashes(store["flat"], c_fast, max(mx_last, 1)) if mx_last <= 64 else None
+    whole = nb.LBVHTraverser()
+    ms_whole, outs_w = time_steps(make_step(whole), frames, warmup, stream)
+    c_whole = counts.clone()
+    h_whole = row_hashes(store["flat"], c_whole, max(outs_w[-1][1], 1)) if outs_w[-1][1] <= 64 else None
     ref_layout = nb.LBVHTraverser()
     ref_layout.set_fast_path(False)
     ms_ref_layout, outs_r = time_steps(make_step(ref_layout), frames, warmup, stream)
@@ -648,6 +666,8 @@ def double_precision(nb, args, stream, n=16_777_216, rc=RC, steps=5, warmup=2, n
     h_ref = row_hashes(store["flat"], c_ref, max(outs_r[-1][1], 1)) if outs_r[-1][1] <= 64 else None
     rows_equal = bool(torch.equal(c_fast, c_ref)) and h_fast is not None and h_ref is not None \
         and bool(torch.equal(h_fast, h_ref))
+    rows_equal_whole = bool(torch.equal(c_fast, c_whole)) and h_fast is not None and h_whole is not None \
+        and bool(torch.equal(h_fast, h_whole))
     pairs = float(sum(o[0] for o in outs)) / len(outs)
     ref = None
     if not args.no_ref_cuda:
@@ -667,6 +687,9 @@ def double_precision(nb, args, stream, n=16_777_216, rc=RC, steps=5, warmup=2, n
     out = {"workload": f"uniform trajectory N={n} in float64, density 0.85 L={L:.2f} rc={rc} sigma={SIGMA}, "
                        f"{n_frames} frames cycled, 27 images; build + count + max read + fill",
            "ms_per_step": ms_fast, "value": pairs / (ms_fast * 1e-3), "unit": "pairs/s", "pairs_per_step": pairs,
+           "route": "traverse_self_f64: symmetric double walk with the pair exchange, rows assembled",
+           "whole_walk_ms": ms_whole,
+           "rows_equal_whole_walk": rows_equal_whole,
            "reference_layout_walk_ms": ms_ref_layout,
            "rows_equal_reference_layout_walk": rows_equal,
            "reference_cuda": ref}

@@ -261,6 +261,18 @@ class LBVHTraverser : public Tunable<unsigned int>
                                 const TransformOpT& transform, bool rows_sorted, const unsigned int* subset,
                                 unsigned int count);
 
+        // Self queries of a tree of double points (built with PointInsertOpF64 from `points`,
+        // indexed by primitive id), exact double predicate: the results of traverse() with
+        // ExactSphereQueryOpF64 over the spheres (points[primitive[s]], rc) in sorted order, with
+        // row s (rows_sorted) or primitive[s].  Counts above getSymmetricMinPoints() points with
+        // SelfOp or PeriodicImagesOp take the symmetric walk with the pair exchange, and a fill
+        // over the same tree, points, cutoff, images and rows assembles the rows from it; other
+        // traversals walk the whole tree per query.  Results do not depend on the route.
+        template<class OutputOpT, class TranslateOpT, class TransformOpT>
+        void traverseSelfF64(const LaunchParameters& params, const LBVH& lbvh, const double3* points, double rc,
+                             double3 box, float pad, const OutputOpT& out, const TranslateOpT& images,
+                             const TransformOpT& transform, bool rows_sorted);
+
     private:
         int m_root;
         shared_array<int4> m_data;
@@ -350,11 +362,17 @@ class LBVHTraverser : public Tunable<unsigned int>
             float3 L = make_float3(0.f, 0.f, 0.f);
             float3 box = make_float3(0.f, 0.f, 0.f);
             int rows_sorted = -1;
+            // double self queries: their points, cutoff and box (an FP32 count leaves them zero)
+            const void* points64 = nullptr;
+            double rc64 = 0.0;
+            double3 box64 = make_double3(0.0, 0.0, 0.0);
             bool operator==(const PassTag& o) const
                 {
                 return tree == o.tree && build == o.build && N == o.N && rc == o.rc && pad == o.pad
                        && lattice == o.lattice && L.x == o.L.x && L.y == o.L.y && L.z == o.L.z && box.x == o.box.x
-                       && box.y == o.box.y && box.z == o.box.z && rows_sorted == o.rows_sorted;
+                       && box.y == o.box.y && box.z == o.box.z && rows_sorted == o.rows_sorted
+                       && points64 == o.points64 && rc64 == o.rc64 && box64.x == o.box64.x && box64.y == o.box64.y
+                       && box64.z == o.box64.z;
                 }
             };
         // results of the last symmetric count: walk lengths (by sorted position), own counts and
@@ -405,10 +423,25 @@ class LBVHTraverser : public Tunable<unsigned int>
         void launch_assemble(const LaunchParameters& params, const LBVH& lbvh, const gpu::FastQueryArgs& a,
                              const OutputOpT& out, const TransformOpT& transform);
 
+        // the assembly of a fill from the last exchanging count (rows, images and outputs from a);
+        // the rows past the exchange are listed for a re-walk
+        template<int kind, class TransformOpT>
+        void assemble_rows(cudaStream_t stream, const LBVH& lbvh, const gpu::FastQueryArgs& a,
+                           const TransformOpT& transform);
+
         PassTag self_tag(const LBVH& lbvh, const gpu::FastQueryArgs& a) const
             {
             return PassTag{&lbvh, lbvh.getBuildId(), lbvh.getN(), a.self_rc, a.pad, a.lattice, a.lattice_L, a.box,
                            a.self_rows_sorted};
+            }
+        PassTag self_tag_f64(const LBVH& lbvh, const gpu::FastQueryArgsF64& a) const
+            {
+            PassTag t{&lbvh, lbvh.getBuildId(), lbvh.getN(), 0.f, a.pad, a.lattice, a.lattice_L,
+                      make_float3(0.f, 0.f, 0.f), a.self_rows_sorted};
+            t.points64 = a.points;
+            t.rc64 = a.self_rc;
+            t.box64 = a.box;
+            return t;
             }
     };
 
@@ -448,6 +481,26 @@ inline void set_output(gpu::FastQueryArgs& a, const CSRNeighborListOp& out)
     a.nneigh = out.nneigh;
     a.list = out.neigh_list;
     a.max_neigh = out.max_capacity;  // 0 = unknown
+    a.offsets = out.offsets;
+    a.caps = out.capacity;
+    }
+inline void set_output_f64(gpu::FastQueryArgsF64& a, const CountNeighborsOp& out)
+    {
+    a.nneigh = out.nneigh;
+    a.list = nullptr;
+    a.max_neigh = 0;
+    }
+inline void set_output_f64(gpu::FastQueryArgsF64& a, const NeighborListOp& out)
+    {
+    a.nneigh = out.nneigh;
+    a.list = out.neigh_list;
+    a.max_neigh = out.max_neigh;
+    }
+inline void set_output_f64(gpu::FastQueryArgsF64& a, const CSRNeighborListOp& out)
+    {
+    a.nneigh = out.nneigh;
+    a.list = out.neigh_list;
+    a.max_neigh = out.max_capacity;
     a.offsets = out.offsets;
     a.caps = out.capacity;
     }
@@ -551,24 +604,7 @@ void LBVHTraverser::traverse(const LaunchParameters& params, const LBVH& lbvh, c
             a.lattice = detail::image_lattice(images);
             a.lattice_L = detail::lattice_box(images, make_float3((float)query.box.x, (float)query.box.y,
                                                                   (float)query.box.z));
-            a.nneigh = out.nneigh;
-            if constexpr (std::is_same<OutputOpT, NeighborListOp>::value)
-                {
-                a.list = out.neigh_list;
-                a.max_neigh = out.max_neigh;
-                }
-            else if constexpr (std::is_same<OutputOpT, CSRNeighborListOp>::value)
-                {
-                a.list = out.neigh_list;
-                a.max_neigh = out.max_capacity;
-                a.offsets = out.offsets;
-                a.caps = out.capacity;
-                }
-            else
-                {
-                a.list = nullptr;
-                a.max_neigh = 0;
-                }
+            detail::set_output_f64(a, out);
             constexpr int kind = output_kind<OutputOpT>::value;
             const unsigned int bs = params.tunable;
             gpu::k_traverse_fast_f64<kind, TransformOpT><<<detail::ceil_div(query.size(), bs), bs, 0, params.stream>>>(
@@ -795,13 +831,11 @@ void LBVHTraverser::launch_half(const LaunchParameters& params, const LBVH& lbvh
     detail::check_cuda(cudaGetLastError(), "half traversal launch");
     }
 
-template<class OutputOpT, class TransformOpT>
-void LBVHTraverser::launch_assemble(const LaunchParameters& params, const LBVH& lbvh, const gpu::FastQueryArgs& a,
-                                    const OutputOpT& out, const TransformOpT& transform)
+template<int kind, class TransformOpT>
+void LBVHTraverser::assemble_rows(cudaStream_t stream, const LBVH& lbvh, const gpu::FastQueryArgs& a,
+                                  const TransformOpT& transform)
     {
-    constexpr int kind = output_kind<OutputOpT>::value;
     const unsigned int N = lbvh.getN();
-    cudaStream_t stream = params.stream;
     m_words.reserve(kWordCount);
     m_subset.reserve(N);
     // the re-walk list's length and the re-walk's ticket start at zero
@@ -826,6 +860,17 @@ void LBVHTraverser::launch_assemble(const LaunchParameters& params, const LBVH& 
     g.subset_count = m_words.get() + gpu::kSummaryWords;
     g.status = lbvh.getStatusPointer();
     gpu::k_half_assemble<kind, TransformOpT><<<detail::ceil_div(N, 256), 256, 0, stream>>>(g, transform);
+    detail::check_cuda(cudaGetLastError(), "assembly launch");
+    }
+
+template<class OutputOpT, class TransformOpT>
+void LBVHTraverser::launch_assemble(const LaunchParameters& params, const LBVH& lbvh, const gpu::FastQueryArgs& a,
+                                    const OutputOpT& out, const TransformOpT& transform)
+    {
+    constexpr int kind = output_kind<OutputOpT>::value;
+    const unsigned int N = lbvh.getN();
+    cudaStream_t stream = params.stream;
+    assemble_rows<kind>(stream, lbvh, a, transform);
     // rows whose pairs did not fit the exchange: walked whole (their count is known on the device)
     gpu::FastQueryArgs b = a;
     b.Q = N;
@@ -842,6 +887,114 @@ void LBVHTraverser::launch_assemble(const LaunchParameters& params, const LBVH& 
         lbvh.fastData(), b, transform, m_words.get() + gpu::kSummaryWords, scan);
     detail::check_cuda(cudaGetLastError(), "assembly launch");
     (void)out;
+    }
+
+template<class OutputOpT, class TranslateOpT, class TransformOpT>
+void LBVHTraverser::traverseSelfF64(const LaunchParameters& params, const LBVH& lbvh, const double3* points,
+                                    double rc, double3 box, float pad, const OutputOpT& out,
+                                    const TranslateOpT& images, const TransformOpT& transform, bool rows_sorted)
+    {
+    const detail::TraceRange trace_range("neighbor::LBVHTraverser::traverseSelfF64");
+    static_assert(output_kind<OutputOpT>::value != 0,
+                  "traverseSelfF64 needs CountNeighborsOp, NeighborListOp or CSRNeighborListOp");
+    static_assert(detail::is_float3_images<TranslateOpT>::value,
+                  "traverseSelfF64 needs SelfOp, ImageListOp<float3> or PeriodicImagesOp");
+    const unsigned int N = lbvh.getN();
+    if (N == 0 || images.size() == 0) return;
+    if (images.size() > 32)
+        throw std::runtime_error("A maximum of 32 image vectors are supported by LBVH traversers.");
+    if (!lbvh.hasFastF64Data())
+        throw std::runtime_error("traverseSelfF64 needs a tree built from double points (PointInsertOpF64).");
+    if (!points) throw std::runtime_error("traverseSelfF64 needs the tree's double points.");
+    checkParameter(params);
+    constexpr int kind = output_kind<OutputOpT>::value;
+    cudaStream_t stream = params.stream;
+    gpu::FastQueryArgsF64 a;
+    a.spheres = nullptr;
+    a.Q = N;
+    a.points = points;
+    a.box = box;
+    a.pad = pad;
+    a.images = detail::image_pointer(images);
+    a.n_images = images.size();
+    a.lattice = detail::image_lattice(images);
+    a.lattice_L = detail::lattice_box(images, make_float3((float)box.x, (float)box.y, (float)box.z));
+    detail::set_output_f64(a, out);
+    a.self_rc = rc;
+    a.self_rows_sorted = rows_sorted ? 1 : 0;
+    const bool symmetric = detail::is_symmetric_images<TranslateOpT>::value && m_symmetric
+                           && m_mode == kThreadTraversal && !m_stats && N < gpu::kHalfMaxN && N > m_symmetric_min;
+    const PassTag tag = self_tag_f64(lbvh, a);
+    const unsigned int bs = params.tunable;
+    if (kind == gpu::kFastCount)
+        {
+        m_count_tag = tag;
+        m_count_cached = symmetric && m_pair_cache && !m_dense;
+        m_summary_self = true;
+        m_summary_read = false;
+        m_summary_exchange = m_count_cached;
+        m_summary_n = N;
+        if (m_count_cached)
+            {
+            clear_summary(stream);
+            m_count_own.reserve(N);
+            m_cache.reserve((size_t)N * gpu::kHalfCacheSlots);
+            m_in_cache.reserve((size_t)N * gpu::kHalfCacheSlots);
+            m_in_count.reserve(N);
+            m_lost.reserve(N);
+            detail::check_cuda(cudaMemsetAsync(m_in_count.get(), 0, (size_t)N * sizeof(unsigned int), stream), "memset");
+            detail::check_cuda(cudaMemsetAsync(m_lost.get(), 0, N, stream), "memset");
+            gpu::HalfArgsF64 h;
+            h.Q = N;
+            h.points = points;
+            h.rc = rc;
+            h.box = box;
+            h.pad = pad;
+            h.lattice = a.lattice;
+            h.lattice_L = a.lattice_L;
+            h.own = m_count_own.get();
+            h.cache_out = m_cache.get();
+            h.in_cache = m_in_cache.get();
+            h.in_count = m_in_count.get();
+            h.in_lost = m_lost.get();
+            gpu::k_traverse_half_f64<><<<detail::ceil_div(N, gpu::kHalfBlock), gpu::kHalfBlock, 0, stream>>>(
+                lbvh.fastData(), h);
+            gpu::k_count_summary<true><<<summary_grid(N), gpu::kSummaryBlock, 0, stream>>>(
+                N, m_count_own.get(), m_in_count.get(), m_lost.get(), lbvh.fastData().primitive, a.self_rows_sorted,
+                a.nneigh, m_words.get(), lbvh.getStatusPointer());
+            detail::check_cuda(cudaGetLastError(), "double half traversal launch");
+            return;
+            }
+        gpu::k_traverse_fast_f64<kind, TransformOpT><<<detail::ceil_div(N, bs), bs, 0, stream>>>(lbvh.fastData(), a,
+                                                                                                 transform);
+        detail::check_cuda(cudaGetLastError(), "double traversal launch");
+        summarize_counts(stream, a.nneigh, N, lbvh.getStatusPointer());
+        return;
+        }
+    if (symmetric && m_count_cached && m_pair_cache && tag == m_count_tag && !(m_summary_read && m_dense))
+        {
+        // rows from the exchange; the rows past it walk the whole tree (listed by the assembly,
+        // their number read on the device)
+        gpu::FastQueryArgs g{};
+        g.self_rows_sorted = a.self_rows_sorted;
+        g.lattice = a.lattice;
+        g.nneigh = a.nneigh;
+        g.list = a.list;
+        g.max_neigh = a.max_neigh;
+        g.offsets = a.offsets;
+        g.caps = a.caps;
+        assemble_rows<kind>(stream, lbvh, g, transform);
+        gpu::FastQueryArgsF64 b = a;
+        b.subset = m_subset.get();
+        b.subset_count = m_words.get() + gpu::kSummaryWords;
+        const unsigned int blocks = std::max(1u, std::min(detail::ceil_div(N, bs), 8u * sm_count()));
+        gpu::k_traverse_fast_f64<kind, TransformOpT><<<blocks, bs, 0, stream>>>(lbvh.fastData(), b, transform);
+        detail::check_cuda(cudaGetLastError(), "double traversal launch");
+        return;
+        }
+    gpu::k_traverse_fast_f64<kind, TransformOpT><<<detail::ceil_div(N, bs), bs, 0, stream>>>(lbvh.fastData(), a,
+                                                                                             transform);
+    detail::check_cuda(cudaGetLastError(), "double traversal launch");
     }
 
 } // namespace neighbor

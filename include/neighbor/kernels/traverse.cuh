@@ -491,9 +491,10 @@ __global__ void k_traverse_fast(const FastLBVHData tree, const FastQueryArgs a,
 // ---------------------------------------------------------------------------------------------
 struct FastQueryArgsF64
     {
-    const double4_16a* spheres;  // (x, y, z, cutoff) per query
+    const double4_16a* spheres;  // (x, y, z, cutoff) per query; NULL: self queries (below)
     unsigned int Q;
-    const double3* points;       // double positions, indexed by the reported id
+    const double3* points;       // double positions, indexed by the reported id (self queries: by
+                                 // primitive id)
     double3 box;                 // periodic lengths for the minimum image (0 = open)
     float pad;
     const float3* images;        // image list; NULL => self image only, or the lattice below
@@ -505,6 +506,14 @@ struct FastQueryArgsF64
     unsigned int max_neigh;
     const unsigned long long* offsets = nullptr;  // kFastCSR
     const unsigned int* caps = nullptr;           // kFastCSR
+    // Self queries (spheres == NULL): query s is sorted position s with centre
+    // points[primitive[s]] and cutoff self_rc; its row is s (self_rows_sorted) or primitive[s].
+    double self_rc = 0.0;
+    int self_rows_sorted = 1;
+    // Optional: only the queries subset[0 .. *subset_count) (the count read on the device), by a
+    // grid-stride loop.
+    const unsigned int* subset = nullptr;
+    const unsigned int* subset_count = nullptr;
     };
 
 __device__ __forceinline__ float3 image_vector_f64(const FastQueryArgsF64& a, int i)
@@ -532,74 +541,119 @@ __device__ __forceinline__ float wrap_f32(float d, float L)
     return d;
     }
 
-template<int OUT, class TransformOpT>
-__global__ void k_traverse_fast_f64(const FastLBVHData tree, const FastQueryArgsF64 a, const TransformOpT transform)
+// FP32 screen of one double query (centre P, cutoff rc, padded radius rs): the query rounded to
+// nearest, the box lengths in FP32, the squared FP32 distances below which a pair is certain (in2)
+// and above which it is excluded (out2), and the padded radius that chooses images in FP32.
+struct ScreenF64
     {
-    __shared__ QuantFrame s_frame;
-    __shared__ unsigned int s_records;
-    if (threadIdx.x == 0)
-        {
-        s_frame = *tree.frame;
-        s_records = ld_status(tree.status) != 0u ? 0u : *tree.n_boxes + tree.N;
-        }
-    __syncthreads();
-    const unsigned int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= a.Q) return;
-    const QuantFrame f = s_frame;
-    const unsigned int n_rec = s_records;
-    const double4_16a s = a.spheres[q];
-    const double3 P = make_double3(s.x, s.y, s.z);
-    const double rs = __dadd_ru(s.w, (double)a.pad);
-    const float3 Pf = make_float3(__double2float_rn(P.x), __double2float_rn(P.y), __double2float_rn(P.z));
-    const float3 Lf = make_float3(__double2float_rn(a.box.x), __double2float_rn(a.box.y), __double2float_rn(a.box.z));
+    float3 Pf;
+    float3 Lf;
+    float in2;
+    float out2;
+    float rsf;
+    };
+
+__device__ __forceinline__ ScreenF64 screen_f64(const QuantFrame& f, const double3& P, double rc, double rs,
+                                                const double3& box)
+    {
+    ScreenF64 S;
+    S.Pf = make_float3(__double2float_rn(P.x), __double2float_rn(P.y), __double2float_rn(P.z));
+    S.Lf = make_float3(__double2float_rn(box.x), __double2float_rn(box.y), __double2float_rn(box.z));
     // M bounds every coordinate of the query, the scene and the box lengths (and the images)
-    float M = fmaxf(fmaxf(fabsf(Pf.x), fabsf(Pf.y)), fabsf(Pf.z));
+    float M = fmaxf(fmaxf(fabsf(S.Pf.x), fabsf(S.Pf.y)), fabsf(S.Pf.z));
     M = fmaxf(M, fmaxf(fmaxf(fabsf(f.lo.x), fabsf(f.lo.y)), fabsf(f.lo.z)));
     M = fmaxf(M, fmaxf(fmaxf(fabsf(f.hi.x), fabsf(f.hi.y)), fabsf(f.hi.z)));
-    M = fmaxf(M, fmaxf(fmaxf(Lf.x, Lf.y), Lf.z));
-    const float rcf = __double2float_ru(s.w);
-    const float eps = 16.f * ulp_of(fmaxf(M, 1.17549435e-38f)) + 4.7683716e-7f * rcf + 2.f * ulp_of(rcf);
-    const float lo_r = approx::fsub_rd(__double2float_rd(s.w), eps);
-    const float in2 = lo_r > 0.f ? approx::fmul_rd(lo_r, lo_r) : -1.f;   // below: a pair
+    M = fmaxf(M, fmaxf(fmaxf(S.Lf.x, S.Lf.y), S.Lf.z));
+    const float uM = ulp_of(fmaxf(M, 1.17549435e-38f));
+    const float rcf = __double2float_ru(rc);
+    const float eps = 16.f * uM + 4.7683716e-7f * rcf + 2.f * ulp_of(rcf);
+    const float lo_r = approx::fsub_rd(__double2float_rd(rc), eps);
+    S.in2 = lo_r > 0.f ? approx::fmul_rd(lo_r, lo_r) : -1.f;   // below: a pair
     const float hi_r = approx::fadd_ru(rcf, eps);
-    const float out2 = approx::fmul_ru(hi_r, hi_r);                        // above: not a pair
+    S.out2 = approx::fmul_ru(hi_r, hi_r);                        // above: not a pair
     // images whose box may meet the scene, in FP32 with a margin for the query's rounding
-    const float rsf = approx::fadd_ru(__double2float_ru(rs), 2.f * ulp_of(fmaxf(M, 1.17549435e-38f)));
+    S.rsf = approx::fadd_ru(__double2float_ru(rs), 2.f * uM);
+    return S;
+    }
+
+// Minimum-image squared distance of a record from the screened query, in FP32.
+__device__ __forceinline__ float screen_dist2(const ScreenF64& S, const float3& x)
+    {
+    const float dx = wrap_f32(__fsub_rn(x.x, S.Pf.x), S.Lf.x);
+    const float dy = wrap_f32(__fsub_rn(x.y, S.Pf.y), S.Lf.y);
+    const float dz = wrap_f32(__fsub_rn(x.z, S.Pf.z), S.Lf.z);
+    return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+    }
+
+// Images of a double query whose FP32 box (radius rsf) may meet the root box: the lattice's, or
+// those of the image list (the self image when there is none).
+__device__ __forceinline__ unsigned int image_flags_f64(const FastQueryArgsF64& a, const QuantFrame& f,
+                                                        const float3& Pf, float rsf)
+    {
+    if (a.lattice) return lattice_flags(a.lattice_L, f, Pf, rsf);
+    const unsigned int nimg = a.images ? min(a.n_images, 32u) : 1u;
     unsigned int flags = 0u;
-    if (n_rec)
+    for (unsigned int k = 0; k < nimg; ++k)
         {
-        if (a.lattice)
-            flags = lattice_flags(a.lattice_L, f, Pf, rsf);
-        else
-            {
-            const unsigned int nimg = a.images ? min(a.n_images, 32u) : 1u;
-            for (unsigned int k = 0; k < nimg; ++k)
-                {
-                const float3 t = image_vector_f64(a, (int)k);
-                const float3 c = make_float3(__fadd_rn(Pf.x, t.x), __fadd_rn(Pf.y, t.y), __fadd_rn(Pf.z, t.z));
-                const float3 lo = make_float3(approx::fsub_rd(c.x, rsf), approx::fsub_rd(c.y, rsf), approx::fsub_rd(c.z, rsf));
-                const float3 hi = make_float3(approx::fadd_ru(c.x, rsf), approx::fadd_ru(c.y, rsf), approx::fadd_ru(c.z, rsf));
-                if (lo.x <= f.hi.x && hi.x >= f.lo.x && lo.y <= f.hi.y && hi.y >= f.lo.y && lo.z <= f.hi.z
-                    && hi.z >= f.lo.z)
-                    flags |= 1u << k;
-                }
-            }
+        const float3 t = image_vector_f64(a, (int)k);
+        const float3 c = make_float3(__fadd_rn(Pf.x, t.x), __fadd_rn(Pf.y, t.y), __fadd_rn(Pf.z, t.z));
+        const float3 lo = make_float3(approx::fsub_rd(c.x, rsf), approx::fsub_rd(c.y, rsf), approx::fsub_rd(c.z, rsf));
+        const float3 hi = make_float3(approx::fadd_ru(c.x, rsf), approx::fadd_ru(c.y, rsf), approx::fadd_ru(c.z, rsf));
+        if (lo.x <= f.hi.x && hi.x >= f.lo.x && lo.y <= f.hi.y && hi.y >= f.lo.y && lo.z <= f.hi.z && hi.z >= f.lo.z)
+            flags |= 1u << k;
         }
+    return flags;
+    }
+
+// The FP32 query box of image t of a double query: the double box (centre + t, radius rs)
+// rounded outward.
+__device__ __forceinline__ void query_box_f64(const double3& P, const float3& t, double rs, float3& qlo, float3& qhi)
+    {
+    const double3 c = make_double3(__dadd_rn(P.x, (double)t.x), __dadd_rn(P.y, (double)t.y), __dadd_rn(P.z, (double)t.z));
+    qlo = make_float3(__double2float_rd(__dsub_rd(c.x, rs)), __double2float_rd(__dsub_rd(c.y, rs)),
+                      __double2float_rd(__dsub_rd(c.z, rs)));
+    qhi = make_float3(__double2float_ru(__dadd_ru(c.x, rs)), __double2float_ru(__dadd_ru(c.y, rs)),
+                      __double2float_ru(__dadd_ru(c.z, rs)));
+    }
+
+// One double query walked by one thread over the whole tree (images in bit order): the body of
+// k_traverse_fast_f64.  Writes the row's entries (list outputs) and its count.
+template<int OUT, class TransformOpT>
+__device__ __forceinline__ void thread_walk_f64(const FastLBVHData& tree, const FastQueryArgsF64& a,
+                                                const TransformOpT& transform, const QuantFrame& f,
+                                                unsigned int n_rec, unsigned int q)
+    {
+    const bool self = a.spheres == nullptr;
+    double3 P;
+    double rq;
+    unsigned int row;
+    if (self)
+        {
+        const unsigned int prim = tree.primitive[q];
+        P = a.points[prim];
+        rq = a.self_rc;
+        row = a.self_rows_sorted ? q : prim;
+        }
+    else
+        {
+        const double4_16a s = a.spheres[q];
+        P = make_double3(s.x, s.y, s.z);
+        rq = s.w;
+        row = q;
+        }
+    const double rs = __dadd_ru(rq, (double)a.pad);
+    const ScreenF64 S = screen_f64(f, P, rq, rs, a.box);
+    unsigned int flags = n_rec ? image_flags_f64(a, f, S.Pf, S.rsf) : 0u;
     unsigned long long row_first = 0;
     unsigned int cap = 0;
-    if (OUT != kFastCount) row_layout<OUT>(a.offsets, a.caps, a.max_neigh, q, row_first, cap);
+    if (OUT != kFastCount) row_layout<OUT>(a.offsets, a.caps, a.max_neigh, row, row_first, cap);
     unsigned int count = 0;
     while (flags)
         {
         const int bit = __ffs(flags) - 1;
         flags &= flags - 1u;
-        const float3 t = image_vector_f64(a, bit);
-        const double3 c = make_double3(__dadd_rn(P.x, (double)t.x), __dadd_rn(P.y, (double)t.y),
-                                       __dadd_rn(P.z, (double)t.z));
-        const float3 qlo = make_float3(__double2float_rd(__dsub_rd(c.x, rs)), __double2float_rd(__dsub_rd(c.y, rs)),
-                                       __double2float_rd(__dsub_rd(c.z, rs)));
-        const float3 qhi = make_float3(__double2float_ru(__dadd_ru(c.x, rs)), __double2float_ru(__dadd_ru(c.y, rs)),
-                                       __double2float_ru(__dadd_ru(c.z, rs)));
+        float3 qlo, qhi;
+        query_box_f64(P, image_vector_f64(a, bit), rs, qlo, qhi);
         const uint3 qb = pack_query_box(f, qlo, qhi);
         unsigned int i = 0;
         while (i < n_rec)
@@ -610,14 +664,12 @@ __global__ void k_traverse_fast_f64(const FastLBVHData tree, const FastQueryArgs
                 const float3 x = make_float3(__uint_as_float(n.x), __uint_as_float(n.y), __uint_as_float(n.z));
                 if (point_in_box(x, qlo, qhi))
                     {
-                    const float dx = wrap_f32(__fsub_rn(x.x, Pf.x), Lf.x);
-                    const float dy = wrap_f32(__fsub_rn(x.y, Pf.y), Lf.y);
-                    const float dz = wrap_f32(__fsub_rn(x.z, Pf.z), Lf.z);
-                    const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
-                    if (d2 <= out2)
+                    const float d2 = screen_dist2(S, x);
+                    if (d2 <= S.out2)
                         {
-                        const unsigned int id = transform(tree.primitive[n.w & ~kLeafFlag]);
-                        if (d2 < in2 || exact_pair_f64(P, a.points[id], s.w, a.box))
+                        const unsigned int prim = tree.primitive[n.w & ~kLeafFlag];
+                        const unsigned int id = transform(prim);
+                        if (d2 < S.in2 || exact_pair_f64(P, a.points[self ? prim : id], rq, a.box))
                             {
                             if (OUT != kFastCount && count < cap) a.list[row_first + count] = id;
                             ++count;
@@ -632,7 +684,34 @@ __global__ void k_traverse_fast_f64(const FastLBVHData tree, const FastQueryArgs
                 }
             }
         }
-    a.nneigh[q] = count;
+    a.nneigh[row] = count;
+    }
+
+// One thread per query (or per listed query, grid-stride, when a.subset is given).
+template<int OUT, class TransformOpT>
+__global__ void k_traverse_fast_f64(const FastLBVHData tree, const FastQueryArgsF64 a, const TransformOpT transform)
+    {
+    __shared__ QuantFrame s_frame;
+    __shared__ unsigned int s_records;
+    __shared__ unsigned int s_n;
+    if (threadIdx.x == 0)
+        {
+        s_frame = *tree.frame;
+        s_records = ld_status(tree.status) != 0u ? 0u : *tree.n_boxes + tree.N;
+        s_n = a.subset_count ? *a.subset_count : a.Q;
+        }
+    __syncthreads();
+    const QuantFrame f = s_frame;
+    const unsigned int n_rec = s_records;
+    const unsigned int n = s_n;
+    if (a.subset)
+        {
+        for (unsigned int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x)
+            thread_walk_f64<OUT>(tree, a, transform, f, n_rec, a.subset[t]);
+        return;
+        }
+    const unsigned int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < n) thread_walk_f64<OUT>(tree, a, transform, f, n_rec, q);
     }
 
 // ---------------------------------------------------------------------------------------------
@@ -1020,6 +1099,131 @@ __global__ void __launch_bounds__(kHalfBlock, OUT == kFastCount ? 16 : 12) k_tra
         a.own[row] = own | (placed ? kOwnPlaced : 0u);
         }
     if (!CACHE && a.walk_out) a.walk_out[q] = (unsigned short)min(visits, 65535u);
+    }
+
+// ---------------------------------------------------------------------------------------------
+// Symmetric count of double self queries with the pair exchange: the exchanging count of
+// k_traverse_half with the double predicate of k_traverse_fast_f64 (FP32 screen, exact_pair_f64 in
+// the band).  The double predicate is symmetric -- the minimum-image difference of (j, q) is the
+// exact negation of that of (q, j), component by component, so both have the same squared length
+// -- and the screen only decides pairs that the double predicate decides the same way, so a pair
+// found from the smaller sorted position counts for both rows.  A point inside a query's padded
+// double box has its rounded-down record inside the FP32 box of that image, and the partner's
+// record lies in the mirror image's box of the partner, as in the FP32 walk.  Own keys, incoming
+// keys and counters are those of k_traverse_half: k_count_summary and k_half_assemble take them
+// unchanged.
+// ---------------------------------------------------------------------------------------------
+struct HalfArgsF64
+    {
+    unsigned int Q;              // number of points (= queries)
+    const double3* points;       // double positions, by primitive id
+    double rc;
+    double3 box;                 // periodic lengths of the minimum image (0 = open)
+    float pad;
+    int lattice;                 // 1: the 27 images of lattice_L; 0: the self image only
+    float3 lattice_L;
+    unsigned int* own;           // pairs each query found itself, by sorted position
+    unsigned int* cache_out;     // own keys, kHalfCacheSlots per sorted position
+    unsigned int* in_cache;      // incoming keys, kHalfCacheSlots per sorted position
+    unsigned int* in_count;      // zero on entry
+    unsigned char* in_lost;      // zero on entry
+    };
+
+template<int MINB = 12>
+__global__ void __launch_bounds__(kHalfBlock, MINB) k_traverse_half_f64(const FastLBVHData tree, const HalfArgsF64 a)
+    {
+    __shared__ QuantFrame s_frame;
+    __shared__ unsigned int s_records;
+    if (threadIdx.x == 0)
+        {
+        s_frame = *tree.frame;
+        s_records = ld_status(tree.status) != 0u ? 0u : *tree.n_boxes + tree.N;
+        }
+    __syncthreads();
+    const unsigned int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= a.Q) return;
+    const QuantFrame f = s_frame;
+    const unsigned int n_rec = s_records;
+    const double3* P = a.points + tree.primitive[q];   // read again only for the band's exact test
+    const double3 Pq = *P;
+    const double rs = __dadd_ru(a.rc, (double)a.pad);
+    const ScreenF64 S = screen_f64(f, Pq, a.rc, rs, a.box);
+    unsigned int flags = 0u;
+    if (n_rec)
+        {
+        if (a.lattice)
+            flags = lattice_flags(a.lattice_L, f, S.Pf, S.rsf);
+        else
+            flags = (approx::fsub_rd(S.Pf.x, S.rsf) <= f.hi.x && approx::fadd_ru(S.Pf.x, S.rsf) >= f.lo.x
+                     && approx::fsub_rd(S.Pf.y, S.rsf) <= f.hi.y && approx::fadd_ru(S.Pf.y, S.rsf) >= f.lo.y
+                     && approx::fsub_rd(S.Pf.z, S.rsf) <= f.hi.z && approx::fadd_ru(S.Pf.z, S.rsf) >= f.lo.z)
+                        ? 1u : 0u;
+        }
+    const bool multi = __popc(flags) > 1;
+    const unsigned int start = n_rec ? tree.pre[q + 1] + q : 0u;
+    unsigned int own = 0;
+    // the pending deposit: partner (mirror image << 27 | position) and its slot (none: 0xffffffff)
+    unsigned int x_jm = 0u, x_slot = 0xffffffffu;
+    const auto deposit = [&]() {
+        if (x_slot < kHalfCacheSlots)
+            a.in_cache[(size_t)(x_jm & kHalfKeyMask) * kHalfCacheSlots + x_slot] = (x_jm & ~kHalfKeyMask) | q;
+    };
+    const auto take = [&](unsigned int j, unsigned int bit, unsigned int mirror) {
+        if (own < kHalfCacheSlots) a.cache_out[(size_t)q * kHalfCacheSlots + own] = (bit << kHalfKeyBits) | j;
+        if (j != q)
+            {
+            if (own < kHalfCacheSlots)
+                {
+                deposit();
+                x_slot = atomicAdd(a.in_count + j, 1u);
+                x_jm = (mirror << kHalfKeyBits) | j;
+                }
+            else
+                {
+                atomicAdd(a.in_count + j, 1u);
+                a.in_lost[j] = 1u;
+                }
+            }
+        ++own;
+    };
+    while (flags)
+        {
+        const int bit = __ffs(flags) - 1;
+        flags &= flags - 1u;
+        const float3 t = a.lattice ? PeriodicImagesOp(a.lattice_L).get((unsigned int)bit) : make_float3(0.f, 0.f, 0.f);
+        const unsigned int mirror = a.lattice ? 26u - (unsigned int)bit : 0u;
+        float3 qlo, qhi;
+        query_box_f64(Pq, t, rs, qlo, qhi);
+        const uint3 qb = pack_query_box(f, qlo, qhi);
+        unsigned int i = start;
+        while (i < n_rec)
+            {
+            const uint4 n = __ldg(tree.nodes + i);
+            if ((int)n.w < 0)
+                {
+                // with one image the predicate alone decides (a pair lies inside its box); with
+                // several, a point is taken only through the image whose box holds its record
+                const float3 x = make_float3(__uint_as_float(n.x), __uint_as_float(n.y), __uint_as_float(n.z));
+                if (!multi || point_in_box(x, qlo, qhi))
+                    {
+                    const float d2 = screen_dist2(S, x);
+                    if (d2 <= S.out2)
+                        {
+                        const unsigned int j = n.w & ~kLeafFlag;
+                        if (d2 < S.in2 || exact_pair_f64(*P, a.points[tree.primitive[j]], a.rc, a.box))
+                            take(j, (unsigned int)bit, mirror);
+                        }
+                    }
+                ++i;
+                }
+            else
+                {
+                i = node_overlaps(n, qb) ? i + 1u : max(n.w, i + 1u);
+                }
+            }
+        }
+    deposit();
+    a.own[q] = own;
     }
 
 // A row is past the pair exchange -- its row is walked again by the fill -- when its own or its

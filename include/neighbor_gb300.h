@@ -262,6 +262,20 @@ int nbr_traverse_f64(nbr_traverser t, nbr_lbvh h, const double* spheres, unsigne
                      const unsigned int* map, unsigned int* nneigh, unsigned int* list, unsigned int max_neigh,
                      unsigned int block_size, void* stream);
 
+/* Addition: self queries of a tree built by nbr_lbvh_build_points_f64 from `points` (double[3N],
+ * indexed by primitive id), exact double predicate: every primitive queries the tree with cutoff
+ * rc, in the tree's sorted order -- the counts and rows of nbr_traverse_f64 over the spheres
+ * (points[primitive[s]], rc) for s = 0..N-1 (LBVHTraverser::traverse with ExactSphereQueryOpF64,
+ * include/neighbor/LBVHTraverser.h:414-450 for the traversal it stands for).  rows_sorted = 1
+ * writes row s for sorted slot s, 0 row primitive[s]; box double[3] periodic lengths (0 = open),
+ * pad as nbr_exact_pad; images, map and outputs as nbr_traverse_self.  A count with SelfOp or the
+ * 27 periodic images finds each pair once and keeps the pairs, so that the next fill over the same
+ * tree, points, cutoff, images and rows writes its rows without walking. */
+int nbr_traverse_self_f64(nbr_traverser t, nbr_lbvh h, const double* points, double rc, const double box[3],
+                          float pad, const float* images, unsigned int n_images, const unsigned int* map,
+                          unsigned int* nneigh, unsigned int* list, unsigned int max_neigh, int rows_sorted,
+                          unsigned int block_size, void* stream);
+
 /* Radius padding for the exact query: 16 ulps of twice the largest coordinate magnitude
  * (centres, points and image translations) plus 1e-6 * rc. */
 float nbr_exact_pad(float rc, float coord_max);

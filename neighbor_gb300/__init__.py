@@ -117,6 +117,7 @@ def _declare(L):
     sig("nbr_exact_pad", [_F, _F], _F)
     sig("nbr_lbvh_build_points_f64", [_P, _P, _U, _P, _P, _U, _P])
     sig("nbr_traverse_f64", [_P, _P, _P, _U, _P, _P, _F, _P, _U, _P, _P, _P, _U, _U, _P])
+    sig("nbr_traverse_self_f64", [_P, _P, _P, ctypes.c_double, _P, _F, _P, _U, _P, _P, _P, _U, _I, _U, _P])
     sig("nbr_debug_wait_timeout", [ctypes.POINTER(_U), _P])
     sig("nbr_morton_sort_noalloc", [_P, _U, _P, _P, _P, _P, _P])
     sig("nbr_morton_sort_noalloc_status", [ctypes.POINTER(_U), _P])
@@ -195,7 +196,7 @@ EXPORTED = ["nbr_last_error", "nbr_version", "nbr_lbvh_create", "nbr_lbvh_destro
             "nbr_batch_create", "nbr_batch_destroy", "nbr_batch_setup", "nbr_batch_set_config",
             "nbr_batch_get_config", "nbr_batch_run", "nbr_batch_tune", "nbr_batch_capture",
             "nbr_batch_replay", "nbr_batch_status", "nbr_batch_sequential_plain",
-            "nbr_lbvh_build_points_f64", "nbr_traverse_f64"]
+            "nbr_lbvh_build_points_f64", "nbr_traverse_f64", "nbr_traverse_self_f64"]
 
 BATCH_MAX_N = 16384
 
@@ -649,6 +650,32 @@ class LBVHTraverser:
                                         27 if lattice else (0 if img is None else img.shape[0]), _ptr(m),
                                         _ptr(nneigh), _ptr(lst), 0 if max_neigh is None else int(max_neigh),
                                         block_size, _stream_ptr(stream)))
+        if max_neigh is None:
+            return nneigh
+        return nneigh, lst
+
+    def traverse_self_f64(self, lbvh: LBVH, points, rc: float, box, pad: float, images=None, map=None,
+                          max_neigh: Optional[int] = None, rows_sorted: bool = True, nneigh=None,
+                          neigh_list=None, block_size: int = 256, stream=None):
+        """Every primitive of a tree of double points queries the tree with cutoff rc (exact double
+        predicate): points float64 [N, 3] are the tree's own points by primitive id; rows and
+        images as traverse_self.  Equals traverse_f64 over the spheres (points[primitives], rc)."""
+        torch = _torch()
+        pts = _dev(points, torch.float64, 3)
+        _, N, _, _ = lbvh.sizes()
+        lattice = isinstance(images, str) and images == "periodic"
+        img = None if images is None or lattice else _dev(images, torch.float32, 3)
+        m = None if map is None else _dev(map, torch.int32)
+        if nneigh is None:
+            nneigh = torch.empty(N, dtype=torch.int32, device=pts.device)
+        lst = neigh_list
+        if max_neigh is not None and lst is None:
+            lst = torch.full((N, max(max_neigh, 1)), -1, dtype=torch.int32, device=pts.device)
+        b = (ctypes.c_double * 3)(*[float(x) for x in box])
+        _check(self._L.nbr_traverse_self_f64(self._h, lbvh.handle, _ptr(pts), float(rc), b, float(pad), _ptr(img),
+                                             27 if lattice else (0 if img is None else img.shape[0]), _ptr(m),
+                                             _ptr(nneigh), _ptr(lst), 0 if max_neigh is None else int(max_neigh),
+                                             1 if rows_sorted else 0, block_size, _stream_ptr(stream)))
         if max_neigh is None:
             return nneigh
         return nneigh, lst

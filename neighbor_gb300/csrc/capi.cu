@@ -453,6 +453,47 @@ int nbr_traverse_f64(nbr_traverser t, nbr_lbvh h, const double* spheres, unsigne
     });
     }
 
+int nbr_traverse_self_f64(nbr_traverser t, nbr_lbvh h, const double* points, double rc, const double box[3],
+                          float pad, const float* images, unsigned int n_images, const unsigned int* map,
+                          unsigned int* nneigh, unsigned int* list, unsigned int max_neigh, int rows_sorted,
+                          unsigned int block_size, void* stream)
+    {
+    if (!t || !h || !box) return fail(NBR_ERR_INVALID, "null argument");
+    if (h->lbvh.getN() > 0 && (!points || !nneigh)) return fail(NBR_ERR_INVALID, "null argument");
+    if (list && max_neigh == 0) return fail(NBR_ERR_INVALID, "max_neigh must be positive with a list");
+    if (images && n_images > 32) return fail(NBR_ERR_INVALID, "A maximum of 32 image vectors are supported by LBVH traversers.");
+    if (!valid_block(block_size)) return fail(NBR_ERR_INVALID, "Invalid tuning parameter.");
+    return guarded([&] {
+        const neighbor::LBVHTraverser::LaunchParameters p(block_size, as_stream(stream));
+        const double3* pts = reinterpret_cast<const double3*>(points);
+        const double3 b = make_double3(box[0], box[1], box[2]);
+        const float3 bf = make_float3((float)box[0], (float)box[1], (float)box[2]);
+        auto go = [&](const auto& out) {
+            auto with_images = [&](const auto& transform) {
+                if (images)
+                    t->trav.traverseSelfF64(p, h->lbvh, pts, rc, b, pad, out,
+                                            neighbor::ImageListOp<float3>(reinterpret_cast<const float3*>(images),
+                                                                          n_images),
+                                            transform, rows_sorted != 0);
+                else if (n_images == 27)
+                    t->trav.traverseSelfF64(p, h->lbvh, pts, rc, b, pad, out, neighbor::PeriodicImagesOp(bf), transform,
+                                            rows_sorted != 0);
+                else
+                    t->trav.traverseSelfF64(p, h->lbvh, pts, rc, b, pad, out, neighbor::SelfOp(), transform,
+                                            rows_sorted != 0);
+            };
+            if (map)
+                with_images(neighbor::MapTransformOp(map));
+            else
+                with_images(neighbor::NullTransformOp());
+        };
+        if (list)
+            go(neighbor::NeighborListOp(list, nneigh, max_neigh));
+        else
+            go(neighbor::CountNeighborsOp(nneigh));
+    });
+    }
+
 int nbr_tune_self(nbr_lbvh h, nbr_traverser t, const float* points, unsigned int N, const float lo[3],
                   const float hi[3], float rc, const float box[3], float pad, int periodic, unsigned int reps,
                   void* stream, unsigned int* leaf_size, unsigned int* radix_bits, unsigned int* climb_block,

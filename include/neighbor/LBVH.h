@@ -286,6 +286,7 @@ class LBVH : public Tunable<unsigned int>
         mutable device_array<unsigned int> m_locks;
         device_array<uint4> m_nodes;
         device_array<float4> m_payload;
+        device_array<unsigned char> m_hi_bits;   // double point trees: upper-corner bits per leaf
         device_array<unsigned int> m_small;
         device_array<unsigned long long> m_sort_status;
         device_array<unsigned long long> m_scan_status;
@@ -298,7 +299,10 @@ class LBVH : public Tunable<unsigned int>
         void materialize(cudaStream_t stream) const
             {
             if (m_ref_valid) return;
-            reference_layout(gpu::PayloadLeafBox{m_payload.get()}, stream);
+            if (m_fast_f64)
+                reference_layout(gpu::PayloadLeafBoxF64{m_payload.get(), m_hi_bits.get()}, stream);
+            else
+                reference_layout(gpu::PayloadLeafBox{m_payload.get()}, stream);
             }
 
         unsigned int next_epoch()
@@ -560,6 +564,11 @@ void LBVH::build(const LaunchParameters& params, const InsertOpT& insert, const 
     c.frame_out = reinterpret_cast<QuantFrame*>(small + kSmallFrame);
     c.leaf_size = m_leaf_size;
     c.error = small + kSmallStatus;
+    if (m_fast_f64)
+        {
+        m_hi_bits.reserve(N);
+        c.hi_bits = m_hi_bits.get();
+        }
     const unsigned int T = m_climb_block;
     if (T == 128)
         gpu::k_climb<InsertOpT, 128><<<detail::ceil_div(N, 128), 128, 0, stream>>>(insert, c);
@@ -589,8 +598,10 @@ void LBVH::build(const LaunchParameters& params, const InsertOpT& insert, const 
     gpu::k_emit<<<detail::ceil_div(N, 256), 256, 0, stream>>>(e);
     detail::check_cuda(cudaGetLastError(), "LBVH build launch");
 
+    // point trees form the reference-layout arrays on first access (from the payload); other
+    // insert ops here, while their inputs are known to be valid
     m_ref_valid = false;
-    if (!is_point_insert<InsertOpT>::value)
+    if (!is_point_insert<InsertOpT>::value && !m_fast_f64)
         reference_layout(gpu::InsertLeafBox<InsertOpT>{insert, m_indexes.current().get()}, stream);
     }
 

@@ -637,6 +637,9 @@ struct ClimbArgs
     QuantFrame* frame_out;
     unsigned int leaf_size;
     const unsigned int* error;
+    // double point trees (PointInsertOpF64): per sorted leaf, bit c set when the leaf box's upper
+    // bound in axis c lies above its lower bound (the double point is not a float); NULL otherwise
+    unsigned char* hi_bits = nullptr;
     };
 
 struct ClimbNode
@@ -659,6 +662,13 @@ __device__ __forceinline__ ClimbNode climb_leaf(const InsertOpT& insert, const C
     const unsigned int prim = A.primitive[s];
     const BoundingBox b = insert.get(prim);
     if (store) A.payload[s] = make_float4(b.lo.x, b.lo.y, b.lo.z, __uint_as_float(prim));
+    if constexpr (std::is_same<InsertOpT, PointInsertOpF64>::value)
+        {
+        // the payload keeps the lower corner; these bits give back the upper one
+        if (store && A.hi_bits)
+            A.hi_bits[s] = (unsigned char)((b.hi.x != b.lo.x ? 1u : 0u) | (b.hi.y != b.lo.y ? 2u : 0u)
+                                           | (b.hi.z != b.lo.z ? 4u : 0u));
+        }
     const uint3 w = pack_node_box(f, b.lo, b.hi);
     ClimbNode n;
     n.box = w;
@@ -1016,6 +1026,33 @@ struct PayloadLeafBox
         const float4 p = payload[s];
         const float3 x = make_float3(p.x, p.y, p.z);
         return BoundingBox(x, x);
+        }
+    };
+
+// The next float above x (x finite, or -inf).
+__device__ __forceinline__ float next_float_up(float x)
+    {
+    const unsigned int u = __float_as_uint(x);
+    if (u == 0x80000000u) return __uint_as_float(1u);   // -0: the smallest positive subnormal
+    return __uint_as_float((u & 0x80000000u) ? u - 1u : u + 1u);
+    }
+
+// Leaf boxes of a double point tree: the payload's lower corner (the point rounded down to FP32)
+// and the upper corner it implies.  The point rounded up is the lower corner where the point is a
+// float, and the next float above it where it is not (hi_bits), so the box is the one
+// BoundingBox(double3, double3) gave at the build.
+struct PayloadLeafBoxF64
+    {
+    const float4* payload;
+    const unsigned char* hi_bits;
+    __device__ __forceinline__ BoundingBox operator()(unsigned int s) const
+        {
+        const float4 p = payload[s];
+        const unsigned int bits = hi_bits[s];
+        const float3 lo = make_float3(p.x, p.y, p.z);
+        const float3 hi = make_float3((bits & 1u) ? next_float_up(p.x) : p.x, (bits & 2u) ? next_float_up(p.y) : p.y,
+                                      (bits & 4u) ? next_float_up(p.z) : p.z);
+        return BoundingBox(lo, hi);
         }
     };
 

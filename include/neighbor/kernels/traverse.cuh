@@ -576,12 +576,22 @@ __device__ __forceinline__ ScreenF64 screen_f64(const QuantFrame& f, const doubl
     return S;
     }
 
-// Minimum-image squared distance of a record from the screened query, in FP32.
+// Minimum-image squared distance of a record from the screened query, in FP32.  WRAP false: the
+// plain difference, for a query that meets the scene through one image with a padded radius below
+// 0.45 box lengths (wrap_free): a point that only the wrap brings within the cutoff would lie in
+// another image's box, which would then meet the scene too.  The screen then still decides only
+// what the double predicate decides the same way: below in2 the plain distance bounds the
+// minimum-image one, and above out2 no image but the query's own can hold a pair.
+template<bool WRAP = true>
 __device__ __forceinline__ float screen_dist2(const ScreenF64& S, const float3& x)
     {
-    const float dx = wrap_f32(__fsub_rn(x.x, S.Pf.x), S.Lf.x);
-    const float dy = wrap_f32(__fsub_rn(x.y, S.Pf.y), S.Lf.y);
-    const float dz = wrap_f32(__fsub_rn(x.z, S.Pf.z), S.Lf.z);
+    float dx = __fsub_rn(x.x, S.Pf.x), dy = __fsub_rn(x.y, S.Pf.y), dz = __fsub_rn(x.z, S.Pf.z);
+    if (WRAP)
+        {
+        dx = wrap_f32(dx, S.Lf.x);
+        dy = wrap_f32(dy, S.Lf.y);
+        dz = wrap_f32(dz, S.Lf.z);
+        }
     return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
     }
 
@@ -1129,7 +1139,9 @@ struct HalfArgsF64
     unsigned char* in_lost;      // zero on entry
     };
 
-template<int MINB = 12>
+// MINB: resident blocks per SM.  16M points, count alone: 16 blocks (32 registers, a few spilled)
+// 4.04 ms, 12 blocks 4.84, 10 blocks 9.30, 8 blocks 5.60.
+template<int MINB = 16>
 __global__ void __launch_bounds__(kHalfBlock, MINB) k_traverse_half_f64(const FastLBVHData tree, const HalfArgsF64 a)
     {
     __shared__ QuantFrame s_frame;
@@ -1160,6 +1172,7 @@ __global__ void __launch_bounds__(kHalfBlock, MINB) k_traverse_half_f64(const Fa
                         ? 1u : 0u;
         }
     const bool multi = __popc(flags) > 1;
+    const bool plain = !multi && wrap_free(S.Lf, S.rsf);
     const unsigned int start = n_rec ? tree.pre[q + 1] + q : 0u;
     unsigned int own = 0;
     // the pending deposit: partner (mirror image << 27 | position) and its slot (none: 0xffffffff)
@@ -1195,32 +1208,40 @@ __global__ void __launch_bounds__(kHalfBlock, MINB) k_traverse_half_f64(const Fa
         float3 qlo, qhi;
         query_box_f64(Pq, t, rs, qlo, qhi);
         const uint3 qb = pack_query_box(f, qlo, qhi);
-        unsigned int i = start;
-        while (i < n_rec)
-            {
-            const uint4 n = __ldg(tree.nodes + i);
-            if ((int)n.w < 0)
+        // the walk, compiled twice: with the plain screen and with the minimum-image one
+        const auto walk = [&](auto plain_tag) {
+            constexpr bool kPlain = decltype(plain_tag)::value;
+            unsigned int i = start;
+            while (i < n_rec)
                 {
-                // with one image the predicate alone decides (a pair lies inside its box); with
-                // several, a point is taken only through the image whose box holds its record
-                const float3 x = make_float3(__uint_as_float(n.x), __uint_as_float(n.y), __uint_as_float(n.z));
-                if (!multi || point_in_box(x, qlo, qhi))
+                const uint4 n = __ldg(tree.nodes + i);
+                if ((int)n.w < 0)
                     {
-                    const float d2 = screen_dist2(S, x);
-                    if (d2 <= S.out2)
+                    // with one image the predicate alone decides (a pair lies inside its box); with
+                    // several, a point is taken only through the image whose box holds its record
+                    const float3 x = make_float3(__uint_as_float(n.x), __uint_as_float(n.y), __uint_as_float(n.z));
+                    if (kPlain || !multi || point_in_box(x, qlo, qhi))
                         {
-                        const unsigned int j = n.w & ~kLeafFlag;
-                        if (d2 < S.in2 || exact_pair_f64(*P, a.points[tree.primitive[j]], a.rc, a.box))
-                            take(j, (unsigned int)bit, mirror);
+                        const float d2 = screen_dist2<!kPlain>(S, x);
+                        if (d2 <= S.out2)
+                            {
+                            const unsigned int j = n.w & ~kLeafFlag;
+                            if (d2 < S.in2 || exact_pair_f64(*P, a.points[tree.primitive[j]], a.rc, a.box))
+                                take(j, (unsigned int)bit, mirror);
+                            }
                         }
+                    ++i;
                     }
-                ++i;
+                else
+                    {
+                    i = node_overlaps(n, qb) ? i + 1u : max(n.w, i + 1u);
+                    }
                 }
-            else
-                {
-                i = node_overlaps(n, qb) ? i + 1u : max(n.w, i + 1u);
-                }
-            }
+        };
+        if (plain)
+            walk(std::true_type());
+        else
+            walk(std::false_type());
         }
     deposit();
     a.own[q] = own;

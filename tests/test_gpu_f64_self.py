@@ -201,3 +201,37 @@ def test_self_f64_near_cutoff_pairs():
     assert np.array_equal(c, want_c)
     for i in range(N):
         assert np.array_equal(np.sort(lst[i, : c[i]]), want_rows[i]), i
+
+
+def _round_f32(x, up):
+    """float64 -> float32 rounded toward +inf (up) or -inf, elementwise."""
+    f = x.astype(np.float32)
+    back = f.astype(np.float64)
+    if up:
+        return np.where(back < x, np.nextafter(f, np.float32(np.inf)), f)
+    return np.where(back > x, np.nextafter(f, np.float32(-np.inf)), f)
+
+
+def test_double_tree_reference_layout_boxes():
+    # a double point tree forms its reference-layout boxes on first access from the payload (the
+    # point rounded down) and the upper-corner bits: leaf boxes must be the points rounded outward
+    # to FP32 -- with coordinates that are floats (multiples of 1/8) and ones that are not -- and
+    # every internal box the union of its children's
+    rng = np.random.default_rng(61)
+    N = 5000
+    L = 20.0
+    P = rng.random((N, 3)) * L
+    exact = rng.random((N, 3)) < 0.4
+    P = np.where(exact, np.round(P * 8.0) / 8.0, P)
+    lbvh = nb.LBVH()
+    lbvh.build_f64(torch.tensor(P, device="cuda"), [0, 0, 0], [L, L, L])
+    arr = {k: v.cpu().numpy() for k, v in lbvh.arrays().items()}
+    ni = N - 1
+    prim = arr["primitive"].view(np.uint32).astype(np.int64)
+    lo_leaf, hi_leaf = arr["lo"][ni:], arr["hi"][ni:]
+    assert np.array_equal(lo_leaf, _round_f32(P[prim], False))
+    assert np.array_equal(hi_leaf, _round_f32(P[prim], True))
+    assert np.array_equal(hi_leaf == lo_leaf, exact[prim] | (P[prim] == P[prim].astype(np.float32)))
+    left, right = arr["left"], arr["right"]
+    assert np.array_equal(arr["lo"][:ni], np.minimum(arr["lo"][left], arr["lo"][right]))
+    assert np.array_equal(arr["hi"][:ni], np.maximum(arr["hi"][left], arr["hi"][right]))

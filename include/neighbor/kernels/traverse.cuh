@@ -615,15 +615,21 @@ __device__ __forceinline__ unsigned int image_flags_f64(const FastQueryArgsF64& 
     return flags;
     }
 
-// The FP32 query box of image t of a double query: the double box (centre + t, radius rs)
-// rounded outward.
-__device__ __forceinline__ void query_box_f64(const double3& P, const float3& t, double rs, float3& qlo, float3& qhi)
+// The FP32 query box of image t of a double query: from the query rounded to nearest (S.Pf) and
+// the padded radius of the image choice (S.rsf, at least rs + 2 ulp(M)), each step rounded away
+// from the box's centre.  Pf lies within ulp(M)/2 of the double centre, so the box holds the exact
+// box [P + t - rs, P + t + rs], and a point inside that has its rounded-down record (a float not
+// above the point) inside this one.  It is a few ulps wider than the exact box rounded outward,
+// which only adds candidates that the predicate turns down, and it keeps the double pipe (about
+// 1/64 of the FP32 rate on this GPU) out of the per-image work.
+__device__ __forceinline__ void query_box_f32(const ScreenF64& S, const float3& t, float3& qlo, float3& qhi)
     {
-    const double3 c = make_double3(__dadd_rn(P.x, (double)t.x), __dadd_rn(P.y, (double)t.y), __dadd_rn(P.z, (double)t.z));
-    qlo = make_float3(__double2float_rd(__dsub_rd(c.x, rs)), __double2float_rd(__dsub_rd(c.y, rs)),
-                      __double2float_rd(__dsub_rd(c.z, rs)));
-    qhi = make_float3(__double2float_ru(__dadd_ru(c.x, rs)), __double2float_ru(__dadd_ru(c.y, rs)),
-                      __double2float_ru(__dadd_ru(c.z, rs)));
+    qlo = make_float3(approx::fsub_rd(approx::fadd_rd(S.Pf.x, t.x), S.rsf),
+                      approx::fsub_rd(approx::fadd_rd(S.Pf.y, t.y), S.rsf),
+                      approx::fsub_rd(approx::fadd_rd(S.Pf.z, t.z), S.rsf));
+    qhi = make_float3(approx::fadd_ru(approx::fadd_ru(S.Pf.x, t.x), S.rsf),
+                      approx::fadd_ru(approx::fadd_ru(S.Pf.y, t.y), S.rsf),
+                      approx::fadd_ru(approx::fadd_ru(S.Pf.z, t.z), S.rsf));
     }
 
 // One double query walked by one thread over the whole tree (images in bit order): the body of
@@ -663,7 +669,7 @@ __device__ __forceinline__ void thread_walk_f64(const FastLBVHData& tree, const 
         const int bit = __ffs(flags) - 1;
         flags &= flags - 1u;
         float3 qlo, qhi;
-        query_box_f64(P, image_vector_f64(a, bit), rs, qlo, qhi);
+        query_box_f32(S, image_vector_f64(a, bit), qlo, qhi);
         const uint3 qb = pack_query_box(f, qlo, qhi);
         unsigned int i = 0;
         while (i < n_rec)
@@ -1140,7 +1146,7 @@ struct HalfArgsF64
     };
 
 // MINB: resident blocks per SM.  16M points, count alone: 16 blocks (32 registers, a few spilled)
-// 4.04 ms, 12 blocks 4.84, 10 blocks 9.30, 8 blocks 5.60.
+// 3.75 ms, 12 blocks 4.20, 10 blocks 4.66, 8 blocks 5.30.
 template<int MINB = 16>
 __global__ void __launch_bounds__(kHalfBlock, MINB) k_traverse_half_f64(const FastLBVHData tree, const HalfArgsF64 a)
     {
@@ -1160,6 +1166,7 @@ __global__ void __launch_bounds__(kHalfBlock, MINB) k_traverse_half_f64(const Fa
     const double3 Pq = *P;
     const double rs = __dadd_ru(a.rc, (double)a.pad);
     const ScreenF64 S = screen_f64(f, Pq, a.rc, rs, a.box);
+
     unsigned int flags = 0u;
     if (n_rec)
         {
@@ -1206,7 +1213,7 @@ __global__ void __launch_bounds__(kHalfBlock, MINB) k_traverse_half_f64(const Fa
         const float3 t = a.lattice ? PeriodicImagesOp(a.lattice_L).get((unsigned int)bit) : make_float3(0.f, 0.f, 0.f);
         const unsigned int mirror = a.lattice ? 26u - (unsigned int)bit : 0u;
         float3 qlo, qhi;
-        query_box_f64(Pq, t, rs, qlo, qhi);
+        query_box_f32(S, t, qlo, qhi);
         const uint3 qb = pack_query_box(f, qlo, qhi);
         // the walk, compiled twice: with the plain screen and with the minimum-image one
         const auto walk = [&](auto plain_tag) {

@@ -663,42 +663,54 @@ __device__ __forceinline__ void thread_walk_f64(const FastLBVHData& tree, const 
     unsigned long long row_first = 0;
     unsigned int cap = 0;
     if (OUT != kFastCount) row_layout<OUT>(a.offsets, a.caps, a.max_neigh, row, row_first, cap);
+    // no distance inside the padded box of the query's own image wraps: that image's walk
+    // screens without the minimum-image wrap (the same numbers for every point it tests)
+    const bool own_plain = wrap_free(S.Lf, S.rsf);
     unsigned int count = 0;
     while (flags)
         {
         const int bit = __ffs(flags) - 1;
         flags &= flags - 1u;
+        const float3 t = image_vector_f64(a, bit);
         float3 qlo, qhi;
-        query_box_f32(S, image_vector_f64(a, bit), qlo, qhi);
+        query_box_f32(S, t, qlo, qhi);
         const uint3 qb = pack_query_box(f, qlo, qhi);
-        unsigned int i = 0;
-        while (i < n_rec)
-            {
-            const uint4 n = __ldg(tree.nodes + i);
-            if ((int)n.w < 0)
+        // the walk, compiled twice: with the plain screen and with the minimum-image one
+        const auto walk = [&](auto plain_tag) {
+            constexpr bool kPlain = decltype(plain_tag)::value;
+            unsigned int i = 0;
+            while (i < n_rec)
                 {
-                const float3 x = make_float3(__uint_as_float(n.x), __uint_as_float(n.y), __uint_as_float(n.z));
-                if (point_in_box(x, qlo, qhi))
+                const uint4 n = __ldg(tree.nodes + i);
+                if ((int)n.w < 0)
                     {
-                    const float d2 = screen_dist2(S, x);
-                    if (d2 <= S.out2)
+                    const float3 x = make_float3(__uint_as_float(n.x), __uint_as_float(n.y), __uint_as_float(n.z));
+                    if (point_in_box(x, qlo, qhi))
                         {
-                        const unsigned int prim = tree.primitive[n.w & ~kLeafFlag];
-                        const unsigned int id = transform(prim);
-                        if (d2 < S.in2 || exact_pair_f64(P, a.points[self ? prim : id], rq, a.box))
+                        const float d2 = screen_dist2<!kPlain>(S, x);
+                        if (d2 <= S.out2)
                             {
-                            if (OUT != kFastCount && count < cap) a.list[row_first + count] = id;
-                            ++count;
+                            const unsigned int prim = tree.primitive[n.w & ~kLeafFlag];
+                            const unsigned int id = transform(prim);
+                            if (d2 < S.in2 || exact_pair_f64(P, a.points[self ? prim : id], rq, a.box))
+                                {
+                                if (OUT != kFastCount && count < cap) a.list[row_first + count] = id;
+                                ++count;
+                                }
                             }
                         }
+                    ++i;
                     }
-                ++i;
+                else
+                    {
+                    i = node_overlaps(n, qb) ? i + 1u : max(n.w, i + 1u);
+                    }
                 }
-            else
-                {
-                i = node_overlaps(n, qb) ? i + 1u : max(n.w, i + 1u);
-                }
-            }
+        };
+        if (own_plain && t.x == 0.f && t.y == 0.f && t.z == 0.f)
+            walk(std::true_type());
+        else
+            walk(std::false_type());
         }
     a.nneigh[row] = count;
     }

@@ -243,6 +243,15 @@ class LBVHTraverser : public Tunable<unsigned int>
             m_walk_lanes = lanes;
             }
         unsigned int getWalkLanes() const { return m_walk_lanes; }
+        // Lanes per query of the symmetric count with the pair exchange: 1 (one thread per
+        // query), 4, 8, 16 or 32; 0 (default) picks by size.  Results do not depend on it.
+        void setHalfWalkLanes(unsigned int lanes)
+            {
+            if (lanes != 0 && lanes != 1 && lanes != 4 && lanes != 8 && lanes != 16 && lanes != 32)
+                throw std::runtime_error("Invalid half-walk lanes (0, 1, 4, 8, 16 or 32).");
+            m_half_lanes = lanes;
+            }
+        unsigned int getHalfWalkLanes() const { return m_half_lanes; }
 
         // Self queries on the fast path: every primitive of the tree queries the tree with cutoff
         // rc.  Queries run in the tree's sorted order; rows_sorted selects whether row s of the
@@ -288,6 +297,7 @@ class LBVHTraverser : public Tunable<unsigned int>
         unsigned int m_warp_walk_max = gpu::kWarpWalkMaxQueries;
         unsigned int m_symmetric_min = gpu::kSymmetricMinPoints;
         unsigned int m_walk_lanes = 0;
+        unsigned int m_half_lanes = 0;
         bool m_pair_cache = true;
         bool m_count_cached = false;
         // the summary words come from a self count (m_summary_self); its summary was read on the
@@ -349,6 +359,15 @@ class LBVHTraverser : public Tunable<unsigned int>
             {
             if (m_walk_lanes) return m_walk_lanes;
             return Q <= 16384u ? 32u : 16u;
+            }
+        // the symmetric count alone (exchange, kernel only): 32,768 points one thread per query
+        // 149 us, lane groups of 4 / 8 / 16 / 32: 114 / 88 / 71 / 57 us; 65,536 points 127 us,
+        // 114 / 90 / 100 / 92 us; 131,072 points 133 us, 159 / 133 / 168 / 178 us; above that one
+        // thread per query leads (262,144 points 147 against 237 us with 8 lanes)
+        unsigned int half_lanes(unsigned int N) const
+            {
+            if (m_half_lanes) return m_half_lanes;
+            return N <= 32768u ? 32u : (N <= 65536u ? 8u : 1u);
             }
         // What a symmetric count ran on (the tree's address and process-unique build id, cutoff,
         // images, box and rows); a fill with the same tag reuses its results.
@@ -785,8 +804,22 @@ void LBVHTraverser::launch_half(const LaunchParameters& params, const LBVH& lbvh
             detail::check_cuda(cudaMemsetAsync(m_in_count.get(), 0, (size_t)N * sizeof(unsigned int), stream), "memset");
             detail::check_cuda(cudaMemsetAsync(m_lost.get(), 0, N, stream), "memset");
             if constexpr (kind == gpu::kFastCount)
-                gpu::k_traverse_half<kind, TransformOpT, true><<<grid, gpu::kHalfBlock, 0, stream>>>(lbvh.fastData(), h,
-                                                                                                     transform);
+                {
+                const unsigned int G = half_lanes(N);
+                const unsigned int ggrid = (unsigned int)(((unsigned long long)N * G + gpu::kWarpWalkBlock - 1u)
+                                                          / gpu::kWarpWalkBlock);
+                if (G == 4)
+                    gpu::k_traverse_half_group<4><<<ggrid, gpu::kWarpWalkBlock, 0, stream>>>(lbvh.fastData(), h);
+                else if (G == 8)
+                    gpu::k_traverse_half_group<8><<<ggrid, gpu::kWarpWalkBlock, 0, stream>>>(lbvh.fastData(), h);
+                else if (G == 16)
+                    gpu::k_traverse_half_group<16><<<ggrid, gpu::kWarpWalkBlock, 0, stream>>>(lbvh.fastData(), h);
+                else if (G == 32)
+                    gpu::k_traverse_half_group<32><<<ggrid, gpu::kWarpWalkBlock, 0, stream>>>(lbvh.fastData(), h);
+                else
+                    gpu::k_traverse_half<kind, TransformOpT, true><<<grid, gpu::kHalfBlock, 0, stream>>>(
+                        lbvh.fastData(), h, transform);
+                }
             gpu::k_count_summary<true><<<summary_grid(N), gpu::kSummaryBlock, 0, stream>>>(
                 N, m_count_own.get(), m_in_count.get(), m_lost.get(), lbvh.fastData().primitive, a.self_rows_sorted, a.nneigh,
                 m_words.get(), lbvh.getStatusPointer());

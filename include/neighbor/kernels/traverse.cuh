@@ -1130,6 +1130,105 @@ __global__ void __launch_bounds__(kHalfBlock, OUT == kFastCount ? 16 : 12) k_tra
     }
 
 // ---------------------------------------------------------------------------------------------
+// The exchanging symmetric count of k_traverse_half, one query per group of G lanes: the group
+// takes the records after the query's own one in chunks of G, as group_walk does over the whole
+// tree (a record is live unless an earlier missed box of the chunk covers it; the next chunk
+// starts past the chunk and past every missed subtree), so it meets the same partners in the same
+// order.  The accepted pairs of a chunk are ranked by lane (ballot), so the own keys stay in the
+// order found; each partner's key goes to the slot its incoming counter hands out.  A pair found
+// past the query's own slots marks the partner's row as counted without a key, as the thread walk
+// does.  Few queries (small systems) leave most of the GPU idle and the longest walks set the time
+// -- a query meeting the scene through up to eight images walks each of them -- and G lanes cut
+// each walk's latency about G times.
+// ---------------------------------------------------------------------------------------------
+template<int G>
+__global__ void __launch_bounds__(kWarpWalkBlock) k_traverse_half_group(const FastLBVHData tree, const HalfArgs a)
+    {
+    static_assert(G == 4 || G == 8 || G == 16 || G == 32, "lane groups of 4, 8, 16 or 32");
+    __shared__ QuantFrame s_frame;
+    __shared__ unsigned int s_records;
+    if (threadIdx.x == 0)
+        {
+        s_frame = *tree.frame;
+        s_records = ld_status(tree.status) != 0u ? 0u : *tree.n_boxes + tree.N;
+        }
+    __syncthreads();
+    const unsigned int lane = threadIdx.x & (unsigned int)(G - 1);
+    const unsigned int gmask = G == 32 ? 0xffffffffu
+                                       : (((1u << (G & 31)) - 1u) << ((threadIdx.x & 31u) & ~(unsigned int)(G - 1)));
+    const unsigned int lt = lanemask_lt() & gmask;
+    const unsigned int q = (blockIdx.x * blockDim.x + threadIdx.x) / (unsigned int)G;
+    if (q >= a.Q) return;   // whole groups
+    const QuantFrame f = s_frame;
+    const unsigned int n_rec = s_records;
+    const float4 me = tree.points[q];
+    const float3 P = make_float3(me.x, me.y, me.z);
+    const float rs = approx::fadd_ru(a.rc, a.pad);
+    unsigned int flags = n_rec ? half_image_flags(a, f, P, rs) : 0u;
+    const bool multi = __popc(flags) > 1;
+    const bool plain = !multi && wrap_free(a.box, rs);
+    const float rc2 = __fmul_rn(a.rc, a.rc);
+    const unsigned int start = n_rec ? tree.pre[q + 1] + q : 0u;
+    unsigned int own = 0;   // group-uniform: own pairs found so far
+    while (flags)
+        {
+        const int bit = __ffs(flags) - 1;
+        flags &= flags - 1u;
+        const float3 t = a.lattice ? PeriodicImagesOp(a.lattice_L).get((unsigned int)bit) : make_float3(0.f, 0.f, 0.f);
+        const unsigned int mirror = a.lattice ? 26u - (unsigned int)bit : 0u;
+        const float3 c = make_float3(__fadd_rn(P.x, t.x), __fadd_rn(P.y, t.y), __fadd_rn(P.z, t.z));
+        const float3 qlo = make_float3(approx::fsub_rd(c.x, rs), approx::fsub_rd(c.y, rs), approx::fsub_rd(c.z, rs));
+        const float3 qhi = make_float3(approx::fadd_ru(c.x, rs), approx::fadd_ru(c.y, rs), approx::fadd_ru(c.z, rs));
+        const uint3 qb = pack_query_box(f, qlo, qhi);
+        unsigned int i = start;
+        while (i < n_rec)   // group-uniform
+            {
+            const unsigned int k = i + lane;
+            const bool valid = k < n_rec;
+            const uint4 n = valid ? __ldg(tree.nodes + k) : make_uint4(0u, 0u, 0u, 0u);
+            const bool is_point = valid && (int)n.w < 0;
+            const bool miss = valid && !is_point && !node_overlaps(n, qb);
+            const unsigned int kill = miss ? max(n.w, k + 1u) : 0u;   // [k + 1, kill) lies under it
+            unsigned int cover = kill;   // inclusive prefix maximum over the group's lanes
+#pragma unroll
+            for (int o = 1; o < G; o <<= 1)
+                {
+                const unsigned int v = __shfl_up_sync(gmask, cover, o, G);
+                if ((int)lane >= o) cover = max(cover, v);
+                }
+            const unsigned int before = __shfl_up_sync(gmask, cover, 1, G);
+            const bool live = valid && (lane == 0u || before <= k);
+            bool accept = false;
+            if (live && is_point)
+                {
+                const float3 x = make_float3(__uint_as_float(n.x), __uint_as_float(n.y), __uint_as_float(n.z));
+                accept = plain ? plain_pair(P, x, rc2)
+                               : ((!multi || point_in_box(x, qlo, qhi)) && exact_pair(P, x, a.rc, a.box));
+                }
+            const unsigned int hits = __ballot_sync(gmask, accept) & gmask;
+            if (accept)
+                {
+                const unsigned int j = n.w & ~kLeafFlag;
+                const unsigned int pos = own + __popc(hits & lt);   // this pair's place among the own keys
+                if (pos < kHalfCacheSlots) a.cache_out[(size_t)q * kHalfCacheSlots + pos] = ((unsigned int)bit << kHalfKeyBits) | j;
+                if (j != q)
+                    {
+                    const unsigned int slot = atomicAdd(a.in_count + j, 1u);
+                    if (pos >= kHalfCacheSlots)
+                        a.in_lost[j] = 1u;
+                    else if (slot < kHalfCacheSlots)
+                        a.in_cache[(size_t)j * kHalfCacheSlots + slot] = (mirror << kHalfKeyBits) | q;
+                    }
+                }
+            own += __popc(hits);
+            const unsigned int next = __shfl_sync(gmask, cover, G - 1, G);
+            i = max(i + (unsigned int)G, next);
+            }
+        }
+    if (lane == 0u) a.own[q] = own;
+    }
+
+// ---------------------------------------------------------------------------------------------
 // Symmetric count of double self queries with the pair exchange: the exchanging count of
 // k_traverse_half with the double predicate of k_traverse_fast_f64 (FP32 screen, exact_pair_f64 in
 // the band).  The double predicate is symmetric -- the minimum-image difference of (j, q) is the

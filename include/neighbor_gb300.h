@@ -159,6 +159,10 @@ int nbr_traverser_set_warp_walk_max(nbr_traverser t, unsigned int max_queries);
 int nbr_traverser_set_symmetric_min_points(nbr_traverser t, unsigned int min_points);
 /* Addition: lanes per query of those small traversals (4, 8, 16 or 32; 0 = by size). */
 int nbr_traverser_set_walk_lanes(nbr_traverser t, unsigned int lanes);
+/* Addition: lanes per query of the exchanging symmetric count (LBVHTraverser::setHalfWalkLanes):
+ * 1 (one thread per query), 4, 8, 16 or 32; 0 picks by size (lane groups up to 65,536 points).
+ * Results do not depend on it; other widths give NBR_ERR_INVALID. */
+int nbr_traverser_set_half_walk_lanes(nbr_traverser t, unsigned int lanes);
 
 /* getData() (LBVHTraverser.h:326-329): int4 nodes in the reference's 10-bit layout (managed),
  * plus the compression frame (lo, hi, bins: managed float[3] each). */

@@ -105,6 +105,7 @@ def _declare(L):
     sig("nbr_traverser_set_pair_cache", [_P, _I])
     sig("nbr_traverser_set_symmetric_min_points", [_P, ctypes.c_uint])
     sig("nbr_traverser_set_walk_lanes", [_P, ctypes.c_uint])
+    sig("nbr_traverser_set_half_walk_lanes", [_P, ctypes.c_uint])
     sig("nbr_traverser_get_data", [_P, _PP, _PP, _PP, _PP])
     sig("nbr_traverser_count_summary", [_P, ctypes.POINTER(_U), ctypes.POINTER(ctypes.c_ulonglong),
                                         ctypes.POINTER(_U), _P])
@@ -178,6 +179,7 @@ EXPORTED = ["nbr_last_error", "nbr_version", "nbr_lbvh_create", "nbr_lbvh_destro
             "nbr_debug_inject_alloc_failures",
             "nbr_traverser_set_work_order", "nbr_traverser_set_warp_walk_max",
             "nbr_traverser_set_symmetric_min_points", "nbr_traverser_set_walk_lanes",
+            "nbr_traverser_set_half_walk_lanes",
             "nbr_traverser_set_pair_cache", "nbr_traverser_count_summary",
             "nbr_traverser_count_summary_device", "nbr_tune_self", "nbr_tune_self_clear",
             "nbr_traverser_get_data", "nbr_traverse", "nbr_traverse_self", "nbr_exact_pad",
@@ -573,6 +575,10 @@ class LBVHTraverser:
     def set_walk_lanes(self, lanes: int):
         """Lanes per query of small traversals: 4, 8, 16 or 32 (0 = by size)."""
         _check(self._L.nbr_traverser_set_walk_lanes(self._h, int(lanes)))
+
+    def set_half_walk_lanes(self, lanes: int):
+        """Lanes per query of the exchanging symmetric count: 1, 4, 8, 16 or 32 (0 = by size)."""
+        _check(self._L.nbr_traverser_set_half_walk_lanes(self._h, int(lanes)))
 
     def force_symmetric(self):
         """The symmetric walk for self traversals of every size (no size routing)."""

@@ -344,6 +344,12 @@ int nbr_traverser_set_walk_lanes(nbr_traverser t, unsigned int lanes)
     return guarded([&] { t->trav.setWalkLanes(lanes); });
     }
 
+int nbr_traverser_set_half_walk_lanes(nbr_traverser t, unsigned int lanes)
+    {
+    if (!t) return fail(NBR_ERR_INVALID, "null handle");
+    return guarded([&] { t->trav.setHalfWalkLanes(lanes); });
+    }
+
 int nbr_traverser_get_data(nbr_traverser t, const int** data, const float** lo, const float** hi,
                            const float** bins)
     {

@@ -138,3 +138,42 @@ def test_walk_lanes_rejects_other_widths():
     with pytest.raises(nb.NeighborError):
         trav.set_walk_lanes(5)
     trav.set_walk_lanes(0)
+
+
+@pytest.mark.parametrize("N,clustered,rc", [(3000, True, 1.3), (40000, False, 1.3), (20000, False, 2.6),
+                                            (70000, True, 1.3)])
+def test_half_walk_lane_groups_give_identical_rows(N, clustered, rc):
+    # the exchanging symmetric count with one thread per query and with lane groups of every width:
+    # the same counts, the same rows in order (assembled from the exchange, or re-walked past it --
+    # the clustered sets and the cutoff of 2.6 put many rows there), and the oracle's counts
+    P, L = _points(N, 300 + N, clustered)
+    box = [L, L, L]
+    lbvh = nb.LBVH()
+    lbvh.build(_t(P), [0, 0, 0], box)
+    pad = nb.exact_pad(rc, 2 * L)
+    out = {}
+    for lanes in (1, 4, 8, 16, 32):
+        trav = nb.LBVHTraverser()
+        trav.force_symmetric()
+        trav.set_half_walk_lanes(lanes)
+        cnt = trav.traverse_self(lbvh, rc, box, pad, images="periodic", rows_sorted=True)
+        c_host = cnt.cpu().numpy().view(np.uint32).copy()
+        mx = max(1, int(c_host.max()))
+        c, lst = _rows(*trav.traverse_self(lbvh, rc, box, pad, images="periodic", rows_sorted=True, max_neigh=mx))
+        out[lanes] = (c_host, c, lst)
+    c0, _, l0 = out[1]
+    for lanes, (cnt, c, lst) in out.items():
+        assert np.array_equal(cnt, c0), lanes
+        assert np.array_equal(c, c0), lanes
+        assert np.array_equal(lst, l0), lanes
+    # rows by sorted slot: the oracle's counts in the tree's order
+    want, _ = O.celllist_counts(P, P, rc, [0, 0, 0], box)
+    prim = lbvh.primitives().cpu().numpy().view(np.uint32).astype(np.int64)
+    assert np.array_equal(c0, want[prim])
+
+
+def test_half_walk_lanes_rejects_other_widths():
+    trav = nb.LBVHTraverser()
+    with pytest.raises(nb.NeighborError):
+        trav.set_half_walk_lanes(2)
+    trav.set_half_walk_lanes(0)

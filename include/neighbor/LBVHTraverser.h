@@ -227,10 +227,12 @@ class LBVHTraverser : public Tunable<unsigned int>
         // getSymmetricMinPoints() points take the symmetric walk with the pair exchange; other
         // traversals of at most getWarpWalkMaxQueries() queries walk one group of lanes per query
         // (getWalkLanes()), which shortens a walk about as many times as the group has lanes, and
-        // larger ones one thread per query.  Build + count + max + fill, median of 30 steps:
-        // 16,384 points lane groups 248 us, symmetric 294; 32,768 points 319 / 304; 65,536
-        // points 429 / 341; 262,144 points 558 / 427 (thread walk 556); 524,288 points thread 773,
-        // symmetric 548.  0 turns a limit off.
+        // larger ones one thread per query.  Build + count + max + fill driven from C++, median of
+        // 200 steps (the symmetric count by lane groups up to 65,536 points): 4,096 points lane
+        // groups 150 us, symmetric 155; 8,192 points 182 / 174; 16,384 points 226 / 194; 32,768
+        // points 295 / 210; 65,536 points 436 / 285.  Larger (python-driven, median of 30):
+        // 262,144 points 558 / 427 (thread walk 556); 524,288 points thread 773, symmetric 548.
+        // 0 turns a limit off.
         void setWarpWalkMaxQueries(unsigned int q) { m_warp_walk_max = q; }
         unsigned int getWarpWalkMaxQueries() const { return m_warp_walk_max; }
         void setSymmetricMinPoints(unsigned int n) { m_symmetric_min = n; }

@@ -758,7 +758,7 @@ constexpr unsigned int kWarpWalkBlock = 256;
 constexpr unsigned int kWarpWalkMaxQueries = 32768;
 // self traversals of at most this many points walk the whole tree (no symmetric walk); above it
 // the symmetric walk with the pair exchange, whatever the lane-group limit
-constexpr unsigned int kSymmetricMinPoints = 16384;
+constexpr unsigned int kSymmetricMinPoints = 4096;
 
 // G < 32: the same walk by groups of G lanes, 32 / G queries per warp (chunks of G records).  A
 // group's shuffles and ballots name only its own lanes, so the groups of a warp may be at

@@ -151,10 +151,10 @@ int nbr_traverser_count_summary(nbr_traverser t, unsigned int* max_count, unsign
  * count. */
 int nbr_traverser_count_summary_device(nbr_traverser t, const unsigned int** words);
 
-/* Addition, routing by size: traversals of at most max_queries queries (self traversals included)
- * walk one warp per query, larger ones one thread per query (default 32,768; 0 = never).  Self
- * traversals take the symmetric walk only above min_points points (default 262,144; 0 = any size
- * above the warp limit).  Results are the same either way. */
+/* Addition, routing by size: traversals of at most max_queries queries walk one group of lanes
+ * per query, larger ones one thread per query (default 32,768; 0 = never).  Self traversals of
+ * more than min_points points take the symmetric walk with the pair exchange whatever the lane
+ * limit (default 4,096; 0 = any size).  Results are the same either way. */
 int nbr_traverser_set_warp_walk_max(nbr_traverser t, unsigned int max_queries);
 int nbr_traverser_set_symmetric_min_points(nbr_traverser t, unsigned int min_points);
 /* Addition: lanes per query of those small traversals (4, 8, 16 or 32; 0 = by size). */

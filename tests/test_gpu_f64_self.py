@@ -235,3 +235,21 @@ def test_double_tree_reference_layout_boxes():
     left, right = arr["left"], arr["right"]
     assert np.array_equal(arr["lo"][:ni], np.minimum(arr["lo"][left], arr["lo"][right]))
     assert np.array_equal(arr["hi"][:ni], np.maximum(arr["hi"][left], arr["hi"][right]))
+
+
+@pytest.mark.parametrize("N", [1, 2, 37, 5000])
+def test_self_f64_small_sets(N):
+    # tiny trees (one point, two, a few dozen: the whole-tree walk) and a set just above the
+    # symmetric minimum: the same counts and rows as traverse_f64 over the sorted points
+    rc = 1.3
+    P, L, _ = _uniform(N, 900 + N, 0.85)
+    L = max(L, 3.0)
+    box = [L, L, L]
+    pad = nb.exact_pad(rc, 2 * L)
+    pts = torch.tensor(P, device="cuda")
+    lbvh = nb.LBVH()
+    lbvh.build_f64(pts, [0, 0, 0], box)
+    c_want, l_want, prims = _expected(lbvh, P, rc, box, pad, "periodic", None, None)
+    trav = nb.LBVHTraverser()
+    c, lst = _self(trav, lbvh, pts, rc, box, pad, "periodic", None, True, max_neigh=l_want.shape[1])
+    _compare(c, lst, c_want, l_want, prims, True)

@@ -552,11 +552,20 @@ def polydisperse_step(nb, trees, travs, species, L, skin=0.4, diam=(1.0, 10.0), 
     and cutoff of each of the 4 traversals (device tensors)."""
     import torch
     box = [L, L, L]
-    for t, pts in zip(trees, species):
-        t.build(pts, [0, 0, 0], box)
-    pairs = [(i, j) for i in range(len(species)) for j in range(len(species))]
     main = torch.cuda.current_stream()
+    pairs = [(i, j) for i in range(len(species)) for j in range(len(species))]
     strm = streams if streams is not None else [main] * len(pairs)
+    if streams is not None:
+        # the two builds are independent: the small tree's (launch-bound) beside the large one's
+        forked = main.record_event()
+        for t, pts, st in zip(trees, species, streams):
+            st.wait_event(forked)
+            t.build(pts, [0, 0, 0], box, stream=st)
+        for st in streams[: len(trees)]:
+            main.wait_event(st.record_event())
+    else:
+        for t, pts in zip(trees, species):
+            t.build(pts, [0, 0, 0], box)
     args = {}
     for k, (i, j) in enumerate(pairs):
         R = 0.5 * (diam[i] + diam[j]) + skin

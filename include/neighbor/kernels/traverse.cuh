@@ -1088,8 +1088,8 @@ __global__ void __launch_bounds__(kHalfBlock, OUT == kFastCount ? 16 : 12) k_tra
         const auto walk = [&](auto plain_tag) {
             constexpr bool kPlain = decltype(plain_tag)::value;
             unsigned int i = start;
-            while (i < n_rec)
-                {
+            // one record: a point goes to the predicate, a box that misses jumps to its skip link
+            const auto step = [&]() {
                 const uint4 n = __ldg(tree.nodes + i);
                 if (OUT == kFastCount && !CACHE) ++visits;   // (an exchanged count's fill walks nothing)
                 if ((int)n.w < 0)
@@ -1103,6 +1103,17 @@ __global__ void __launch_bounds__(kHalfBlock, OUT == kFastCount ? 16 : 12) k_tra
                 else
                     {
                     i = node_overlaps(n, qb) ? i + 1u : max(n.w, i + 1u);
+                    }
+            };
+            while (i < n_rec)
+                {
+                step();
+                // counts take two records per trip of the loop (16M points, the count stage of the
+                // step: 3.34 ms with one, 3.26 with two, 3.29 with four)
+                if (OUT == kFastCount)
+                    {
+                    if (i >= n_rec) break;
+                    step();
                     }
                 }
         };
@@ -1330,8 +1341,7 @@ __global__ void __launch_bounds__(kHalfBlock, MINB) k_traverse_half_f64(const Fa
         const auto walk = [&](auto plain_tag) {
             constexpr bool kPlain = decltype(plain_tag)::value;
             unsigned int i = start;
-            while (i < n_rec)
-                {
+            const auto step = [&]() {
                 const uint4 n = __ldg(tree.nodes + i);
                 if ((int)n.w < 0)
                     {
@@ -1354,7 +1364,8 @@ __global__ void __launch_bounds__(kHalfBlock, MINB) k_traverse_half_f64(const Fa
                     {
                     i = node_overlaps(n, qb) ? i + 1u : max(n.w, i + 1u);
                     }
-                }
+            };
+            while (i < n_rec) step();
         };
         if (plain)
             walk(std::true_type());

@@ -385,8 +385,7 @@ __device__ __forceinline__ void thread_walk(const FastLBVHData& tree, const Fast
         const auto walk = [&](auto plain_tag) {
             constexpr bool kPlain = decltype(plain_tag)::value;
             unsigned int i = 0;
-            while (i < n_rec)
-                {
+            const auto step = [&]() {
                 const uint4 n = __ldg(tree.nodes + i);
                 if (STATS) ++visits;
                 if ((int)n.w < 0)
@@ -409,6 +408,14 @@ __device__ __forceinline__ void thread_walk(const FastLBVHData& tree, const Fast
                     // skip links point forward in a valid tree; max() keeps a damaged one from looping
                     i = node_overlaps(n, qb) ? i + 1u : max(n.w, i + 1u);
                     }
+            };
+            // two records per trip of the loop (clustered 4M plain step, whose CSR fill walks the
+            // whole tree: 9.34 -> 9.20 ms)
+            while (i < n_rec)
+                {
+                step();
+                if (i >= n_rec) break;
+                step();
                 }
         };
         if (plain)
@@ -1365,7 +1372,13 @@ __global__ void __launch_bounds__(kHalfBlock, MINB) k_traverse_half_f64(const Fa
                     i = node_overlaps(n, qb) ? i + 1u : max(n.w, i + 1u);
                     }
             };
-            while (i < n_rec) step();
+            // two records per trip of the loop (16M points, count alone: 3.75 -> 3.67 ms; four: 3.72)
+            while (i < n_rec)
+                {
+                step();
+                if (i >= n_rec) break;
+                step();
+                }
         };
         if (plain)
             walk(std::true_type());

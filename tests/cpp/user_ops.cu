@@ -327,8 +327,36 @@ int run_ops(const char* in_path, unsigned int N, double L, double r, const char*
     traverser.traverse(neighbor::LBVHTraverser::LaunchParameters(64, st), lbvh,
                        ExactParticleQueryOp(spheres.get(), N, particles.get(), L),
                        NearestOp(count.get(), idsum.get(), nearest.get(), particles.get(), L), img);
+    // the same particles as double self queries with the library's exact double op: a tree of
+    // PointInsertOpF64 and the two-pass list of traverseSelfF64 (count, largest count on the host,
+    // fill), rows by particle index
+    neighbor::shared_array<double3> pos(N);
+    for (unsigned int i = 0; i < N; ++i) pos[i] = make_double3(hp[i].x, hp[i].y, hp[i].z);
+    neighbor::LBVH lbvh64;
+    lbvh64.build(neighbor::LBVH::LaunchParameters(256, st), neighbor::PointInsertOpF64(pos.get(), N),
+                 make_float3(0.f, 0.f, 0.f), make_float3(Lf, Lf, Lf));
+    neighbor::LBVHTraverser self_traverser;
+    const neighbor::LBVHTraverser::LaunchParameters lp(256, st);
+    const float pad = neighbor::exact_query_pad((float)r, 2.f * Lf);
+    const double3 box64 = make_double3(L, L, L);
+    neighbor::shared_array<unsigned int> self_count(N);
+    self_traverser.traverseSelfF64(lp, lbvh64, pos.get(), r, box64, pad, neighbor::CountNeighborsOp(self_count.get()),
+                                   neighbor::PeriodicImagesOp(make_float3(Lf, Lf, Lf)), neighbor::NullTransformOp(),
+                                   false);
+    unsigned int max_count = 0, past = 0;
+    unsigned long long total = 0;
+    self_traverser.readCountSummary(st, max_count, total, past);
+    const unsigned int stride = max_count > 0 ? max_count : 1u;
+    neighbor::shared_array<unsigned int> self_list((size_t)N * stride), self_rows(N);
+    self_traverser.traverseSelfF64(lp, lbvh64, pos.get(), r, box64, pad,
+                                   neighbor::NeighborListOp(self_list.get(), self_rows.get(), stride),
+                                   neighbor::PeriodicImagesOp(make_float3(Lf, Lf, Lf)), neighbor::NullTransformOp(),
+                                   false);
     check(cudaStreamSynchronize(st), "sync");
     check(cudaStreamDestroy(st), "stream");
+    std::vector<unsigned long long> self_idsum(N, 0ull);
+    for (unsigned int i = 0; i < N; ++i)
+        for (unsigned int k = 0; k < self_rows[i] && k < stride; ++k) self_idsum[i] += self_list[(size_t)i * stride + k];
     auto dump = [&](const char* name, const void* p, size_t bytes) {
         const std::string path = std::string(prefix) + "." + name;
         FILE* o = fopen(path.c_str(), "wb");
@@ -339,6 +367,8 @@ int run_ops(const char* in_path, unsigned int N, double L, double r, const char*
     dump("count", count.get(), (size_t)N * 4);
     dump("idsum", idsum.get(), (size_t)N * 8);
     dump("nearest", nearest.get(), (size_t)N * 4);
+    dump("self_count", self_rows.get(), (size_t)N * 4);
+    dump("self_idsum", self_idsum.data(), (size_t)N * 8);
     printf("{\"ops\": %u}\n", N);
     return 0;
     }

@@ -9,7 +9,9 @@ drives LBVH::build and LBVHTraverser::traverse with its own ops:
 - the double-precision ParticleInsertOp / ParticleQueryOp of the reference's benchmark
   (benchmark/lbvh_benchmark.cuh:25-92) with 27 double3 images, a user exact query and a user
   output op (count, sum of ids, nearest other particle) -- compared with a float64 brute force
-  that applies the same minimum-image predicate.
+  that applies the same minimum-image predicate;
+- the same particles through the library's double self queries (PointInsertOpF64 and
+  LBVHTraverser::traverseSelfF64, count, readCountSummary, fill) -- the same brute force.
 """
 import json
 import os
@@ -83,7 +85,7 @@ def _brute(P, L, r):
     return count, idsum, nearest
 
 
-@pytest.mark.parametrize("n,L,r", [(3000, 14.0, 1.1), (2500, 6.0, 2.6)])
+@pytest.mark.parametrize("n,L,r", [(3000, 14.0, 1.1), (2500, 6.0, 2.6), (5000, 16.0, 1.3)])
 def test_double_particle_ops_and_user_output_op(user_ops, tmp_path, n, L, r):
     rng = np.random.default_rng(n)
     P = np.zeros((n, 4))
@@ -103,3 +105,7 @@ def test_double_particle_ops_and_user_output_op(user_ops, tmp_path, n, L, r):
     assert np.array_equal(nearest, want_nearest)
     # the stock-style particle query (refine() == true) returns a superset of the exact set
     assert np.all(superset >= count) and superset.sum() > count.sum()
+    # the same particles as the library's double self queries from C++ (traverseSelfF64, two
+    # passes; above 4,096 points the symmetric double walk): the exact sets by particle index
+    assert np.array_equal(np.fromfile(prefix + ".self_count", np.uint32), want_count)
+    assert np.array_equal(np.fromfile(prefix + ".self_idsum", np.uint64), want_idsum)

@@ -686,8 +686,7 @@ __device__ __forceinline__ void thread_walk_f64(const FastLBVHData& tree, const 
         const auto walk = [&](auto plain_tag) {
             constexpr bool kPlain = decltype(plain_tag)::value;
             unsigned int i = 0;
-            while (i < n_rec)
-                {
+            const auto step = [&]() {
                 const uint4 n = __ldg(tree.nodes + i);
                 if ((int)n.w < 0)
                     {
@@ -712,6 +711,13 @@ __device__ __forceinline__ void thread_walk_f64(const FastLBVHData& tree, const 
                     {
                     i = node_overlaps(n, qb) ? i + 1u : max(n.w, i + 1u);
                     }
+            };
+            // two records per trip of the loop (16M double count, whole tree: 7.26 -> 7.03 ms)
+            while (i < n_rec)
+                {
+                step();
+                if (i >= n_rec) break;
+                step();
                 }
         };
         if (own_plain && t.x == 0.f && t.y == 0.f && t.z == 0.f)
